@@ -1,0 +1,213 @@
+"""Pin the CPU oracle to golden vectors produced by the reference itself.
+
+The fixtures in ``tests/golden`` were generated by ``tests/golden/make_golden.py``
+from the reference's own block functions (CuPy -> NumPy, cupyx.scipy.ndimage ->
+scipy.ndimage).  The oracle must reproduce them bit-exactly: it restates the
+same float32 operation order with the same library calls.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import restated as R
+
+
+def _load(golden_dir, name):
+    return np.load(os.path.join(golden_dir, name + ".npz"))
+
+
+def _meta(golden_dir, name):
+    with open(os.path.join(golden_dir, name + ".json")) as f:
+        return json.load(f)
+
+
+def _eq(a, b):
+    assert a.dtype == b.dtype, (a.dtype, b.dtype)
+    assert a.shape == b.shape
+    assert np.array_equal(a, b, equal_nan=True), float(np.nanmax(np.abs(a.astype(np.float64) - b)))
+
+
+STENCIL_CASES = ["s1_fbm_10m", "s2_fbm_5m_nan", "s3_geo_edges_nan", "s4_tiny_3x5", "s5_single_valid",
+                 "s6_all_nan", "s7_parabolic_cylinder", "s8_dome", "s9_big_void"]
+
+
+@pytest.mark.parametrize("case", STENCIL_CASES)
+def test_stencil_products_bit_exact(golden_dir, case):
+    g = _load(golden_dir, "stencil")
+    m = _meta(golden_dir, "stencil")[case]
+    dem = g[f"{case}/dem"]
+    kw = dict(pixel_size=m["pixel_size"], psx=m["psx"], psy=m["psy"])
+    _eq(R.hillshade(dem.copy(), azimuth=m["azimuth"], altitude=m["altitude"], z_factor=m["z_factor"], **kw),
+        g[f"{case}/hillshade"])
+    for unit in ("degree", "percent", "radian"):
+        _eq(R.slope(dem.copy(), unit=unit, **kw), g[f"{case}/slope_{unit}"])
+    for ct in ("mean", "gaussian", "planform", "profile"):
+        _eq(R.curvature(dem.copy(), curvature_type=ct, **kw), g[f"{case}/curvature_{ct}"])
+
+
+def test_reference_curvature_known_answers(golden_dir):
+    """tests/test_curvature_analytic.py:26-54 of the reference, on the oracle."""
+    g = _load(golden_dir, "stencil")
+    zero = 0.5 ** (1.0 / 2.2)
+    cyl = g["s7_parabolic_cylinder/dem"]
+    plan = R.curvature(cyl, curvature_type="planform")
+    prof = R.curvature(cyl, curvature_type="profile")
+    assert float(np.abs(plan[20:44, 20:44] - zero).max()) < 0.02
+    assert float(np.abs(prof[20:44, 20:44] - zero).max()) > 0.05
+    dome = g["s8_dome/dem"]
+    for ct in ("planform", "profile"):
+        assert float(np.abs(R.curvature(dome, curvature_type=ct)[20:44, 20:44] - zero).max()) > 0.05
+
+
+@pytest.mark.parametrize("variant", ["clean", "nan"])
+def test_spatial_smoothing_bit_exact(golden_dir, variant):
+    g = _load(golden_dir, "smooth")
+    dem = g[f"{variant}/dem"]
+    for r, algo in ((1.0, "hillshade"), (4.0, "hillshade"), (16.0, "slope"), (40.0, "curvature"),
+                    (100.0, "hillshade")):
+        _eq(np.asarray(R.smooth_for_radius(dem.copy(), r, pixel_size=5.0, algorithm=algo), np.float32),
+            g[f"{variant}/smooth_{algo}_{int(r)}"])
+
+
+@pytest.mark.parametrize("case", ["t1_clean", "t2_nan", "t3_halfmetre", "t4_nan_r2"])
+def test_topousm_block_bit_exact(golden_dir, case):
+    g = _load(golden_dir, "topousm")
+    m = _meta(golden_dir, "topousm")[case]
+    out = R.topousm_block(g[f"{case}/dem"].copy(), radii=[int(r) for r in g[f"{case}/radii"]],
+                          weights=[float(w) for w in g[f"{case}/weights"]], pixel_size=m["pixel_size"])
+    _eq(out, g[f"{case}/out"])
+
+
+def test_down_up_sampling_bit_exact(golden_dir):
+    g = _load(golden_dir, "topousm")
+    dem = g["down/dem"]
+    for f in (2, 4, 8):
+        small = R.downsample_nan_aware(dem.copy(), f)
+        _eq(small, g[f"down/f{f}"])
+        _eq(R.upsample_to_shape(small, dem.shape), g[f"down/up{f}"])
+
+
+def test_coarse_field_and_global_sampling_bit_exact(golden_dir):
+    g = _load(golden_dir, "topousm")
+    field = R.coarse_field(g["coarse/dem"].copy(), large_radii=[512, 2048],
+                           large_weights=[2.0 / 63.0, 1.0 / 63.0], decimation=16.0)
+    _eq(field, g["coarse/field"])
+    _eq(R.bilinear_sample_coarse(field, 100, 180, 333, 433, 1024, 1280), g["coarse/sample"])
+    _eq(R.bilinear_sample_coarse(field, 0, 40, 1240, 1280, 1024, 1280), g["coarse/sample_edge"])
+
+
+def test_normalisation_statistics(golden_dir):
+    g = _load(golden_dir, "topousm")
+    assert R.topousm_scale(g["stats/outliers"])[0] == float(g["stats/outliers_scale"][0])
+    assert R.topousm_scale(g["stats/ridge"])[0] == float(g["stats/ridge_scale"][0])
+    # reference tests/test_topousm_fast_normalization.py:6-32 known answers
+    assert 0.0 < R.topousm_scale(g["stats/outliers"])[0] < 0.2
+    assert R.topousm_scale(g["stats/ridge"])[0] == pytest.approx(0.5, rel=1e-2)
+    t2 = g["t2_nan/out"]
+    s = R.topousm_scale(t2)
+    assert s[0] == float(g["stats/t2_scale"][0])
+    _eq(R.topousm_normalize(t2.copy(), s), g["stats/t2_norm"])
+    st = R.stretch_stats(g["stats/stretch_in"])
+    assert st == tuple(float(x) for x in g["stats/stretch"])
+
+
+def test_topousm_norm_is_linear_without_clip():
+    """reference tests/test_topousm_fast_normalization.py:35-44."""
+    d = np.asarray([-4.0, -1.0, 0.0, 1.0, 4.0], np.float32)
+    assert R.topousm_normalize(d, (2.0,)).tolist() == pytest.approx([-2.0, -0.5, 0.0, 0.5, 2.0])
+
+
+OPEN_CASES = ["o1_fbm_nan", "o2_peak", "o2_pit", "o2_flat", "o3_aniso_d5", "o4_r256"]
+
+
+@pytest.mark.parametrize("case", OPEN_CASES)
+def test_openness_bit_exact(golden_dir, case):
+    g = _load(golden_dir, "openness")
+    m = _meta(golden_dir, "openness")[case]
+    for ot in ("positive", "negative"):
+        out = R.openness(g[f"{case}/dem"].copy(), openness_type=ot, num_directions=m["num_directions"],
+                         max_distance=m["max_distance"], pixel_size=m["pixel_size"], psx=m["psx"], psy=m["psy"])
+        _eq(out, g[f"{case}/{ot}"])
+
+
+def test_openness_reference_known_answers(golden_dir):
+    """reference tests/test_openness_yokoyama.py:1-47 on the oracle."""
+    g = _load(golden_dir, "openness")
+    c = 50
+
+    def run(n, ot):
+        return R.openness(g[f"{n}/dem"], openness_type=ot, num_directions=16, max_distance=40)[c, c]
+
+    assert run("o2_peak", "positive") > run("o2_pit", "positive")
+    assert run("o2_pit", "negative") > run("o2_peak", "negative")
+    assert run("o2_flat", "positive") == pytest.approx(1.0, abs=1e-3)
+    assert run("o2_flat", "negative") == pytest.approx(1.0, abs=1e-3)
+
+
+def test_openness_r256_distances():
+    assert R.openness_distances(256).tolist() == [25, 51, 76, 102, 128, 153, 179, 204, 230, 256]
+    assert R.openness_distances(5).tolist() == [1, 2, 3, 4, 5]
+
+
+def test_quantize_bit_exact(golden_dir):
+    g = _load(golden_dir, "encoding")
+    with open(os.path.join(golden_dir, "tables.json")) as f:
+        t = json.load(f)
+    qin = g["q/in"]
+    for key, qp_ref in t["quantize_params"].items():
+        algo, dt = key.split("/")
+        if algo == "slope_radian":
+            rng = R.resolve_output_range("slope", params={"unit": "radian"})
+        else:
+            rng = R.resolve_output_range(algo, params={})
+        qp = R.quantize_params(rng[0], rng[1], dt)
+        for k, v in qp_ref.items():
+            assert qp[k] == v, (key, k)
+        _eq(R.quantize_array(qin, qp, dt), g[f"q/{key}"])
+
+
+def test_logic_tables(golden_dir):
+    with open(os.path.join(golden_dir, "tables.json")) as f:
+        t = json.load(f)
+    for r, px, algo, f_ in t["downsample_factor"]:
+        assert R.downsample_factor(r, pixel_size=px, algorithm=algo) == f_, (r, px, algo)
+    for s, radii in t["auto_radii"]:
+        assert R.auto_spatial_radii(s) == radii
+    for n, w in t["auto_weights"]:
+        assert R.auto_spatial_weights(n) == w
+    for lat, mpd in t["meters_per_degree"]:
+        assert list(R.meters_per_degree(lat)) == mpd
+    for r, w, out in t["dedup"]:
+        got = R.dedup_radii_weights(r, w)
+        assert [got[0], got[1]] == out
+    for r, w, out in t["resolve_radii_weights"]:
+        got = R.resolve_spatial_radii_weights(r, w, 10.0, 3000)
+        assert [list(got[0]), list(got[1])] == out
+    for r, w, thr, out in t["split_radii"]:
+        assert [list(x) for x in R.split_radii_by_threshold(r, w, thr)] == out
+    for mr, mw, px, out in t["topousm_radii_norm"]:
+        got = R.normalize_topousm_radii(mr, mw, px)
+        assert [None if x is None else list(x) for x in got] == out
+
+
+def test_tile_grid_clips_at_raster_edges():
+    tiles = R.tile_grid(10000, 9000, 4096, 160)
+    assert len(tiles) == 3 * 3
+    ty, tx, cx, cy, cw, ch, wx, wy, ww, wh = tiles[0]
+    assert (cx, cy, cw, ch, wx, wy, ww, wh) == (0, 0, 4096, 4096, 0, 0, 4256, 4256)
+    ty, tx, cx, cy, cw, ch, wx, wy, ww, wh = tiles[4]
+    assert (cx, cy, cw, ch, wx, wy, ww, wh) == (4096, 4096, 4096, 4096, 3936, 3936, 4416, 4416)
+    ty, tx, cx, cy, cw, ch, wx, wy, ww, wh = tiles[-1]
+    assert (cx, cy, cw, ch) == (8192, 8192, 808, 1808)
+    assert (wx, wy, ww, wh) == (8032, 8032, 968, 1968)
+
+
+def test_nodata_mask_merges_nan_and_sentinel():
+    """core/tile_processor.py:185-196; reference tests/test_audit_p1_regressions.py:20-43."""
+    d = np.asarray([[-9999.0, -9999.0000005, 1.0, np.nan], [-9998.99, 0.0, 2.0, 3.0]], np.float32)
+    m = R.nodata_mask(d, -9999.0)
+    assert m.tolist() == [[True, True, False, True], [False, False, False, False]]
+    assert R.nodata_mask(d, float("nan")).tolist() == np.isnan(d).tolist()
+    assert R.nodata_mask(d, None) is None
