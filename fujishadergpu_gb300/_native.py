@@ -1,0 +1,127 @@
+"""ctypes binding of libfsg.so (the C ABI declared in include/fsg.h).
+
+The library is loaded from ``fujishadergpu_gb300/lib/libfsg.so``.  There is no
+CPU fallback: if the library is missing or no CUDA device is present every
+entry point raises, so a run that "works" is always the CUDA path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libfsg.so")
+_lock = threading.Lock()
+_lib = None
+
+# ----------------------------------------------------------------- constants
+FSG_OK = 0
+FSG_ERR_INVALID = -1
+FSG_ERR_SHAPE = -2
+FSG_ERR_DTYPE = -3
+FSG_ERR_CUDA = -4
+FSG_ERR_TIMEOUT = -5
+FSG_ERR_ABORTED = -6
+FSG_ERR_WORKSPACE = -7
+FSG_ERR_UNSUPPORTED = -8
+
+FSG_F32, FSG_U8, FSG_I16 = 0, 1, 2
+DTYPE_CODES = {"float32": FSG_F32, "uint8": FSG_U8, "int16": FSG_I16}
+
+FSG_OUT_HILLSHADE = 0
+FSG_OUT_SLOPE = 1
+FSG_OUT_CURV_MEAN = 2
+FSG_OUT_CURV_GAUSSIAN = 3
+FSG_OUT_CURV_PLANFORM = 4
+FSG_OUT_CURV_PROFILE = 5
+FSG_OUT_DX = 6
+FSG_OUT_DY = 7
+FSG_STENCIL_NOUT = 8
+CURVATURE_OUT = {"mean": FSG_OUT_CURV_MEAN, "gaussian": FSG_OUT_CURV_GAUSSIAN,
+                 "planform": FSG_OUT_CURV_PLANFORM, "profile": FSG_OUT_CURV_PROFILE}
+SLOPE_UNITS = {"degree": 0, "percent": 1, "radian": 2}
+
+
+class FsgError(RuntimeError):
+    """A libfsg.so call failed; ``code`` is the FSG_ERR_* status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"libfsg error {code}: {message}")
+        self.code = code
+
+
+class FsgValueError(FsgError, ValueError):
+    """Invalid argument / shape: the reference raises ValueError in these cases."""
+
+
+# ------------------------------------------------------------------- structs
+class Plane(C.Structure):
+    _fields_ = [("ptr", C.c_void_p), ("ld", C.c_int64), ("dtype", C.c_int32), ("reserved", C.c_int32),
+                ("q_a", C.c_float), ("q_b", C.c_float), ("q_min", C.c_int32), ("q_max", C.c_int32)]
+
+
+class Tile(C.Structure):
+    _fields_ = [("win_y0", C.c_int32), ("win_x0", C.c_int32), ("win_h", C.c_int32), ("win_w", C.c_int32),
+                ("core_y0", C.c_int32), ("core_x0", C.c_int32), ("core_h", C.c_int32), ("core_w", C.c_int32),
+                ("out_y0", C.c_int32), ("out_x0", C.c_int32), ("reserved0", C.c_int32), ("reserved1", C.c_int32),
+                ("pixel_scale_x", C.c_double), ("pixel_scale_y", C.c_double)]
+
+
+class StencilParams(C.Structure):
+    _fields_ = [("azimuth", C.c_double), ("altitude", C.c_double), ("z_factor", C.c_double),
+                ("pixel_size", C.c_double), ("nodata", C.c_double), ("has_nodata", C.c_int32),
+                ("slope_unit", C.c_int32)]
+
+
+# Exported symbols and their signatures (kept in sync with include/fsg.h).
+_SIGNATURES = {
+    "fsg_abi_version": (C.c_int, []),
+    "fsg_version": (C.c_char_p, []),
+    "fsg_last_error": (C.c_char_p, []),
+    "fsg_launch_count": (C.c_int64, []),
+    "fsg_nodata_mask": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_int32,
+                                  C.c_void_p, C.c_int64, C.c_void_p]),
+    "fsg_stencil": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
+                              C.POINTER(StencilParams), C.POINTER(Plane), C.c_void_p]),
+}
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+def lib():
+    """Load libfsg.so once; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(_LIB_PATH):
+                raise FsgError(FSG_ERR_UNSUPPORTED,
+                               f"{_LIB_PATH} is missing: build it with "
+                               "`python -m fujishadergpu_gb300.build` (needs nvcc)")
+            L = C.CDLL(_LIB_PATH)
+            for name, (res, args) in _SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return list(_SIGNATURES)
+
+
+def check(status: int) -> None:
+    if status == FSG_OK:
+        return
+    msg = lib().fsg_last_error().decode("utf-8", "replace")
+    if status in (FSG_ERR_INVALID, FSG_ERR_SHAPE, FSG_ERR_DTYPE):
+        raise FsgValueError(status, msg)
+    raise FsgError(status, msg)
+
+
+def launch_count() -> int:
+    return int(lib().fsg_launch_count())

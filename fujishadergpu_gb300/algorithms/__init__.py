@@ -1,0 +1,18 @@
+"""Drop-in algorithm layer: the reference's block functions and tile classes.
+
+Block functions keep the reference names and keyword arguments
+(``compute_hillshade_block`` ...) and take one halo window as a CUDA device
+array; the classes keep the ``process(dem_gpu, **params)`` /
+``get_default_params()`` interface of algorithms/tile_shared.py:19-44.
+"""
+from ._base import Constants, TileAlgorithm
+from ._impl_curvature import CurvatureAlgorithm, compute_curvature_block
+from ._impl_hillshade import HillshadeAlgorithm, compute_hillshade_block
+from ._impl_slope import SlopeAlgorithm, compute_slope_block
+
+__all__ = [
+    "Constants", "TileAlgorithm",
+    "compute_hillshade_block", "HillshadeAlgorithm",
+    "compute_slope_block", "SlopeAlgorithm",
+    "compute_curvature_block", "CurvatureAlgorithm",
+]

@@ -1,0 +1,100 @@
+// Shared helpers of libfsg.so: error reporting, launch accounting, device
+// properties and the exactly-rounded float32 primitives the kernels use to
+// reproduce NumPy's float32 operation order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstdio>
+
+#include "fsg.h"
+
+namespace fsg {
+
+// ------------------------------------------------------------------ errors
+void set_error(const char* fmt, ...);
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+void count_launches(int64_t n);
+
+#define FSG_CUDA(call)                                      \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return ::fsg::cuda_fail(e_, #call); \
+  } while (0)
+
+// Checks the launch that was just queued.
+#define FSG_LAUNCHED(n)                                     \
+  do {                                                      \
+    cudaError_t e_ = cudaGetLastError();                    \
+    if (e_ != cudaSuccess) return ::fsg::cuda_fail(e_, "kernel launch"); \
+    ::fsg::count_launches(n);                               \
+  } while (0)
+
+struct DeviceInfo {
+  int device = -1;
+  int sms = 0;
+  size_t smem_optin = 0;
+};
+// Properties of the current device (cached per device).
+int device_info(DeviceInfo* out);
+
+// Stream-ordered scratch: cudaMallocAsync on `stream`, freed with
+// cudaFreeAsync on the same stream by the destructor.
+struct StreamScratch {
+  void* ptr = nullptr;
+  cudaStream_t stream = nullptr;
+  StreamScratch() = default;
+  StreamScratch(const StreamScratch&) = delete;
+  StreamScratch& operator=(const StreamScratch&) = delete;
+  int alloc(size_t bytes, cudaStream_t s) {
+    stream = s;
+    cudaError_t e = cudaMallocAsync(&ptr, bytes ? bytes : 1, s);
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      return cuda_fail(e, "cudaMallocAsync(scratch)");
+    }
+    return FSG_OK;
+  }
+  ~StreamScratch() {
+    if (ptr) cudaFreeAsync(ptr, stream);
+  }
+};
+
+// --------------------------------------------------------- device numerics
+// Float32 operations that the compiler may not contract into FMAs: NumPy
+// evaluates `a*b + c` on float32 arrays as two separately rounded ufuncs.
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+
+// a / d for a divisor d fixed per launch, correctly rounded: q = RN(a*r) with
+// r = RN(1/d), then one residual correction q + RN(a - q*d)*r computed with
+// fused multiply-adds (P. Markstein, "Computation of elementary functions on
+// the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990).  Tested
+// against IEEE division on the GPU (tests/test_gpu_numerics.py).
+__device__ __forceinline__ float div_by(float a, float d, float r) {
+  float q = __fmul_rn(a, r);
+  float e = __fmaf_rn(-q, d, a);
+  return __fmaf_rn(e, r, q);
+}
+
+__device__ __forceinline__ bool is_nodata(float v, float ndf, bool has_nodata) {
+  // core/tile_processor.py:185-196 with NumPy 2 scalar rules: the Python
+  // float sentinel is applied as a float32 ("weak") scalar.
+  if (v != v) return true;
+  if (!has_nodata) return false;
+  return fabsf(__fsub_rn(v, ndf)) <= 1e-6f || v == ndf;
+}
+
+// io/output_encoding.py:178-190: DN = clip(rint(f32(a)*v + f32(b)), lo, hi),
+// non-finite -> 0.  Two separately rounded float32 ops, as NumPy does.
+__device__ __forceinline__ float quantize(float v, float qa, float qb, int qmin, int qmax) {
+  if (!isfinite(v)) return 0.0f;
+  float dn = rintf(__fadd_rn(__fmul_rn(qa, v), qb));
+  return fminf(fmaxf(dn, (float)qmin), (float)qmax);
+}
+
+}  // namespace fsg

@@ -1,0 +1,105 @@
+// libfsg.so runtime: version, thread-local error messages, launch accounting,
+// device properties and the NoData mask kernel.
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <mutex>
+#include <string>
+
+#include "fsg_common.cuh"
+
+namespace fsg {
+
+namespace {
+thread_local std::string g_last_error;
+std::atomic<int64_t> g_launches{0};
+std::mutex g_dev_mutex;
+DeviceInfo g_dev_cache[64];
+}  // namespace
+
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+}
+
+int fail(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(FSG_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+void count_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int device_info(DeviceInfo* out) {
+  int dev = 0;
+  FSG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(FSG_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_dev_mutex);
+  DeviceInfo& d = g_dev_cache[dev];
+  if (d.device != dev) {
+    int sms = 0, optin = 0;
+    FSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    FSG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    d.sms = sms;
+    d.smem_optin = (size_t)optin;
+    d.device = dev;
+  }
+  *out = d;
+  return FSG_OK;
+}
+
+namespace {
+__global__ void nodata_mask_kernel(const float* __restrict__ r, long long ld, int h, int w, float ndf,
+                                   int has_nodata, uint8_t* __restrict__ m, long long mld) {
+  long long n = (long long)h * w;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long y = i / w, x = i - y * w;
+    m[y * mld + x] = is_nodata(__ldg(r + y * ld + x), ndf, has_nodata != 0) ? 1 : 0;
+  }
+}
+}  // namespace
+
+}  // namespace fsg
+
+extern "C" {
+
+int fsg_abi_version(void) { return FSG_ABI_VERSION; }
+
+const char* fsg_version(void) { return "fsg-gb300 0.1.0 (sm_103a)"; }
+
+const char* fsg_last_error(void) { return fsg::g_last_error.c_str(); }
+
+int64_t fsg_launch_count(void) { return fsg::g_launches.load(); }
+
+int fsg_nodata_mask(const float* raster_dev, int64_t ld, int32_t h, int32_t w, double nodata,
+                    int32_t has_nodata, uint8_t* mask_dev, int64_t mask_ld, void* stream) {
+  using namespace fsg;
+  if (h < 0 || w < 0) return fail(FSG_ERR_INVALID, "negative raster shape %d x %d", h, w);
+  if ((long long)h * w == 0) return FSG_OK;
+  if (!raster_dev || !mask_dev) return fail(FSG_ERR_INVALID, "null pointer");
+  if (ld < w || mask_ld < w) return fail(FSG_ERR_INVALID, "row pitch smaller than width");
+  DeviceInfo di;
+  int st = device_info(&di);
+  if (st) return st;
+  long long n = (long long)h * w;
+  int blocks = (int)std::min<long long>((n + 255) / 256, (long long)di.sms * 8);
+  nodata_mask_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(raster_dev, ld, h, w, (float)nodata,
+                                                               has_nodata, mask_dev, mask_ld);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+}  // extern "C"

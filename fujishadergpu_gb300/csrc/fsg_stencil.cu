@@ -1,0 +1,574 @@
+// Fused 3x3-class stencils: hillshade, slope and the four curvature products
+// from one read of each halo window.
+//
+// Reference semantics, per tile window (algorithms/tile/dask_bridge.py:72-151):
+//   handle_nan_for_gradient (_nan_utils.py:50-74): NaN cells are replaced by a
+//     NaN-aware Gaussian(sigma=1, truncate 4, mode 'nearest') mean, computed
+//     as two separable passes (axis 0 then axis 1) in float64 with a float32
+//     intermediate, as scipy.ndimage.gaussian_filter does;
+//   np.gradient(filled, |sy|, |sx|, edge_order=2): central differences inside
+//     the window, second-order one-sided formulas on its first/last row/col;
+//   hillshade (_impl_hillshade.py:20-54), slope (_impl_slope.py:19-35),
+//   curvature with a second np.gradient on the SIGNED steps
+//   (_impl_curvature.py:19-57); NaN restored at NoData cells.
+//
+// Work decomposition: every tile core is cut into TY x TX pixel blocks; a
+// persistent grid walks the flattened (tile, block) list.  Each block stages
+// its (TY+6) x (TX+8) halo region in shared memory (float4 loads when the
+// rows are 16-byte aligned), takes the NaN-fill slow path only when a NaN
+// lies in that region, computes dx/dy once into shared memory and emits all
+// requested planes with 4-pixel vector stores.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "fsg_common.cuh"
+
+namespace fsg {
+namespace {
+
+constexpr int TX = 64, TY = 32, NT = 256;
+constexpr int FHY = 3, FHX = 4;           // halo of the staged DEM region
+constexpr int FR = TY + 2 * FHY;          // 38 rows
+constexpr int FC = TX + 2 * FHX;          // 72 cols
+constexpr int DHY = 2, DHX = 2;           // halo of the dx/dy region
+constexpr int DR = TY + 2 * DHY;          // 36
+constexpr int DC = TX + 2 * DHX;          // 68
+constexpr int WHY = FHY + 4, WHX = FHX + 4;  // +4: reach of the 9-tap Gaussian fill
+constexpr int WR = TY + 2 * WHY;          // 46
+constexpr int WC = TX + 2 * WHX;          // 80
+constexpr int INLINE_TILES = 8;
+
+constexpr size_t SMEM_F = sizeof(float) * FR * FC;
+constexpr size_t SMEM_D = sizeof(float) * 2 * DR * DC;
+constexpr size_t SMEM_FILL = sizeof(float) * (WR * WC + 2 * FR * WC) + FR * FC;
+constexpr size_t SMEM_BYTES = SMEM_F + (SMEM_D > SMEM_FILL ? SMEM_D : SMEM_FILL);
+
+// np.gradient constants along one axis for one step size (float32, as NumPy
+// applies the Python-float coefficients to float32 arrays).
+struct Axis {
+  float d2, rcp;      // central: (f[+1] - f[-1]) / d2, d2 = f32(2*step), rcp = RN(1/d2)
+  float fa, fb, fc;   // first index:  fa*f0 + fb*f1 + fc*f2
+  float ba, bb, bc;   // last index:   ba*f[-2] + bb*f[-1] + bc*f0
+};
+
+struct TileK {
+  int wy0, wx0, wy1, wx1;   // window [y0, y1) x [x0, x1)
+  int cy0, cx0, cy1, cx1;   // core
+  int oy0, ox0;             // plane coords of (cy0, cx0)
+  int nbx, block0;
+  Axis g1x, g1y;            // first derivatives: |step| (handle_nan_for_gradient)
+  Axis c2x, c2y;            // second derivatives: signed steps (compute_curvature_block)
+  float sign_x, sign_y;     // hillshade east/north orientation
+};
+
+struct PlaneK {
+  void* ptr;
+  long long ld;
+  int dtype, qmin, qmax;
+  float qa, qb;
+};
+
+struct StencilArgs {
+  const float* raster;
+  long long ld;
+  int rh, rw;
+  const TileK* tiles_dev;
+  int ntiles, total_blocks;
+  float lx, ly, lz, z;
+  int z_is_one;
+  float ndf;
+  int has_nodata;
+  int slope_unit;
+  unsigned outmask;
+  double gw[5];             // scipy Gaussian(sigma=1, radius 4) weights, w[0] = centre
+  PlaneK planes[FSG_STENCIL_NOUT];
+  TileK inl[INLINE_TILES];
+};
+
+// Derivative of a line at index k of a window [lo, hi); f(o) = value at k+o.
+template <class Fn>
+__device__ __forceinline__ float deriv(const Axis& a, int k, int lo, int hi, Fn f) {
+  if (k > lo && k < hi - 1) return div_by(fsub(f(1), f(-1)), a.d2, a.rcp);
+  if (k == lo) return fadd(fadd(fmul(a.fa, f(0)), fmul(a.fb, f(1))), fmul(a.fc, f(2)));
+  return fadd(fadd(fmul(a.ba, f(-2)), fmul(a.bb, f(-1))), fmul(a.bc, f(0)));
+}
+
+__device__ __forceinline__ float gamma_display(float k) {
+  // ((tanh(100k) + 1) / 2) ** (1/2.2): tanhf is the function CuPy's cp.tanh
+  // calls; the sum and halving are the reference's float32 ops.
+  float t = tanhf(k * 100.0f);
+  float u = __fadd_rn(t, 1.0f) * 0.5f;
+  return exp2f(0.45454545454545453f * __log2f(u));
+}
+
+__device__ __forceinline__ float slope_value(float p, float q, int unit) {
+  float g = __fsqrt_rn(fadd(fmul(p, p), fmul(q, q)));
+  float r = atanf(g);
+  if (unit == FSG_SLOPE_DEGREE) return fmul(r, 57.295780181884765625f);  // f32(180/pi)
+  if (unit == FSG_SLOPE_PERCENT) return fmul(tanf(r), 100.0f);
+  return r;
+}
+
+template <int DT>
+__device__ __forceinline__ void store4(const PlaneK& P, long long off, const float* v, int n) {
+  if (DT == FSG_F32) {
+    float* p = static_cast<float*>(P.ptr) + off;
+    if (n == 4 && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
+      *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (k < n) p[k] = v[k];
+    }
+  } else if (DT == FSG_U8) {
+    uint8_t* p = static_cast<uint8_t*>(P.ptr) + off;
+    uint8_t b[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) b[k] = (uint8_t)(int)quantize(v[k], P.qa, P.qb, P.qmin, P.qmax);
+    if (n == 4 && ((reinterpret_cast<uintptr_t>(p) & 3) == 0)) {
+      *reinterpret_cast<uchar4*>(p) = make_uchar4(b[0], b[1], b[2], b[3]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (k < n) p[k] = b[k];
+    }
+  } else {
+    int16_t* p = static_cast<int16_t*>(P.ptr) + off;
+    int16_t s[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) s[k] = (int16_t)(int)quantize(v[k], P.qa, P.qb, P.qmin, P.qmax);
+    if (n == 4 && ((reinterpret_cast<uintptr_t>(p) & 7) == 0)) {
+      *reinterpret_cast<short4*>(p) = make_short4(s[0], s[1], s[2], s[3]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (k < n) p[k] = s[k];
+    }
+  }
+}
+
+__device__ __forceinline__ void store_plane(const PlaneK& P, long long off, const float* v, int n) {
+  if (P.dtype == FSG_F32) store4<FSG_F32>(P, off, v, n);
+  else if (P.dtype == FSG_U8) store4<FSG_U8>(P, off, v, n);
+  else store4<FSG_I16>(P, off, v, n);
+}
+
+// Loads rows [gy0, gy0+R) x cols [gx0, gx0+C) of the raster into S (row pitch
+// C), NoData -> NaN, cells outside the raster -> 0.  Returns true if this
+// thread saw a NaN inside the window.
+template <int R, int C>
+__device__ __forceinline__ bool load_region(const StencilArgs& A, const TileK& T, float* S, int gy0,
+                                            int gx0) {
+  bool vec = ((reinterpret_cast<uintptr_t>(A.raster) & 15) == 0) && ((A.ld & 3) == 0) && ((gx0 & 3) == 0);
+  bool saw_nan = false;
+  const bool hn = A.has_nodata != 0;
+  for (int i = threadIdx.x; i < R * (C / 4); i += NT) {
+    int r = i / (C / 4);
+    int c = (i - r * (C / 4)) * 4;
+    int gy = gy0 + r, gx = gx0 + c;
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    if (gy >= 0 && gy < A.rh) {
+      long long row = (long long)gy * A.ld;
+      if (vec && gx >= 0 && gx + 3 < A.rw) {
+        float4 t = __ldg(reinterpret_cast<const float4*>(A.raster + row + gx));
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+      } else {
+        for (int k = 0; k < 4; ++k)
+          if (gx + k >= 0 && gx + k < A.rw) v[k] = __ldg(A.raster + row + gx + k);
+      }
+    }
+    bool row_in = gy >= T.wy0 && gy < T.wy1;
+    for (int k = 0; k < 4; ++k) {
+      if (is_nodata(v[k], A.ndf, hn)) {
+        v[k] = __int_as_float(0x7fc00000);
+        if (row_in && gx + k >= T.wx0 && gx + k < T.wx1) saw_nan = true;
+      }
+    }
+    *reinterpret_cast<float4*>(S + r * C + c) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+  return saw_nan;
+}
+
+// Separable 9-tap Gaussian in float64 (scipy's symmetric correlate1d order),
+// result rounded to float32.
+__device__ __forceinline__ double gsum(const double* w, const double* x) {
+  double acc = __dmul_rn(x[4], w[0]);
+  acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(x[0], x[8]), w[4]));
+  acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(x[1], x[7]), w[3]));
+  acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(x[2], x[6]), w[2]));
+  acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(x[3], x[5]), w[1]));
+  return acc;
+}
+
+template <bool CURV>
+__global__ void __launch_bounds__(NT) stencil_kernel(const __grid_constant__ StencilArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* F = reinterpret_cast<float*>(smem);                       // [FR][FC]
+  unsigned char* U = smem + SMEM_F;
+  float* DX = reinterpret_cast<float*>(U);                         // [DR][DC]
+  float* DY = DX + DR * DC;
+  float* W = reinterpret_cast<float*>(U);                          // [WR][WC] (fill path)
+  float* VV = W + WR * WC;                                         // [FR][WC]
+  float* VW = VV + FR * WC;                                        // [FR][WC]
+  unsigned char* need = reinterpret_cast<unsigned char*>(VW + FR * WC);  // [FR][FC]
+
+  const TileK* tiles = A.ntiles <= INLINE_TILES ? A.inl : A.tiles_dev;
+  const int tid = threadIdx.x;
+  const int tcol = (tid & 15) * 4;
+  const int trow = tid >> 4;
+  const unsigned om = A.outmask;
+
+  for (int blk = blockIdx.x; blk < A.total_blocks; blk += gridDim.x) {
+    int lo = 0, hi = A.ntiles - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (tiles[mid].block0 <= blk) lo = mid; else hi = mid - 1;
+    }
+    const TileK& T = tiles[lo];
+    const int lb = blk - T.block0;
+    const int by = lb / T.nbx, bx = lb - (lb / T.nbx) * T.nbx;
+    const int y0 = T.cy0 + by * TY, x0 = T.cx0 + bx * TX;
+    const int fy0 = y0 - FHY, fx0 = x0 - FHX;
+
+    __syncthreads();  // the previous block is done with shared memory
+    bool saw = load_region<FR, FC>(A, T, F, fy0, fx0);
+    const int any_nan = __syncthreads_or(saw);
+
+    // NoData flags of this thread's 8 core pixels, before the fill rewrites F.
+    unsigned nanbits = 0;
+#pragma unroll
+    for (int g = 0; g < 2; ++g)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        float v = F[(FHY + trow + 16 * g) * FC + FHX + tcol + k];
+        if (v != v) nanbits |= 1u << (g * 4 + k);
+      }
+
+    if (any_nan) {
+      // (a) NaN cells of the window whose fill value can reach a valid pixel
+      //     (a valid window cell within Chebyshev distance 3).
+      for (int i = tid; i < FR * FC; i += NT) {
+        int r = i / FC, c = i - (i / FC) * FC;
+        int gy = fy0 + r, gx = fx0 + c;
+        unsigned char nd = 0;
+        if (gy >= T.wy0 && gy < T.wy1 && gx >= T.wx0 && gx < T.wx1 && F[i] != F[i]) {
+          for (int dr = -3; dr <= 3 && !nd; ++dr) {
+            int rr = r + dr, yy = gy + dr;
+            if (rr < 0 || rr >= FR || yy < T.wy0 || yy >= T.wy1) continue;
+            for (int dc = -3; dc <= 3; ++dc) {
+              int cc = c + dc, xx = gx + dc;
+              if (cc < 0 || cc >= FC || xx < T.wx0 || xx >= T.wx1) continue;
+              float v = F[rr * FC + cc];
+              if (v == v) { nd = 1; break; }
+            }
+          }
+        }
+        need[i] = nd;
+      }
+      // (b) the wider region the 9x9 Gaussian reaches
+      load_region<WR, WC>(A, T, W, y0 - WHY, x0 - WHX);
+      __syncthreads();
+      double gw[5];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) gw[j] = A.gw[j];
+      // (c) axis-0 pass (values and valid weights) where a needed cell of the
+      //     same row lies within 4 columns (nearest-mode clamping at window edges)
+      for (int i = tid; i < FR * WC; i += NT) {
+        int r = i / WC, xc = i - (i / WC) * WC;
+        int gy = fy0 + r, gx = x0 - WHX + xc;
+        if (gy < T.wy0 || gy >= T.wy1 || gx < T.wx0 || gx >= T.wx1) continue;
+        bool want = false;
+        for (int c = max(0, xc - 8); c <= min(FC - 1, xc) && !want; ++c) want = need[r * FC + c] != 0;
+        if (!want) continue;
+        double xv[9], xw[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+          int yy = min(max(gy + j - 4, T.wy0), T.wy1 - 1);
+          float v = W[(yy - (y0 - WHY)) * WC + xc];
+          bool ok = v == v;
+          xv[j] = ok ? (double)v : 0.0;
+          xw[j] = ok ? 1.0 : 0.0;
+        }
+        VV[r * WC + xc] = (float)gsum(gw, xv);
+        VW[r * WC + xc] = (float)gsum(gw, xw);
+      }
+      __syncthreads();
+      // (d) axis-1 pass and the normalised fill value
+      for (int i = tid; i < FR * FC; i += NT) {
+        if (!need[i]) continue;
+        int r = i / FC, c = i - (i / FC) * FC;
+        int gx = fx0 + c;
+        double xv[9], xw[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+          int xx = min(max(gx + j - 4, T.wx0), T.wx1 - 1);
+          int xc = xx - (x0 - WHX);
+          xv[j] = (double)VV[r * WC + xc];
+          xw[j] = (double)VW[r * WC + xc];
+        }
+        float sv = (float)gsum(gw, xv);
+        float sw = (float)gsum(gw, xw);
+        F[i] = sw > 0.0f ? __fdiv_rn(sv, sw) : 0.0f;
+      }
+      __syncthreads();
+    }
+
+    if (CURV) {
+      for (int i = tid; i < DR * DC; i += NT) {
+        int r = i / DC, c = i - (i / DC) * DC;
+        int gy = y0 - DHY + r, gx = x0 - DHX + c;
+        if (gy < T.wy0 || gy >= T.wy1 || gx < T.wx0 || gx >= T.wx1) continue;
+        const float* f = F + (r + FHY - DHY) * FC + (c + FHX - DHX);
+        DX[i] = deriv(T.g1x, gx, T.wx0, T.wx1, [&](int o) { return f[o]; });
+        DY[i] = deriv(T.g1y, gy, T.wy0, T.wy1, [&](int o) { return f[o * FC]; });
+      }
+      __syncthreads();
+    }
+
+#pragma unroll 1
+    for (int g = 0; g < 2; ++g) {
+      const int ly = trow + 16 * g;
+      const int gy = y0 + ly;
+      if (gy >= T.cy1) continue;
+      const int gx0 = x0 + tcol;
+      const int n = min(4, T.cx1 - gx0);
+      if (n <= 0) continue;
+      float o_hs[4], o_sl[4], o_cm[4], o_cg[4], o_cp[4], o_cr[4], o_dx[4], o_dy[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float qnan = __int_as_float(0x7fc00000);
+        o_hs[k] = o_sl[k] = o_cm[k] = o_cg[k] = o_cp[k] = o_cr[k] = o_dx[k] = o_dy[k] = qnan;
+        if (k >= n || ((nanbits >> (g * 4 + k)) & 1u)) continue;
+        const int gx = gx0 + k;
+        const float* f = F + (ly + FHY) * FC + (tcol + k + FHX);
+        float p, q;
+        if (CURV) {
+          p = DX[(ly + DHY) * DC + tcol + k + DHX];
+          q = DY[(ly + DHY) * DC + tcol + k + DHX];
+        } else {
+          p = deriv(T.g1x, gx, T.wx0, T.wx1, [&](int o) { return f[o]; });
+          q = deriv(T.g1y, gy, T.wy0, T.wy1, [&](int o) { return f[o * FC]; });
+        }
+        o_dx[k] = p;
+        o_dy[k] = q;
+        if (om & (1u << FSG_OUT_HILLSHADE)) {
+          float px = p, qy = q;
+          if (!A.z_is_one) {
+            const float z = A.z;
+            px = deriv(T.g1x, gx, T.wx0, T.wx1, [&](int o) { return fmul(f[o], z); });
+            qy = deriv(T.g1y, gy, T.wy0, T.wy1, [&](int o) { return fmul(f[o * FC], z); });
+          }
+          float e = px * T.sign_x, nn = qy * T.sign_y;
+          float nrm = sqrtf(fadd(fadd(fmul(e, e), fmul(nn, nn)), 1.0f));
+          float hs = (fadd(fadd(-fmul(e, A.lx), -fmul(nn, A.ly)), A.lz)) / nrm;
+          o_hs[k] = fminf(fmaxf(hs, 0.0f), 1.0f);
+        }
+        if (om & (1u << FSG_OUT_SLOPE)) o_sl[k] = slope_value(p, q, A.slope_unit);
+        if (CURV) {
+          const float* dxp = DX + (ly + DHY) * DC + tcol + k + DHX;
+          const float* dyp = DY + (ly + DHY) * DC + tcol + k + DHX;
+          float dxx = deriv(T.c2x, gx, T.wx0, T.wx1, [&](int o) { return dxp[o]; });
+          float dxy = deriv(T.c2y, gy, T.wy0, T.wy1, [&](int o) { return dxp[o * DC]; });
+          float dyy = deriv(T.c2y, gy, T.wy0, T.wy1, [&](int o) { return dyp[o * DC]; });
+          float p2 = p * p, q2 = q * q, pq = p * q;
+          float g2 = p2 + q2, one_g2 = 1.0f + g2;
+          float s15 = one_g2 * sqrtf(one_g2);  // (1 + p^2 + q^2)^1.5
+          if (om & (1u << FSG_OUT_CURV_MEAN)) {
+            float dyx = deriv(T.c2x, gx, T.wx0, T.wx1, [&](int o) { return dyp[o]; });
+            float s = (dxy + dyx) * 0.5f;
+            float num = (1.0f + q2) * dxx - 2.0f * pq * s + (1.0f + p2) * dyy;
+            o_cm[k] = gamma_display(-num / (2.0f * s15 + 1e-10f));
+          }
+          if (om & (1u << FSG_OUT_CURV_GAUSSIAN))
+            o_cg[k] = gamma_display((dxx * dyy - dxy * dxy) / (one_g2 * one_g2));
+          if (om & (1u << FSG_OUT_CURV_PLANFORM)) {
+            float num = q2 * dxx - 2.0f * pq * dxy + p2 * dyy;
+            o_cp[k] = gamma_display(-num / (g2 * sqrtf(g2) + 1e-10f));
+          }
+          if (om & (1u << FSG_OUT_CURV_PROFILE)) {
+            float num = p2 * dxx + 2.0f * pq * dxy + q2 * dyy;
+            o_cr[k] = gamma_display(-num / (g2 * s15 + 1e-10f));
+          }
+        }
+      }
+      const long long prow = (long long)(T.oy0 + gy - T.cy0);
+      const long long pcol = (long long)(T.ox0 + gx0 - T.cx0);
+      const float* outs[FSG_STENCIL_NOUT] = {o_hs, o_sl, o_cm, o_cg, o_cp, o_cr, o_dx, o_dy};
+#pragma unroll
+      for (int o = 0; o < FSG_STENCIL_NOUT; ++o) {
+        if (!(om & (1u << o))) continue;
+        const PlaneK& P = A.planes[o];
+        store_plane(P, prow * P.ld + pcol, outs[o], n);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------- host
+Axis make_axis(double step) {
+  Axis a;
+  a.d2 = (float)(2.0 * step);
+  a.rcp = 1.0f / a.d2;  // host IEEE division: RN(1/d2)
+  a.fa = (float)(-1.5 / step);
+  a.fb = (float)(2.0 / step);
+  a.fc = (float)(-0.5 / step);
+  a.ba = (float)(0.5 / step);
+  a.bb = (float)(-2.0 / step);
+  a.bc = (float)(1.5 / step);
+  return a;
+}
+
+// Step sizes of _nan_utils.py:67-72 (first derivatives) and
+// _impl_curvature.py:263-268 (second derivatives).
+void tile_steps(double pixel_size, double psx, double psy, double* g1x, double* g1y, double* c2x,
+                double* c2y) {
+  double fallback = pixel_size != 0.0 ? pixel_size : 1.0;
+  double cx = psx, cy = psy;
+  if (std::fabs(cy) < 1e-9) cy = fallback;
+  if (std::fabs(cx) < 1e-9) cx = fallback;
+  *c2x = cx;
+  *c2y = cy;
+  double gx = std::fabs(cx), gy = std::fabs(cy);
+  if (gx < 1e-9) gx = fallback;
+  if (gy < 1e-9) gy = fallback;
+  *g1x = gx;
+  *g1y = gy;
+}
+
+const double kGaussW[5] = {0x1.9884a307594fbp-2, 0x1.ef8eb9ad499bap-3, 0x1.ba4b99d1799abp-5,
+                           0x1.22724cb7eb269p-8, 0x1.18a9c4fd536c6p-13};
+
+}  // namespace
+
+int validate_tiles(int32_t raster_h, int32_t raster_w, const fsg_tile* tiles, int32_t ntiles,
+                   int min_window) {
+  for (int t = 0; t < ntiles; ++t) {
+    const fsg_tile& s = tiles[t];
+    if (s.win_h < 0 || s.win_w < 0 || s.core_h < 0 || s.core_w < 0)
+      return fail(FSG_ERR_INVALID, "tile %d: negative size", t);
+    if (s.win_y0 < 0 || s.win_x0 < 0 || (int64_t)s.win_y0 + s.win_h > raster_h ||
+        (int64_t)s.win_x0 + s.win_w > raster_w)
+      return fail(FSG_ERR_INVALID, "tile %d: window outside the %d x %d raster", t, raster_h, raster_w);
+    if (s.core_h == 0 || s.core_w == 0) continue;
+    if (s.core_y0 < s.win_y0 || s.core_x0 < s.win_x0 || s.core_y0 + s.core_h > s.win_y0 + s.win_h ||
+        s.core_x0 + s.core_w > s.win_x0 + s.win_w)
+      return fail(FSG_ERR_INVALID, "tile %d: core outside its window", t);
+    if (s.out_y0 < 0 || s.out_x0 < 0) return fail(FSG_ERR_INVALID, "tile %d: negative output origin", t);
+    if (s.win_h < min_window || s.win_w < min_window)
+      return fail(FSG_ERR_SHAPE,
+                  "tile %d: window %d x %d too small to calculate a numerical gradient, at least "
+                  "(edge_order + 1) = 3 elements are required",
+                  t, s.win_h, s.win_w);
+  }
+  return FSG_OK;
+}
+
+}  // namespace fsg
+
+extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                           const fsg_tile* tiles, int32_t ntiles, const fsg_stencil_params* params,
+                           const fsg_plane* planes, void* stream) {
+  using namespace fsg;
+  if (!params || !planes || (ntiles > 0 && !tiles)) return fail(FSG_ERR_INVALID, "null argument");
+  if (ntiles < 0 || raster_h < 0 || raster_w < 0) return fail(FSG_ERR_INVALID, "negative size");
+  if (ld < raster_w) return fail(FSG_ERR_INVALID, "row pitch %lld < width %d", (long long)ld, raster_w);
+  if (params->slope_unit < 0 || params->slope_unit > 2)
+    return fail(FSG_ERR_INVALID, "slope_unit %d", params->slope_unit);
+  unsigned outmask = 0;
+  for (int o = 0; o < FSG_STENCIL_NOUT; ++o) {
+    if (!planes[o].ptr) continue;
+    if (planes[o].dtype < FSG_F32 || planes[o].dtype > FSG_I16)
+      return fail(FSG_ERR_DTYPE, "plane %d: dtype %d", o, planes[o].dtype);
+    outmask |= 1u << o;
+  }
+  if (!outmask) return fail(FSG_ERR_INVALID, "no output plane requested");
+  int st = validate_tiles(raster_h, raster_w, tiles, ntiles, 3);
+  if (st) return st;
+
+  StencilArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.raster = raster_dev;
+  A.ld = ld;
+  A.rh = raster_h;
+  A.rw = raster_w;
+  double alt = params->altitude * M_PI / 180.0;
+  double az = params->azimuth * M_PI / 180.0;
+  A.lx = (float)(std::sin(az) * std::cos(alt));
+  A.ly = (float)(std::cos(az) * std::cos(alt));
+  A.lz = (float)std::sin(alt);
+  A.z = (float)params->z_factor;
+  A.z_is_one = params->z_factor == 1.0;
+  A.ndf = (float)params->nodata;
+  A.has_nodata = params->has_nodata != 0;
+  A.slope_unit = params->slope_unit;
+  A.outmask = outmask;
+  for (int j = 0; j < 5; ++j) A.gw[j] = kGaussW[j];
+  for (int o = 0; o < FSG_STENCIL_NOUT; ++o) {
+    A.planes[o].ptr = planes[o].ptr;
+    A.planes[o].ld = planes[o].ld;
+    A.planes[o].dtype = planes[o].dtype;
+    A.planes[o].qa = planes[o].q_a;
+    A.planes[o].qb = planes[o].q_b;
+    A.planes[o].qmin = planes[o].q_min;
+    A.planes[o].qmax = planes[o].q_max;
+  }
+  std::vector<TileK> tk;
+  tk.reserve(ntiles);
+  int total = 0;
+  for (int t = 0; t < ntiles; ++t) {
+    const fsg_tile& s = tiles[t];
+    if (s.core_h == 0 || s.core_w == 0) continue;
+    TileK k;
+    k.wy0 = s.win_y0;
+    k.wx0 = s.win_x0;
+    k.wy1 = s.win_y0 + s.win_h;
+    k.wx1 = s.win_x0 + s.win_w;
+    k.cy0 = s.core_y0;
+    k.cx0 = s.core_x0;
+    k.cy1 = s.core_y0 + s.core_h;
+    k.cx1 = s.core_x0 + s.core_w;
+    k.oy0 = s.out_y0;
+    k.ox0 = s.out_x0;
+    k.nbx = (s.core_w + TX - 1) / TX;
+    int nby = (s.core_h + TY - 1) / TY;
+    k.block0 = total;
+    total += k.nbx * nby;
+    double g1x, g1y, c2x, c2y;
+    tile_steps(params->pixel_size, s.pixel_scale_x, s.pixel_scale_y, &g1x, &g1y, &c2x, &c2y);
+    k.g1x = make_axis(g1x);
+    k.g1y = make_axis(g1y);
+    k.c2x = make_axis(c2x);
+    k.c2y = make_axis(c2y);
+    k.sign_x = s.pixel_scale_x >= 0.0 ? 1.0f : -1.0f;
+    k.sign_y = s.pixel_scale_y >= 0.0 ? 1.0f : -1.0f;
+    tk.push_back(k);
+  }
+  if (total == 0) return FSG_OK;
+  A.ntiles = (int)tk.size();
+  A.total_blocks = total;
+  cudaStream_t s = (cudaStream_t)stream;
+  StreamScratch scratch;
+  if (A.ntiles <= INLINE_TILES) {
+    std::copy(tk.begin(), tk.end(), A.inl);
+  } else {
+    st = scratch.alloc(sizeof(TileK) * tk.size(), s);
+    if (st) return st;
+    FSG_CUDA(cudaMemcpyAsync(scratch.ptr, tk.data(), sizeof(TileK) * tk.size(), cudaMemcpyHostToDevice, s));
+    A.tiles_dev = static_cast<const TileK*>(scratch.ptr);
+  }
+  DeviceInfo di;
+  st = device_info(&di);
+  if (st) return st;
+  const bool curv = (outmask & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) |
+                                (1u << FSG_OUT_CURV_PLANFORM) | (1u << FSG_OUT_CURV_PROFILE))) != 0;
+  auto kern = curv ? stencil_kernel<true> : stencil_kernel<false>;
+  FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+  int per_sm = 0;
+  FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, SMEM_BYTES));
+  if (per_sm < 1) per_sm = 1;
+  int grid = std::min(total, di.sms * per_sm);
+  kern<<<grid, NT, SMEM_BYTES, s>>>(A);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}

@@ -1,0 +1,126 @@
+/*
+ * fsg.h -- C ABI of libfsg.so, the GB300 (sm_103a) raster hot path of
+ * FujiShaderGPU: fused 3x3-class stencils (hillshade / slope / curvature),
+ * the multiscale topousm_fast unsharp mask, openness ray-marching, FP64
+ * order statistics and the integer output encoding.
+ *
+ * Conventions
+ *   - Every pointer named `*_dev` or documented as "device" is CUDA device
+ *     memory owned by the caller; the library never frees it.  Host structs
+ *     (tile lists, parameter blocks) are read during the call only.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *     All work is stream-ordered: a call returns once its kernels are queued.
+ *   - Rasters are row-major float32 with NaN as NoData; `ld` is the row pitch
+ *     in elements.  Coordinates are (row, col) = (y, x), 0-based.
+ *   - Return value: FSG_OK (0) or a negative FSG_ERR_* code.  A human-readable
+ *     message for the last error on the calling thread is fsg_last_error().
+ *
+ * Each entry point names the reference interface it replaces, as a path:line
+ * inside the FujiShaderGPU source tree.
+ */
+#ifndef FSG_H_
+#define FSG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FSG_ABI_VERSION 1
+
+/* ---------------------------------------------------------------- status */
+enum fsg_status {
+  FSG_OK = 0,
+  FSG_ERR_INVALID = -1,     /* bad argument: null pointer, bad size, core outside window (ValueError) */
+  FSG_ERR_SHAPE = -2,       /* window < 3 px along an axis: np.gradient(edge_order=2) raises ValueError */
+  FSG_ERR_DTYPE = -3,       /* unsupported output dtype */
+  FSG_ERR_CUDA = -4,        /* a CUDA runtime call failed */
+  FSG_ERR_TIMEOUT = -5,     /* a bounded device-side wait ran out; the kernel returned early */
+  FSG_ERR_ABORTED = -6,     /* a tile in a queue reported an error; see the per-tile status */
+  FSG_ERR_WORKSPACE = -7,   /* caller workspace too small / scratch over its maximum */
+  FSG_ERR_UNSUPPORTED = -8  /* combination not supported (e.g. no CUDA device) */
+};
+
+/* ----------------------------------------------------------- output planes */
+enum fsg_dtype { FSG_F32 = 0, FSG_U8 = 1, FSG_I16 = 2 };
+
+/* Output plane of a kernel.  Pixel (y, x) of a tile core is written at
+ * ptr[(out_y0 + y - core_y0) * ld + (out_x0 + x - core_x0)] (see fsg_tile).
+ * For FSG_U8/FSG_I16 the value is encoded as
+ *   DN = clip(rint(q_a * v + q_b), q_min, q_max), non-finite v -> 0
+ * (io/output_encoding.py:178-190; q_a/q_b from quantize_params :130-175). */
+typedef struct fsg_plane {
+  void* ptr;          /* device pointer; NULL = output not requested */
+  int64_t ld;         /* elements per row */
+  int32_t dtype;      /* enum fsg_dtype */
+  int32_t reserved;
+  float q_a, q_b;
+  int32_t q_min, q_max;
+} fsg_plane;
+
+/* One tile of the reference tile loop (core/tile_processor.py:1610-1627):
+ * the window (core + clipped halo) is what the reference block function sees,
+ * so its edges carry the edge rules (np.gradient edge_order=2, 'nearest' /
+ * 'reflect' filter modes); only the core is written. */
+typedef struct fsg_tile {
+  int32_t win_y0, win_x0, win_h, win_w;      /* raster coords */
+  int32_t core_y0, core_x0, core_h, core_w;  /* raster coords, inside the window */
+  int32_t out_y0, out_x0;                    /* plane coords of the core's first pixel */
+  int32_t reserved0, reserved1;
+  double pixel_scale_x, pixel_scale_y;       /* signed metres per pixel (tile_processor.py:910-932) */
+} fsg_tile;
+
+/* ------------------------------------------------------------- utilities */
+int fsg_abi_version(void);
+const char* fsg_version(void);
+const char* fsg_last_error(void);
+/* Number of kernels launched by this library on the calling process (all devices). */
+int64_t fsg_launch_count(void);
+
+/* NoData mask (core/tile_processor.py:185-196): mask_dev[i] = 1 where
+ * isnan(v) or (has_nodata and (|v - nodata| <= 1e-6 in float32, or v == nodata)). */
+int fsg_nodata_mask(const float* raster_dev, int64_t ld, int32_t h, int32_t w,
+                    double nodata, int32_t has_nodata, uint8_t* mask_dev, int64_t mask_ld,
+                    void* stream);
+
+/* ------------------------------------------------------- fused stencils */
+enum fsg_stencil_out {
+  FSG_OUT_HILLSHADE = 0,     /* algorithms/_impl_hillshade.py:20-54 */
+  FSG_OUT_SLOPE = 1,         /* algorithms/_impl_slope.py:19-35 */
+  FSG_OUT_CURV_MEAN = 2,     /* algorithms/_impl_curvature.py:19-57, curvature_type='mean' */
+  FSG_OUT_CURV_GAUSSIAN = 3,
+  FSG_OUT_CURV_PLANFORM = 4,
+  FSG_OUT_CURV_PROFILE = 5,
+  FSG_OUT_DX = 6,            /* dz/dx of handle_nan_for_gradient (_nan_utils.py:50-74), float32 */
+  FSG_OUT_DY = 7,            /* dz/dy of handle_nan_for_gradient, float32 */
+  FSG_STENCIL_NOUT = 8
+};
+enum fsg_slope_unit { FSG_SLOPE_DEGREE = 0, FSG_SLOPE_PERCENT = 1, FSG_SLOPE_RADIAN = 2 };
+
+typedef struct fsg_stencil_params {
+  double azimuth;       /* degrees (default 315) */
+  double altitude;      /* degrees (default 45) */
+  double z_factor;      /* hillshade vertical exaggeration (default 1) */
+  double pixel_size;    /* fallback step when |pixel_scale| < 1e-9 */
+  double nodata;        /* NoData sentinel, used when has_nodata != 0 */
+  int32_t has_nodata;
+  int32_t slope_unit;   /* enum fsg_slope_unit */
+} fsg_stencil_params;
+
+/* One fused pass over a list of tiles: reads each halo window once and writes
+ * every requested plane of planes[FSG_STENCIL_NOUT] (ptr NULL = skip).
+ * Replaces, per tile, handle_nan_for_gradient (_nan_utils.py:50-74) followed by
+ * compute_hillshade_block / compute_slope_block / compute_curvature_block, the
+ * NoData re-mask (core/tile_compute.py:132-152) and quantize_array
+ * (io/output_encoding.py:178-190), as called from process_single_tile
+ * (core/tile_processor.py:822-1024) via algorithms/tile/dask_bridge.py:72-151. */
+int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                const fsg_tile* tiles, int32_t ntiles, const fsg_stencil_params* params,
+                const fsg_plane* planes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FSG_H_ */

@@ -1,0 +1,80 @@
+"""CPU checks of the C ABI: libfsg.so builds, loads and exports every symbol
+that include/*.h declares; the ctypes signatures cover the same set.  No
+compute calls (no GPU here)."""
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names.update(re.findall(r"\b(fsg_[a-z0-9_]+)\s*\(", src))
+    return names
+
+
+@pytest.fixture(scope="module")
+def built_lib():
+    from fujishadergpu_gb300 import build
+    try:
+        return build.build()
+    except RuntimeError as e:  # nvcc missing
+        pytest.skip(str(e))
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    import ctypes
+    lib = ctypes.CDLL(built_lib)
+    names = declared_symbols()
+    assert names, "no fsg_* declarations found"
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_ctypes_signatures_cover_header(built_lib):
+    from fujishadergpu_gb300 import _native
+    assert set(_native.exported_symbols()) == declared_symbols()
+    L = _native.lib()
+    assert L.fsg_abi_version() == 1
+    assert b"sm_103a" in L.fsg_version()
+
+
+STRUCTS = {"fsg_plane": "Plane", "fsg_tile": "Tile", "fsg_stencil_params": "StencilParams"}
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Compile a C probe against include/fsg.h and compare sizeof/offsetof with ctypes."""
+    import ctypes
+    import shutil
+    import subprocess
+    from fujishadergpu_gb300 import _native as N
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "fsg.h"', "int main(void){"]
+    for cname, pyname in STRUCTS.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in getattr(N, pyname)._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0;}")
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        if line.strip():
+            a, b, v = line.split()
+            got[(a, b)] = int(v)
+    for cname, pyname in STRUCTS.items():
+        cls = getattr(N, pyname)
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
