@@ -41,6 +41,11 @@ struct DeviceInfo {
 // Properties of the current device (cached per device).
 int device_info(DeviceInfo* out);
 
+// Checks a tile list against a raster (windows inside, cores inside windows,
+// windows at least `min_window` px on each axis).
+int validate_tiles(int32_t raster_h, int32_t raster_w, const fsg_tile* tiles, int32_t ntiles,
+                   int min_window);
+
 // Stream-ordered scratch: cudaMallocAsync on `stream`, freed with
 // cudaFreeAsync on the same stream by the destructor.
 struct StreamScratch {

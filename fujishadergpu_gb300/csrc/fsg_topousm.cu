@@ -1,0 +1,722 @@
+// topousm_fast: multiscale box-mean unsharp mask.
+//
+// Per tile window (algorithms/_impl_topousm_fast.py:49-100 with the tile split
+// of algorithms/tile/dask_bridge.py:225-271):
+//   for each (small) radius r with weight w:
+//     f = downsample factor (_nan_utils.py:555-601, algorithm 'topousm_fast')
+//     f > 1 : small = NaN-aware f x f block mean (+ enclosed-void fill),
+//             r_s = max(1, round(r/f)); mean_s = box(2r_s+1, reflect) or
+//             Gaussian(sigma=1, nearest) if r_s <= 1, both NaN-aware;
+//             mean = corner-aligned bilinear zoom of mean_s to the window
+//     f == 1: mean = box(2r+1, reflect) (Gaussian(1, nearest) if r <= 1)
+//     acc (+)= w * (z - mean)                       (float32, radius order)
+//   + large radii: w_large * z - bilinear(coarse field at global coords)
+//   / p99 scale, NaN at NoData, optional int16/uint8 encoding of the core.
+//
+// Box means are separable: a column pass writes float32 vertical means (the
+// reference's float32 intermediate) and a row pass, fused with the
+// accumulation, consumes them.  Running sums are error-free (TwoSum) so long
+// windows do not drift.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fsg_filters.cuh"
+
+namespace fsg {
+namespace {
+
+constexpr int NT = 256;
+constexpr float kQNaN = __builtin_nanf("");
+
+// ----------------------------------------------------------- column passes
+// Box: vm = mean over rows [y-r, y+r] of v (NaN -> 0), wm = mean of valid.
+template <class Src>
+__global__ void __launch_bounds__(NT) box_cols(Src src, int r, int chunk, int nan_aware, AView vm, AView wm) {
+  const int x = blockIdx.x * NT + threadIdx.x;
+  if (x >= src.w) return;
+  const int y0 = blockIdx.y * chunk;
+  const int y1 = min(src.h, y0 + chunk);
+  if (y0 >= y1) return;
+  const int n = 2 * r + 1;
+  const float fn = (float)n;
+  CSum s;
+  int cnt = 0;
+  for (int k = y0 - r; k <= y0 + r; ++k) {
+    float v = src.at(reflect_idx(k, src.h), x);
+    bool ok = v == v;
+    s.add(ok ? v : 0.f);
+    cnt += ok;
+  }
+  for (int y = y0; y < y1; ++y) {
+    vm.ref(y, x) = __fdiv_rn(s.value(), fn);
+    if (nan_aware) wm.ref(y, x) = __fdiv_rn((float)cnt, fn);
+    if (y + 1 < y1) {
+      float a = src.at(reflect_idx(y + r + 1, src.h), x);
+      float b = src.at(reflect_idx(y - r, src.h), x);
+      bool oa = a == a, ob = b == b;
+      s.add(oa ? a : 0.f);
+      s.add(ob ? -b : -0.f);
+      cnt += (int)oa - (int)ob;
+    }
+  }
+}
+
+// Gaussian column pass (mode 'nearest'): weights g[0..R] (g[0] centre).
+template <class Src>
+__global__ void __launch_bounds__(NT) gauss_cols(Src src, const float* __restrict__ g, int R, int nan_aware,
+                                                 AView vm, AView wm) {
+  const int x = blockIdx.x * NT + threadIdx.x;
+  if (x >= src.w) return;
+  for (int y = blockIdx.y; y < src.h; y += gridDim.y) {
+  float v0 = src.at(y, x);
+  bool o0 = v0 == v0;
+  float sv = g[0] * (o0 ? v0 : 0.f);
+  float sw = g[0] * (o0 ? 1.f : 0.f);
+  for (int k = 1; k <= R; ++k) {
+    float a = src.at(clamp_idx(y - k, src.h), x);
+    float b = src.at(clamp_idx(y + k, src.h), x);
+    bool oa = a == a, ob = b == b;
+    sv = fmaf(g[k], __fadd_rn(oa ? a : 0.f, ob ? b : 0.f), sv);
+    sw = fmaf(g[k], (float)((int)oa + (int)ob), sw);
+  }
+  vm.ref(y, x) = sv;
+  if (nan_aware) wm.ref(y, x) = sw;
+  }
+}
+
+// ------------------------------------------------------------- row passes
+// Output modes of the row pass.
+enum RowOut { ROW_MEAN = 0, ROW_ACCUM = 1, ROW_PAIR = 2 };
+
+struct RowArgs {
+  AView vm, wm;        // column-pass outputs (wm only if nan_aware)
+  int r;               // box radius, or Gaussian radius R
+  int nan_aware;
+  int gauss;           // 1: Gaussian weights g[0..R] with 'nearest'; 0: box with 'reflect'
+  const float* g;
+  int mode;            // RowOut
+  AView out;           // ROW_MEAN: mean; ROW_ACCUM: acc; ROW_PAIR: numerator
+  AView out2;          // ROW_PAIR: denominator
+  ZView z;             // ROW_ACCUM: window values
+  float weight;
+  int first;
+  int th, tw;          // tile of outputs per block (th * tw == NT * SEG)
+};
+
+constexpr int SEG = 8;
+
+__global__ void __launch_bounds__(NT) row_pass(const __grid_constant__ RowArgs A) {
+  extern __shared__ float sm[];
+  const int w = A.vm.w, h = A.vm.h;
+  const int r = A.r;
+  const int span = A.tw + 2 * r;
+  float* sv = sm;
+  float* sw = sm + A.th * span;
+  const int ty0 = blockIdx.y * A.th, tx0 = blockIdx.x * A.tw;
+  for (int i = threadIdx.x; i < A.th * span; i += NT) {
+    int rr = i / span, c = i - rr * span;
+    int y = ty0 + rr;
+    if (y >= h) continue;
+    int xs = tx0 - r + c;
+    int x = A.gauss ? clamp_idx(xs, w) : reflect_idx(xs, w);
+    sv[i] = A.vm.at(y, x);
+    if (A.nan_aware) sw[i] = A.wm.at(y, x);
+  }
+  __syncthreads();
+  const int segs_per_row = A.tw / SEG;
+  const int rr = threadIdx.x / segs_per_row;
+  const int x_begin = tx0 + (threadIdx.x - rr * segs_per_row) * SEG;
+  const int y = ty0 + rr;
+  if (rr >= A.th || y >= h || x_begin >= w) return;
+  const float* rv = sv + rr * span;
+  const float* rw = sw + rr * span;
+  const int n = 2 * r + 1;
+  const float fn = (float)n;
+  CSum hv, hw;
+  const int c0 = x_begin - tx0;  // smem column of x_begin - r
+  if (!A.gauss) {
+    for (int k = 0; k < n; ++k) {
+      hv.add(rv[c0 + k]);
+      if (A.nan_aware) hw.add(rw[c0 + k]);
+    }
+  }
+  for (int j = 0; j < SEG; ++j) {
+    const int x = x_begin + j;
+    if (x >= w) break;
+    float num, den;
+    if (A.gauss) {
+      const float* pv = rv + c0 + j + r;
+      const float* pw = rw + c0 + j + r;
+      float a = A.g[0] * pv[0];
+      float b = A.nan_aware ? A.g[0] * pw[0] : 0.f;
+      for (int k = 1; k <= r; ++k) {
+        a = fmaf(A.g[k], __fadd_rn(pv[-k], pv[k]), a);
+        if (A.nan_aware) b = fmaf(A.g[k], __fadd_rn(pw[-k], pw[k]), b);
+      }
+      num = a;
+      den = b;
+    } else {
+      num = __fdiv_rn(hv.value(), fn);
+      den = A.nan_aware ? __fdiv_rn(hw.value(), fn) : 1.f;
+      if (j + 1 < SEG) {
+        hv.add(rv[c0 + j + n]);
+        hv.add(-rv[c0 + j]);
+        if (A.nan_aware) {
+          hw.add(rw[c0 + j + n]);
+          hw.add(-rw[c0 + j]);
+        }
+      }
+    }
+    if (A.mode == ROW_PAIR) {
+      A.out.ref(y, x) = num;
+      A.out2.ref(y, x) = den;
+      continue;
+    }
+    float mean = num;
+    if (A.nan_aware) mean = den > 0.f ? __fdiv_rn(num, den) : 0.f;
+    if (A.mode == ROW_MEAN) {
+      A.out.ref(y, x) = mean;
+    } else {
+      float d = __fmul_rn(A.weight, __fsub_rn(A.z.at(y, x), mean));
+      float& acc = A.out.ref(y, x);
+      acc = A.first ? d : __fadd_rn(acc, d);
+    }
+  }
+}
+
+// ------------------------------------------------------------ decimation
+// NaN-aware f x f block mean (ragged cells padded with NaN); flag |= any NaN.
+__global__ void downsample_kernel(ZView z, int f, AView out, int* flag) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= out.h || j >= out.w) return;
+  float tot = 0.f, cnt = 0.f;
+  const int y0 = i * f, x0 = j * f;
+  for (int a = 0; a < f; ++a) {
+    int y = y0 + a;
+    if (y >= z.h) break;
+    for (int b = 0; b < f; ++b) {
+      int x = x0 + b;
+      if (x >= z.w) break;
+      float v = z.at(y, x);
+      if (isfinite(v)) {
+        tot = __fadd_rn(tot, v);
+        cnt = __fadd_rn(cnt, 1.f);
+      }
+    }
+  }
+  float m = cnt > 0.f ? __fdiv_rn(tot, fmaxf(cnt, 1.f)) : kQNaN;
+  out.ref(i, j) = m;
+  if (m != m) atomicOr(flag, 1);
+}
+
+// _nan_utils.py:655-667: coarse = where(nan & sw > 0.5, sv / max(sw, 1e-6), coarse)
+__global__ void voidfill_combine(AView coarse, AView sv, AView sw, const int* flag) {
+  if (*flag == 0) return;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= coarse.h || j >= coarse.w) return;
+  float c = coarse.at(i, j);
+  float w = sw.at(i, j);
+  if (c != c && w > 0.5f) coarse.ref(i, j) = __fdiv_rn(sv.at(i, j), fmaxf(w, 1e-6f));
+}
+
+// ------------------------------------------------------------- upsample
+// acc (+)= w * (z - zoom(mean_s)), scipy zoom order 1, grid_mode False
+// (corner-aligned: in = out * (n_in - 1) / (n_out - 1)), mode 'nearest'.
+__global__ void accum_upsample(ZView z, AView ms, double zy, double zx, float weight, int first, AView acc) {
+  __shared__ int iy0[32], iy1[32];
+  __shared__ float fy[32];
+  __shared__ int ix0[32], ix1[32];
+  __shared__ float fx[32];
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  const int bx0 = blockIdx.x * 32, by0 = blockIdx.y * 32;
+  const int lin = ty * 32 + tx;
+  if (lin < 32) {
+    int o = by0 + lin;
+    double c = (double)o * zy;
+    int s = (int)floor(c);
+    fy[lin] = (float)(c - (double)s);
+    iy0[lin] = clamp_idx(s, ms.h);
+    iy1[lin] = clamp_idx(s + 1, ms.h);
+  } else if (lin < 64) {
+    int k = lin - 32;
+    int o = bx0 + k;
+    double c = (double)o * zx;
+    int s = (int)floor(c);
+    fx[k] = (float)(c - (double)s);
+    ix0[k] = clamp_idx(s, ms.w);
+    ix1[k] = clamp_idx(s + 1, ms.w);
+  }
+  __syncthreads();
+  const int x = bx0 + tx;
+  if (x >= z.w) return;
+  for (int k = ty; k < 32; k += 8) {
+    const int y = by0 + k;
+    if (y >= z.h) break;
+    float a = ms.at(iy0[k], ix0[tx]), b = ms.at(iy0[k], ix1[tx]);
+    float c = ms.at(iy1[k], ix0[tx]), d = ms.at(iy1[k], ix1[tx]);
+    float top = fmaf(fx[tx], b - a, a);
+    float bot = fmaf(fx[tx], d - c, c);
+    float mean = fmaf(fy[k], bot - top, top);
+    float dd = __fmul_rn(weight, __fsub_rn(z.at(y, x), mean));
+    float& o = acc.ref(y, x);
+    o = first ? dd : __fadd_rn(o, dd);
+  }
+}
+
+// --------------------------------------------------------------- final
+struct FinalArgs {
+  ZView z;             // window
+  AView acc;           // small-radius sum (valid if have_small)
+  int have_small;
+  const float* field;  // coarse field (nullable)
+  long long fld;
+  int fh, fw;
+  float sy, sx;        // f32(ch / full_h), f32(cw / full_w)
+  float w_large;
+  int gy0, gx0;        // global coords of the window origin
+  int cy0, cx0, ch, cw;  // core, window coords
+  float scale;         // 0: raw
+  void* out;
+  long long old;
+  int dtype;
+  float qa, qb;
+  int qmin, qmax;
+};
+
+__device__ __forceinline__ float field_sample(const FinalArgs& A, int gy, int gx) {
+  // _nan_utils.py:276-281: coords in float32, map_coordinates order 1, 'nearest'.
+  float cy = __fsub_rn(__fmul_rn(__fadd_rn((float)gy, 0.5f), A.sy), 0.5f);
+  float cx = __fsub_rn(__fmul_rn(__fadd_rn((float)gx, 0.5f), A.sx), 0.5f);
+  float fy0 = floorf(cy), fx0 = floorf(cx);
+  float ty = cy - fy0, tx = cx - fx0;
+  int y0 = clamp_idx((int)fy0, A.fh), y1 = clamp_idx((int)fy0 + 1, A.fh);
+  int x0 = clamp_idx((int)fx0, A.fw), x1 = clamp_idx((int)fx0 + 1, A.fw);
+  const float* F = A.field;
+  float a = __ldg(F + y0 * A.fld + x0), b = __ldg(F + y0 * A.fld + x1);
+  float c = __ldg(F + y1 * A.fld + x0), d = __ldg(F + y1 * A.fld + x1);
+  float top = fmaf(tx, b - a, a);
+  float bot = fmaf(tx, d - c, c);
+  return fmaf(ty, bot - top, top);
+}
+
+__global__ void final_kernel(const __grid_constant__ FinalArgs A) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= A.cw || y >= A.ch) return;
+  const int wy = A.cy0 + y, wx = A.cx0 + x;
+  float zv = A.z.at(wy, wx);
+  float v;
+  if (zv != zv) {
+    v = kQNaN;
+  } else {
+    float large = 0.f;
+    bool have_large = A.field != nullptr;
+    if (have_large) large = __fsub_rn(__fmul_rn(A.w_large, zv), field_sample(A, A.gy0 + wy, A.gx0 + wx));
+    if (A.have_small) v = have_large ? __fadd_rn(A.acc.at(wy, wx), large) : A.acc.at(wy, wx);
+    else v = large;
+    if (A.scale > 0.f) v = __fdiv_rn(v, A.scale);
+  }
+  long long off = (long long)y * A.old + x;
+  if (A.dtype == FSG_F32) {
+    static_cast<float*>(A.out)[off] = v;
+  } else if (A.dtype == FSG_U8) {
+    static_cast<uint8_t*>(A.out)[off] = (uint8_t)(int)quantize(v, A.qa, A.qb, A.qmin, A.qmax);
+  } else {
+    static_cast<int16_t*>(A.out)[off] = (int16_t)(int)quantize(v, A.qa, A.qb, A.qmin, A.qmax);
+  }
+}
+
+// Coarse field accumulation: field (+)= f32(w) * mean (_impl_topousm_fast.py:153-154).
+__global__ void field_accum(AView mean, float w, int first, AView field) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= mean.w || y >= mean.h) return;
+  float t = __fmul_rn(w, mean.at(y, x));
+  float& f = field.ref(y, x);
+  f = first ? t : __fadd_rn(f, t);
+}
+
+// Overview decimation: NaN-aware mean of the source pixels whose centres fall
+// in each output cell (an exact f x f block mean for integer factors).
+__global__ void overview_kernel(ZView z, AView out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= out.h || j >= out.w) return;
+  long long ya = ((long long)i * z.h) / out.h, yb = ((long long)(i + 1) * z.h) / out.h;
+  long long xa = ((long long)j * z.w) / out.w, xb = ((long long)(j + 1) * z.w) / out.w;
+  double tot = 0.0;
+  long long cnt = 0;
+  for (long long y = ya; y < yb; ++y)
+    for (long long x = xa; x < xb; ++x) {
+      float v = z.at((int)y, (int)x);
+      if (v == v) {
+        tot += v;
+        ++cnt;
+      }
+    }
+  out.ref(i, j) = cnt ? (float)(tot / (double)cnt) : kQNaN;
+}
+
+// ------------------------------------------------------------------- host
+struct Grid2 {
+  dim3 g, b;
+};
+
+Grid2 grid2d(int h, int w) {
+  Grid2 r;
+  r.b = dim3(32, 8);
+  r.g = dim3((w + 31) / 32, (h + 7) / 8);
+  return r;
+}
+
+std::vector<float> gaussian_weights(double sigma, int* radius) {
+  // scipy.ndimage._gaussian_kernel1d(sigma, 0, int(4*sigma + 0.5)), normalised in double.
+  int R = (int)(4.0 * sigma + 0.5);
+  std::vector<double> phi(2 * R + 1);
+  double s = 0;
+  for (int k = -R; k <= R; ++k) {
+    phi[k + R] = std::exp(-0.5 / (sigma * sigma) * (double)k * (double)k);
+    s += phi[k + R];
+  }
+  std::vector<float> g(R + 1);
+  for (int k = 0; k <= R; ++k) g[k] = (float)(phi[k + R] / s);
+  *radius = R;
+  return g;
+}
+
+}  // namespace
+
+// Filter engine with scratch; used by fsg_topousm, the coarse field and smoothing.
+struct FilterCtx {
+  cudaStream_t s;
+  // Gaussian weight tables (device) for sigma = 1 and for the current void fill.
+  float* g1 = nullptr;
+  int r1 = 4;
+};
+
+static int upload(float* dst, const std::vector<float>& v, cudaStream_t s) {
+  FSG_CUDA(cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+  return FSG_OK;
+}
+
+// Row-pass launch geometry: th rows x tw cols per block, shared-memory bounded.
+static void row_geometry(int r, int nan_aware, int w, int* th, int* tw, size_t* smem) {
+  static const int THS[] = {8, 4, 2, 1};
+  for (int t : THS) {
+    int ttw = NT * SEG / t;
+    size_t bytes = (size_t)t * (ttw + 2 * r) * sizeof(float) * (nan_aware ? 2 : 1);
+    if (bytes <= 96 * 1024 || t == 1) {
+      *th = t;
+      *tw = ttw;
+      *smem = bytes;
+      return;
+    }
+  }
+}
+
+template <class Src>
+static int launch_box(const Src& src, int r, int nan_aware, AView vm, AView wm, RowArgs ra, cudaStream_t s) {
+  int chunk = std::max(64, 2 * r);
+  dim3 g((src.w + NT - 1) / NT, (src.h + chunk - 1) / chunk);
+  box_cols<Src><<<g, NT, 0, s>>>(src, r, chunk, nan_aware, vm, wm);
+  FSG_LAUNCHED(1);
+  ra.vm = vm;
+  ra.wm = wm;
+  ra.r = r;
+  ra.nan_aware = nan_aware;
+  ra.gauss = 0;
+  int th, tw;
+  size_t smem;
+  row_geometry(r, nan_aware, src.w, &th, &tw, &smem);
+  ra.th = th;
+  ra.tw = tw;
+  if (smem > 48 * 1024) FSG_CUDA(cudaFuncSetAttribute(row_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 g2((src.w + tw - 1) / tw, (src.h + th - 1) / th);
+  if (g2.y > 65535) return fail(FSG_ERR_UNSUPPORTED, "window of %d rows too tall for radius %d", src.h, r);
+  row_pass<<<g2, NT, smem, s>>>(ra);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+template <class Src>
+static int launch_gauss(const Src& src, const float* g, int R, int nan_aware, AView vm, AView wm, RowArgs ra,
+                        cudaStream_t s) {
+  dim3 gg((src.w + NT - 1) / NT, std::min(src.h, 65535));
+  gauss_cols<Src><<<gg, NT, 0, s>>>(src, g, R, nan_aware, vm, wm);
+  FSG_LAUNCHED(1);
+  ra.vm = vm;
+  ra.wm = wm;
+  ra.r = R;
+  ra.nan_aware = nan_aware;
+  ra.gauss = 1;
+  ra.g = g;
+  int th, tw;
+  size_t smem;
+  row_geometry(R, nan_aware, src.w, &th, &tw, &smem);
+  ra.th = th;
+  ra.tw = tw;
+  if (smem > 48 * 1024) FSG_CUDA(cudaFuncSetAttribute(row_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 g2((src.w + tw - 1) / tw, (src.h + th - 1) / th);
+  row_pass<<<g2, NT, smem, s>>>(ra);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+// _nan_utils.py:555-601 for algorithm 'topousm_fast' (algo factor 1.15).
+int topousm_downsample_factor(double radius, double pixel_size) {
+  double r = std::max(1.0, radius);
+  double px = std::max(1e-3, pixel_size != 0.0 ? pixel_size : 1.0);
+  double score = (r / 24.0) * 1.15 * 1.0 * std::pow(std::max(1.0, 1.0 / px), 0.35);
+  if (score <= 1.0) return 1;
+  double f = std::pow(2.0, std::floor(std::log2(score)));
+  return (int)std::max(1.0, std::min(f, 16.0));
+}
+
+// Scratch for one window of at most h x w pixels.
+struct TopoScratch {
+  AView acc, vm, wm;       // h x w
+  AView small, svm, swm, smean, ssv, ssw;  // (h/2+1) x (w/2+1)
+  int* flag;
+  float* g1;               // sigma = 1 weights (5 floats)
+  float* gv;               // void-fill weights (<= 4097 floats)
+  static size_t bytes(int h, int w) {
+    size_t full = (size_t)h * w, sm = (size_t)((h + 1) / 2) * ((w + 1) / 2);
+    return (3 * full + 6 * sm) * sizeof(float) + 256 + 8 * 1024 + 16 * 1024 + 6 * 256;
+  }
+  void carve(void* base, int h, int w) {
+    char* p = static_cast<char*>(base);
+    auto take = [&](size_t n) {
+      char* q = p;
+      p += (n + 255) & ~(size_t)255;
+      return q;
+    };
+    size_t full = (size_t)h * w;
+    int hs = (h + 1) / 2, ws = (w + 1) / 2;
+    size_t sm = (size_t)hs * ws;
+    acc = {reinterpret_cast<float*>(take(full * 4)), w, h, w};
+    vm = {reinterpret_cast<float*>(take(full * 4)), w, h, w};
+    wm = {reinterpret_cast<float*>(take(full * 4)), w, h, w};
+    AView* smalls[] = {&small, &svm, &swm, &smean, &ssv, &ssw};
+    for (AView* a : smalls) *a = {reinterpret_cast<float*>(take(sm * 4)), ws, hs, ws};
+    flag = reinterpret_cast<int*>(take(256));
+    g1 = reinterpret_cast<float*>(take(8 * 1024));
+    gv = reinterpret_cast<float*>(take(16 * 1024));
+  }
+};
+
+static AView resize(AView a, int h, int w) {
+  a.h = h;
+  a.w = w;
+  a.ld = w;
+  return a;
+}
+
+// Mean of `src` (an h x w view) for one radius at its own resolution, written
+// into `out` (ROW_MEAN) -- used for decimated grids and the coarse field.
+template <class Src>
+static int mean_for_radius(const Src& src, int rr, TopoScratch& S, AView out, cudaStream_t s) {
+  RowArgs ra;
+  std::memset(&ra, 0, sizeof(ra));
+  ra.mode = ROW_MEAN;
+  ra.out = out;
+  AView vm = resize(S.svm, src.h, src.w), wm = resize(S.swm, src.h, src.w);
+  if (rr <= 1) return launch_gauss(src, S.g1, 4, 1, vm, wm, ra, s);
+  return launch_box(src, rr, 1, vm, wm, ra, s);
+}
+
+// One window of topousm_fast: accumulates sum_r w_r (z - mean_r) into S.acc.
+static int topousm_window(const ZView& z, const std::vector<int>& radii, const std::vector<float>& weights,
+                          double pixel_size, TopoScratch& S, cudaStream_t s) {
+  for (size_t i = 0; i < radii.size(); ++i) {
+    const int r = radii[i];
+    const float w = weights[i];
+    const int first = i == 0;
+    const int f = topousm_downsample_factor((double)r, pixel_size);
+    if (f > 1) {
+      const int hs = std::max(1, (z.h + f - 1) / f), ws = std::max(1, (z.w + f - 1) / f);
+      AView small = resize(S.small, hs, ws);
+      FSG_CUDA(cudaMemsetAsync(S.flag, 0, sizeof(int), s));
+      Grid2 gd = grid2d(hs, ws);
+      downsample_kernel<<<gd.g, gd.b, 0, s>>>(z, f, small, S.flag);
+      FSG_LAUNCHED(1);
+      // enclosed-void fill (runs only if the decimated grid holds NaN)
+      double sigma = std::max(1.0, (double)std::min(hs, ws) / 64.0);
+      int R;
+      std::vector<float> gw = gaussian_weights(sigma, &R);
+      if (R + 1 > 4096) return fail(FSG_ERR_UNSUPPORTED, "void-fill Gaussian radius %d too large", R);
+      int st = upload(S.gv, gw, s);
+      if (st) return st;
+      {
+        RowArgs ra;
+        std::memset(&ra, 0, sizeof(ra));
+        ra.mode = ROW_PAIR;
+        ra.out = resize(S.ssv, hs, ws);
+        ra.out2 = resize(S.ssw, hs, ws);
+        st = launch_gauss(small, S.gv, R, 1, resize(S.svm, hs, ws), resize(S.swm, hs, ws), ra, s);
+        if (st) return st;
+        voidfill_combine<<<gd.g, gd.b, 0, s>>>(small, resize(S.ssv, hs, ws), resize(S.ssw, hs, ws), S.flag);
+        FSG_LAUNCHED(1);
+      }
+      const int rs = std::max(1, (int)std::nearbyint((double)r / f));
+      AView ms = resize(S.smean, hs, ws);
+      st = mean_for_radius(small, rs, S, ms, s);
+      if (st) return st;
+      double zy = z.h > 1 ? (double)(hs - 1) / (double)(z.h - 1) : 1.0;
+      double zx = z.w > 1 ? (double)(ws - 1) / (double)(z.w - 1) : 1.0;
+      dim3 g((z.w + 31) / 32, (z.h + 31) / 32);
+      accum_upsample<<<g, dim3(32, 8), 0, s>>>(z, ms, zy, zx, w, first, S.acc);
+      FSG_LAUNCHED(1);
+    } else {
+      RowArgs ra;
+      std::memset(&ra, 0, sizeof(ra));
+      ra.mode = ROW_ACCUM;
+      ra.out = S.acc;
+      ra.z = z;
+      ra.weight = w;
+      ra.first = first;
+      int st = r <= 1 ? launch_gauss(z, S.g1, 4, 1, S.vm, S.wm, ra, s) : launch_box(z, r, 1, S.vm, S.wm, ra, s);
+      if (st) return st;
+    }
+  }
+  return FSG_OK;
+}
+
+int prepare_g1(TopoScratch& S, cudaStream_t s) {
+  int R;
+  std::vector<float> g = gaussian_weights(1.0, &R);
+  return upload(S.g1, g, s);
+}
+
+}  // namespace fsg
+
+using namespace fsg;
+
+extern "C" int fsg_topousm(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                           const fsg_tile* tiles, int32_t ntiles, const fsg_topousm_params* p,
+                           const fsg_plane* out, void* stream) {
+  if (!p || !out || (ntiles > 0 && !tiles)) return fail(FSG_ERR_INVALID, "null argument");
+  if (ntiles < 0 || raster_h < 0 || raster_w < 0 || ld < raster_w) return fail(FSG_ERR_INVALID, "bad raster shape");
+  if (!out->ptr) return fail(FSG_ERR_INVALID, "output plane is NULL");
+  if (out->dtype < FSG_F32 || out->dtype > FSG_I16) return fail(FSG_ERR_DTYPE, "dtype %d", out->dtype);
+  if (p->nradii < 0 || (p->nradii > 0 && (!p->radii || !p->weights)))
+    return fail(FSG_ERR_INVALID, "radii/weights");
+  if (p->nradii == 0 && !p->coarse_dev) return fail(FSG_ERR_INVALID, "no radius and no coarse field");
+  for (int i = 0; i < p->nradii; ++i)
+    if (p->radii[i] < 1) return fail(FSG_ERR_INVALID, "radius %d < 1", p->radii[i]);
+  if (p->coarse_dev && (p->coarse_h < 1 || p->coarse_w < 1 || p->coarse_ld < p->coarse_w || p->full_h < 1 ||
+                        p->full_w < 1))
+    return fail(FSG_ERR_INVALID, "coarse field shape");
+  int st = validate_tiles(raster_h, raster_w, tiles, ntiles, 1);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  int maxh = 1, maxw = 1;
+  for (int t = 0; t < ntiles; ++t) {
+    maxh = std::max(maxh, tiles[t].win_h);
+    maxw = std::max(maxw, tiles[t].win_w);
+  }
+  StreamScratch scratch;
+  st = scratch.alloc(TopoScratch::bytes(maxh, maxw), s);
+  if (st) return st;
+  TopoScratch S;
+  S.carve(scratch.ptr, maxh, maxw);
+  st = prepare_g1(S, s);
+  if (st) return st;
+  std::vector<int> radii(p->radii, p->radii + p->nradii);
+  std::vector<float> weights(p->nradii);
+  for (int i = 0; i < p->nradii; ++i) weights[i] = (float)p->weights[i];
+  for (int t = 0; t < ntiles; ++t) {
+    const fsg_tile& T = tiles[t];
+    if (T.core_h == 0 || T.core_w == 0) continue;
+    ZView z{raster_dev + (long long)T.win_y0 * ld + T.win_x0, ld, T.win_h, T.win_w, (float)p->nodata,
+            p->has_nodata != 0};
+    TopoScratch W = S;
+    W.acc = resize(S.acc, T.win_h, T.win_w);
+    W.vm = resize(S.vm, T.win_h, T.win_w);
+    W.wm = resize(S.wm, T.win_h, T.win_w);
+    if (p->nradii > 0) {
+      st = topousm_window(z, radii, weights, p->pixel_size, W, s);
+      if (st) return st;
+    }
+    FinalArgs A;
+    std::memset(&A, 0, sizeof(A));
+    A.z = z;
+    A.acc = W.acc;
+    A.have_small = p->nradii > 0;
+    A.field = p->coarse_dev;
+    A.fld = p->coarse_ld;
+    A.fh = p->coarse_h;
+    A.fw = p->coarse_w;
+    A.sy = (float)((double)p->coarse_h / (double)p->full_h);
+    A.sx = (float)((double)p->coarse_w / (double)p->full_w);
+    A.w_large = (float)p->w_large;
+    A.gy0 = T.win_y0;
+    A.gx0 = T.win_x0;
+    A.cy0 = T.core_y0 - T.win_y0;
+    A.cx0 = T.core_x0 - T.win_x0;
+    A.ch = T.core_h;
+    A.cw = T.core_w;
+    A.scale = (float)p->scale;
+    size_t esz = out->dtype == FSG_F32 ? 4 : (out->dtype == FSG_I16 ? 2 : 1);
+    A.out = static_cast<char*>(out->ptr) + ((long long)T.out_y0 * out->ld + T.out_x0) * esz;
+    A.old = out->ld;
+    A.dtype = out->dtype;
+    A.qa = out->q_a;
+    A.qb = out->q_b;
+    A.qmin = out->q_min;
+    A.qmax = out->q_max;
+    Grid2 gd = grid2d(T.core_h, T.core_w);
+    final_kernel<<<gd.g, gd.b, 0, s>>>(A);
+    FSG_LAUNCHED(1);
+  }
+  return FSG_OK;
+}
+
+extern "C" int fsg_topousm_coarse_field(const float* coarse_dev, int64_t ld, int32_t h, int32_t w,
+                                        const int32_t* radii, const double* weights, int32_t n,
+                                        double decimation, float* field_dev, int64_t field_ld, void* stream) {
+  if (!coarse_dev || !field_dev || n < 1 || !radii || !weights) return fail(FSG_ERR_INVALID, "null argument");
+  if (h < 1 || w < 1 || ld < w || field_ld < w) return fail(FSG_ERR_INVALID, "bad shape");
+  cudaStream_t s = (cudaStream_t)stream;
+  StreamScratch scratch;
+  int st = scratch.alloc(TopoScratch::bytes(2 * h, 2 * w), s);
+  if (st) return st;
+  TopoScratch S;
+  S.carve(scratch.ptr, 2 * h, 2 * w);
+  st = prepare_g1(S, s);
+  if (st) return st;
+  ZView z{coarse_dev, ld, h, w, 0.f, 0};
+  AView field{field_dev, field_ld, h, w};
+  AView mean = resize(S.acc, h, w);
+  for (int i = 0; i < n; ++i) {
+    // _impl_topousm_fast.py:147-154
+    int rc = std::max(1, (int)std::nearbyint((double)radii[i] / std::max(decimation, 1.0)));
+    st = mean_for_radius(z, rc, S, mean, s);
+    if (st) return st;
+    Grid2 gd = grid2d(h, w);
+    field_accum<<<gd.g, gd.b, 0, s>>>(mean, (float)weights[i], i == 0, field);
+    FSG_LAUNCHED(1);
+  }
+  return FSG_OK;
+}
+
+extern "C" int fsg_overview(const float* raster_dev, int64_t ld, int32_t h, int32_t w, double nodata,
+                            int32_t has_nodata, float* out_dev, int32_t out_h, int32_t out_w, int64_t out_ld,
+                            void* stream) {
+  if (!raster_dev || !out_dev) return fail(FSG_ERR_INVALID, "null argument");
+  if (h < 1 || w < 1 || out_h < 1 || out_w < 1 || out_h > h || out_w > w || ld < w || out_ld < out_w)
+    return fail(FSG_ERR_INVALID, "bad shape");
+  ZView z{raster_dev, ld, h, w, (float)nodata, has_nodata != 0};
+  AView o{out_dev, out_ld, out_h, out_w};
+  Grid2 gd = grid2d(out_h, out_w);
+  overview_kernel<<<gd.g, gd.b, 0, (cudaStream_t)stream>>>(z, o);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+extern "C" int fsg_topousm_downsample_factor(double radius, double pixel_size) {
+  return topousm_downsample_factor(radius, pixel_size);
+}

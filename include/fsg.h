@@ -120,6 +120,81 @@ int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t r
                 const fsg_tile* tiles, int32_t ntiles, const fsg_stencil_params* params,
                 const fsg_plane* planes, void* stream);
 
+/* ------------------------------------------------------------ topousm_fast */
+typedef struct fsg_topousm_params {
+  /* Small radii computed per window (algorithms/_impl_topousm_fast.py:49-100) with
+   * their absolute weights (not renormalised after the large-radius split,
+   * _impl_topousm_fast.py:113-130).  nradii may be 0 when only the coarse field
+   * contributes. */
+  const int32_t* radii;
+  const double* weights;
+  int32_t nradii;
+  int32_t has_nodata;
+  double pixel_size;        /* drives the per-radius decimation factor (_nan_utils.py:555-601) */
+  double nodata;
+  /* Large radii from one global overview field (dask_bridge.py:237-249):
+   * result += w_large * z - bilinear(field at global pixel centres).  coarse_dev
+   * NULL = no large part.  full_h/full_w: the raster the field spans; each
+   * tile's global origin is its window origin. */
+  const float* coarse_dev;
+  int64_t coarse_ld;
+  int32_t coarse_h, coarse_w;
+  int64_t full_h, full_w;
+  double w_large;
+  /* p99(|raw|) divisor (_normalization.py:35-41); 0 = write the raw sum. */
+  double scale;
+} fsg_topousm_params;
+
+/* topousm_fast over a list of tiles; writes each core into `out` (float32 or
+ * int16/uint8 codes).  Replaces, per tile, dask_bridge._direct_topousm_fast
+ * (algorithms/tile/dask_bridge.py:225-271) = compute_topousm_fast_efficient_block
+ * + the large-radius part + apply_global_normalization, and quantize_array. */
+int fsg_topousm(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                const fsg_tile* tiles, int32_t ntiles, const fsg_topousm_params* params,
+                const fsg_plane* out, void* stream);
+
+/* Large-radius field on the overview grid: sum_i f32(w_i) * mean_{r_i}(coarse), r_i =
+ * max(1, round(radius_i / decimation)) -- compute_topousm_fast_large_coarse_field
+ * (algorithms/_impl_topousm_fast.py:133-155). */
+int fsg_topousm_coarse_field(const float* coarse_dev, int64_t ld, int32_t h, int32_t w,
+                             const int32_t* radii, const double* weights, int32_t n,
+                             double decimation, float* field_dev, int64_t field_ld, void* stream);
+
+/* Overview DEM for the coarse field: NaN-aware mean of the source pixels whose
+ * centres fall in each output cell (an exact block mean for integer factors).
+ * Stands in for the GDAL average-resampled overview read of
+ * core/tile_processor.py:575-585. */
+int fsg_overview(const float* raster_dev, int64_t ld, int32_t h, int32_t w, double nodata,
+                 int32_t has_nodata, float* out_dev, int32_t out_h, int32_t out_w, int64_t out_ld,
+                 void* stream);
+
+/* _radius_to_downsample_factor(radius, pixel_size, 'topousm_fast') (_nan_utils.py:555-601). */
+int fsg_topousm_downsample_factor(double radius, double pixel_size);
+
+/* --------------------------------------------------------------- statistics */
+/* numpy.percentile(v[~isnan(v)], q, method='linear') of float32 device data
+ * (|v| when abs_values != 0): exact order statistics by radix select, FP64
+ * interpolation.  Writes nq doubles to host `out` (NaN if no valid value) and
+ * the valid count to *nvalid (may be NULL).  Synchronises `stream`.
+ * Replaces cp.percentile in topousm_fast_stat_func (_normalization.py:21-32) and
+ * robust_unsigned_stretch_stat_func (_global_stats.py:181-203). */
+int fsg_percentile(const float* values_dev, int64_t n, int32_t abs_values, const double* q, int32_t nq,
+                   double* out, int64_t* nvalid, void* stream);
+
+/* Population standard deviation of the valid (non-NaN) values, FP64
+ * (the fallback scale of _normalization.py:30).  Synchronises `stream`. */
+int fsg_std(const float* values_dev, int64_t n, double* out, void* stream);
+
+/* ----------------------------------------------------------------- encoding */
+/* out = (v - offset) / scale in float32 (scale <= 0: unchanged), max(., 0) when
+ * clamp_min0, NaN kept; stored as float32 or int16/uint8 codes.  Replaces
+ * apply_global_normalization (_global_stats.py:123-153) with
+ * topousm_fast_norm_func (_normalization.py:35-41), the openness display
+ * stretch (algorithms/tile/dask_bridge.py:173-187) and quantize_array
+ * (io/output_encoding.py:178-190). */
+int fsg_affine(const float* in_dev, int64_t ld, int32_t h, int32_t w, double offset, double scale,
+               int32_t clamp_min0, const fsg_plane* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
