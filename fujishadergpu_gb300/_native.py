@@ -73,6 +73,14 @@ class StencilParams(C.Structure):
                 ("slope_unit", C.c_int32)]
 
 
+class TopoUSMParams(C.Structure):
+    _fields_ = [("radii", C.POINTER(C.c_int32)), ("weights", C.POINTER(C.c_double)), ("nradii", C.c_int32),
+                ("has_nodata", C.c_int32), ("pixel_size", C.c_double), ("nodata", C.c_double),
+                ("coarse_dev", C.c_void_p), ("coarse_ld", C.c_int64), ("coarse_h", C.c_int32),
+                ("coarse_w", C.c_int32), ("full_h", C.c_int64), ("full_w", C.c_int64), ("w_large", C.c_double),
+                ("scale", C.c_double)]
+
+
 # Exported symbols and their signatures (kept in sync with include/fsg.h).
 _SIGNATURES = {
     "fsg_abi_version": (C.c_int, []),
@@ -83,6 +91,19 @@ _SIGNATURES = {
                                   C.c_void_p, C.c_int64, C.c_void_p]),
     "fsg_stencil": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
                               C.POINTER(StencilParams), C.POINTER(Plane), C.c_void_p]),
+    "fsg_topousm": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
+                              C.POINTER(TopoUSMParams), C.POINTER(Plane), C.c_void_p]),
+    "fsg_topousm_coarse_field": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
+                                           C.POINTER(C.c_double), C.c_int32, C.c_double, C.c_void_p, C.c_int64,
+                                           C.c_void_p]),
+    "fsg_overview": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.c_void_p,
+                               C.c_int32, C.c_int32, C.c_int64, C.c_void_p]),
+    "fsg_topousm_downsample_factor": (C.c_int, [C.c_double, C.c_double]),
+    "fsg_percentile": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_double), C.c_int32,
+                                 C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_void_p]),
+    "fsg_std": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.c_void_p]),
+    "fsg_affine": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32,
+                             C.POINTER(Plane), C.c_void_p]),
 }
 
 

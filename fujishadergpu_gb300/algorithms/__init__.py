@@ -9,10 +9,17 @@ from ._base import Constants, TileAlgorithm
 from ._impl_curvature import CurvatureAlgorithm, compute_curvature_block
 from ._impl_hillshade import HillshadeAlgorithm, compute_hillshade_block
 from ._impl_slope import SlopeAlgorithm, compute_slope_block
+from ._impl_topousm_fast import (TopoUSMFastAlgorithm, compute_topousm_fast_efficient_block,
+                                 compute_topousm_fast_large_coarse_field, split_radii_by_threshold,
+                                 topousm_fast_default_large_radius_threshold)
+from ._stats import robust_unsigned_stretch_stat_func, topousm_fast_stat_func
 
 __all__ = [
     "Constants", "TileAlgorithm",
     "compute_hillshade_block", "HillshadeAlgorithm",
     "compute_slope_block", "SlopeAlgorithm",
     "compute_curvature_block", "CurvatureAlgorithm",
+    "compute_topousm_fast_efficient_block", "compute_topousm_fast_large_coarse_field",
+    "split_radii_by_threshold", "topousm_fast_default_large_radius_threshold", "TopoUSMFastAlgorithm",
+    "topousm_fast_stat_func", "robust_unsigned_stretch_stat_func",
 ]

@@ -15,12 +15,7 @@ from ._base import TileAlgorithm
 from ._stats import topousm_fast_stat_func
 
 
-class TopoUSMParams(C.Structure):
-    _fields_ = [("radii", C.POINTER(C.c_int32)), ("weights", C.POINTER(C.c_double)), ("nradii", C.c_int32),
-                ("has_nodata", C.c_int32), ("pixel_size", C.c_double), ("nodata", C.c_double),
-                ("coarse_dev", C.c_void_p), ("coarse_ld", C.c_int64), ("coarse_h", C.c_int32),
-                ("coarse_w", C.c_int32), ("full_h", C.c_int64), ("full_w", C.c_int64), ("w_large", C.c_double),
-                ("scale", C.c_double)]
+TopoUSMParams = N.TopoUSMParams
 
 
 def downsample_factor(radius: float, pixel_size: float) -> int:
@@ -84,10 +79,6 @@ def _raw_topousm(block, radii, weights, pixel_size, *, coarse=None, w_large=0.0,
     out = _arrays.empty(v.h, v.w, out_dtype, device=v.tensor.device)
     if v.h * v.w == 0:
         return out, v
-    if coarse is not None:
-        # The large part samples the field at global coords: shift the window by
-        # its origin through a raster view whose (0, 0) is the tile origin.
-        pass
     params, keep = make_params(radii, weights, pixel_size, coarse=coarse, w_large=w_large,
                                full_shape=full_shape, scale=scale)
     t = _window_tile(v.h, v.w)

@@ -201,6 +201,155 @@ __device__ __forceinline__ double gsum(const double* w, const double* x) {
   return acc;
 }
 
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void store1(const PlaneK& P, long long off, float v) {
+  if (P.dtype == FSG_F32) static_cast<float*>(P.ptr)[off] = v;
+  else if (P.dtype == FSG_U8) static_cast<uint8_t*>(P.ptr)[off] = (uint8_t)(int)quantize(v, P.qa, P.qb, P.qmin, P.qmax);
+  else static_cast<int16_t*>(P.ptr)[off] = (int16_t)(int)quantize(v, P.qa, P.qb, P.qmin, P.qmax);
+}
+
+// Output products of one pixel from its derivatives.  Hillshade, slope and
+// the curvature formulas use hardware approximations of sqrt/rcp (relative
+// error ~1e-7, far inside the 1e-5 x range parity bound); tanh is CUDA's tanhf,
+// the function the reference's cp.tanh evaluates.
+__device__ __forceinline__ void pixel_products(const StencilArgs& A, const TileK& T, unsigned om, float p, float q,
+                                               float pz, float qz, float dxx, float dxy, float dyy, float dyx,
+                                               float* o) {
+  if (om & (1u << FSG_OUT_HILLSHADE)) {
+    float e = pz * T.sign_x, nn = qz * T.sign_y;
+    float hs = fadd(fadd(-fmul(e, A.lx), -fmul(nn, A.ly)), A.lz) * rsqrtf(fadd(fadd(fmul(e, e), fmul(nn, nn)), 1.0f));
+    o[FSG_OUT_HILLSHADE] = fminf(fmaxf(hs, 0.0f), 1.0f);
+  }
+  if (om & (1u << FSG_OUT_SLOPE)) {
+    float g2 = fadd(fmul(p, p), fmul(q, q));
+    if (A.slope_unit == FSG_SLOPE_DEGREE) o[FSG_OUT_SLOPE] = atanf(sqrt_approx(g2)) * 57.295780181884765625f;
+    else o[FSG_OUT_SLOPE] = slope_value(p, q, A.slope_unit);
+  }
+  if (om & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) | (1u << FSG_OUT_CURV_PLANFORM) |
+            (1u << FSG_OUT_CURV_PROFILE))) {
+    float p2 = p * p, q2 = q * q, pq = p * q;
+    float g2 = p2 + q2, one_g2 = 1.0f + g2;
+    float s15 = one_g2 * sqrt_approx(one_g2);  // (1 + p^2 + q^2)^1.5
+    if (om & (1u << FSG_OUT_CURV_MEAN)) {
+      float s = (dxy + dyx) * 0.5f;
+      float num = (1.0f + q2) * dxx - 2.0f * pq * s + (1.0f + p2) * dyy;
+      o[FSG_OUT_CURV_MEAN] = gamma_display(-num * rcp_approx(2.0f * s15 + 1e-10f));
+    }
+    if (om & (1u << FSG_OUT_CURV_GAUSSIAN))
+      o[FSG_OUT_CURV_GAUSSIAN] = gamma_display((dxx * dyy - dxy * dxy) * rcp_approx(one_g2 * one_g2));
+    if (om & (1u << FSG_OUT_CURV_PLANFORM)) {
+      float num = q2 * dxx - 2.0f * pq * dxy + p2 * dyy;
+      o[FSG_OUT_CURV_PLANFORM] = gamma_display(-num * rcp_approx(g2 * sqrt_approx(g2) + 1e-10f));
+    }
+    if (om & (1u << FSG_OUT_CURV_PROFILE)) {
+      float num = p2 * dxx + 2.0f * pq * dxy + q2 * dyy;
+      o[FSG_OUT_CURV_PROFILE] = gamma_display(-num * rcp_approx(g2 * s15 + 1e-10f));
+    }
+  }
+  o[FSG_OUT_DX] = p;
+  o[FSG_OUT_DY] = q;
+}
+
+// dx/dy over the (TY+4) x (TX+4) region; INTERIOR: the whole staged region lies
+// inside the window, so every derivative is a central difference.
+template <bool INTERIOR>
+__device__ __forceinline__ void stage_first_derivs(const TileK& T, const float* F, float* DX, float* DY, int y0,
+                                                   int x0) {
+  for (int i = threadIdx.x; i < DR * DC; i += NT) {
+    int r = i / DC, c = i - (i / DC) * DC;
+    const float* f = F + (r + FHY - DHY) * FC + (c + FHX - DHX);
+    if (INTERIOR) {
+      DX[i] = div_by(fsub(f[1], f[-1]), T.g1x.d2, T.g1x.rcp);
+      DY[i] = div_by(fsub(f[FC], f[-FC]), T.g1y.d2, T.g1y.rcp);
+    } else {
+      int gy = y0 - DHY + r, gx = x0 - DHX + c;
+      if (gy < T.wy0 || gy >= T.wy1 || gx < T.wx0 || gx >= T.wx1) continue;
+      DX[i] = deriv(T.g1x, gx, T.wx0, T.wx1, [&](int o) { return f[o]; });
+      DY[i] = deriv(T.g1y, gy, T.wy0, T.wy1, [&](int o) { return f[o * FC]; });
+    }
+  }
+}
+
+// Per-pixel stage: thread = one column of the block, 8 consecutive rows, so a
+// warp touches 32 consecutive shared-memory words and stores 32 consecutive
+// output pixels of a row.
+template <bool CURV, bool INTERIOR>
+__device__ __forceinline__ void stage_pixels(const StencilArgs& A, const TileK& T, unsigned om, const float* F,
+                                             const float* DX, const float* DY, int y0, int x0, unsigned nanbits) {
+  const int j = threadIdx.x & (TX - 1);
+  const int i0 = (threadIdx.x / TX) * (TY * TX / NT);
+  const int gx = x0 + j;
+  if (gx >= T.cx1) return;
+  const long long pcol = (long long)(T.ox0 + gx - T.cx0);
+#pragma unroll 1
+  for (int ii = 0; ii < TY * TX / NT; ++ii) {
+    const int i = i0 + ii;
+    const int gy = y0 + i;
+    if (gy >= T.cy1) break;
+    float o[FSG_STENCIL_NOUT];
+    if ((nanbits >> ii) & 1u) {
+#pragma unroll
+      for (int k = 0; k < FSG_STENCIL_NOUT; ++k) o[k] = __int_as_float(0x7fc00000);
+    } else {
+      const float* f = F + (i + FHY) * FC + (j + FHX);
+      float p, q, dxx = 0.f, dxy = 0.f, dyy = 0.f, dyx = 0.f;
+      const float* dxp = DX + (i + DHY) * DC + j + DHX;
+      const float* dyp = DY + (i + DHY) * DC + j + DHX;
+      if (CURV) {
+        p = dxp[0];
+        q = dyp[0];
+        if (INTERIOR) {
+          dxx = div_by(fsub(dxp[1], dxp[-1]), T.c2x.d2, T.c2x.rcp);
+          dxy = div_by(fsub(dxp[DC], dxp[-DC]), T.c2y.d2, T.c2y.rcp);
+          dyy = div_by(fsub(dyp[DC], dyp[-DC]), T.c2y.d2, T.c2y.rcp);
+          if (om & (1u << FSG_OUT_CURV_MEAN)) dyx = div_by(fsub(dyp[1], dyp[-1]), T.c2x.d2, T.c2x.rcp);
+        } else {
+          dxx = deriv(T.c2x, gx, T.wx0, T.wx1, [&](int o2) { return dxp[o2]; });
+          dxy = deriv(T.c2y, gy, T.wy0, T.wy1, [&](int o2) { return dxp[o2 * DC]; });
+          dyy = deriv(T.c2y, gy, T.wy0, T.wy1, [&](int o2) { return dyp[o2 * DC]; });
+          if (om & (1u << FSG_OUT_CURV_MEAN))
+            dyx = deriv(T.c2x, gx, T.wx0, T.wx1, [&](int o2) { return dyp[o2]; });
+        }
+      } else if (INTERIOR) {
+        p = div_by(fsub(f[1], f[-1]), T.g1x.d2, T.g1x.rcp);
+        q = div_by(fsub(f[FC], f[-FC]), T.g1y.d2, T.g1y.rcp);
+      } else {
+        p = deriv(T.g1x, gx, T.wx0, T.wx1, [&](int o2) { return f[o2]; });
+        q = deriv(T.g1y, gy, T.wy0, T.wy1, [&](int o2) { return f[o2 * FC]; });
+      }
+      float pz = p, qz = q;
+      if ((om & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) {
+        const float z = A.z;
+        if (INTERIOR) {
+          pz = div_by(fsub(fmul(f[1], z), fmul(f[-1], z)), T.g1x.d2, T.g1x.rcp);
+          qz = div_by(fsub(fmul(f[FC], z), fmul(f[-FC], z)), T.g1y.d2, T.g1y.rcp);
+        } else {
+          pz = deriv(T.g1x, gx, T.wx0, T.wx1, [&](int o2) { return fmul(f[o2], z); });
+          qz = deriv(T.g1y, gy, T.wy0, T.wy1, [&](int o2) { return fmul(f[o2 * FC], z); });
+        }
+      }
+      pixel_products(A, T, om, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
+    }
+    const long long prow = (long long)(T.oy0 + gy - T.cy0);
+#pragma unroll
+    for (int k = 0; k < FSG_STENCIL_NOUT; ++k) {
+      if (!(om & (1u << k))) continue;
+      const PlaneK& P = A.planes[k];
+      store1(P, prow * P.ld + pcol, o[k]);
+    }
+  }
+}
+
 template <bool CURV>
 __global__ void __launch_bounds__(NT) stencil_kernel(const __grid_constant__ StencilArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -215,8 +364,6 @@ __global__ void __launch_bounds__(NT) stencil_kernel(const __grid_constant__ Ste
 
   const TileK* tiles = A.ntiles <= INLINE_TILES ? A.inl : A.tiles_dev;
   const int tid = threadIdx.x;
-  const int tcol = (tid & 15) * 4;
-  const int trow = tid >> 4;
   const unsigned om = A.outmask;
 
   for (int blk = blockIdx.x; blk < A.total_blocks; blk += gridDim.x) {
@@ -230,6 +377,7 @@ __global__ void __launch_bounds__(NT) stencil_kernel(const __grid_constant__ Ste
     const int by = lb / T.nbx, bx = lb - (lb / T.nbx) * T.nbx;
     const int y0 = T.cy0 + by * TY, x0 = T.cx0 + bx * TX;
     const int fy0 = y0 - FHY, fx0 = x0 - FHX;
+    const bool interior = fy0 >= T.wy0 && fy0 + FR <= T.wy1 && fx0 >= T.wx0 && fx0 + FC <= T.wx1;
 
     __syncthreads();  // the previous block is done with shared memory
     bool saw = load_region<FR, FC>(A, T, F, fy0, fx0);
@@ -237,13 +385,15 @@ __global__ void __launch_bounds__(NT) stencil_kernel(const __grid_constant__ Ste
 
     // NoData flags of this thread's 8 core pixels, before the fill rewrites F.
     unsigned nanbits = 0;
+    {
+      const int j = tid & (TX - 1);
+      const int i0 = (tid / TX) * (TY * TX / NT);
 #pragma unroll
-    for (int g = 0; g < 2; ++g)
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        float v = F[(FHY + trow + 16 * g) * FC + FHX + tcol + k];
-        if (v != v) nanbits |= 1u << (g * 4 + k);
+      for (int ii = 0; ii < TY * TX / NT; ++ii) {
+        float v = F[(FHY + i0 + ii) * FC + FHX + j];
+        if (v != v) nanbits |= 1u << ii;
       }
+    }
 
     if (any_nan) {
       // (a) NaN cells of the window whose fill value can reach a valid pixel
@@ -315,93 +465,12 @@ __global__ void __launch_bounds__(NT) stencil_kernel(const __grid_constant__ Ste
     }
 
     if (CURV) {
-      for (int i = tid; i < DR * DC; i += NT) {
-        int r = i / DC, c = i - (i / DC) * DC;
-        int gy = y0 - DHY + r, gx = x0 - DHX + c;
-        if (gy < T.wy0 || gy >= T.wy1 || gx < T.wx0 || gx >= T.wx1) continue;
-        const float* f = F + (r + FHY - DHY) * FC + (c + FHX - DHX);
-        DX[i] = deriv(T.g1x, gx, T.wx0, T.wx1, [&](int o) { return f[o]; });
-        DY[i] = deriv(T.g1y, gy, T.wy0, T.wy1, [&](int o) { return f[o * FC]; });
-      }
+      if (interior) stage_first_derivs<true>(T, F, DX, DY, y0, x0);
+      else stage_first_derivs<false>(T, F, DX, DY, y0, x0);
       __syncthreads();
     }
-
-#pragma unroll 1
-    for (int g = 0; g < 2; ++g) {
-      const int ly = trow + 16 * g;
-      const int gy = y0 + ly;
-      if (gy >= T.cy1) continue;
-      const int gx0 = x0 + tcol;
-      const int n = min(4, T.cx1 - gx0);
-      if (n <= 0) continue;
-      float o_hs[4], o_sl[4], o_cm[4], o_cg[4], o_cp[4], o_cr[4], o_dx[4], o_dy[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float qnan = __int_as_float(0x7fc00000);
-        o_hs[k] = o_sl[k] = o_cm[k] = o_cg[k] = o_cp[k] = o_cr[k] = o_dx[k] = o_dy[k] = qnan;
-        if (k >= n || ((nanbits >> (g * 4 + k)) & 1u)) continue;
-        const int gx = gx0 + k;
-        const float* f = F + (ly + FHY) * FC + (tcol + k + FHX);
-        float p, q;
-        if (CURV) {
-          p = DX[(ly + DHY) * DC + tcol + k + DHX];
-          q = DY[(ly + DHY) * DC + tcol + k + DHX];
-        } else {
-          p = deriv(T.g1x, gx, T.wx0, T.wx1, [&](int o) { return f[o]; });
-          q = deriv(T.g1y, gy, T.wy0, T.wy1, [&](int o) { return f[o * FC]; });
-        }
-        o_dx[k] = p;
-        o_dy[k] = q;
-        if (om & (1u << FSG_OUT_HILLSHADE)) {
-          float px = p, qy = q;
-          if (!A.z_is_one) {
-            const float z = A.z;
-            px = deriv(T.g1x, gx, T.wx0, T.wx1, [&](int o) { return fmul(f[o], z); });
-            qy = deriv(T.g1y, gy, T.wy0, T.wy1, [&](int o) { return fmul(f[o * FC], z); });
-          }
-          float e = px * T.sign_x, nn = qy * T.sign_y;
-          float nrm = sqrtf(fadd(fadd(fmul(e, e), fmul(nn, nn)), 1.0f));
-          float hs = (fadd(fadd(-fmul(e, A.lx), -fmul(nn, A.ly)), A.lz)) / nrm;
-          o_hs[k] = fminf(fmaxf(hs, 0.0f), 1.0f);
-        }
-        if (om & (1u << FSG_OUT_SLOPE)) o_sl[k] = slope_value(p, q, A.slope_unit);
-        if (CURV) {
-          const float* dxp = DX + (ly + DHY) * DC + tcol + k + DHX;
-          const float* dyp = DY + (ly + DHY) * DC + tcol + k + DHX;
-          float dxx = deriv(T.c2x, gx, T.wx0, T.wx1, [&](int o) { return dxp[o]; });
-          float dxy = deriv(T.c2y, gy, T.wy0, T.wy1, [&](int o) { return dxp[o * DC]; });
-          float dyy = deriv(T.c2y, gy, T.wy0, T.wy1, [&](int o) { return dyp[o * DC]; });
-          float p2 = p * p, q2 = q * q, pq = p * q;
-          float g2 = p2 + q2, one_g2 = 1.0f + g2;
-          float s15 = one_g2 * sqrtf(one_g2);  // (1 + p^2 + q^2)^1.5
-          if (om & (1u << FSG_OUT_CURV_MEAN)) {
-            float dyx = deriv(T.c2x, gx, T.wx0, T.wx1, [&](int o) { return dyp[o]; });
-            float s = (dxy + dyx) * 0.5f;
-            float num = (1.0f + q2) * dxx - 2.0f * pq * s + (1.0f + p2) * dyy;
-            o_cm[k] = gamma_display(-num / (2.0f * s15 + 1e-10f));
-          }
-          if (om & (1u << FSG_OUT_CURV_GAUSSIAN))
-            o_cg[k] = gamma_display((dxx * dyy - dxy * dxy) / (one_g2 * one_g2));
-          if (om & (1u << FSG_OUT_CURV_PLANFORM)) {
-            float num = q2 * dxx - 2.0f * pq * dxy + p2 * dyy;
-            o_cp[k] = gamma_display(-num / (g2 * sqrtf(g2) + 1e-10f));
-          }
-          if (om & (1u << FSG_OUT_CURV_PROFILE)) {
-            float num = p2 * dxx + 2.0f * pq * dxy + q2 * dyy;
-            o_cr[k] = gamma_display(-num / (g2 * s15 + 1e-10f));
-          }
-        }
-      }
-      const long long prow = (long long)(T.oy0 + gy - T.cy0);
-      const long long pcol = (long long)(T.ox0 + gx0 - T.cx0);
-      const float* outs[FSG_STENCIL_NOUT] = {o_hs, o_sl, o_cm, o_cg, o_cp, o_cr, o_dx, o_dy};
-#pragma unroll
-      for (int o = 0; o < FSG_STENCIL_NOUT; ++o) {
-        if (!(om & (1u << o))) continue;
-        const PlaneK& P = A.planes[o];
-        store_plane(P, prow * P.ld + pcol, outs[o], n);
-      }
-    }
+    if (interior) stage_pixels<CURV, true>(A, T, om, F, DX, DY, y0, x0, nanbits);
+    else stage_pixels<CURV, false>(A, T, om, F, DX, DY, y0, x0, nanbits);
   }
 }
 

@@ -45,7 +45,8 @@ def test_ctypes_signatures_cover_header(built_lib):
     assert b"sm_103a" in L.fsg_version()
 
 
-STRUCTS = {"fsg_plane": "Plane", "fsg_tile": "Tile", "fsg_stencil_params": "StencilParams"}
+STRUCTS = {"fsg_plane": "Plane", "fsg_tile": "Tile", "fsg_stencil_params": "StencilParams",
+           "fsg_topousm_params": "TopoUSMParams"}
 
 
 def test_struct_layouts_match_header(tmp_path):
