@@ -81,6 +81,13 @@ class TopoUSMParams(C.Structure):
                 ("scale", C.c_double)]
 
 
+class OpennessParams(C.Structure):
+    _fields_ = [("openness_type", C.c_int32), ("num_directions", C.c_int32), ("max_distance", C.c_int32),
+                ("mode", C.c_int32), ("pixel_size", C.c_double), ("nodata", C.c_double),
+                ("has_nodata", C.c_int32), ("reserved", C.c_int32), ("stretch_lo", C.c_double),
+                ("stretch_scale", C.c_double)]
+
+
 # Exported symbols and their signatures (kept in sync with include/fsg.h).
 _SIGNATURES = {
     "fsg_abi_version": (C.c_int, []),
@@ -102,6 +109,10 @@ _SIGNATURES = {
     "fsg_percentile": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_double), C.c_int32,
                                  C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_void_p]),
     "fsg_std": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.c_void_p]),
+    "fsg_openness": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
+                               C.POINTER(OpennessParams), C.POINTER(Plane), C.c_void_p, C.c_int64, C.c_void_p]),
+    "fsg_openness_offsets": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32]),
     "fsg_affine": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32,
                              C.POINTER(Plane), C.c_void_p]),
 }

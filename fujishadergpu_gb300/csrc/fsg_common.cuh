@@ -102,4 +102,49 @@ __device__ __forceinline__ float quantize(float v, float qa, float qb, int qmin,
   return fminf(fmaxf(dn, (float)qmin), (float)qmax);
 }
 
+// ---------------------------------------------------- fast transcendentals
+// Hardware approximations (PTX *.approx instructions): relative error ~2^-22.
+__device__ __forceinline__ float ex2_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+  float r;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// arctan with |error| <= 1.5e-7 rad: atan(a) = a * P(a^2) on [0, 1], P of
+// degree 7 fitted to atan(a)/a by iteratively reweighted least squares
+// (Lawson's algorithm) on Chebyshev-distributed nodes, and
+// atan(x) = pi/2 - atan(1/x) for |x| > 1.
+__device__ __forceinline__ float atan_poly(float x) {
+  float ax = fabsf(x);
+  bool inv = ax > 1.0f;
+  float a = inv ? rcp_approx(ax) : ax;
+  float a2 = a * a;
+  float p = -0x1.09b3ep-8f;
+  p = fmaf(a2, p, 0x1.662f9cp-6f);
+  p = fmaf(a2, p, -0x1.ca055ep-5f);
+  p = fmaf(a2, p, 0x1.8af07cp-4f);
+  p = fmaf(a2, p, -0x1.1cd902p-3f);
+  p = fmaf(a2, p, 0x1.988166p-3f);
+  p = fmaf(a2, p, -0x1.554c3ap-2f);
+  p = fmaf(a2, p, 0x1.ffffeap-1f);
+  float r = a * p;
+  if (inv) r = 1.57079632679489661923f - r;
+  return copysignf(r, x);
+}
+
 }  // namespace fsg

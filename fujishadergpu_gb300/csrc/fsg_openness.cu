@@ -1,0 +1,312 @@
+// Topographic openness (Yokoyama et al. 2002), exact ray-march.
+//
+// Reference semantics (algorithms/_impl_openness.py:31-132), per tile window:
+//   directions theta_d = 2*pi*d/n (np.linspace(0, 2pi, n, endpoint=False));
+//   sample offsets (int(round(r cos)), int(round(r sin))) with Python's
+//   round-half-to-even, (0, 0) skipped, for the distances
+//     reference mode: unique(int(linspace(0.1, 1, 10) * D)) > 0   (:65-68)
+//     dense mode    : every step r = 1..D (the O(px * dirs * D) ray-march);
+//   a sample is valid inside the window and off NoData (:81-83, :112);
+//   angle = atan((z_s - z) / hypot(ox*|sx|, oy*|sy|)); per direction the max
+//   (positive) / min (negative) over valid samples; directional mean of
+//   pi/2 - max (positive) or pi/2 + min (negative) over directions with a
+//   valid sample (:119-126); display = clip(mean/(pi/2), 0, 1)^(1/2.2)
+//   (:127-129), optionally stretched by global (p1, p99 - p1) stats
+//   (algorithms/tile/dask_bridge.py:173-187).
+//
+// atan is monotonic, so the per-direction extreme angle is atan of the
+// extreme slope ratio: each sample costs one load, one subtract, one
+// correctly rounded divide by the float32 distance (the reference's float32
+// division) and one max; atan runs once per direction.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fsg_common.cuh"
+
+namespace fsg {
+namespace {
+
+constexpr int BX = 32, BY = 8, RPT = 4;  // block 32 x 8 threads, 4 rows per thread: 32 x 32 pixels
+
+struct RaySample {
+  short ox, oy;
+  float d, r;  // f32(distance), RN(1/d)
+};
+
+struct OpenArgs {
+  const float* raster;
+  long long ld;
+  int rh, rw;
+  float ndf;
+  int has_nodata;
+  int positive;
+  int ndir;
+  const int* ray_begin;        // [ntiles * (ndir + 1)] offsets into samples
+  const RaySample* samples;    // per tile: its own distance table
+  const int* tile_sample0;     // first sample index of each tile
+  const fsg_tile* tiles;       // device copy
+  const int* block0;           // first block of each tile
+  int ntiles, total_blocks;
+  float lo, scale;             // display stretch (scale <= 0: none)
+  void* disp;
+  long long dld;
+  int ddtype;
+  float qa, qb;
+  int qmin, qmax;
+  float* raw;                  // mean angle in degrees (nullable)
+  long long rld;
+};
+
+__device__ __forceinline__ float load_z(const OpenArgs& A, int y, int x, const fsg_tile& T) {
+  if (y < T.win_y0 || y >= T.win_y0 + T.win_h || x < T.win_x0 || x >= T.win_x0 + T.win_w)
+    return __int_as_float(0x7fc00000);
+  float v = __ldg(A.raster + (long long)y * A.ld + x);
+  return is_nodata(v, A.ndf, A.has_nodata != 0) ? __int_as_float(0x7fc00000) : v;
+}
+
+__global__ void __launch_bounds__(BX * BY) openness_kernel(const __grid_constant__ OpenArgs A) {
+  for (int blk = blockIdx.x; blk < A.total_blocks; blk += gridDim.x) {
+    int lo = 0, hi = A.ntiles - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (A.block0[mid] <= blk) lo = mid; else hi = mid - 1;
+    }
+    const fsg_tile T = A.tiles[lo];
+    const int nbx = (T.core_w + BX - 1) / BX;
+    const int lb = blk - A.block0[lo];
+    const int by = lb / nbx, bx = lb - by * nbx;
+    const int x = T.core_x0 + bx * BX + threadIdx.x;
+    const int yb = T.core_y0 + by * (BY * RPT) + threadIdx.y * RPT;
+    const RaySample* S = A.samples + A.tile_sample0[lo];
+    const int* rb = A.ray_begin + lo * (A.ndir + 1);
+    float z[RPT], sum[RPT], cnt[RPT];
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      z[k] = (x < T.core_x0 + T.core_w && yb + k < T.core_y0 + T.core_h) ? load_z(A, yb + k, x, T)
+                                                                          : __int_as_float(0x7fc00000);
+      sum[k] = 0.f;
+      cnt[k] = 0.f;
+    }
+    const float half_pi = 1.57079637050628662109375f;  // f32(pi/2)
+    for (int d = 0; d < A.ndir; ++d) {
+      float ext[RPT];
+#pragma unroll
+      for (int k = 0; k < RPT; ++k) ext[k] = A.positive ? -INFINITY : INFINITY;
+      for (int s = rb[d]; s < rb[d + 1]; ++s) {
+        const RaySample rs = S[s];
+#pragma unroll
+        for (int k = 0; k < RPT; ++k) {
+          float v = load_z(A, yb + k + rs.oy, x + rs.ox, T);
+          if (v == v) {
+            float t = div_by(__fsub_rn(v, z[k]), rs.d, rs.r);
+            ext[k] = A.positive ? fmaxf(ext[k], t) : fminf(ext[k], t);
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < RPT; ++k) {
+        if (ext[k] != (A.positive ? -INFINITY : INFINITY)) {
+          float a = atanf(ext[k]);
+          sum[k] = __fadd_rn(sum[k], A.positive ? __fsub_rn(half_pi, a) : __fadd_rn(half_pi, a));
+          cnt[k] = __fadd_rn(cnt[k], 1.0f);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int y = yb + k;
+      if (x >= T.core_x0 + T.core_w || y >= T.core_y0 + T.core_h) continue;
+      float mean = __fdiv_rn(sum[k], fmaxf(cnt[k], 1.0f));
+      float disp, rawd;
+      if (z[k] != z[k]) {
+        disp = rawd = __int_as_float(0x7fc00000);
+      } else {
+        float op = fminf(fmaxf(__fdiv_rn(mean, half_pi), 0.0f), 1.0f);
+        disp = op > 0.f ? exp2f(0.45454545454545453f * __log2f(op)) : 0.0f;
+        if (A.scale > 0.f) disp = fmaxf(__fdiv_rn(__fsub_rn(disp, A.lo), A.scale), 0.0f);
+        rawd = mean * 57.295780181884765625f;
+      }
+      const long long py = T.out_y0 + (y - T.core_y0), px = T.out_x0 + (x - T.core_x0);
+      if (A.disp) {
+        long long o = py * A.dld + px;
+        if (A.ddtype == FSG_F32) static_cast<float*>(A.disp)[o] = disp;
+        else if (A.ddtype == FSG_U8) static_cast<uint8_t*>(A.disp)[o] = (uint8_t)(int)quantize(disp, A.qa, A.qb, A.qmin, A.qmax);
+        else static_cast<int16_t*>(A.disp)[o] = (int16_t)(int)quantize(disp, A.qa, A.qb, A.qmin, A.qmax);
+      }
+      if (A.raw) A.raw[py * A.rld + px] = rawd;
+    }
+  }
+}
+
+}  // namespace
+
+// Python's round(): nearest integer, ties to even.
+static int py_round(double v) { return (int)std::nearbyint(v); }
+
+// Ray offsets in pixels: per direction a list of (ox, oy).
+static void ray_offsets(int ndir, int max_distance, int mode, std::vector<std::vector<std::pair<int, int>>>* out) {
+  std::vector<int> dist;
+  if (mode == 0) {
+    // np.unique((np.linspace(0.1, 1.0, 10) * D).astype(int)), > 0
+    for (int i = 0; i < 10; ++i) {
+      double t = 0.1 + (double)i * ((1.0 - 0.1) / 9.0);
+      if (i == 9) t = 1.0;
+      dist.push_back((int)(t * (double)max_distance));
+    }
+    std::sort(dist.begin(), dist.end());
+    dist.erase(std::unique(dist.begin(), dist.end()), dist.end());
+    dist.erase(std::remove_if(dist.begin(), dist.end(), [](int r) { return r <= 0; }), dist.end());
+  } else {
+    for (int r = 1; r <= max_distance; ++r) dist.push_back(r);
+  }
+  out->assign(ndir, {});
+  const double step = (2.0 * M_PI) / (double)ndir;
+  for (int d = 0; d < ndir; ++d) {
+    double th = (double)d * step;
+    double c = std::cos(th), s = std::sin(th);
+    for (int r : dist) {
+      int ox = py_round((double)r * c), oy = py_round((double)r * s);
+      if (ox == 0 && oy == 0) continue;
+      (*out)[d].push_back({ox, oy});
+    }
+  }
+}
+
+}  // namespace fsg
+
+using namespace fsg;
+
+extern "C" int fsg_openness_offsets(int32_t num_directions, int32_t max_distance, int32_t mode, int32_t* ox,
+                                    int32_t* oy, int32_t* ray_len, int32_t capacity) {
+  if (num_directions < 1 || max_distance < 0 || mode < 0 || mode > 1 || !ray_len)
+    return fail(FSG_ERR_INVALID, "bad openness ray parameters");
+  std::vector<std::vector<std::pair<int, int>>> rays;
+  ray_offsets(num_directions, max_distance, mode, &rays);
+  int n = 0;
+  for (int d = 0; d < num_directions; ++d) {
+    ray_len[d] = (int32_t)rays[d].size();
+    for (auto& o : rays[d]) {
+      if (n < capacity && ox && oy) {
+        ox[n] = o.first;
+        oy[n] = o.second;
+      }
+      ++n;
+    }
+  }
+  if (n > capacity) return fail(FSG_ERR_WORKSPACE, "need %d offset slots, have %d", n, capacity);
+  return FSG_OK;
+}
+
+extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                            const fsg_tile* tiles, int32_t ntiles, const fsg_openness_params* p,
+                            const fsg_plane* display, float* raw_deg_dev, int64_t raw_ld, void* stream) {
+  if (!p || (ntiles > 0 && !tiles)) return fail(FSG_ERR_INVALID, "null argument");
+  if (ntiles < 0 || raster_h < 0 || raster_w < 0 || ld < raster_w) return fail(FSG_ERR_INVALID, "bad raster shape");
+  if ((!display || !display->ptr) && !raw_deg_dev) return fail(FSG_ERR_INVALID, "no output requested");
+  if (display && display->ptr && (display->dtype < FSG_F32 || display->dtype > FSG_I16))
+    return fail(FSG_ERR_DTYPE, "dtype %d", display->dtype);
+  if (p->num_directions < 1 || p->num_directions > 4096 || p->max_distance < 0 || p->mode < 0 || p->mode > 1)
+    return fail(FSG_ERR_INVALID, "bad openness parameters");
+  int st = validate_tiles(raster_h, raster_w, tiles, ntiles, 1);
+  if (st) return st;
+  std::vector<std::vector<std::pair<int, int>>> rays;
+  ray_offsets(p->num_directions, p->max_distance, p->mode, &rays);
+  const int ndir = p->num_directions;
+  int per_tile = 0;
+  for (auto& r : rays) per_tile += (int)r.size();
+  // Host tables: per tile its distance table (pixel scales may differ per tile).
+  std::vector<RaySample> samples;
+  std::vector<int> ray_begin, tile_sample0, block0;
+  samples.reserve((size_t)per_tile * ntiles);
+  int total = 0;
+  for (int t = 0; t < ntiles; ++t) {
+    const fsg_tile& T = tiles[t];
+    // _impl_openness.py:70-75
+    double sx = std::fabs(T.pixel_scale_x), sy = std::fabs(T.pixel_scale_y);
+    double fb = p->pixel_size != 0.0 ? p->pixel_size : 1.0;
+    if (sx < 1e-9) sx = fb;
+    if (sy < 1e-9) sy = fb;
+    tile_sample0.push_back((int)samples.size());
+    int acc = 0;
+    for (int d = 0; d < ndir; ++d) {
+      ray_begin.push_back(acc);
+      for (auto& o : rays[d]) {
+        double dist = std::max(std::hypot((double)o.first * sx, (double)o.second * sy), 1e-9);
+        RaySample rs;
+        rs.ox = (short)o.first;
+        rs.oy = (short)o.second;
+        rs.d = (float)dist;
+        rs.r = 1.0f / rs.d;
+        samples.push_back(rs);
+        ++acc;
+      }
+    }
+    ray_begin.push_back(acc);
+    block0.push_back(total);
+    if (T.core_h > 0 && T.core_w > 0)
+      total += ((T.core_w + BX - 1) / BX) * ((T.core_h + BY * RPT - 1) / (BY * RPT));
+  }
+  if (total == 0) return FSG_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  size_t b_samples = samples.size() * sizeof(RaySample), b_rb = ray_begin.size() * sizeof(int);
+  size_t b_ts = tile_sample0.size() * sizeof(int), b_b0 = block0.size() * sizeof(int);
+  size_t b_tiles = (size_t)ntiles * sizeof(fsg_tile);
+  auto al = [](size_t n) { return (n + 255) & ~(size_t)255; };
+  size_t bytes = al(b_samples) + al(b_rb) + al(b_ts) + al(b_b0) + al(b_tiles);
+  std::vector<char> host(bytes);
+  size_t off = 0;
+  auto put = [&](const void* src, size_t n) {
+    std::memcpy(host.data() + off, src, n);
+    size_t o = off;
+    off += al(n);
+    return o;
+  };
+  size_t o_s = put(samples.data(), b_samples), o_rb = put(ray_begin.data(), b_rb);
+  size_t o_ts = put(tile_sample0.data(), b_ts), o_b0 = put(block0.data(), b_b0), o_t = put(tiles, b_tiles);
+  StreamScratch scratch;
+  st = scratch.alloc(bytes, s);
+  if (st) return st;
+  FSG_CUDA(cudaMemcpyAsync(scratch.ptr, host.data(), bytes, cudaMemcpyHostToDevice, s));
+  char* base = static_cast<char*>(scratch.ptr);
+  OpenArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.raster = raster_dev;
+  A.ld = ld;
+  A.rh = raster_h;
+  A.rw = raster_w;
+  A.ndf = (float)p->nodata;
+  A.has_nodata = p->has_nodata != 0;
+  A.positive = p->openness_type == 0;
+  A.ndir = ndir;
+  A.samples = reinterpret_cast<const RaySample*>(base + o_s);
+  A.ray_begin = reinterpret_cast<const int*>(base + o_rb);
+  A.tile_sample0 = reinterpret_cast<const int*>(base + o_ts);
+  A.block0 = reinterpret_cast<const int*>(base + o_b0);
+  A.tiles = reinterpret_cast<const fsg_tile*>(base + o_t);
+  A.ntiles = ntiles;
+  A.total_blocks = total;
+  A.lo = (float)p->stretch_lo;
+  A.scale = p->stretch_scale > 1e-12 ? (float)p->stretch_scale : 0.0f;
+  if (display && display->ptr) {
+    A.disp = display->ptr;
+    A.dld = display->ld;
+    A.ddtype = display->dtype;
+    A.qa = display->q_a;
+    A.qb = display->q_b;
+    A.qmin = display->q_min;
+    A.qmax = display->q_max;
+  }
+  A.raw = raw_deg_dev;
+  A.rld = raw_ld;
+  DeviceInfo di;
+  st = device_info(&di);
+  if (st) return st;
+  int per_sm = 0;
+  FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, openness_kernel, BX * BY, 0));
+  int grid = std::min(total, di.sms * std::max(1, per_sm));
+  openness_kernel<<<grid, dim3(BX, BY), 0, s>>>(A);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}

@@ -7,8 +7,9 @@
 // per-pass bin choice runs on the device, so a percentile costs 1 + 3 * ranks
 // streaming passes and a single host synchronisation.  The linear
 // interpolation between neighbouring ranks follows numpy.percentile's
-// 'linear' method (virtual index n*q + (1 - q) - 1, float32 difference times a
-// float64 fraction), evaluated in FP64.
+// 'linear' method (virtual index n*q + (1 - q) - 1, _lerp), evaluated in FP64
+// (NumPy and CuPy interpolate float32 data in float32 for a scalar q; the two
+// differ by at most one float32 ulp of the result).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -138,10 +139,11 @@ static LinearPick linear_pick(long long n, double q) {
   return p;
 }
 
+// numpy's _lerp in FP64: a + (b - a) t, or b - (b - a)(1 - t) for t >= 0.5.
 static double lerp_numpy(float a, float b, double t) {
-  float diff = b - a;  // float32 subtraction, as in numpy's _lerp on float32 operands
-  double r = (double)a + (double)diff * t;
-  if (t >= 0.5) r = (double)b - (double)diff * (1.0 - t);
+  double diff = (double)b - (double)a;
+  double r = (double)a + diff * t;
+  if (t >= 0.5) r = (double)b - diff * (1.0 - t);
   return r;
 }
 

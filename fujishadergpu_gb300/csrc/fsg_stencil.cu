@@ -95,11 +95,12 @@ __device__ __forceinline__ float deriv(const Axis& a, int k, int lo, int hi, Fn 
 }
 
 __device__ __forceinline__ float gamma_display(float k) {
-  // ((tanh(100k) + 1) / 2) ** (1/2.2): tanhf is the function CuPy's cp.tanh
-  // calls; the sum and halving are the reference's float32 ops.
-  float t = tanhf(k * 100.0f);
-  float u = __fadd_rn(t, 1.0f) * 0.5f;
-  return exp2f(0.45454545454545453f * __log2f(u));
+  // ((tanh(100k) + 1) / 2) ** (1/2.2) == (1 + exp(-200k)) ** (-1/2.2): three
+  // hardware approximations (absolute error ~1e-7 on [0, 1]).  Where tanh
+  // rounds to within a few float32 ulps of -1 the reference's own value is
+  // quantised by that rounding; this form gives the unquantised value.
+  float e = ex2_approx(k * -288.53900817779268f);  // exp(-200k) = 2^(-200 k log2(e))
+  return ex2_approx(-0.45454545454545453f * lg2_approx(1.0f + e));
 }
 
 __device__ __forceinline__ float slope_value(float p, float q, int unit) {
@@ -163,9 +164,14 @@ __device__ __forceinline__ bool load_region(const StencilArgs& A, const TileK& T
   bool vec = ((reinterpret_cast<uintptr_t>(A.raster) & 15) == 0) && ((A.ld & 3) == 0) && ((gx0 & 3) == 0);
   bool saw_nan = false;
   const bool hn = A.has_nodata != 0;
-  for (int i = threadIdx.x; i < R * (C / 4); i += NT) {
-    int r = i / (C / 4);
-    int c = (i - r * (C / 4)) * 4;
+  constexpr int C4 = C / 4, SR = NT / C4, SC = NT % C4;
+  int r = threadIdx.x / C4, c4 = threadIdx.x % C4;
+  for (int i = threadIdx.x; i < R * C4; i += NT, r += SR, c4 += SC) {
+    if (c4 >= C4) {
+      c4 -= C4;
+      ++r;
+    }
+    const int c = c4 * 4;
     int gy = gy0 + r, gx = gx0 + c;
     float v[4] = {0.f, 0.f, 0.f, 0.f};
     if (gy >= 0 && gy < A.rh) {
@@ -201,17 +207,6 @@ __device__ __forceinline__ double gsum(const double* w, const double* x) {
   return acc;
 }
 
-__device__ __forceinline__ float sqrt_approx(float x) {
-  float r;
-  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
-__device__ __forceinline__ float rcp_approx(float x) {
-  float r;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
-
 __device__ __forceinline__ void store1(const PlaneK& P, long long off, float v) {
   if (P.dtype == FSG_F32) static_cast<float*>(P.ptr)[off] = v;
   else if (P.dtype == FSG_U8) static_cast<uint8_t*>(P.ptr)[off] = (uint8_t)(int)quantize(v, P.qa, P.qb, P.qmin, P.qmax);
@@ -232,7 +227,7 @@ __device__ __forceinline__ void pixel_products(const StencilArgs& A, const TileK
   }
   if (om & (1u << FSG_OUT_SLOPE)) {
     float g2 = fadd(fmul(p, p), fmul(q, q));
-    if (A.slope_unit == FSG_SLOPE_DEGREE) o[FSG_OUT_SLOPE] = atanf(sqrt_approx(g2)) * 57.295780181884765625f;
+    if (A.slope_unit == FSG_SLOPE_DEGREE) o[FSG_OUT_SLOPE] = atan_poly(sqrt_approx(g2)) * 57.295780181884765625f;
     else o[FSG_OUT_SLOPE] = slope_value(p, q, A.slope_unit);
   }
   if (om & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) | (1u << FSG_OUT_CURV_PLANFORM) |
@@ -265,8 +260,13 @@ __device__ __forceinline__ void pixel_products(const StencilArgs& A, const TileK
 template <bool INTERIOR>
 __device__ __forceinline__ void stage_first_derivs(const TileK& T, const float* F, float* DX, float* DY, int y0,
                                                    int x0) {
-  for (int i = threadIdx.x; i < DR * DC; i += NT) {
-    int r = i / DC, c = i - (i / DC) * DC;
+  constexpr int SR = NT / DC, SC = NT % DC;
+  int r = threadIdx.x / DC, c = threadIdx.x % DC;
+  for (int i = threadIdx.x; i < DR * DC; i += NT, r += SR, c += SC) {
+    if (c >= DC) {
+      c -= DC;
+      ++r;
+    }
     const float* f = F + (r + FHY - DHY) * FC + (c + FHX - DHX);
     if (INTERIOR) {
       DX[i] = div_by(fsub(f[1], f[-1]), T.g1x.d2, T.g1x.rcp);
@@ -291,6 +291,16 @@ __device__ __forceinline__ void stage_pixels(const StencilArgs& A, const TileK& 
   const int gx = x0 + j;
   if (gx >= T.cx1) return;
   const long long pcol = (long long)(T.ox0 + gx - T.cx0);
+  const long long prow0 = (long long)(T.oy0 + y0 + i0 - T.cy0);
+  char* optr[FSG_STENCIL_NOUT];
+  long long ostep[FSG_STENCIL_NOUT];
+#pragma unroll
+  for (int k = 0; k < FSG_STENCIL_NOUT; ++k) {
+    const PlaneK& P = A.planes[k];
+    const int esz = P.dtype == FSG_F32 ? 4 : (P.dtype == FSG_I16 ? 2 : 1);
+    optr[k] = static_cast<char*>(P.ptr) + (prow0 * P.ld + pcol) * esz;
+    ostep[k] = P.ld * esz;
+  }
 #pragma unroll 1
   for (int ii = 0; ii < TY * TX / NT; ++ii) {
     const int i = i0 + ii;
@@ -340,17 +350,21 @@ __device__ __forceinline__ void stage_pixels(const StencilArgs& A, const TileK& 
       }
       pixel_products(A, T, om, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
     }
-    const long long prow = (long long)(T.oy0 + gy - T.cy0);
 #pragma unroll
     for (int k = 0; k < FSG_STENCIL_NOUT; ++k) {
       if (!(om & (1u << k))) continue;
       const PlaneK& P = A.planes[k];
-      store1(P, prow * P.ld + pcol, o[k]);
+      char* dst = optr[k] + ii * ostep[k];
+      if (P.dtype == FSG_F32) *reinterpret_cast<float*>(dst) = o[k];
+      else if (P.dtype == FSG_U8) *reinterpret_cast<uint8_t*>(dst) = (uint8_t)(int)quantize(o[k], P.qa, P.qb, P.qmin, P.qmax);
+      else *reinterpret_cast<int16_t*>(dst) = (int16_t)(int)quantize(o[k], P.qa, P.qb, P.qmin, P.qmax);
     }
   }
 }
 
-template <bool CURV>
+// FIXED != 0: the output mask is known at compile time (unrequested planes are
+// compiled out); FIXED == 0 reads it from the arguments.
+template <bool CURV, unsigned FIXED>
 __global__ void __launch_bounds__(NT) stencil_kernel(const __grid_constant__ StencilArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   float* F = reinterpret_cast<float*>(smem);                       // [FR][FC]
@@ -364,7 +378,7 @@ __global__ void __launch_bounds__(NT) stencil_kernel(const __grid_constant__ Ste
 
   const TileK* tiles = A.ntiles <= INLINE_TILES ? A.inl : A.tiles_dev;
   const int tid = threadIdx.x;
-  const unsigned om = A.outmask;
+  const unsigned om = FIXED ? FIXED : A.outmask;
 
   for (int blk = blockIdx.x; blk < A.total_blocks; blk += gridDim.x) {
     int lo = 0, hi = A.ntiles - 1;
@@ -631,7 +645,22 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
   if (st) return st;
   const bool curv = (outmask & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) |
                                 (1u << FSG_OUT_CURV_PLANFORM) | (1u << FSG_OUT_CURV_PROFILE))) != 0;
-  auto kern = curv ? stencil_kernel<true> : stencil_kernel<false>;
+  auto kern = curv ? stencil_kernel<true, 0u> : stencil_kernel<false, 0u>;
+  constexpr unsigned HS = 1u << FSG_OUT_HILLSHADE, SL = 1u << FSG_OUT_SLOPE, CM = 1u << FSG_OUT_CURV_MEAN,
+                     CG = 1u << FSG_OUT_CURV_GAUSSIAN, CP = 1u << FSG_OUT_CURV_PLANFORM,
+                     CR = 1u << FSG_OUT_CURV_PROFILE;
+  switch (outmask) {
+    case HS | SL | CP | CR: kern = stencil_kernel<true, HS | SL | CP | CR>; break;
+    case HS | SL | CM | CG | CP | CR: kern = stencil_kernel<true, HS | SL | CM | CG | CP | CR>; break;
+    case HS: kern = stencil_kernel<false, HS>; break;
+    case SL: kern = stencil_kernel<false, SL>; break;
+    case HS | SL: kern = stencil_kernel<false, HS | SL>; break;
+    case CM: kern = stencil_kernel<true, CM>; break;
+    case CG: kern = stencil_kernel<true, CG>; break;
+    case CP: kern = stencil_kernel<true, CP>; break;
+    case CR: kern = stencil_kernel<true, CR>; break;
+    default: break;
+  }
   FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
   int per_sm = 0;
   FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, SMEM_BYTES));

@@ -195,6 +195,41 @@ int fsg_std(const float* values_dev, int64_t n, double* out, void* stream);
 int fsg_affine(const float* in_dev, int64_t ld, int32_t h, int32_t w, double offset, double scale,
                int32_t clamp_min0, const fsg_plane* out, void* stream);
 
+/* ------------------------------------------------------------------ openness */
+enum fsg_openness_mode {
+  FSG_OPENNESS_REFERENCE = 0,  /* 10 sampled distances per ray (_impl_openness.py:65-68) */
+  FSG_OPENNESS_DENSE = 1       /* every pixel step r = 1..max_distance */
+};
+
+typedef struct fsg_openness_params {
+  int32_t openness_type;    /* 0 positive, 1 negative */
+  int32_t num_directions;   /* default 16 */
+  int32_t max_distance;     /* pixels, default 50 */
+  int32_t mode;             /* enum fsg_openness_mode */
+  double pixel_size;        /* fallback when |pixel_scale| < 1e-9 */
+  double nodata;
+  int32_t has_nodata;
+  int32_t reserved;
+  double stretch_lo, stretch_scale;  /* display stretch (p1, p99 - p1); scale <= 1e-12: none */
+} fsg_openness_params;
+
+/* Exact openness ray-march over a list of tiles.  `display` receives
+ * ((mean/(pi/2)) clipped to [0,1])^(1/2.2) (then the optional stretch) as float32
+ * or int16/uint8 codes; `raw_deg_dev` (nullable, float32, same addressing as the
+ * display plane, row pitch raw_ld) receives the directional mean angle in
+ * degrees.  Replaces compute_openness_vectorized
+ * (algorithms/_impl_openness.py:31-132) and _direct_openness
+ * (algorithms/tile/dask_bridge.py:208-222). */
+int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                 const fsg_tile* tiles, int32_t ntiles, const fsg_openness_params* params,
+                 const fsg_plane* display, float* raw_deg_dev, int64_t raw_ld, void* stream);
+
+/* Host-only: the ray offsets the kernel uses (dx, dy per sample, directions in
+ * order; ray_len[d] samples for direction d).  Returns FSG_ERR_WORKSPACE with
+ * ray_len filled if `capacity` is too small. */
+int fsg_openness_offsets(int32_t num_directions, int32_t max_distance, int32_t mode, int32_t* ox, int32_t* oy,
+                         int32_t* ray_len, int32_t capacity);
+
 #ifdef __cplusplus
 }
 #endif

@@ -127,6 +127,9 @@ def test_tiled_topousm_with_coarse_field_and_normalisation(tu, dtype):
         ref = R.topousm_normalize(raw, (scale,))[cy - wy:cy - wy + ch, cx - wx:cx - wx + cw]
         g = got[cy:cy + ch, cx:cx + cw]
         if dtype == "float32":
+            d = np.abs(g.astype(np.float64) - ref)
+            print(f"tile {ty},{tx}: max|d|={np.nanmax(d) if np.isfinite(d).any() else 0:.3e} "
+                  f"nan mismatch={int((np.isnan(g) != np.isnan(ref)).sum())}")
             assert_close_range(g, ref, NORM_RANGE, f"tile {ty},{tx}")
         else:
             assert_codes_close(g, R.quantize_array(ref, qp, "int16"), f"tile {ty},{tx} int16")
@@ -143,10 +146,13 @@ def test_percentiles_exact_against_numpy():
         qs = [0.0, 1.0, 37.5, 50.0, 99.0, 100.0]
         got, nv = _stats.percentile(torch.from_numpy(x).cuda(), qs)
         assert nv == v.size
-        ref = [float(np.percentile(v, q)) for q in qs]
+        v64 = v.astype(np.float64)  # FP64 interpolation between the exact float32 order statistics
+        ref = [float(np.percentile(v64, q)) for q in qs]
         assert got == pytest.approx(ref, rel=1e-12, abs=1e-12), (n, got, ref)
+        ref32 = [float(np.percentile(v, q)) for q in qs]  # NumPy's float32 interpolation (scalar q)
+        assert got == pytest.approx(ref32, rel=2.5e-7, abs=1e-30)
         ga, _ = _stats.percentile(torch.from_numpy(x).cuda(), [99.0], absolute=True)
-        assert ga[0] == pytest.approx(float(np.percentile(np.abs(v), 99.0)), rel=1e-12)
+        assert ga[0] == pytest.approx(float(np.percentile(np.abs(v64), 99.0)), rel=1e-12)
 
 
 def test_stat_funcs_match_reference_golden(golden_dir):

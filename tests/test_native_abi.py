@@ -46,7 +46,7 @@ def test_ctypes_signatures_cover_header(built_lib):
 
 
 STRUCTS = {"fsg_plane": "Plane", "fsg_tile": "Tile", "fsg_stencil_params": "StencilParams",
-           "fsg_topousm_params": "TopoUSMParams"}
+           "fsg_topousm_params": "TopoUSMParams", "fsg_openness_params": "OpennessParams"}
 
 
 def test_struct_layouts_match_header(tmp_path):
@@ -79,3 +79,25 @@ def test_struct_layouts_match_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(cls), cname
         for fname, _ in cls._fields_:
             assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
+
+
+@pytest.mark.parametrize("ndir", [4, 8, 12, 16, 24, 32, 36])
+@pytest.mark.parametrize("dist", [1, 5, 40, 50, 256, 300])
+def test_openness_ray_offsets_match_numpy(built_lib, ndir, dist):
+    """Host-only table: Python banker's rounding of r*cos/sin of np.linspace angles."""
+    import ctypes as C
+    import numpy as np
+    from fujishadergpu_gb300 import _native as N
+    from oracle import restated as R
+    for mode, rays in ((0, R.openness_offsets(ndir, dist)), (1, R.dense_offsets(ndir, dist))):
+        cap = sum(len(r) for r in rays)
+        ox = (C.c_int32 * max(1, cap))()
+        oy = (C.c_int32 * max(1, cap))()
+        rl = (C.c_int32 * ndir)()
+        assert N.lib().fsg_openness_offsets(ndir, dist, mode, ox, oy, rl, cap) == 0
+        k = 0
+        for d, ray in enumerate(rays):
+            assert rl[d] == len(ray), (mode, d)
+            for (x, y) in ray:
+                assert (ox[k], oy[k]) == (x, y), (mode, d, k)
+                k += 1
