@@ -10,7 +10,8 @@ import ctypes as C
 import os
 import threading
 
-_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libfsg.so")
+_LIB_PATH = os.environ.get("FSG_LIBRARY") or os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib",
+                                                          "libfsg.so")
 _lock = threading.Lock()
 _lib = None
 

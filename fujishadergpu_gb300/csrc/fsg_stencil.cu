@@ -27,6 +27,10 @@
 namespace fsg {
 namespace {
 
+#ifndef FSG_STENCIL_MINB
+#define FSG_STENCIL_MINB 1  // minimum resident blocks per SM requested from ptxas
+#endif
+
 constexpr int TX = 64, TY = 32, NT = 256;
 constexpr int FHY = 3, FHX = 4;           // halo of the staged DEM region
 constexpr int FR = TY + 2 * FHY;          // 38 rows
@@ -158,43 +162,76 @@ __device__ __forceinline__ void store_plane(const PlaneK& P, long long off, cons
 // Loads rows [gy0, gy0+R) x cols [gx0, gx0+C) of the raster into S (row pitch
 // C), NoData -> NaN, cells outside the raster -> 0.  Returns true if this
 // thread saw a NaN inside the window.
+// Stages rows [gy0, gy0+R) x cols [gx0, gx0+C) of the raster in shared memory
+// (row pitch C).  issue() starts every global load of the calling thread
+// (float4 when the rows are 16-byte aligned) into registers; commit() maps
+// NoData to NaN, stores to shared memory and reports whether this thread saw
+// a NaN inside the window.  Splitting the two lets a block prefetch the next
+// block's halo while it computes the current one.  Cells outside the raster
+// read as 0 (they lie outside every window and are never used).
 template <int R, int C>
-__device__ __forceinline__ bool load_region(const StencilArgs& A, const TileK& T, float* S, int gy0,
-                                            int gx0) {
-  bool vec = ((reinterpret_cast<uintptr_t>(A.raster) & 15) == 0) && ((A.ld & 3) == 0) && ((gx0 & 3) == 0);
-  bool saw_nan = false;
-  const bool hn = A.has_nodata != 0;
-  constexpr int C4 = C / 4, SR = NT / C4, SC = NT % C4;
-  int r = threadIdx.x / C4, c4 = threadIdx.x % C4;
-  for (int i = threadIdx.x; i < R * C4; i += NT, r += SR, c4 += SC) {
-    if (c4 >= C4) {
-      c4 -= C4;
-      ++r;
-    }
-    const int c = c4 * 4;
-    int gy = gy0 + r, gx = gx0 + c;
-    float v[4] = {0.f, 0.f, 0.f, 0.f};
-    if (gy >= 0 && gy < A.rh) {
-      long long row = (long long)gy * A.ld;
-      if (vec && gx >= 0 && gx + 3 < A.rw) {
-        float4 t = __ldg(reinterpret_cast<const float4*>(A.raster + row + gx));
-        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
-      } else {
-        for (int k = 0; k < 4; ++k)
-          if (gx + k >= 0 && gx + k < A.rw) v[k] = __ldg(A.raster + row + gx + k);
+struct Region {
+  static constexpr int C4 = C / 4, N = R * C4, ITER = (N + NT - 1) / NT;
+  float4 v[ITER];
+  int gy0, gx0;
+
+  __device__ __forceinline__ void issue(const StencilArgs& A, int y0, int x0) {
+    gy0 = y0;
+    gx0 = x0;
+    const bool vec = ((reinterpret_cast<uintptr_t>(A.raster) & 15) == 0) && ((A.ld & 3) == 0) && ((x0 & 3) == 0);
+#pragma unroll
+    for (int k = 0; k < ITER; ++k) {
+      const int i = threadIdx.x + k * NT;
+      float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (i < N) {
+        const int r = i / C4, c = (i - (i / C4) * C4) * 4;
+        const int gy = y0 + r, gx = x0 + c;
+        if (gy >= 0 && gy < A.rh) {
+          const float* row = A.raster + (long long)gy * A.ld;
+          if (vec && gx >= 0 && gx + 3 < A.rw) {
+            t = __ldg(reinterpret_cast<const float4*>(row + gx));
+          } else {
+            if (gx >= 0 && gx < A.rw) t.x = __ldg(row + gx);
+            if (gx + 1 >= 0 && gx + 1 < A.rw) t.y = __ldg(row + gx + 1);
+            if (gx + 2 >= 0 && gx + 2 < A.rw) t.z = __ldg(row + gx + 2);
+            if (gx + 3 >= 0 && gx + 3 < A.rw) t.w = __ldg(row + gx + 3);
+          }
+        }
       }
+      v[k] = t;
     }
-    bool row_in = gy >= T.wy0 && gy < T.wy1;
-    for (int k = 0; k < 4; ++k) {
-      if (is_nodata(v[k], A.ndf, hn)) {
-        v[k] = __int_as_float(0x7fc00000);
-        if (row_in && gx + k >= T.wx0 && gx + k < T.wx1) saw_nan = true;
-      }
-    }
-    *reinterpret_cast<float4*>(S + r * C + c) = make_float4(v[0], v[1], v[2], v[3]);
   }
-  return saw_nan;
-}
+
+  __device__ __forceinline__ bool commit(const StencilArgs& A, const TileK& T, float* S) const {
+    bool saw_nan = false;
+    const bool hn = A.has_nodata != 0;
+#pragma unroll
+    for (int k = 0; k < ITER; ++k) {
+      const int i = threadIdx.x + k * NT;
+      if (i >= N) break;
+      const int r = i / C4, c = (i - (i / C4) * C4) * 4;
+      float e[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+      bool any = false;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (is_nodata(e[q], A.ndf, hn)) {
+          e[q] = __int_as_float(0x7fc00000);
+          any = true;
+        }
+      }
+      if (any) {
+        const int gy = gy0 + r, gx = gx0 + c;
+        if (gy >= T.wy0 && gy < T.wy1) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (e[q] != e[q] && gx + q >= T.wx0 && gx + q < T.wx1) saw_nan = true;
+        }
+      }
+      *reinterpret_cast<float4*>(S + r * C + c) = make_float4(e[0], e[1], e[2], e[3]);
+    }
+    return saw_nan;
+  }
+};
 
 // Separable 9-tap Gaussian in float64 (scipy's symmetric correlate1d order),
 // result rounded to float32.
@@ -365,7 +402,7 @@ __device__ __forceinline__ void stage_pixels(const StencilArgs& A, const TileK& 
 // FIXED != 0: the output mask is known at compile time (unrequested planes are
 // compiled out); FIXED == 0 reads it from the arguments.
 template <bool CURV, unsigned FIXED>
-__global__ void __launch_bounds__(NT) stencil_kernel(const __grid_constant__ StencilArgs A) {
+__global__ void __launch_bounds__(NT, FSG_STENCIL_MINB) stencil_kernel(const __grid_constant__ StencilArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   float* F = reinterpret_cast<float*>(smem);                       // [FR][FC]
   unsigned char* U = smem + SMEM_F;
@@ -380,22 +417,41 @@ __global__ void __launch_bounds__(NT) stencil_kernel(const __grid_constant__ Ste
   const int tid = threadIdx.x;
   const unsigned om = FIXED ? FIXED : A.outmask;
 
-  for (int blk = blockIdx.x; blk < A.total_blocks; blk += gridDim.x) {
+  // Block geometry of a flat block index.
+  auto locate = [&](int blk, int* t_out, int* y0_out, int* x0_out) {
     int lo = 0, hi = A.ntiles - 1;
     while (lo < hi) {
       int mid = (lo + hi + 1) >> 1;
       if (tiles[mid].block0 <= blk) lo = mid; else hi = mid - 1;
     }
-    const TileK& T = tiles[lo];
-    const int lb = blk - T.block0;
-    const int by = lb / T.nbx, bx = lb - (lb / T.nbx) * T.nbx;
-    const int y0 = T.cy0 + by * TY, x0 = T.cx0 + bx * TX;
+    const TileK& Tl = tiles[lo];
+    const int lb = blk - Tl.block0;
+    const int by = lb / Tl.nbx, bx = lb - (lb / Tl.nbx) * Tl.nbx;
+    *t_out = lo;
+    *y0_out = Tl.cy0 + by * TY;
+    *x0_out = Tl.cx0 + bx * TX;
+  };
+
+  Region<FR, FC> halo;
+  int t_cur = 0, y0 = 0, x0 = 0;
+  if (blockIdx.x < A.total_blocks) {
+    locate(blockIdx.x, &t_cur, &y0, &x0);
+    halo.issue(A, y0 - FHY, x0 - FHX);
+  }
+  for (int blk = blockIdx.x; blk < A.total_blocks; blk += gridDim.x) {
+    const TileK& T = tiles[t_cur];
     const int fy0 = y0 - FHY, fx0 = x0 - FHX;
     const bool interior = fy0 >= T.wy0 && fy0 + FR <= T.wy1 && fx0 >= T.wx0 && fx0 + FC <= T.wx1;
 
     __syncthreads();  // the previous block is done with shared memory
-    bool saw = load_region<FR, FC>(A, T, F, fy0, fx0);
+    bool saw = halo.commit(A, T, F);
     const int any_nan = __syncthreads_or(saw);
+    // prefetch the next block's halo; its loads overlap this block's compute
+    int t_next = t_cur, y0n = y0, x0n = x0;
+    if (blk + (int)gridDim.x < A.total_blocks) {
+      locate(blk + gridDim.x, &t_next, &y0n, &x0n);
+      halo.issue(A, y0n - FHY, x0n - FHX);
+    }
 
     // NoData flags of this thread's 8 core pixels, before the fill rewrites F.
     unsigned nanbits = 0;
@@ -431,7 +487,11 @@ __global__ void __launch_bounds__(NT) stencil_kernel(const __grid_constant__ Ste
         need[i] = nd;
       }
       // (b) the wider region the 9x9 Gaussian reaches
-      load_region<WR, WC>(A, T, W, y0 - WHY, x0 - WHX);
+      {
+        Region<WR, WC> wide;
+        wide.issue(A, y0 - WHY, x0 - WHX);
+        wide.commit(A, T, W);
+      }
       __syncthreads();
       double gw[5];
 #pragma unroll
@@ -485,6 +545,9 @@ __global__ void __launch_bounds__(NT) stencil_kernel(const __grid_constant__ Ste
     }
     if (interior) stage_pixels<CURV, true>(A, T, om, F, DX, DY, y0, x0, nanbits);
     else stage_pixels<CURV, false>(A, T, om, F, DX, DY, y0, x0, nanbits);
+    t_cur = t_next;
+    y0 = y0n;
+    x0 = x0n;
   }
 }
 

@@ -91,7 +91,7 @@ def test_tiled_topousm_with_coarse_field_and_normalisation(tu, dtype):
     large radii from a global coarse field sampled at global coords, / p99 scale."""
     from fujishadergpu_gb300 import _arrays, synth
     from fujishadergpu_gb300.algorithms._stencil import make_plane
-    H, W = 520, 610
+    H, W = 520, 608
     dem = synth.fbm_ridged(H, W, hurst=0.8, seed_fbm=71, seed_ridged=72, lo=0.0, hi=3500.0)
     dem[synth.nodata_disks(H, W, count=5, seed=73, rmin=5.0, rmax=25.0)] = np.nan
     small_r, small_w = [2, 8, 32], [32 / 63, 16 / 63, 8 / 63]
