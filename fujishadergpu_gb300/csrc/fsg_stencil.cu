@@ -86,6 +86,7 @@ struct StencilArgs {
   int slope_unit;
   unsigned outmask;
   double gw[5];             // scipy Gaussian(sigma=1, radius 4) weights, w[0] = centre
+  unsigned char* block_flags;  // per (tile, block): 1 = needs the exact shared-memory pass; NULL = all
   PlaneK planes[FSG_STENCIL_NOUT];
   TileK inl[INLINE_TILES];
 };
@@ -254,18 +255,23 @@ __device__ __forceinline__ void store1(const PlaneK& P, long long off, float v) 
 // the curvature formulas use hardware approximations of sqrt/rcp (relative
 // error ~1e-7, far inside the 1e-5 x range parity bound); tanh is CUDA's tanhf,
 // the function the reference's cp.tanh evaluates.
-__device__ __forceinline__ void pixel_products(const StencilArgs& A, const TileK& T, unsigned om, float p, float q,
-                                               float pz, float qz, float dxx, float dxy, float dyy, float dyx,
-                                               float* o) {
+struct Light {
+  float lx, ly, lz;
+  int slope_unit;
+};
+
+__device__ __forceinline__ void pixel_products(const Light& L, float sign_x, float sign_y, unsigned om, float p,
+                                               float q, float pz, float qz, float dxx, float dxy, float dyy,
+                                               float dyx, float* o) {
   if (om & (1u << FSG_OUT_HILLSHADE)) {
-    float e = pz * T.sign_x, nn = qz * T.sign_y;
-    float hs = fadd(fadd(-fmul(e, A.lx), -fmul(nn, A.ly)), A.lz) * rsqrtf(fadd(fadd(fmul(e, e), fmul(nn, nn)), 1.0f));
+    float e = pz * sign_x, nn = qz * sign_y;
+    float hs = fadd(fadd(-fmul(e, L.lx), -fmul(nn, L.ly)), L.lz) * rsqrtf(fadd(fadd(fmul(e, e), fmul(nn, nn)), 1.0f));
     o[FSG_OUT_HILLSHADE] = fminf(fmaxf(hs, 0.0f), 1.0f);
   }
   if (om & (1u << FSG_OUT_SLOPE)) {
     float g2 = fadd(fmul(p, p), fmul(q, q));
-    if (A.slope_unit == FSG_SLOPE_DEGREE) o[FSG_OUT_SLOPE] = atan_poly(sqrt_approx(g2)) * 57.295780181884765625f;
-    else o[FSG_OUT_SLOPE] = slope_value(p, q, A.slope_unit);
+    if (L.slope_unit == FSG_SLOPE_DEGREE) o[FSG_OUT_SLOPE] = atan_poly(sqrt_approx(g2)) * 57.295780181884765625f;
+    else o[FSG_OUT_SLOPE] = slope_value(p, q, L.slope_unit);
   }
   if (om & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) | (1u << FSG_OUT_CURV_PLANFORM) |
             (1u << FSG_OUT_CURV_PROFILE))) {
@@ -385,7 +391,8 @@ __device__ __forceinline__ void stage_pixels(const StencilArgs& A, const TileK& 
           qz = deriv(T.g1y, gy, T.wy0, T.wy1, [&](int o2) { return fmul(f[o2 * FC], z); });
         }
       }
-      pixel_products(A, T, om, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
+      const Light L{A.lx, A.ly, A.lz, A.slope_unit};
+      pixel_products(L, T.sign_x, T.sign_y, om, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
     }
 #pragma unroll
     for (int k = 0; k < FSG_STENCIL_NOUT; ++k) {
@@ -432,26 +439,19 @@ __global__ void __launch_bounds__(NT, FSG_STENCIL_MINB) stencil_kernel(const __g
     *x0_out = Tl.cx0 + bx * TX;
   };
 
-  Region<FR, FC> halo;
-  int t_cur = 0, y0 = 0, x0 = 0;
-  if (blockIdx.x < A.total_blocks) {
-    locate(blockIdx.x, &t_cur, &y0, &x0);
-    halo.issue(A, y0 - FHY, x0 - FHX);
-  }
   for (int blk = blockIdx.x; blk < A.total_blocks; blk += gridDim.x) {
+    if (A.block_flags && !A.block_flags[blk]) continue;  // the fast pass produced this block exactly
+    int t_cur, y0, x0;
+    locate(blk, &t_cur, &y0, &x0);
     const TileK& T = tiles[t_cur];
     const int fy0 = y0 - FHY, fx0 = x0 - FHX;
     const bool interior = fy0 >= T.wy0 && fy0 + FR <= T.wy1 && fx0 >= T.wx0 && fx0 + FC <= T.wx1;
 
     __syncthreads();  // the previous block is done with shared memory
+    Region<FR, FC> halo;
+    halo.issue(A, fy0, fx0);
     bool saw = halo.commit(A, T, F);
     const int any_nan = __syncthreads_or(saw);
-    // prefetch the next block's halo; its loads overlap this block's compute
-    int t_next = t_cur, y0n = y0, x0n = x0;
-    if (blk + (int)gridDim.x < A.total_blocks) {
-      locate(blk + gridDim.x, &t_next, &y0n, &x0n);
-      halo.issue(A, y0n - FHY, x0n - FHX);
-    }
 
     // NoData flags of this thread's 8 core pixels, before the fill rewrites F.
     unsigned nanbits = 0;
@@ -545,9 +545,177 @@ __global__ void __launch_bounds__(NT, FSG_STENCIL_MINB) stencil_kernel(const __g
     }
     if (interior) stage_pixels<CURV, true>(A, T, om, F, DX, DY, y0, x0, nanbits);
     else stage_pixels<CURV, false>(A, T, om, F, DX, DY, y0, x0, nanbits);
-    t_cur = t_next;
-    y0 = y0n;
-    x0 = x0n;
+  }
+}
+
+
+// ------------------------------------------------------------ fast pass
+// Streaming kernel for the common case: a warp owns a strip of SW = 28 output
+// columns and SH rows; lane l holds column x0 - 2 + l, walks down the rows
+// keeping f, dx, dy of the neighbouring rows in registers, and takes the
+// horizontal neighbours from warp shuffles (lanes 2..29 emit outputs).  No
+// shared memory, no barriers.  A unit that touches a window edge, and any
+// valid pixel whose stencil reaches NoData (NaN propagates into its
+// derivatives), flags its 32 x 64 block; the exact shared-memory kernel then
+// recomputes every flagged block (NaN fill, one-sided edge formulas).
+constexpr int SW = 28, SH = 64;
+
+struct FastTile {
+  int wy0, wx0, wy1, wx1, cy0, cx0, cy1, cx1, oy0, ox0;
+  int nstrip, unit0;   // strips across the core, first flat unit index
+  int nbx, block0;     // slow-pass block grid of this tile
+  float d1x, r1x, d1y, r1y, d2x, r2x, d2y, r2y, sx, sy;
+};
+
+struct FastArgs {
+  const float* raster;
+  long long ld;
+  float lx, ly, lz, z;
+  int z_is_one;
+  float ndf;
+  int has_nodata;
+  int slope_unit;
+  const FastTile* tiles;
+  int ntiles, total_units;
+  unsigned char* block_flags;
+  PlaneK planes[FSG_STENCIL_NOUT];
+};
+
+__device__ __forceinline__ float shfl_up1(float v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+__device__ __forceinline__ float shfl_dn1(float v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+
+// Marks every exact-pass block (32 x 64) overlapping rows [y0, y1) x cols [x0, x1).
+__device__ __forceinline__ void flag_blocks(const FastArgs& A, const FastTile& T, int y0, int y1, int x0, int x1) {
+  for (int by = (y0 - T.cy0) / 32; by <= (y1 - 1 - T.cy0) / 32; ++by)
+    for (int bx = (x0 - T.cx0) / 64; bx <= (x1 - 1 - T.cx0) / 64; ++bx) A.block_flags[T.block0 + by * T.nbx + bx] = 1;
+}
+
+template <bool CURV, unsigned OM>
+__global__ void __launch_bounds__(256) stencil_fast_kernel(const __grid_constant__ FastArgs A) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const bool hn = A.has_nodata != 0;
+  for (int u = warp; u < A.total_units; u += nwarps) {
+    int lo = 0, hi = A.ntiles - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (A.tiles[mid].unit0 <= u) lo = mid; else hi = mid - 1;
+    }
+    const FastTile& T = A.tiles[lo];
+    const int lu = u - T.unit0;
+    const int cy = lu / T.nstrip, sx = lu - (lu / T.nstrip) * T.nstrip;
+    // the last strip of a core is moved left to end at the core edge (it
+    // recomputes a few columns of its neighbour with identical values)
+    const int x0 = (T.cx1 - T.cx0 >= SW) ? min(T.cx0 + sx * SW, T.cx1 - SW) : T.cx0;
+    const int y0 = T.cy0 + cy * SH;
+    const int y1 = min(y0 + SH, T.cy1);
+    const int xo = min(x0 + SW, T.cx1);  // end of this strip's outputs
+    // stencil reach: rows y0-2 .. y1+1 and cols x0-2 .. x0+29 must be strictly
+    // inside the window (no one-sided formulas)
+    const bool interior = y0 - 2 >= T.wy0 && y1 + 2 <= T.wy1 - 0 && x0 - 2 >= T.wx0 && x0 + SW + 2 <= T.wx1;
+    const int x = x0 - 2 + lane;
+    const bool out_lane = lane >= 2 && lane < 2 + SW && x < xo;
+    if (!interior) {
+      if (lane == 0) flag_blocks(A, T, y0, y1, x0, xo);
+      continue;
+    }
+    const float* col = A.raster + x;
+    auto ld = [&](int y) {
+      float v = __ldg(col + (long long)y * A.ld);
+      return is_nodata(v, A.ndf, hn) ? __int_as_float(0x7fc00000) : v;
+    };
+    // per-plane output row pointers
+    char* optr[FSG_STENCIL_NOUT];
+    long long ostep[FSG_STENCIL_NOUT];
+#pragma unroll
+    for (int k = 0; k < FSG_STENCIL_NOUT; ++k) {
+      if (!(OM & (1u << k))) continue;
+      const PlaneK& P = A.planes[k];
+      const int esz = P.dtype == FSG_F32 ? 4 : (P.dtype == FSG_I16 ? 2 : 1);
+      optr[k] = static_cast<char*>(P.ptr) +
+                ((long long)(T.oy0 + y0 - T.cy0) * P.ld + (T.ox0 + x - T.cx0)) * esz;
+      ostep[k] = P.ld * esz;
+    }
+    // rolling state: f at rows y-2..y+2 (CURV) or y-1..y+1, dx/dy at y-1..y+1,
+    // and a queue of the next PF rows already in flight
+    constexpr int PF = 8;
+    const int last = CURV ? y1 + 1 : y1;  // last row the unit reads
+    float fm2 = CURV ? ld(y0 - 2) : 0.f, fm1 = ld(y0 - 1), f0 = ld(y0), fp1 = ld(y0 + 1);
+    float fp2 = CURV ? ld(y0 + 2) : 0.f;
+    const int qstart = CURV ? y0 + 3 : y0 + 2;
+    float qv[PF];
+#pragma unroll
+    for (int k = 0; k < PF; ++k) qv[k] = (qstart + k <= last) ? ld(qstart + k) : 0.f;
+    auto dxof = [&](float f) { return div_by(fsub(shfl_dn1(f), shfl_up1(f)), T.d1x, T.r1x); };
+    float dxm1 = 0.f, dym1 = 0.f, dx0 = 0.f, dy0 = 0.f, dxp1 = 0.f, dyp1 = 0.f;
+    if (CURV) {
+      dxm1 = dxof(fm1);
+      dym1 = div_by(fsub(f0, fm2), T.d1y, T.r1y);
+      dx0 = dxof(f0);
+      dy0 = div_by(fsub(fp1, fm1), T.d1y, T.r1y);
+    }
+    bool bad = false;
+#pragma unroll 1
+    for (int y = y0; y < y1; ++y) {
+      float p, q, dxx = 0.f, dxy = 0.f, dyy = 0.f, dyx = 0.f;
+      if (CURV) {
+        dxp1 = dxof(fp1);
+        dyp1 = div_by(fsub(fp2, f0), T.d1y, T.r1y);
+        p = dx0;
+        q = dy0;
+        dxx = div_by(fsub(shfl_dn1(dx0), shfl_up1(dx0)), T.d2x, T.r2x);
+        dxy = div_by(fsub(dxp1, dxm1), T.d2y, T.r2y);
+        dyy = div_by(fsub(dyp1, dym1), T.d2y, T.r2y);
+        if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = div_by(fsub(shfl_dn1(dy0), shfl_up1(dy0)), T.d2x, T.r2x);
+      } else {
+        p = dxof(f0);
+        q = div_by(fsub(fp1, fm1), T.d1y, T.r1y);
+      }
+      float pz = p, qz = q;
+      if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) {
+        const float zf = A.z;
+        pz = div_by(fsub(shfl_dn1(fmul(f0, zf)), shfl_up1(fmul(f0, zf))), T.d1x, T.r1x);
+        qz = div_by(fsub(fmul(fp1, zf), fmul(fm1, zf)), T.d1y, T.r1y);
+      }
+      float o[FSG_STENCIL_NOUT];
+      const bool valid = f0 == f0;
+      float chk = p + q + pz + qz;
+      if (CURV) chk += dxx + dxy + dyy + dyx;
+      if (out_lane && valid && chk != chk) bad = true;
+      if (valid) {
+        const Light L{A.lx, A.ly, A.lz, A.slope_unit};
+        pixel_products(L, T.sx, T.sy, OM, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
+      } else {
+#pragma unroll
+        for (int k = 0; k < FSG_STENCIL_NOUT; ++k) o[k] = __int_as_float(0x7fc00000);
+      }
+      if (out_lane) {
+#pragma unroll
+        for (int k = 0; k < FSG_STENCIL_NOUT; ++k) {
+          if (!(OM & (1u << k))) continue;
+          const PlaneK& P = A.planes[k];
+          char* dst = optr[k];
+          if (P.dtype == FSG_F32) *reinterpret_cast<float*>(dst) = o[k];
+          else if (P.dtype == FSG_U8) *reinterpret_cast<uint8_t*>(dst) = (uint8_t)(int)quantize(o[k], P.qa, P.qb, P.qmin, P.qmax);
+          else *reinterpret_cast<int16_t*>(dst) = (int16_t)(int)quantize(o[k], P.qa, P.qb, P.qmin, P.qmax);
+          optr[k] = dst + ostep[k];
+        }
+      }
+      // slide one row down; the queue head enters the window, a new row is requested
+      const float nxt = qv[0];
+#pragma unroll
+      for (int k = 0; k + 1 < PF; ++k) qv[k] = qv[k + 1];
+      const int ynew = qstart + (y - y0) + PF;
+      qv[PF - 1] = (ynew <= last) ? ld(ynew) : 0.f;
+      if (CURV) {
+        fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2; fp2 = nxt;
+        dxm1 = dx0; dym1 = dy0; dx0 = dxp1; dy0 = dyp1;
+      } else {
+        fm1 = f0; f0 = fp1; fp1 = nxt;
+      }
+    }
+    if (__ballot_sync(0xffffffffu, bad) && lane == 0) flag_blocks(A, T, y0, y1, x0, xo);
   }
 }
 
@@ -709,26 +877,83 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
   const bool curv = (outmask & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) |
                                 (1u << FSG_OUT_CURV_PLANFORM) | (1u << FSG_OUT_CURV_PROFILE))) != 0;
   auto kern = curv ? stencil_kernel<true, 0u> : stencil_kernel<false, 0u>;
+  void (*fast)(FastArgs) = nullptr;
   constexpr unsigned HS = 1u << FSG_OUT_HILLSHADE, SL = 1u << FSG_OUT_SLOPE, CM = 1u << FSG_OUT_CURV_MEAN,
                      CG = 1u << FSG_OUT_CURV_GAUSSIAN, CP = 1u << FSG_OUT_CURV_PLANFORM,
-                     CR = 1u << FSG_OUT_CURV_PROFILE;
+                     CR = 1u << FSG_OUT_CURV_PROFILE, DXY = (1u << FSG_OUT_DX) | (1u << FSG_OUT_DY);
   switch (outmask) {
-    case HS | SL | CP | CR: kern = stencil_kernel<true, HS | SL | CP | CR>; break;
-    case HS | SL | CM | CG | CP | CR: kern = stencil_kernel<true, HS | SL | CM | CG | CP | CR>; break;
-    case HS: kern = stencil_kernel<false, HS>; break;
-    case SL: kern = stencil_kernel<false, SL>; break;
-    case HS | SL: kern = stencil_kernel<false, HS | SL>; break;
-    case CM: kern = stencil_kernel<true, CM>; break;
-    case CG: kern = stencil_kernel<true, CG>; break;
-    case CP: kern = stencil_kernel<true, CP>; break;
-    case CR: kern = stencil_kernel<true, CR>; break;
+#define FSG_CASE(M, C)                        \
+  case (M):                                   \
+    kern = stencil_kernel<C, (M)>;            \
+    fast = stencil_fast_kernel<C, (M)>;       \
+    break;
+    FSG_CASE(HS | SL | CP | CR, true)
+    FSG_CASE(HS | SL | CM | CG | CP | CR, true)
+    FSG_CASE(HS, false)
+    FSG_CASE(SL, false)
+    FSG_CASE(HS | SL, false)
+    FSG_CASE(CM, true)
+    FSG_CASE(CG, true)
+    FSG_CASE(CP, true)
+    FSG_CASE(CR, true)
+    FSG_CASE(DXY, false)
+#undef FSG_CASE
     default: break;
   }
   FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+  FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int per_sm = 0;
   FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, SMEM_BYTES));
   if (per_sm < 1) per_sm = 1;
   int grid = std::min(total, di.sms * per_sm);
+  StreamScratch flag_scratch, fast_tiles;
+  if (fast) {
+    // fast streaming pass over every tile; flags the blocks it cannot produce exactly
+    std::vector<FastTile> ft;
+    int units = 0;
+    for (const TileK& k : tk) {
+      FastTile f;
+      f.wy0 = k.wy0; f.wx0 = k.wx0; f.wy1 = k.wy1; f.wx1 = k.wx1;
+      f.cy0 = k.cy0; f.cx0 = k.cx0; f.cy1 = k.cy1; f.cx1 = k.cx1;
+      f.oy0 = k.oy0; f.ox0 = k.ox0;
+      int cw = k.cx1 - k.cx0, ch = k.cy1 - k.cy0;
+      f.nstrip = std::max(1, (cw + SW - 1) / SW);
+      f.unit0 = units;
+      units += f.nstrip * ((ch + SH - 1) / SH);
+      f.nbx = k.nbx;
+      f.block0 = k.block0;
+      f.d1x = k.g1x.d2; f.r1x = k.g1x.rcp; f.d1y = k.g1y.d2; f.r1y = k.g1y.rcp;
+      f.d2x = k.c2x.d2; f.r2x = k.c2x.rcp; f.d2y = k.c2y.d2; f.r2y = k.c2y.rcp;
+      f.sx = k.sign_x; f.sy = k.sign_y;
+      ft.push_back(f);
+    }
+    st = flag_scratch.alloc((size_t)total, s);
+    if (st) return st;
+    FSG_CUDA(cudaMemsetAsync(flag_scratch.ptr, 0, (size_t)total, s));
+    st = fast_tiles.alloc(sizeof(FastTile) * ft.size(), s);
+    if (st) return st;
+    FSG_CUDA(cudaMemcpyAsync(fast_tiles.ptr, ft.data(), sizeof(FastTile) * ft.size(), cudaMemcpyHostToDevice, s));
+    FastArgs F;
+    std::memset(&F, 0, sizeof(F));
+    F.raster = A.raster;
+    F.ld = A.ld;
+    F.lx = A.lx; F.ly = A.ly; F.lz = A.lz; F.z = A.z;
+    F.z_is_one = A.z_is_one;
+    F.ndf = A.ndf;
+    F.has_nodata = A.has_nodata;
+    F.slope_unit = A.slope_unit;
+    F.tiles = static_cast<const FastTile*>(fast_tiles.ptr);
+    F.ntiles = (int)ft.size();
+    F.total_units = units;
+    F.block_flags = static_cast<unsigned char*>(flag_scratch.ptr);
+    std::copy(A.planes, A.planes + FSG_STENCIL_NOUT, F.planes);
+    int fper = 0;
+    FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fper, fast, 256, 0));
+    int fgrid = std::min((units + 7) / 8, di.sms * std::max(1, fper));
+    fast<<<fgrid, 256, 0, s>>>(F);
+    FSG_LAUNCHED(1);
+    A.block_flags = static_cast<unsigned char*>(flag_scratch.ptr);
+  }
   kern<<<grid, NT, SMEM_BYTES, s>>>(A);
   FSG_LAUNCHED(1);
   return FSG_OK;
