@@ -77,10 +77,13 @@ def test_topousm_overview_split_given_stats(loop):
     dem = _dem(H, W, 95, disks=3)
     radii = [2, 8, 32, 128, 512]
     wts = [16 / 31, 8 / 31, 4 / 31, 2 / 31, 1 / 31]
-    res = loop.process_dem_array(torch.from_numpy(dem).cuda(), "topousm_fast", tile_size=256, pixel_size=10.0,
-                                 radii=radii, weights=wts, global_stats=(6.0,))
     # threshold max(256, 256//16) = 256 -> 512 is a large radius; overview factor 1 (raster < 2048 px)
     field = R.coarse_field(dem, large_radii=[512], large_weights=[1 / 31], decimation=1.0)
+    scale = R.topousm_scale(R.topousm_tile(dem, radii=None, weights=None, pixel_size=10.0, coarse=field,
+                                           small_radii=radii[:4], small_weights=wts[:4], w_large=1 / 31,
+                                           offset=(0, 0), full_shape=(H, W)))[0]
+    res = loop.process_dem_array(torch.from_numpy(dem).cuda(), "topousm_fast", tile_size=256, pixel_size=10.0,
+                                 radii=radii, weights=wts, global_stats=(scale,))
     pad = res.padding
     assert pad == 160
     got = to_np(res.output)
@@ -89,7 +92,7 @@ def test_topousm_overview_split_given_stats(loop):
         raw = R.topousm_tile(win, radii=None, weights=None, pixel_size=10.0, coarse=field,
                              small_radii=radii[:4], small_weights=wts[:4], w_large=1 / 31, offset=(wy, wx),
                              full_shape=(H, W))
-        ref = R.topousm_normalize(raw, (6.0,))[cy - wy:cy - wy + ch, cx - wx:cx - wx + cw]
+        ref = R.topousm_normalize(raw, (scale,))[cy - wy:cy - wy + ch, cx - wx:cx - wx + cw]
         assert_close_range(got[cy:cy + ch, cx:cx + cw], ref, 2 * 1.176, f"tile {ty},{tx}")
 
 
