@@ -110,6 +110,8 @@ _SIGNATURES = {
     "fsg_percentile": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_double), C.c_int32,
                                  C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_void_p]),
     "fsg_std": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.c_void_p]),
+    "fsg_percentile_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_double), C.c_int32,
+                                         C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_void_p]),
     "fsg_openness": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
                                C.POINTER(OpennessParams), C.POINTER(Plane), C.c_void_p, C.c_int64, C.c_void_p]),
     "fsg_openness_offsets": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32),

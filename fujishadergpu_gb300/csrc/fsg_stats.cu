@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "fsg_common.cuh"
@@ -272,6 +273,105 @@ extern "C" int fsg_std(const float* values_dev, int64_t n, double* out, void* st
     }
     if (pass == 0) centre = h[0] / (double)c;
     else *out = std::sqrt(h[1] / (double)c);
+  }
+  return FSG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Percentiles without any allocation.
+//
+// Some callers cannot allocate device memory during a run: a host application
+// whose GPU memory is owned and budgeted by its own pool (every byte must come
+// from that pool), or a latency-critical caller that cannot accept the
+// implicit device synchronisation cudaMalloc / cudaFree may cause.  For them
+// fsg_percentile_noalloc keeps its scratch (the radix-select state, the valid
+// count and the selected keys) in the fixed array below, which every GPU that
+// loads this library holds until the process exits.
+namespace fsg {
+namespace {
+
+constexpr int kNoAllocMaxQ = 16;  // at most 16 percentiles per call (32 ranks)
+struct NoAllocScratch {
+  SelState state;
+  unsigned long long count;
+  unsigned keys[2 * kNoAllocMaxQ];
+};
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[64] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once per
+// device (host code only has a stand-in for the symbol, not its address).
+int noalloc_scratch(NoAllocScratch** out) {
+  int dev = 0;
+  FSG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(FSG_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = static_cast<NoAllocScratch*>(g_noalloc_ptr[dev]);
+  return FSG_OK;
+}
+
+}  // namespace
+}  // namespace fsg
+
+extern "C" int fsg_percentile_noalloc(const float* values_dev, int64_t n, int32_t abs_values, const double* q,
+                                      int32_t nq, double* out, int64_t* nvalid, void* stream) {
+  if ((n > 0 && !values_dev) || nq < 0 || (nq > 0 && (!q || !out))) return fail(FSG_ERR_INVALID, "null argument");
+  if (nq > kNoAllocMaxQ)
+    return fail(FSG_ERR_WORKSPACE, "fsg_percentile_noalloc takes at most %d percentiles per call, got %d",
+                kNoAllocMaxQ, nq);
+  for (int i = 0; i < nq; ++i)
+    if (!(q[i] >= 0.0 && q[i] <= 100.0)) return fail(FSG_ERR_INVALID, "percentile %g outside [0, 100]", q[i]);
+  cudaStream_t s = (cudaStream_t)stream;
+  DeviceInfo di;
+  int st = device_info(&di);
+  if (st) return st;
+  NoAllocScratch* scr = nullptr;
+  st = noalloc_scratch(&scr);
+  if (st) return st;
+  int grid = (int)std::max<long long>(1, std::min<long long>((n + NT - 1) / NT, (long long)di.sms * 8));
+  FSG_CUDA(cudaMemsetAsync(&scr->count, 0, sizeof(unsigned long long), s));  // the array keeps the last call's data
+  if (n > 0) {
+    count_valid<<<grid, NT, 0, s>>>(values_dev, n, abs_values, &scr->count);
+    FSG_LAUNCHED(1);
+  }
+  unsigned long long nv = 0;
+  FSG_CUDA(cudaMemcpyAsync(&nv, &scr->count, sizeof(nv), cudaMemcpyDeviceToHost, s));
+  FSG_CUDA(cudaStreamSynchronize(s));
+  if (nvalid) *nvalid = (int64_t)nv;
+  if (nv == 0) {
+    for (int i = 0; i < nq; ++i) out[i] = std::nan("");
+    return FSG_OK;
+  }
+  unsigned long long ranks[2 * kNoAllocMaxQ];
+  LinearPick picks[kNoAllocMaxQ];
+  int nr = 0;
+  for (int i = 0; i < nq; ++i) {
+    picks[i] = linear_pick((long long)nv, q[i]);
+    ranks[nr++] = (unsigned long long)picks[i].lo;
+    ranks[nr++] = (unsigned long long)picks[i].hi;
+  }
+  std::sort(ranks, ranks + nr);
+  nr = (int)(std::unique(ranks, ranks + nr) - ranks);
+  for (int r = 0; r < nr; ++r) {
+    st = select_rank(values_dev, n, abs_values, ranks[r], &scr->state, grid, s);  // init_state clears the state
+    if (st) return st;
+    FSG_CUDA(cudaMemcpyAsync(&scr->keys[r], &scr->state.prefix, sizeof(unsigned), cudaMemcpyDeviceToDevice, s));
+  }
+  unsigned keys[2 * kNoAllocMaxQ];
+  FSG_CUDA(cudaMemcpyAsync(keys, scr->keys, sizeof(unsigned) * nr, cudaMemcpyDeviceToHost, s));
+  FSG_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < nq; ++i) {
+    int ia = (int)(std::lower_bound(ranks, ranks + nr, (unsigned long long)picks[i].lo) - ranks);
+    int ib = (int)(std::lower_bound(ranks, ranks + nr, (unsigned long long)picks[i].hi) - ranks);
+    out[i] = lerp_numpy(key_to_float(keys[ia]), key_to_float(keys[ib]), picks[i].gamma);
   }
   return FSG_OK;
 }

@@ -185,6 +185,21 @@ int fsg_percentile(const float* values_dev, int64_t n, int32_t abs_values, const
  * (the fallback scale of _normalization.py:30).  Synchronises `stream`. */
 int fsg_std(const float* values_dev, int64_t n, double* out, void* stream);
 
+/* Same result as fsg_percentile, but allocates nothing.  It has no counterpart in
+ * the reference.  It is for callers that cannot allocate device memory during a
+ * run: an application whose GPU memory is owned and budgeted by its own pool, or
+ * a latency-critical caller that cannot accept the implicit device
+ * synchronisation cudaMalloc / cudaFree may cause.  Its scratch (~17 KB) is a
+ * fixed array that every GPU loading libfsg.so holds until the process exits.
+ * Limits: at most 16 percentiles per call (nq > 16 -> FSG_ERR_WORKSPACE); any n.
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller.
+ * Synchronises `stream`. */
+int fsg_percentile_noalloc(const float* values_dev, int64_t n, int32_t abs_values, const double* q, int32_t nq,
+                           double* out, int64_t* nvalid, void* stream);
+
 /* ----------------------------------------------------------------- encoding */
 /* out = (v - offset) / scale in float32 (scale <= 0: unchanged), max(., 0) when
  * clamp_min0, NaN kept; stored as float32 or int16/uint8 codes.  Replaces
