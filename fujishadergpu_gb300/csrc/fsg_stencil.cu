@@ -45,7 +45,7 @@ constexpr int INLINE_TILES = 8;
 
 constexpr size_t SMEM_F = sizeof(float) * FR * FC;
 constexpr size_t SMEM_D = sizeof(float) * 2 * DR * DC;
-constexpr size_t SMEM_FILL = sizeof(float) * (WR * WC + 2 * FR * WC) + FR * FC;
+constexpr size_t SMEM_FILL = sizeof(float) * (WR * WC + 2 * FR * WC) + 4 * sizeof(unsigned) * FR * 3;
 constexpr size_t SMEM_BYTES = SMEM_F + (SMEM_D > SMEM_FILL ? SMEM_D : SMEM_FILL);
 
 // np.gradient constants along one axis for one step size (float32, as NumPy
@@ -85,7 +85,7 @@ struct StencilArgs {
   int has_nodata;
   int slope_unit;
   unsigned outmask;
-  double gw[5];             // scipy Gaussian(sigma=1, radius 4) weights, w[0] = centre
+  float gw_hi[5], gw_lo[5];  // scipy Gaussian(sigma=1, radius 4) weights as float-float, [0] = centre
   unsigned char* block_flags;  // per (tile, block): 1 = needs the exact shared-memory pass; NULL = all
   PlaneK planes[FSG_STENCIL_NOUT];
   TileK inl[INLINE_TILES];
@@ -234,15 +234,44 @@ struct Region {
   }
 };
 
-// Separable 9-tap Gaussian in float64 (scipy's symmetric correlate1d order),
-// result rounded to float32.
-__device__ __forceinline__ double gsum(const double* w, const double* x) {
-  double acc = __dmul_rn(x[4], w[0]);
-  acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(x[0], x[8]), w[4]));
-  acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(x[1], x[7]), w[3]));
-  acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(x[2], x[6]), w[2]));
-  acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(x[3], x[5]), w[1]));
-  return acc;
+// Float-float ("double-single") arithmetic on the FP32 pipes: a value is
+// hi + lo with |lo| <= ulp(hi)/2, about 48 significant bits.  Used for the
+// NaN-fill Gaussian, which scipy evaluates in float64: the float-float sum
+// rounds to the same float32 as scipy's float64 sum except when the exact value
+// lies within ~2^-44 (relative) of a float32 rounding boundary.  (GB300's FP64
+// rate is a small fraction of its FP32 rate.)
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ FF fast_two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  FF s = two_sum(a.hi, b.hi);
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+// scipy's symmetric 9-tap correlate1d, sum x[4]*w0 + (x[0]+x[8])*w4 + ...
+// + (x[3]+x[5])*w1 in float-float, rounded to float32.
+__device__ __forceinline__ float gsum_ff(const FF* w, const float* x) {
+  FF acc = ff_mul({x[4], 0.f}, w[0]);
+#pragma unroll
+  for (int k = 4; k >= 1; --k) acc = ff_add(acc, ff_mul(two_sum(x[4 - k], x[4 + k]), w[k]));
+  return __fadd_rn(acc.hi, acc.lo);
 }
 
 __device__ __forceinline__ void store1(const PlaneK& P, long long off, float v) {
@@ -418,7 +447,10 @@ __global__ void __launch_bounds__(NT, FSG_STENCIL_MINB) stencil_kernel(const __g
   float* W = reinterpret_cast<float*>(U);                          // [WR][WC] (fill path)
   float* VV = W + WR * WC;                                         // [FR][WC]
   float* VW = VV + FR * WC;                                        // [FR][WC]
-  unsigned char* need = reinterpret_cast<unsigned char*>(VW + FR * WC);  // [FR][FC]
+  unsigned* vmask = reinterpret_cast<unsigned*>(VW + FR * WC);    // [FR][3] valid cells (fill path)
+  unsigned* nmask = vmask + FR * 3;                                // [FR][3] NaN cells
+  unsigned* needm = nmask + FR * 3;                                // [FR][3] needed NaN cells
+  unsigned* wantm = needm + FR * 3;                                // [FR][3] wanted axis-0 columns
 
   const TileK* tiles = A.ntiles <= INLINE_TILES ? A.inl : A.tiles_dev;
   const int tid = threadIdx.x;
@@ -466,73 +498,99 @@ __global__ void __launch_bounds__(NT, FSG_STENCIL_MINB) stencil_kernel(const __g
     }
 
     if (any_nan) {
-      // (a) NaN cells of the window whose fill value can reach a valid pixel
-      //     (a valid window cell within Chebyshev distance 3).
-      for (int i = tid; i < FR * FC; i += NT) {
-        int r = i / FC, c = i - (i / FC) * FC;
-        int gy = fy0 + r, gx = fx0 + c;
-        unsigned char nd = 0;
-        if (gy >= T.wy0 && gy < T.wy1 && gx >= T.wx0 && gx < T.wx1 && F[i] != F[i]) {
-          for (int dr = -3; dr <= 3 && !nd; ++dr) {
-            int rr = r + dr, yy = gy + dr;
-            if (rr < 0 || rr >= FR || yy < T.wy0 || yy >= T.wy1) continue;
-            for (int dc = -3; dc <= 3; ++dc) {
-              int cc = c + dc, xx = gx + dc;
-              if (cc < 0 || cc >= FC || xx < T.wx0 || xx >= T.wx1) continue;
-              float v = F[rr * FC + cc];
-              if (v == v) { nd = 1; break; }
-            }
+      // (a) row bitmasks over the 72 staged columns: in-window valid cells and
+      //     in-window NaN cells
+      for (int i = tid; i < FR * 3; i += NT) {
+        const int r = i / 3, k = i - (i / 3) * 3;
+        const int gy = fy0 + r;
+        unsigned vb = 0, nb = 0;
+        if (gy >= T.wy0 && gy < T.wy1) {
+          for (int b = 0; b < 32; ++b) {
+            const int c = 32 * k + b, gx = fx0 + c;
+            if (c >= FC || gx < T.wx0 || gx >= T.wx1) continue;
+            const float v = F[r * FC + c];
+            if (v == v) vb |= 1u << b; else nb |= 1u << b;
           }
         }
-        need[i] = nd;
+        vmask[i] = vb;
+        nmask[i] = nb;
       }
-      // (b) the wider region the 9x9 Gaussian reaches
+      __syncthreads();
+      // (b) needed NaN cells: a valid cell within Chebyshev distance 3 (whose
+      //     stencil may read the fill value); wanted axis-0 columns: within 8
+      //     columns to the right of a needed cell (in the wide region's columns)
+      for (int r = tid; r < FR; r += NT) {
+        unsigned long long dil_lo = 0, dil_hi = 0;  // 96-bit OR of valid rows r-3..r+3, dilated by 3 columns
+        for (int dr = -3; dr <= 3; ++dr) {
+          const int rr = r + dr;
+          if (rr < 0 || rr >= FR) continue;
+          dil_lo |= (unsigned long long)vmask[rr * 3] | ((unsigned long long)vmask[rr * 3 + 1] << 32);
+          dil_hi |= vmask[rr * 3 + 2];
+        }
+        unsigned long long d_lo = dil_lo, d_hi = dil_hi;
+        for (int s1 = 1; s1 <= 3; ++s1) {
+          d_lo |= (dil_lo << s1) | (dil_lo >> s1) | (dil_hi << (64 - s1));
+          d_hi |= (dil_hi << s1) | (dil_hi >> s1) | (dil_lo >> (64 - s1));
+        }
+        const unsigned long long n_lo = ((unsigned long long)nmask[r * 3] | ((unsigned long long)nmask[r * 3 + 1] << 32)) & d_lo;
+        const unsigned long long n_hi = nmask[r * 3 + 2] & d_hi;
+        needm[r * 3] = (unsigned)n_lo;
+        needm[r * 3 + 1] = (unsigned)(n_lo >> 32);
+        needm[r * 3 + 2] = (unsigned)n_hi;
+        unsigned long long w_lo = 0, w_hi = 0;  // W column xc = F column c + d, d = 0..8
+        for (int d = 0; d <= 8; ++d) {
+          w_lo |= n_lo << d;
+          w_hi |= (n_hi << d) | (d ? (n_lo >> (64 - d)) : 0ull);
+        }
+        wantm[r * 3] = (unsigned)w_lo;
+        wantm[r * 3 + 1] = (unsigned)(w_lo >> 32);
+        wantm[r * 3 + 2] = (unsigned)w_hi;
+      }
+      // (c) the wider region the 9x9 Gaussian reaches
       {
         Region<WR, WC> wide;
         wide.issue(A, y0 - WHY, x0 - WHX);
         wide.commit(A, T, W);
       }
       __syncthreads();
-      double gw[5];
+      FF gw[5];
 #pragma unroll
-      for (int j = 0; j < 5; ++j) gw[j] = A.gw[j];
-      // (c) axis-0 pass (values and valid weights) where a needed cell of the
-      //     same row lies within 4 columns (nearest-mode clamping at window edges)
+      for (int j = 0; j < 5; ++j) gw[j] = {A.gw_hi[j], A.gw_lo[j]};
+      // (d) axis-0 pass (values and valid weights) at the wanted columns,
+      //     'nearest' clamping at the window rows
       for (int i = tid; i < FR * WC; i += NT) {
-        int r = i / WC, xc = i - (i / WC) * WC;
-        int gy = fy0 + r, gx = x0 - WHX + xc;
+        const int r = i / WC, xc = i - (i / WC) * WC;
+        if (!((wantm[r * 3 + (xc >> 5)] >> (xc & 31)) & 1u)) continue;
+        const int gy = fy0 + r, gx = x0 - WHX + xc;
         if (gy < T.wy0 || gy >= T.wy1 || gx < T.wx0 || gx >= T.wx1) continue;
-        bool want = false;
-        for (int c = max(0, xc - 8); c <= min(FC - 1, xc) && !want; ++c) want = need[r * FC + c] != 0;
-        if (!want) continue;
-        double xv[9], xw[9];
+        float xv[9], xw[9];
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
-          int yy = min(max(gy + j - 4, T.wy0), T.wy1 - 1);
-          float v = W[(yy - (y0 - WHY)) * WC + xc];
-          bool ok = v == v;
-          xv[j] = ok ? (double)v : 0.0;
-          xw[j] = ok ? 1.0 : 0.0;
+          const int yy = min(max(gy + j - 4, T.wy0), T.wy1 - 1);
+          const float v = W[(yy - (y0 - WHY)) * WC + xc];
+          const bool ok = v == v;
+          xv[j] = ok ? v : 0.f;
+          xw[j] = ok ? 1.f : 0.f;
         }
-        VV[r * WC + xc] = (float)gsum(gw, xv);
-        VW[r * WC + xc] = (float)gsum(gw, xw);
+        VV[r * WC + xc] = gsum_ff(gw, xv);
+        VW[r * WC + xc] = gsum_ff(gw, xw);
       }
       __syncthreads();
-      // (d) axis-1 pass and the normalised fill value
+      // (e) axis-1 pass and the normalised fill value of each needed cell
       for (int i = tid; i < FR * FC; i += NT) {
-        if (!need[i]) continue;
-        int r = i / FC, c = i - (i / FC) * FC;
-        int gx = fx0 + c;
-        double xv[9], xw[9];
+        const int r = i / FC, c = i - (i / FC) * FC;
+        if (!((needm[r * 3 + (c >> 5)] >> (c & 31)) & 1u)) continue;
+        const int gx = fx0 + c;
+        float xv[9], xw[9];
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
-          int xx = min(max(gx + j - 4, T.wx0), T.wx1 - 1);
-          int xc = xx - (x0 - WHX);
-          xv[j] = (double)VV[r * WC + xc];
-          xw[j] = (double)VW[r * WC + xc];
+          const int xx = min(max(gx + j - 4, T.wx0), T.wx1 - 1);
+          const int xc = xx - (x0 - WHX);
+          xv[j] = VV[r * WC + xc];
+          xw[j] = VW[r * WC + xc];
         }
-        float sv = (float)gsum(gw, xv);
-        float sw = (float)gsum(gw, xw);
+        const float sv = gsum_ff(gw, xv);
+        const float sw = gsum_ff(gw, xw);
         F[i] = sw > 0.0f ? __fdiv_rn(sv, sw) : 0.0f;
       }
       __syncthreads();
@@ -590,12 +648,13 @@ __device__ __forceinline__ void flag_blocks(const FastArgs& A, const FastTile& T
     for (int bx = (x0 - T.cx0) / 64; bx <= (x1 - 1 - T.cx0) / 64; ++bx) A.block_flags[T.block0 + by * T.nbx + bx] = 1;
 }
 
-template <bool CURV, unsigned OM>
+template <bool CURV, unsigned OM, bool ALLF32>
 __global__ void __launch_bounds__(256) stencil_fast_kernel(const __grid_constant__ FastArgs A) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const bool hn = A.has_nodata != 0;
+  const Light L{A.lx, A.ly, A.lz, A.slope_unit};
   for (int u = warp; u < A.total_units; u += nwarps) {
     int lo = 0, hi = A.ntiles - 1;
     while (lo < hi) {
@@ -611,44 +670,41 @@ __global__ void __launch_bounds__(256) stencil_fast_kernel(const __grid_constant
     const int y0 = T.cy0 + cy * SH;
     const int y1 = min(y0 + SH, T.cy1);
     const int xo = min(x0 + SW, T.cx1);  // end of this strip's outputs
-    // stencil reach: rows y0-2 .. y1+1 and cols x0-2 .. x0+29 must be strictly
-    // inside the window (no one-sided formulas)
-    const bool interior = y0 - 2 >= T.wy0 && y1 + 2 <= T.wy1 - 0 && x0 - 2 >= T.wx0 && x0 + SW + 2 <= T.wx1;
-    const int x = x0 - 2 + lane;
-    const bool out_lane = lane >= 2 && lane < 2 + SW && x < xo;
+    // stencil reach: rows y0-2 .. y1+1 and cols x0-2 .. x0+29 strictly inside
+    // the window, so every derivative is a central difference
+    const bool interior = y0 - 2 >= T.wy0 && y1 + 2 <= T.wy1 && x0 - 2 >= T.wx0 && x0 + SW + 2 <= T.wx1;
     if (!interior) {
       if (lane == 0) flag_blocks(A, T, y0, y1, x0, xo);
       continue;
     }
+    const int x = x0 - 2 + lane;
+    const bool out_lane = lane >= 2 && lane < 2 + SW && x < xo;
     const float* col = A.raster + x;
     auto ld = [&](int y) {
       float v = __ldg(col + (long long)y * A.ld);
       return is_nodata(v, A.ndf, hn) ? __int_as_float(0x7fc00000) : v;
     };
-    // per-plane output row pointers
     char* optr[FSG_STENCIL_NOUT];
     long long ostep[FSG_STENCIL_NOUT];
 #pragma unroll
     for (int k = 0; k < FSG_STENCIL_NOUT; ++k) {
       if (!(OM & (1u << k))) continue;
       const PlaneK& P = A.planes[k];
-      const int esz = P.dtype == FSG_F32 ? 4 : (P.dtype == FSG_I16 ? 2 : 1);
-      optr[k] = static_cast<char*>(P.ptr) +
-                ((long long)(T.oy0 + y0 - T.cy0) * P.ld + (T.ox0 + x - T.cx0)) * esz;
+      const int esz = ALLF32 ? 4 : (P.dtype == FSG_F32 ? 4 : (P.dtype == FSG_I16 ? 2 : 1));
+      optr[k] = static_cast<char*>(P.ptr) + ((long long)(T.oy0 + y0 - T.cy0) * P.ld + (T.ox0 + x - T.cx0)) * esz;
       ostep[k] = P.ld * esz;
     }
-    // rolling state: f at rows y-2..y+2 (CURV) or y-1..y+1, dx/dy at y-1..y+1,
-    // and a queue of the next PF rows already in flight
-    constexpr int PF = 8;
-    const int last = CURV ? y1 + 1 : y1;  // last row the unit reads
+    // sliding window: f at rows y-2..y+2 (CURV) / y-1..y+1, dx/dy at y-1..y+1
+    constexpr int G = 8;
+    const int last = CURV ? y1 + 1 : y1;          // last row read
+    const int first_q = CURV ? y0 + 3 : y0 + 2;   // first row delivered through the group buffer
     float fm2 = CURV ? ld(y0 - 2) : 0.f, fm1 = ld(y0 - 1), f0 = ld(y0), fp1 = ld(y0 + 1);
     float fp2 = CURV ? ld(y0 + 2) : 0.f;
-    const int qstart = CURV ? y0 + 3 : y0 + 2;
-    float qv[PF];
+    float cur[G];
 #pragma unroll
-    for (int k = 0; k < PF; ++k) qv[k] = (qstart + k <= last) ? ld(qstart + k) : 0.f;
+    for (int k = 0; k < G; ++k) cur[k] = (first_q + k <= last) ? ld(first_q + k) : 0.f;
     auto dxof = [&](float f) { return div_by(fsub(shfl_dn1(f), shfl_up1(f)), T.d1x, T.r1x); };
-    float dxm1 = 0.f, dym1 = 0.f, dx0 = 0.f, dy0 = 0.f, dxp1 = 0.f, dyp1 = 0.f;
+    float dxm1 = 0.f, dym1 = 0.f, dx0 = 0.f, dy0 = 0.f;
     if (CURV) {
       dxm1 = dxof(fm1);
       dym1 = div_by(fsub(f0, fm2), T.d1y, T.r1y);
@@ -656,64 +712,71 @@ __global__ void __launch_bounds__(256) stencil_fast_kernel(const __grid_constant
       dy0 = div_by(fsub(fp1, fm1), T.d1y, T.r1y);
     }
     bool bad = false;
-#pragma unroll 1
-    for (int y = y0; y < y1; ++y) {
-      float p, q, dxx = 0.f, dxy = 0.f, dyy = 0.f, dyx = 0.f;
-      if (CURV) {
-        dxp1 = dxof(fp1);
-        dyp1 = div_by(fsub(fp2, f0), T.d1y, T.r1y);
-        p = dx0;
-        q = dy0;
-        dxx = div_by(fsub(shfl_dn1(dx0), shfl_up1(dx0)), T.d2x, T.r2x);
-        dxy = div_by(fsub(dxp1, dxm1), T.d2y, T.r2y);
-        dyy = div_by(fsub(dyp1, dym1), T.d2y, T.r2y);
-        if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = div_by(fsub(shfl_dn1(dy0), shfl_up1(dy0)), T.d2x, T.r2x);
-      } else {
-        p = dxof(f0);
-        q = div_by(fsub(fp1, fm1), T.d1y, T.r1y);
-      }
-      float pz = p, qz = q;
-      if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) {
-        const float zf = A.z;
-        pz = div_by(fsub(shfl_dn1(fmul(f0, zf)), shfl_up1(fmul(f0, zf))), T.d1x, T.r1x);
-        qz = div_by(fsub(fmul(fp1, zf), fmul(fm1, zf)), T.d1y, T.r1y);
-      }
-      float o[FSG_STENCIL_NOUT];
-      const bool valid = f0 == f0;
-      float chk = p + q + pz + qz;
-      if (CURV) chk += dxx + dxy + dyy + dyx;
-      if (out_lane && valid && chk != chk) bad = true;
-      if (valid) {
-        const Light L{A.lx, A.ly, A.lz, A.slope_unit};
-        pixel_products(L, T.sx, T.sy, OM, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
-      } else {
+    for (int yb = y0; yb < y1; yb += G) {
+      float nxt[G];
 #pragma unroll
-        for (int k = 0; k < FSG_STENCIL_NOUT; ++k) o[k] = __int_as_float(0x7fc00000);
+      for (int k = 0; k < G; ++k) {
+        const int row = first_q + (yb - y0) + G + k;
+        nxt[k] = (row <= last) ? ld(row) : 0.f;
       }
-      if (out_lane) {
 #pragma unroll
-        for (int k = 0; k < FSG_STENCIL_NOUT; ++k) {
-          if (!(OM & (1u << k))) continue;
-          const PlaneK& P = A.planes[k];
-          char* dst = optr[k];
-          if (P.dtype == FSG_F32) *reinterpret_cast<float*>(dst) = o[k];
-          else if (P.dtype == FSG_U8) *reinterpret_cast<uint8_t*>(dst) = (uint8_t)(int)quantize(o[k], P.qa, P.qb, P.qmin, P.qmax);
-          else *reinterpret_cast<int16_t*>(dst) = (int16_t)(int)quantize(o[k], P.qa, P.qb, P.qmin, P.qmax);
-          optr[k] = dst + ostep[k];
+      for (int k = 0; k < G; ++k) {
+        const int y = yb + k;
+        if (y >= y1) break;
+        float p, q, dxx = 0.f, dxy = 0.f, dyy = 0.f, dyx = 0.f, dxp1 = 0.f, dyp1 = 0.f;
+        if (CURV) {
+          dxp1 = dxof(fp1);
+          dyp1 = div_by(fsub(fp2, f0), T.d1y, T.r1y);
+          p = dx0;
+          q = dy0;
+          dxx = div_by(fsub(shfl_dn1(dx0), shfl_up1(dx0)), T.d2x, T.r2x);
+          dxy = div_by(fsub(dxp1, dxm1), T.d2y, T.r2y);
+          dyy = div_by(fsub(dyp1, dym1), T.d2y, T.r2y);
+          if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = div_by(fsub(shfl_dn1(dy0), shfl_up1(dy0)), T.d2x, T.r2x);
+        } else {
+          p = dxof(f0);
+          q = div_by(fsub(fp1, fm1), T.d1y, T.r1y);
+        }
+        float pz = p, qz = q;
+        if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) {
+          const float zf = A.z;
+          pz = div_by(fsub(shfl_dn1(fmul(f0, zf)), shfl_up1(fmul(f0, zf))), T.d1x, T.r1x);
+          qz = div_by(fsub(fmul(fp1, zf), fmul(fm1, zf)), T.d1y, T.r1y);
+        }
+        float o[FSG_STENCIL_NOUT];
+        const bool valid = f0 == f0;
+        float chk = p + q;
+        if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) chk += pz + qz;
+        if (CURV) chk += dxx + dxy + dyy + dyx;
+        bad |= out_lane && valid && chk != chk;
+        if (valid) {
+          pixel_products(L, T.sx, T.sy, OM, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
+        } else {
+#pragma unroll
+          for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) o[kk] = __int_as_float(0x7fc00000);
+        }
+        if (out_lane) {
+#pragma unroll
+          for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) {
+            if (!(OM & (1u << kk))) continue;
+            const PlaneK& P = A.planes[kk];
+            char* dst = optr[kk];
+            if (ALLF32 || P.dtype == FSG_F32) *reinterpret_cast<float*>(dst) = o[kk];
+            else if (P.dtype == FSG_U8) *reinterpret_cast<uint8_t*>(dst) = (uint8_t)(int)quantize(o[kk], P.qa, P.qb, P.qmin, P.qmax);
+            else *reinterpret_cast<int16_t*>(dst) = (int16_t)(int)quantize(o[kk], P.qa, P.qb, P.qmin, P.qmax);
+            optr[kk] = dst + ostep[kk];
+          }
+        }
+        // slide one row down
+        if (CURV) {
+          fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2; fp2 = cur[k];
+          dxm1 = dx0; dym1 = dy0; dx0 = dxp1; dy0 = dyp1;
+        } else {
+          fm1 = f0; f0 = fp1; fp1 = cur[k];
         }
       }
-      // slide one row down; the queue head enters the window, a new row is requested
-      const float nxt = qv[0];
 #pragma unroll
-      for (int k = 0; k + 1 < PF; ++k) qv[k] = qv[k + 1];
-      const int ynew = qstart + (y - y0) + PF;
-      qv[PF - 1] = (ynew <= last) ? ld(ynew) : 0.f;
-      if (CURV) {
-        fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2; fp2 = nxt;
-        dxm1 = dx0; dym1 = dy0; dx0 = dxp1; dy0 = dyp1;
-      } else {
-        fm1 = f0; f0 = fp1; fp1 = nxt;
-      }
+      for (int k = 0; k < G; ++k) cur[k] = nxt[k];
     }
     if (__ballot_sync(0xffffffffu, bad) && lane == 0) flag_blocks(A, T, y0, y1, x0, xo);
   }
@@ -817,7 +880,10 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
   A.has_nodata = params->has_nodata != 0;
   A.slope_unit = params->slope_unit;
   A.outmask = outmask;
-  for (int j = 0; j < 5; ++j) A.gw[j] = kGaussW[j];
+  for (int j = 0; j < 5; ++j) {
+    A.gw_hi[j] = (float)kGaussW[j];
+    A.gw_lo[j] = (float)(kGaussW[j] - (double)A.gw_hi[j]);
+  }
   for (int o = 0; o < FSG_STENCIL_NOUT; ++o) {
     A.planes[o].ptr = planes[o].ptr;
     A.planes[o].ld = planes[o].ld;
@@ -881,11 +947,14 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
   constexpr unsigned HS = 1u << FSG_OUT_HILLSHADE, SL = 1u << FSG_OUT_SLOPE, CM = 1u << FSG_OUT_CURV_MEAN,
                      CG = 1u << FSG_OUT_CURV_GAUSSIAN, CP = 1u << FSG_OUT_CURV_PLANFORM,
                      CR = 1u << FSG_OUT_CURV_PROFILE, DXY = (1u << FSG_OUT_DX) | (1u << FSG_OUT_DY);
+  bool allf32 = true;
+  for (int o = 0; o < FSG_STENCIL_NOUT; ++o)
+    if ((outmask >> o) & 1u) allf32 = allf32 && planes[o].dtype == FSG_F32;
   switch (outmask) {
-#define FSG_CASE(M, C)                        \
-  case (M):                                   \
-    kern = stencil_kernel<C, (M)>;            \
-    fast = stencil_fast_kernel<C, (M)>;       \
+#define FSG_CASE(M, C)                                                                         \
+  case (M):                                                                                    \
+    kern = stencil_kernel<C, (M)>;                                                             \
+    fast = allf32 ? stencil_fast_kernel<C, (M), true> : stencil_fast_kernel<C, (M), false>;    \
     break;
     FSG_CASE(HS | SL | CP | CR, true)
     FSG_CASE(HS | SL | CM | CG | CP | CR, true)
