@@ -99,6 +99,8 @@ _SIGNATURES = {
                                   C.c_void_p, C.c_int64, C.c_void_p]),
     "fsg_stencil": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
                               C.POINTER(StencilParams), C.POINTER(Plane), C.c_void_p]),
+    "fsg_stencil_host": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
+                                   C.POINTER(StencilParams), C.POINTER(Plane), C.c_void_p]),
     "fsg_topousm": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
                               C.POINTER(TopoUSMParams), C.POINTER(Plane), C.c_void_p]),
     "fsg_topousm_coarse_field": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(C.c_int32),

@@ -104,3 +104,30 @@ def stencil_block(block, outputs: Iterable[str], *, azimuth=315.0, altitude=45.0
         return {k: _arrays.wrap_result(t, v.origin) for k, t in res.items()}
     launch(v, [whole_window_tile(v.h, v.w, psx, psy)], params, planes)
     return {k: _arrays.wrap_result(t, v.origin) for k, t in res.items()}
+
+
+def launch_host(raster_host, tiles: Sequence[Tile], params: StencilParams, planes_host: Dict[int, Plane],
+                stream: Optional[int] = None) -> None:
+    """``fsg_stencil_host``: raster and output planes in host memory (pinned for overlap)."""
+    arr = (Plane * N.FSG_STENCIL_NOUT)()
+    for idx, pl in planes_host.items():
+        arr[idx] = pl
+    tarr = (Tile * max(1, len(tiles)))(*tiles)
+    h, w = int(raster_host.shape[0]), int(raster_host.shape[1])
+    ld = int(raster_host.stride(0)) if hasattr(raster_host, "stride") else int(raster_host.strides[0] // 4)
+    ptr = int(raster_host.data_ptr()) if hasattr(raster_host, "data_ptr") else int(raster_host.ctypes.data)
+    s = _arrays.current_stream_handle() if stream is None else stream
+    N.check(N.lib().fsg_stencil_host(C.c_void_p(ptr), ld, h, w, tarr, len(tiles), C.byref(params), arr,
+                                     C.c_void_p(s)))
+
+
+def host_plane(t, dtype: str = "float32", qp: Optional[dict] = None) -> Plane:
+    """Plane over a host tensor / array (pinned memory recommended)."""
+    pl = Plane()
+    pl.ptr = int(t.data_ptr()) if hasattr(t, "data_ptr") else int(t.ctypes.data)
+    pl.ld = int(t.stride(0)) if hasattr(t, "stride") else int(t.strides[0] // t.itemsize)
+    pl.dtype = N.DTYPE_CODES[dtype]
+    if dtype != "float32":
+        pl.q_a, pl.q_b = float(qp["a_coef"]), float(qp["b_coef"])
+        pl.q_min, pl.q_max = int(qp["dn_min"]), int(qp["dn_max"])
+    return pl

@@ -86,7 +86,7 @@ struct StencilArgs {
   int slope_unit;
   unsigned outmask;
   float gw_hi[5], gw_lo[5];  // scipy Gaussian(sigma=1, radius 4) weights as float-float, [0] = centre
-  unsigned char* block_flags;  // per (tile, block): 1 = needs the exact shared-memory pass; NULL = all
+  unsigned char* block_flags;  // per (tile, block): nonzero = process; NULL = every block
   PlaneK planes[FSG_STENCIL_NOUT];
   TileK inl[INLINE_TILES];
 };
@@ -621,8 +621,8 @@ constexpr int SW = 28, SH = 64;
 struct FastTile {
   int wy0, wx0, wy1, wx1, cy0, cx0, cy1, cx1, oy0, ox0;
   int nstrip, unit0;   // strips across the core, first flat unit index
-  int nbx, block0;     // slow-pass block grid of this tile
-  float d1x, r1x, d1y, r1y, d2x, r2x, d2y, r2y, sx, sy;
+  Axis g1x, g1y, c2x, c2y;
+  float sx, sy;
 };
 
 struct FastArgs {
@@ -635,55 +635,89 @@ struct FastArgs {
   int slope_unit;
   const FastTile* tiles;
   int ntiles, total_units;
-  unsigned char* block_flags;
+  unsigned char* unit_flags;  // 1: a pixel's stencil reaches NoData; 2: the unit touches a window edge
+  FF gw[5];                   // Gaussian fill weights (float-float)
   PlaneK planes[FSG_STENCIL_NOUT];
 };
 
 __device__ __forceinline__ float shfl_up1(float v) { return __shfl_up_sync(0xffffffffu, v, 1); }
 __device__ __forceinline__ float shfl_dn1(float v) { return __shfl_down_sync(0xffffffffu, v, 1); }
 
-// Marks every exact-pass block (32 x 64) overlapping rows [y0, y1) x cols [x0, x1).
-__device__ __forceinline__ void flag_blocks(const FastArgs& A, const FastTile& T, int y0, int y1, int x0, int x1) {
-  for (int by = (y0 - T.cy0) / 32; by <= (y1 - 1 - T.cy0) / 32; ++by)
-    for (int bx = (x0 - T.cx0) / 64; bx <= (x1 - 1 - T.cx0) / 64; ++bx) A.block_flags[T.block0 + by * T.nbx + bx] = 1;
+// Unit geometry shared by the fast pass and the fix-up pass.
+struct UnitGeom {
+  int t, x0, y0, y1, xo;
+};
+__device__ __forceinline__ UnitGeom unit_geom(const FastArgs& A, int u) {
+  int lo = 0, hi = A.ntiles - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (A.tiles[mid].unit0 <= u) lo = mid; else hi = mid - 1;
+  }
+  const FastTile& T = A.tiles[lo];
+  const int lu = u - T.unit0;
+  const int cy = lu / T.nstrip, sx = lu - (lu / T.nstrip) * T.nstrip;
+  UnitGeom g;
+  g.t = lo;
+  // the last strip of a core is moved left to end at the core edge (it
+  // recomputes a few columns of its neighbour with identical values)
+  g.x0 = (T.cx1 - T.cx0 >= SW) ? min(T.cx0 + sx * SW, T.cx1 - SW) : T.cx0;
+  g.y0 = T.cy0 + cy * SH;
+  g.y1 = min(g.y0 + SH, T.cy1);
+  g.xo = min(g.x0 + SW, T.cx1);
+  return g;
 }
 
+__device__ __forceinline__ void store_pixel(const FastArgs& A, unsigned om, bool allf32, char* const* optr,
+                                            const float* o) {
+#pragma unroll
+  for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) {
+    if (!(om & (1u << kk))) continue;
+    const PlaneK& P = A.planes[kk];
+    char* dst = optr[kk];
+    if (allf32 || P.dtype == FSG_F32) *reinterpret_cast<float*>(dst) = o[kk];
+    else if (P.dtype == FSG_U8) *reinterpret_cast<uint8_t*>(dst) = (uint8_t)(int)quantize(o[kk], P.qa, P.qb, P.qmin, P.qmax);
+    else *reinterpret_cast<int16_t*>(dst) = (int16_t)(int)quantize(o[kk], P.qa, P.qb, P.qmin, P.qmax);
+  }
+}
+
+// Fast streaming pass for the common case: a warp owns a strip of SW = 28
+// output columns and SH rows; lane l holds column x0 - 2 + l, walks down the
+// rows keeping f, dx, dy of the neighbouring rows in registers, and takes the
+// horizontal neighbours from warp shuffles (lanes 2..29 emit outputs).  No
+// shared memory, no barriers.  Row groups of G are loaded one group ahead.  A
+// warp ballot per group tells whether any NoData feeds it; only then are the
+// per-pixel checks evaluated.  Units touching a window edge, and units with a
+// valid pixel whose stencil reaches NoData, are flagged for the fix-up pass.
+// DIV: derivatives use the correctly rounded division (bit-exact np.gradient,
+// needed for the dx/dy planes); otherwise a multiply by the reciprocal.
 template <bool CURV, unsigned OM, bool ALLF32>
 __global__ void __launch_bounds__(256) stencil_fast_kernel(const __grid_constant__ FastArgs A) {
+  constexpr bool DIV = (OM & ((1u << FSG_OUT_DX) | (1u << FSG_OUT_DY))) != 0;
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const bool hn = A.has_nodata != 0;
   const Light L{A.lx, A.ly, A.lz, A.slope_unit};
   for (int u = warp; u < A.total_units; u += nwarps) {
-    int lo = 0, hi = A.ntiles - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (A.tiles[mid].unit0 <= u) lo = mid; else hi = mid - 1;
-    }
-    const FastTile& T = A.tiles[lo];
-    const int lu = u - T.unit0;
-    const int cy = lu / T.nstrip, sx = lu - (lu / T.nstrip) * T.nstrip;
-    // the last strip of a core is moved left to end at the core edge (it
-    // recomputes a few columns of its neighbour with identical values)
-    const int x0 = (T.cx1 - T.cx0 >= SW) ? min(T.cx0 + sx * SW, T.cx1 - SW) : T.cx0;
-    const int y0 = T.cy0 + cy * SH;
-    const int y1 = min(y0 + SH, T.cy1);
-    const int xo = min(x0 + SW, T.cx1);  // end of this strip's outputs
+    const UnitGeom g = unit_geom(A, u);
+    const FastTile& T = A.tiles[g.t];
+    const int x0 = g.x0, y0 = g.y0, y1 = g.y1, xo = g.xo;
     // stencil reach: rows y0-2 .. y1+1 and cols x0-2 .. x0+29 strictly inside
     // the window, so every derivative is a central difference
     const bool interior = y0 - 2 >= T.wy0 && y1 + 2 <= T.wy1 && x0 - 2 >= T.wx0 && x0 + SW + 2 <= T.wx1;
     if (!interior) {
-      if (lane == 0) flag_blocks(A, T, y0, y1, x0, xo);
+      if (lane == 0) A.unit_flags[u] = 2;
       continue;
     }
     const int x = x0 - 2 + lane;
     const bool out_lane = lane >= 2 && lane < 2 + SW && x < xo;
-    const float* col = A.raster + x;
-    auto ld = [&](int y) {
-      float v = __ldg(col + (long long)y * A.ld);
+    const float* rp = A.raster + (long long)(y0 - (CURV ? 2 : 1)) * A.ld + x;  // next row to read
+    auto ld_next = [&]() {
+      float v = __ldg(rp);
+      rp += A.ld;
       return is_nodata(v, A.ndf, hn) ? __int_as_float(0x7fc00000) : v;
     };
+    auto dv = [&](float num, const Axis& a) { return DIV ? div_by(num, a.d2, a.rcp) : fmul(num, a.rcp); };
     char* optr[FSG_STENCIL_NOUT];
     long long ostep[FSG_STENCIL_NOUT];
 #pragma unroll
@@ -694,31 +728,39 @@ __global__ void __launch_bounds__(256) stencil_fast_kernel(const __grid_constant
       optr[k] = static_cast<char*>(P.ptr) + ((long long)(T.oy0 + y0 - T.cy0) * P.ld + (T.ox0 + x - T.cx0)) * esz;
       ostep[k] = P.ld * esz;
     }
-    // sliding window: f at rows y-2..y+2 (CURV) / y-1..y+1, dx/dy at y-1..y+1
     constexpr int G = 8;
-    const int last = CURV ? y1 + 1 : y1;          // last row read
-    const int first_q = CURV ? y0 + 3 : y0 + 2;   // first row delivered through the group buffer
-    float fm2 = CURV ? ld(y0 - 2) : 0.f, fm1 = ld(y0 - 1), f0 = ld(y0), fp1 = ld(y0 + 1);
-    float fp2 = CURV ? ld(y0 + 2) : 0.f;
+    const int last = CURV ? y1 + 1 : y1;  // last row read
+    int next_row = y0 - (CURV ? 2 : 1);
+    float fm2 = 0.f, fm1, f0, fp1, fp2 = 0.f;
+    if (CURV) fm2 = ld_next();
+    fm1 = ld_next();
+    f0 = ld_next();
+    fp1 = ld_next();
+    if (CURV) fp2 = ld_next();
+    next_row += CURV ? 5 : 3;
     float cur[G];
 #pragma unroll
-    for (int k = 0; k < G; ++k) cur[k] = (first_q + k <= last) ? ld(first_q + k) : 0.f;
-    auto dxof = [&](float f) { return div_by(fsub(shfl_dn1(f), shfl_up1(f)), T.d1x, T.r1x); };
+    for (int k = 0; k < G; ++k) cur[k] = (next_row + k <= last) ? ld_next() : 0.f;
+    next_row += G;
+    auto dxof = [&](float f) { return dv(fsub(shfl_dn1(f), shfl_up1(f)), T.g1x); };
     float dxm1 = 0.f, dym1 = 0.f, dx0 = 0.f, dy0 = 0.f;
     if (CURV) {
       dxm1 = dxof(fm1);
-      dym1 = div_by(fsub(f0, fm2), T.d1y, T.r1y);
+      dym1 = dv(fsub(f0, fm2), T.g1y);
       dx0 = dxof(f0);
-      dy0 = div_by(fsub(fp1, fm1), T.d1y, T.r1y);
+      dy0 = dv(fsub(fp1, fm1), T.g1y);
     }
     bool bad = false;
     for (int yb = y0; yb < y1; yb += G) {
       float nxt[G];
 #pragma unroll
-      for (int k = 0; k < G; ++k) {
-        const int row = first_q + (yb - y0) + G + k;
-        nxt[k] = (row <= last) ? ld(row) : 0.f;
-      }
+      for (int k = 0; k < G; ++k) nxt[k] = (next_row + k <= last) ? ld_next() : 0.f;
+      next_row += G;
+      // NoData anywhere in the rows feeding this group (the window and the group buffer)?
+      bool gn = (fm2 != fm2) | (fm1 != fm1) | (f0 != f0) | (fp1 != fp1) | (fp2 != fp2);
+#pragma unroll
+      for (int k = 0; k < G; ++k) gn |= cur[k] != cur[k];
+      const bool group_nan = __any_sync(0xffffffffu, gn);
 #pragma unroll
       for (int k = 0; k < G; ++k) {
         const int y = yb + k;
@@ -726,47 +768,40 @@ __global__ void __launch_bounds__(256) stencil_fast_kernel(const __grid_constant
         float p, q, dxx = 0.f, dxy = 0.f, dyy = 0.f, dyx = 0.f, dxp1 = 0.f, dyp1 = 0.f;
         if (CURV) {
           dxp1 = dxof(fp1);
-          dyp1 = div_by(fsub(fp2, f0), T.d1y, T.r1y);
+          dyp1 = dv(fsub(fp2, f0), T.g1y);
           p = dx0;
           q = dy0;
-          dxx = div_by(fsub(shfl_dn1(dx0), shfl_up1(dx0)), T.d2x, T.r2x);
-          dxy = div_by(fsub(dxp1, dxm1), T.d2y, T.r2y);
-          dyy = div_by(fsub(dyp1, dym1), T.d2y, T.r2y);
-          if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = div_by(fsub(shfl_dn1(dy0), shfl_up1(dy0)), T.d2x, T.r2x);
+          dxx = dv(fsub(shfl_dn1(dx0), shfl_up1(dx0)), T.c2x);
+          dxy = dv(fsub(dxp1, dxm1), T.c2y);
+          dyy = dv(fsub(dyp1, dym1), T.c2y);
+          if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = dv(fsub(shfl_dn1(dy0), shfl_up1(dy0)), T.c2x);
         } else {
           p = dxof(f0);
-          q = div_by(fsub(fp1, fm1), T.d1y, T.r1y);
+          q = dv(fsub(fp1, fm1), T.g1y);
         }
         float pz = p, qz = q;
         if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) {
           const float zf = A.z;
-          pz = div_by(fsub(shfl_dn1(fmul(f0, zf)), shfl_up1(fmul(f0, zf))), T.d1x, T.r1x);
-          qz = div_by(fsub(fmul(fp1, zf), fmul(fm1, zf)), T.d1y, T.r1y);
+          pz = dv(fsub(shfl_dn1(fmul(f0, zf)), shfl_up1(fmul(f0, zf))), T.g1x);
+          qz = dv(fsub(fmul(fp1, zf), fmul(fm1, zf)), T.g1y);
+        }
+        const bool valid = f0 == f0;
+        if (group_nan) {
+          float chk = p + q;
+          if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) chk += pz + qz;
+          if (CURV) chk += dxx + dxy + dyy + dyx;
+          bad |= out_lane && valid && chk != chk;
         }
         float o[FSG_STENCIL_NOUT];
-        const bool valid = f0 == f0;
-        float chk = p + q;
-        if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) chk += pz + qz;
-        if (CURV) chk += dxx + dxy + dyy + dyx;
-        bad |= out_lane && valid && chk != chk;
         if (valid) {
           pixel_products(L, T.sx, T.sy, OM, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
         } else {
 #pragma unroll
           for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) o[kk] = __int_as_float(0x7fc00000);
         }
-        if (out_lane) {
+        if (out_lane) store_pixel(A, OM, ALLF32, optr, o);
 #pragma unroll
-          for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) {
-            if (!(OM & (1u << kk))) continue;
-            const PlaneK& P = A.planes[kk];
-            char* dst = optr[kk];
-            if (ALLF32 || P.dtype == FSG_F32) *reinterpret_cast<float*>(dst) = o[kk];
-            else if (P.dtype == FSG_U8) *reinterpret_cast<uint8_t*>(dst) = (uint8_t)(int)quantize(o[kk], P.qa, P.qb, P.qmin, P.qmax);
-            else *reinterpret_cast<int16_t*>(dst) = (int16_t)(int)quantize(o[kk], P.qa, P.qb, P.qmin, P.qmax);
-            optr[kk] = dst + ostep[kk];
-          }
-        }
+        for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) optr[kk] += ostep[kk];
         // slide one row down
         if (CURV) {
           fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2; fp2 = cur[k];
@@ -778,7 +813,137 @@ __global__ void __launch_bounds__(256) stencil_fast_kernel(const __grid_constant
 #pragma unroll
       for (int k = 0; k < G; ++k) cur[k] = nxt[k];
     }
-    if (__ballot_sync(0xffffffffu, bad) && lane == 0) flag_blocks(A, T, y0, y1, x0, xo);
+    if (__ballot_sync(0xffffffffu, bad) && lane == 0) A.unit_flags[u] = 1;
+  }
+}
+
+// ------------------------------------------------------------- fix-up pass
+// NaN-aware Gaussian fill value of window cell (gy, gx): separable 9x9
+// normalised convolution with 'nearest' clamping at the window edges, in
+// float-float (_nan_utils.py:18-31 with the axis order of scipy).
+__device__ float fill_value(const FastArgs& A, const FastTile& T, int gy, int gx) {
+  const bool hn = A.has_nodata != 0;
+  float vv[9], vw[9];
+#pragma unroll 1
+  for (int j = 0; j < 9; ++j) {
+    const int xx = min(max(gx + j - 4, T.wx0), T.wx1 - 1);
+    float xv[9], xw[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      const int yy = min(max(gy + i - 4, T.wy0), T.wy1 - 1);
+      float v = __ldg(A.raster + (long long)yy * A.ld + xx);
+      const bool ok = !is_nodata(v, A.ndf, hn);
+      xv[i] = ok ? v : 0.f;
+      xw[i] = ok ? 1.f : 0.f;
+    }
+    vv[j] = gsum_ff(A.gw, xv);
+    vw[j] = gsum_ff(A.gw, xw);
+  }
+  const float sv = gsum_ff(A.gw, vv), sw = gsum_ff(A.gw, vw);
+  return sw > 0.0f ? __fdiv_rn(sv, sw) : 0.0f;
+}
+
+// Outputs of one valid pixel with the full reference semantics: the filled
+// values of its 9 x 9 neighbourhood (fills only for the NaN cells the formulas
+// read), np.gradient with the window's edge rules, second derivatives on the
+// signed steps.
+template <unsigned OM>
+__device__ void exact_pixel(const FastArgs& A, const FastTile& T, int gy, int gx, float* o) {
+  constexpr bool CURV = (OM & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) |
+                               (1u << FSG_OUT_CURV_PLANFORM) | (1u << FSG_OUT_CURV_PROFILE))) != 0;
+  const bool hn = A.has_nodata != 0;
+  float f[9][9];
+#pragma unroll 1
+  for (int r = 0; r < 9; ++r)
+#pragma unroll 1
+    for (int c = 0; c < 9; ++c) {
+      const int yy = gy + r - 4, xx = gx + c - 4;
+      // cells the derivative formulas can read: |dr| + |dc| <= 4 (central
+      // differences reach 2, one-sided edge formulas one more step)
+      const bool used = (abs(r - 4) + abs(c - 4)) <= (CURV ? 4 : 2) && (CURV || abs(r - 4) <= 2) &&
+                        (CURV || abs(c - 4) <= 2);
+      float v = __int_as_float(0x7fc00000);
+      if (used && yy >= T.wy0 && yy < T.wy1 && xx >= T.wx0 && xx < T.wx1) {
+        v = __ldg(A.raster + (long long)yy * A.ld + xx);
+        if (is_nodata(v, A.ndf, hn)) v = fill_value(A, T, yy, xx);
+      }
+      f[r][c] = v;
+    }
+  auto dx_at = [&](int r, int c) {
+    return deriv(T.g1x, gx + c, T.wx0, T.wx1, [&](int k) { return f[r + 4][c + 4 + k]; });
+  };
+  auto dy_at = [&](int r, int c) {
+    return deriv(T.g1y, gy + r, T.wy0, T.wy1, [&](int k) { return f[r + 4 + k][c + 4]; });
+  };
+  const float p = dx_at(0, 0), q = dy_at(0, 0);
+  float dxx = 0.f, dxy = 0.f, dyy = 0.f, dyx = 0.f;
+  if (CURV) {
+    dxx = deriv(T.c2x, gx, T.wx0, T.wx1, [&](int k) { return dx_at(0, k); });
+    dxy = deriv(T.c2y, gy, T.wy0, T.wy1, [&](int k) { return dx_at(k, 0); });
+    dyy = deriv(T.c2y, gy, T.wy0, T.wy1, [&](int k) { return dy_at(k, 0); });
+    if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = deriv(T.c2x, gx, T.wx0, T.wx1, [&](int k) { return dy_at(0, k); });
+  }
+  float pz = p, qz = q;
+  if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) {
+    const float zf = A.z;
+    pz = deriv(T.g1x, gx, T.wx0, T.wx1, [&](int k) { return fmul(f[4][4 + k], zf); });
+    qz = deriv(T.g1y, gy, T.wy0, T.wy1, [&](int k) { return fmul(f[4 + k][4], zf); });
+  }
+  const Light L{A.lx, A.ly, A.lz, A.slope_unit};
+  pixel_products(L, T.sx, T.sy, OM, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
+}
+
+// Recomputes the pixels of flagged units that the fast pass could not produce
+// exactly: every pixel of a unit touching a window edge, and in the other
+// flagged units the valid pixels whose stencil footprint holds NoData.
+template <unsigned OM, bool ALLF32>
+__global__ void __launch_bounds__(128) stencil_fixup_kernel(const __grid_constant__ FastArgs A) {
+  constexpr bool CURV = (OM & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) |
+                               (1u << FSG_OUT_CURV_PLANFORM) | (1u << FSG_OUT_CURV_PROFILE))) != 0;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const bool hn = A.has_nodata != 0;
+  const int reach = CURV ? 2 : 1;
+  for (int u = warp; u < A.total_units; u += nwarps) {
+    const int flag = A.unit_flags[u];
+    if (!flag) continue;
+    const UnitGeom g = unit_geom(A, u);
+    const FastTile& T = A.tiles[g.t];
+    const int x = g.x0 + lane;
+    if (lane >= SW || x >= g.xo) continue;
+    for (int y = g.y0; y < g.y1; ++y) {
+      float zc = __ldg(A.raster + (long long)y * A.ld + x);
+      const bool valid = !is_nodata(zc, A.ndf, hn);
+      bool need = flag == 2;
+      if (!need && valid) {
+        for (int dr = -reach; dr <= reach && !need; ++dr)
+          for (int dc = -reach; dc <= reach; ++dc) {
+            const float v = __ldg(A.raster + (long long)(y + dr) * A.ld + x + dc);
+            if (is_nodata(v, A.ndf, hn)) {
+              need = true;
+              break;
+            }
+          }
+      }
+      if (!need) continue;
+      float o[FSG_STENCIL_NOUT];
+      if (valid) {
+        exact_pixel<OM>(A, T, y, x, o);
+      } else {
+#pragma unroll
+        for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) o[kk] = __int_as_float(0x7fc00000);
+      }
+      char* optr[FSG_STENCIL_NOUT];
+#pragma unroll
+      for (int k = 0; k < FSG_STENCIL_NOUT; ++k) {
+        if (!(OM & (1u << k))) continue;
+        const PlaneK& P = A.planes[k];
+        const int esz = ALLF32 ? 4 : (P.dtype == FSG_F32 ? 4 : (P.dtype == FSG_I16 ? 2 : 1));
+        optr[k] = static_cast<char*>(P.ptr) + ((long long)(T.oy0 + y - T.cy0) * P.ld + (T.ox0 + x - T.cx0)) * esz;
+      }
+      store_pixel(A, OM, ALLF32, optr, o);
+    }
   }
 }
 
@@ -944,6 +1109,7 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
                                 (1u << FSG_OUT_CURV_PLANFORM) | (1u << FSG_OUT_CURV_PROFILE))) != 0;
   auto kern = curv ? stencil_kernel<true, 0u> : stencil_kernel<false, 0u>;
   void (*fast)(FastArgs) = nullptr;
+  void (*fixup)(FastArgs) = nullptr;
   constexpr unsigned HS = 1u << FSG_OUT_HILLSHADE, SL = 1u << FSG_OUT_SLOPE, CM = 1u << FSG_OUT_CURV_MEAN,
                      CG = 1u << FSG_OUT_CURV_GAUSSIAN, CP = 1u << FSG_OUT_CURV_PLANFORM,
                      CR = 1u << FSG_OUT_CURV_PROFILE, DXY = (1u << FSG_OUT_DX) | (1u << FSG_OUT_DY);
@@ -953,8 +1119,8 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
   switch (outmask) {
 #define FSG_CASE(M, C)                                                                         \
   case (M):                                                                                    \
-    kern = stencil_kernel<C, (M)>;                                                             \
     fast = allf32 ? stencil_fast_kernel<C, (M), true> : stencil_fast_kernel<C, (M), false>;    \
+    fixup = allf32 ? stencil_fixup_kernel<(M), true> : stencil_fixup_kernel<(M), false>;       \
     break;
     FSG_CASE(HS | SL | CP | CR, true)
     FSG_CASE(HS | SL | CM | CG | CP | CR, true)
@@ -969,15 +1135,8 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
 #undef FSG_CASE
     default: break;
   }
-  FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
-  FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-  int per_sm = 0;
-  FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, SMEM_BYTES));
-  if (per_sm < 1) per_sm = 1;
-  int grid = std::min(total, di.sms * per_sm);
-  StreamScratch flag_scratch, fast_tiles;
   if (fast) {
-    // fast streaming pass over every tile; flags the blocks it cannot produce exactly
+    // fast streaming pass over every tile, then the exact fix-up of the units it flagged
     std::vector<FastTile> ft;
     int units = 0;
     for (const TileK& k : tk) {
@@ -985,23 +1144,21 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
       f.wy0 = k.wy0; f.wx0 = k.wx0; f.wy1 = k.wy1; f.wx1 = k.wx1;
       f.cy0 = k.cy0; f.cx0 = k.cx0; f.cy1 = k.cy1; f.cx1 = k.cx1;
       f.oy0 = k.oy0; f.ox0 = k.ox0;
-      int cw = k.cx1 - k.cx0, ch = k.cy1 - k.cy0;
+      const int cw = k.cx1 - k.cx0, ch = k.cy1 - k.cy0;
       f.nstrip = std::max(1, (cw + SW - 1) / SW);
       f.unit0 = units;
       units += f.nstrip * ((ch + SH - 1) / SH);
-      f.nbx = k.nbx;
-      f.block0 = k.block0;
-      f.d1x = k.g1x.d2; f.r1x = k.g1x.rcp; f.d1y = k.g1y.d2; f.r1y = k.g1y.rcp;
-      f.d2x = k.c2x.d2; f.r2x = k.c2x.rcp; f.d2y = k.c2y.d2; f.r2y = k.c2y.rcp;
+      f.g1x = k.g1x; f.g1y = k.g1y; f.c2x = k.c2x; f.c2y = k.c2y;
       f.sx = k.sign_x; f.sy = k.sign_y;
       ft.push_back(f);
     }
-    st = flag_scratch.alloc((size_t)total, s);
+    StreamScratch fscr;
+    const size_t tiles_bytes = (sizeof(FastTile) * ft.size() + 255) & ~(size_t)255;
+    st = fscr.alloc(tiles_bytes + (size_t)units, s);
     if (st) return st;
-    FSG_CUDA(cudaMemsetAsync(flag_scratch.ptr, 0, (size_t)total, s));
-    st = fast_tiles.alloc(sizeof(FastTile) * ft.size(), s);
-    if (st) return st;
-    FSG_CUDA(cudaMemcpyAsync(fast_tiles.ptr, ft.data(), sizeof(FastTile) * ft.size(), cudaMemcpyHostToDevice, s));
+    unsigned char* uflags = static_cast<unsigned char*>(fscr.ptr) + tiles_bytes;
+    FSG_CUDA(cudaMemcpyAsync(fscr.ptr, ft.data(), sizeof(FastTile) * ft.size(), cudaMemcpyHostToDevice, s));
+    FSG_CUDA(cudaMemsetAsync(uflags, 0, (size_t)units, s));
     FastArgs F;
     std::memset(&F, 0, sizeof(F));
     F.raster = A.raster;
@@ -1011,18 +1168,30 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
     F.ndf = A.ndf;
     F.has_nodata = A.has_nodata;
     F.slope_unit = A.slope_unit;
-    F.tiles = static_cast<const FastTile*>(fast_tiles.ptr);
+    F.tiles = static_cast<const FastTile*>(fscr.ptr);
     F.ntiles = (int)ft.size();
     F.total_units = units;
-    F.block_flags = static_cast<unsigned char*>(flag_scratch.ptr);
+    F.unit_flags = uflags;
+    for (int j = 0; j < 5; ++j) F.gw[j] = {A.gw_hi[j], A.gw_lo[j]};
     std::copy(A.planes, A.planes + FSG_STENCIL_NOUT, F.planes);
     int fper = 0;
     FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fper, fast, 256, 0));
-    int fgrid = std::min((units + 7) / 8, di.sms * std::max(1, fper));
+    const int fgrid = std::min((units + 7) / 8, di.sms * std::max(1, fper));
     fast<<<fgrid, 256, 0, s>>>(F);
     FSG_LAUNCHED(1);
-    A.block_flags = static_cast<unsigned char*>(flag_scratch.ptr);
+    int xper = 0;
+    FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&xper, fixup, 128, 0));
+    const int xgrid = std::min((units + 3) / 4, di.sms * std::max(1, xper));
+    fixup<<<xgrid, 128, 0, s>>>(F);
+    FSG_LAUNCHED(1);
+    return FSG_OK;
   }
+  FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+  FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  int per_sm = 0;
+  FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, SMEM_BYTES));
+  if (per_sm < 1) per_sm = 1;
+  int grid = std::min(total, di.sms * per_sm);
   kern<<<grid, NT, SMEM_BYTES, s>>>(A);
   FSG_LAUNCHED(1);
   return FSG_OK;

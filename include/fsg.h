@@ -120,6 +120,19 @@ int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t r
                 const fsg_tile* tiles, int32_t ntiles, const fsg_stencil_params* params,
                 const fsg_plane* planes, void* stream);
 
+/* The same fused pass over a raster and output planes in HOST memory (pinned
+ * memory gives asynchronous copies): per tile, the window is copied to the
+ * device, the kernels run, and every requested core is copied back into the
+ * host planes at (out_y0, out_x0); three tiles are in flight at once (H2D /
+ * compute / D2H overlapped on library-owned streams ordered after `stream`;
+ * `stream` waits for all of them).  Replaces the per-tile read -> cp.asarray ->
+ * block function -> cp.asnumpy cycle of process_single_tile
+ * (core/tile_processor.py:851-996) driven by process_dem_tiles' executor
+ * (:1629-1683).  Host buffers must stay valid until `stream` completes. */
+int fsg_stencil_host(const float* raster_host, int64_t ld, int32_t raster_h, int32_t raster_w,
+                     const fsg_tile* tiles, int32_t ntiles, const fsg_stencil_params* params,
+                     const fsg_plane* planes_host, void* stream);
+
 /* ------------------------------------------------------------ topousm_fast */
 typedef struct fsg_topousm_params {
   /* Small radii computed per window (algorithms/_impl_topousm_fast.py:49-100) with

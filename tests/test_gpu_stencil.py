@@ -204,3 +204,27 @@ def test_z_factor_and_azimuth(fsg):
                                           pixel_size=2.0, pixel_scale_x=-2.0, pixel_scale_y=3.0)
         ref = R.hillshade(dem, azimuth=az, altitude=alt, z_factor=z, pixel_size=2.0, psx=-2.0, psy=3.0)
         assert_close_range(got, ref, 1.0, f"hs z={z}")
+
+
+@pytest.mark.parametrize("dtype", ["float32", "uint8"])
+def test_host_buffer_tile_loop_equals_device_path(fsg, dtype):
+    """fsg_stencil_host (pinned host raster and planes, overlapped copies) == fsg_stencil."""
+    from fujishadergpu_gb300 import _arrays
+    from fujishadergpu_gb300.algorithms import _stencil as S
+    H, W = 700, 910
+    dem = _fbm_nan(H, W, 101, 6)
+    names = ["hillshade", "slope", "curvature_profile", "curvature_planform"]
+    qp = R.quantize_params(0.0, 1.0, "uint8") if dtype == "uint8" else None
+    tdt = torch.float32 if dtype == "float32" else torch.uint8
+    tiles = _tile_descs(H, W, 256, 8, 5.0, -5.0)
+    params = S.make_params(pixel_size=5.0)
+    dev = {n: torch.empty((H, W), device="cuda", dtype=tdt) for n in names}
+    S.launch(_arrays.as_device_f32_2d(torch.from_numpy(dem).cuda()), tiles, params,
+             {S.OUTPUT_INDEX[n]: S.make_plane(dev[n], dtype, qp) for n in names})
+    host_in = torch.from_numpy(dem).pin_memory()
+    host = {n: torch.full((H, W), 7, dtype=tdt).pin_memory() for n in names}
+    S.launch_host(host_in, tiles, params, {S.OUTPUT_INDEX[n]: S.host_plane(host[n], dtype, qp) for n in names})
+    torch.cuda.synchronize()
+    for n in names:
+        a, b = to_np(dev[n]), host[n].numpy()
+        assert np.array_equal(a, b, equal_nan=True), n
