@@ -7,9 +7,9 @@ slope (degrees) + profile and planform curvature, float32 outputs -- over a
 disks) cut into 4096^2 tiles with an 8 px halo, all tiles in one launch.
 
   value      Mpix/s with the DEM resident in HBM (device-timed, CUDA events)
-  e2e        Mpix/s through the C ABI with host (pinned) buffers: the H2D copy
-             of the DEM and the D2H copies of the four planes are inside the
-             timed region
+  e2e        Mpix/s through the C ABI with host (pinned) buffers
+             (fsg_stencil_host): the per-tile H2D copies of the DEM windows
+             and the D2H copies of the four planes are inside the timed region
   roofline   the fused kernel against the measured HBM copy bandwidth
   cpu_baseline  the CPU oracle (NumPy/SciPy restatement of the reference's
              block functions) on a bounded sample, on the host cores
@@ -18,7 +18,10 @@ disks) cut into 4096^2 tiles with an 8 px halo, all tiles in one launch.
 the reference itself is CuPy-only and cannot run on the host) with all host
 cores on the same workload definition.
 
-``--workload topousm|openness`` select the other hot-path kernels.
+The line also carries ``extra``: the topousm_fast tile loop (32768^2, radii
+2..2048) and openness (16384^2, 16 directions, R = 256; reference 10-sample
+rays and the dense every-step march on a 4096^2 crop), each device-timed
+(``--no-extra`` skips them).
 """
 from __future__ import annotations
 
@@ -237,18 +240,17 @@ def stencil_workload(args, rank, world):
     hbm, _, peak_kind = peaks()
     achieved = ALG_BYTES_STENCIL_F32 * px / (ms * 1e-3) / 1e9
 
-    # ---- e2e: host buffers through the C ABI, copies inside the timed region
+    # ---- e2e: host (pinned) buffers through the C ABI (fsg_stencil_host):
+    # per tile H2D window -> kernels -> D2H cores, three tiles in flight
     host_dem = torch.empty((H, W), dtype=torch.float32, pin_memory=True)
-    host_dem.copy_(dem.cpu())
+    host_dem.copy_(dem)
     host_out = {n: torch.empty((H, W), dtype=torch.float32, pin_memory=True) for n in names}
-    dev_in = torch.empty_like(dem)
-    view_in = _arrays.as_device_f32_2d(dev_in)
+    hplanes = {S.OUTPUT_INDEX[n]: S.host_plane(host_out[n]) for n in names}
+    h2d_bytes = sum(int(t.win_h) * int(t.win_w) * 4 for t in tiles)
+    d2h_bytes = px * 4 * len(names)
 
     def e2e_step():
-        dev_in.copy_(host_dem, non_blocking=True)
-        S.launch(view_in, tiles, params, planes, stream=sh)
-        for n in names:
-            host_out[n].copy_(outs[n], non_blocking=True)
+        S.launch_host(host_dem, tiles, params, hplanes, stream=sh)
 
     for _ in range(max(1, min(args.warmup, 2))):
         e2e_step()
@@ -261,7 +263,10 @@ def stencil_workload(args, rank, world):
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e2e_steps, world)
-    del host_dem, host_out, dev_in
+    # correctness spot check of the host path against the device planes
+    ok = all(torch.equal(host_out[n][::4097, ::4097].cuda().nan_to_num(-7.0), outs[n][::4097, ::4097].nan_to_num(-7.0))
+             for n in names)
+    del host_dem, host_out
 
     line = {
         "metric": METRIC,
@@ -286,9 +291,10 @@ def stencil_workload(args, rank, world):
                      "algorithmic_bytes_per_px": ALG_BYTES_STENCIL_F32,
                      "traffic": profiled_traffic("stencil", px)},
         "e2e": {"value": round(world * px / (e2e_ms * 1e-3) / 1e6, 1), "unit": "Mpix/s",
-                "h2d_bytes_per_step": px * 4, "d2h_bytes_per_step": px * 4 * len(names),
-                "ms_per_step": round(e2e_ms, 3),
-                "path": "pinned host DEM -> cudaMemcpyAsync -> fsg_stencil (C ABI) -> 4 planes D2H"},
+                "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
+                "ms_per_step": round(e2e_ms, 3), "matches_device_path": bool(ok),
+                "path": "fsg_stencil_host (C ABI): pinned host DEM and planes, per-tile H2D/compute/D2H "
+                        "overlapped on 3 streams"},
         "gpu_launches": int(launches),
         "clocks": clk,
     }
@@ -305,6 +311,93 @@ def profiled_traffic(kind: str, px: int):
     return int(round(d["dram_bytes_per_px"] * px))
 
 
+# ------------------------------------------------------------ extra sections
+def _time_ms(fn, steps, warmup, stream):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def topousm_section(args):
+    """topousm_fast on a 32768^2 fBm+ridged DEM (Hurst 0.8, 0-3500 m, 10 m), radii 2..2048 with
+    2^n weights, 4096^2 tiles.  One step = the whole tile loop with the global scale known: NaN-aware
+    overview + large-radius coarse field + every tile's small-radius pass and normalisation."""
+    import torch
+    from fujishadergpu_gb300 import synth
+    from fujishadergpu_gb300.core import tile_loop
+    n = args.topousm_size
+    dem = synth.fbm_ridged_device(n, n, hurst=0.8, seed_fbm=3, seed_ridged=4, lo=0.0, hi=3500.0)
+    radii = [2, 8, 32, 128, 512, 2048]
+    w = [2.0 ** (5 - i) for i in range(6)]
+    w = [x / sum(w) for x in w]
+    kw = dict(tile_size=4096, pixel_size=10.0, radii=radii, weights=w)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = tile_loop.process_dem_array(dem, "topousm_fast", **kw)
+    torch.cuda.synchronize()
+    first_s = time.perf_counter() - t0
+    stats = res.stats
+    del res
+    stream = torch.cuda.current_stream()
+    ms = _time_ms(lambda: tile_loop.process_dem_array(dem, "topousm_fast", global_stats=stats, **kw),
+                  args.extra_steps, 2, stream)
+    px = n * n
+    hbm, _, _ = peaks()
+    gbs = 8.0 * px / (ms * 1e-3) / 1e9
+    del dem
+    return {"workload": f"topousm_fast {n}x{n} fBm+ridged, radii {radii}, 2^n weights, 10 m, 4096^2 tiles",
+            "value": round(px / (ms * 1e-3) / 1e6, 1), "unit": "Mpix/s", "ms_per_step": round(ms, 3),
+            "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(gbs / hbm, 4), "algorithmic_bytes_per_px": 8},
+            "first_call_s_incl_stats_prepass": round(first_s, 3),
+            "p99_scale": float(stats[0]) if stats else None, "dtype": "f32"}
+
+
+def openness_section(args):
+    """Exact openness (positive, 16 directions, R = 256, 5 m) on a 16384^2 fBm+ridged DEM with the
+    reference's 10 samples per ray; the dense every-step ray-march on a 4096^2 crop."""
+    import torch
+    from fujishadergpu_gb300 import _arrays, synth
+    from fujishadergpu_gb300.algorithms import _impl_openness as OP
+    from fujishadergpu_gb300.core import tile_loop
+    n = args.openness_size
+    dem = synth.fbm_ridged_device(n, n, hurst=0.7, seed_fbm=5, seed_ridged=6, lo=0.0, hi=3000.0)
+    v = _arrays.as_device_f32_2d(dem)
+    tiles = tile_loop.make_tiles(tile_loop.tile_grid(n, n, 4096, 256), pixel_scale_x=5.0, pixel_scale_y=-5.0)
+    out = torch.empty((n, n), device="cuda")
+    stream = torch.cuda.current_stream()
+    from fujishadergpu_gb300.algorithms._stencil import make_plane
+    res = {}
+    for mode, size in (("reference", n), ("dense", min(n, 4096))):
+        params = OP.make_params(max_distance=256, pixel_size=5.0, sampling=mode)
+        if mode == "dense":
+            sub = dem[:size, :size].contiguous()
+            vv = _arrays.as_device_f32_2d(sub)
+            tt = tile_loop.make_tiles(tile_loop.tile_grid(size, size, 4096, 256), pixel_scale_x=5.0,
+                                      pixel_scale_y=-5.0)
+            o = out[:size, :size]
+        else:
+            vv, tt, o = v, tiles, out
+        plane = make_plane(o)
+        ms = _time_ms(lambda: OP.run_openness(vv, tt, params, plane, None, stream=int(stream.cuda_stream)),
+                      max(1, args.extra_steps // 2), 1, stream)
+        px = size * size
+        samples = 160 if mode == "reference" else 16 * 256
+        res[mode] = {"raster": [size, size], "value": round(px / (ms * 1e-3) / 1e6, 1), "unit": "Mpix/s",
+                     "ms_per_step": round(ms, 3), "samples_per_px": samples,
+                     "gsamples_per_s": round(px * samples / (ms * 1e-3) / 1e9, 1)}
+    del dem, out
+    return {"workload": f"openness positive, 16 dirs, R=256, 5 m, {n}x{n} (reference sampling)", **res}
+
+
 # --------------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -317,6 +410,10 @@ def main():
     ap.add_argument("--tile", type=int, default=4096)
     ap.add_argument("--halo", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the topousm / openness sections")
+    ap.add_argument("--topousm-size", type=int, default=32768)
+    ap.add_argument("--openness-size", type=int, default=16384)
+    ap.add_argument("--extra-steps", type=int, default=4)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -325,6 +422,12 @@ def main():
 
     rank, world, _ = dist_setup(args.gpus)
     line = stencil_workload(args, rank, world)
+    if not args.no_extra:
+        import torch
+        torch.cuda.empty_cache()
+        line["extra"] = {"topousm_fast": topousm_section(args)}
+        torch.cuda.empty_cache()
+        line["extra"]["openness"] = openness_section(args)
     if rank == 0:
         if not args.no_cpu_baseline and world == 1:
             procs = max(1, os.cpu_count() or 1)

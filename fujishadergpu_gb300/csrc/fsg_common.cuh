@@ -103,6 +103,37 @@ __device__ __forceinline__ float quantize(float v, float qa, float qb, int qmin,
 }
 
 // ---------------------------------------------------- fast transcendentals
+// Float-float ("double-single") arithmetic on the FP32 pipes: a value is
+// hi + lo with |lo| <= ulp(hi)/2, about 48 significant bits.  Used for the
+// Gaussian filters, which scipy evaluates in float64: the float-float sum
+// rounds to the same float32 as scipy's float64 sum except when the exact value
+// lies within ~2^-44 (relative) of a float32 rounding boundary.  (GB300's FP64
+// rate is a small fraction of its FP32 rate.)
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ FF fast_two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  FF s = two_sum(a.hi, b.hi);
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
 // Hardware approximations (PTX *.approx instructions): relative error ~2^-22.
 __device__ __forceinline__ float ex2_approx(float x) {
   float r;

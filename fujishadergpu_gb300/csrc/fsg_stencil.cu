@@ -116,49 +116,6 @@ __device__ __forceinline__ float slope_value(float p, float q, int unit) {
   return r;
 }
 
-template <int DT>
-__device__ __forceinline__ void store4(const PlaneK& P, long long off, const float* v, int n) {
-  if (DT == FSG_F32) {
-    float* p = static_cast<float*>(P.ptr) + off;
-    if (n == 4 && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
-      *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
-    } else {
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if (k < n) p[k] = v[k];
-    }
-  } else if (DT == FSG_U8) {
-    uint8_t* p = static_cast<uint8_t*>(P.ptr) + off;
-    uint8_t b[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) b[k] = (uint8_t)(int)quantize(v[k], P.qa, P.qb, P.qmin, P.qmax);
-    if (n == 4 && ((reinterpret_cast<uintptr_t>(p) & 3) == 0)) {
-      *reinterpret_cast<uchar4*>(p) = make_uchar4(b[0], b[1], b[2], b[3]);
-    } else {
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if (k < n) p[k] = b[k];
-    }
-  } else {
-    int16_t* p = static_cast<int16_t*>(P.ptr) + off;
-    int16_t s[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) s[k] = (int16_t)(int)quantize(v[k], P.qa, P.qb, P.qmin, P.qmax);
-    if (n == 4 && ((reinterpret_cast<uintptr_t>(p) & 7) == 0)) {
-      *reinterpret_cast<short4*>(p) = make_short4(s[0], s[1], s[2], s[3]);
-    } else {
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if (k < n) p[k] = s[k];
-    }
-  }
-}
-
-__device__ __forceinline__ void store_plane(const PlaneK& P, long long off, const float* v, int n) {
-  if (P.dtype == FSG_F32) store4<FSG_F32>(P, off, v, n);
-  else if (P.dtype == FSG_U8) store4<FSG_U8>(P, off, v, n);
-  else store4<FSG_I16>(P, off, v, n);
-}
 
 // Loads rows [gy0, gy0+R) x cols [gx0, gx0+C) of the raster into S (row pitch
 // C), NoData -> NaN, cells outside the raster -> 0.  Returns true if this
@@ -234,37 +191,6 @@ struct Region {
   }
 };
 
-// Float-float ("double-single") arithmetic on the FP32 pipes: a value is
-// hi + lo with |lo| <= ulp(hi)/2, about 48 significant bits.  Used for the
-// NaN-fill Gaussian, which scipy evaluates in float64: the float-float sum
-// rounds to the same float32 as scipy's float64 sum except when the exact value
-// lies within ~2^-44 (relative) of a float32 rounding boundary.  (GB300's FP64
-// rate is a small fraction of its FP32 rate.)
-struct FF {
-  float hi, lo;
-};
-__device__ __forceinline__ FF two_sum(float a, float b) {
-  float s = __fadd_rn(a, b);
-  float bb = __fsub_rn(s, a);
-  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-  return {s, e};
-}
-__device__ __forceinline__ FF fast_two_sum(float a, float b) {
-  float s = __fadd_rn(a, b);
-  return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ FF ff_mul(FF a, FF b) {
-  float p = __fmul_rn(a.hi, b.hi);
-  float e = __fmaf_rn(a.hi, b.hi, -p);
-  e = __fmaf_rn(a.hi, b.lo, e);
-  e = __fmaf_rn(a.lo, b.hi, e);
-  return fast_two_sum(p, e);
-}
-__device__ __forceinline__ FF ff_add(FF a, FF b) {
-  FF s = two_sum(a.hi, b.hi);
-  return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
-}
-
 // scipy's symmetric 9-tap correlate1d, sum x[4]*w0 + (x[0]+x[8])*w4 + ...
 // + (x[3]+x[5])*w1 in float-float, rounded to float32.
 __device__ __forceinline__ float gsum_ff(const FF* w, const float* x) {
@@ -274,11 +200,6 @@ __device__ __forceinline__ float gsum_ff(const FF* w, const float* x) {
   return __fadd_rn(acc.hi, acc.lo);
 }
 
-__device__ __forceinline__ void store1(const PlaneK& P, long long off, float v) {
-  if (P.dtype == FSG_F32) static_cast<float*>(P.ptr)[off] = v;
-  else if (P.dtype == FSG_U8) static_cast<uint8_t*>(P.ptr)[off] = (uint8_t)(int)quantize(v, P.qa, P.qb, P.qmin, P.qmax);
-  else static_cast<int16_t*>(P.ptr)[off] = (int16_t)(int)quantize(v, P.qa, P.qb, P.qmin, P.qmax);
-}
 
 // Output products of one pixel from its derivatives.  Hillshade, slope and
 // the curvature formulas use hardware approximations of sqrt/rcp (relative
@@ -612,10 +533,10 @@ __global__ void __launch_bounds__(NT, FSG_STENCIL_MINB) stencil_kernel(const __g
 // columns and SH rows; lane l holds column x0 - 2 + l, walks down the rows
 // keeping f, dx, dy of the neighbouring rows in registers, and takes the
 // horizontal neighbours from warp shuffles (lanes 2..29 emit outputs).  No
-// shared memory, no barriers.  A unit that touches a window edge, and any
+// shared memory, no barriers.  A unit that touches a window edge, or holds a
 // valid pixel whose stencil reaches NoData (NaN propagates into its
-// derivatives), flags its 32 x 64 block; the exact shared-memory kernel then
-// recomputes every flagged block (NaN fill, one-sided edge formulas).
+// derivatives), is appended to a list; the fix-up kernel recomputes every
+// listed unit exactly (NaN fill, one-sided edge formulas).
 constexpr int SW = 28, SH = 64;
 
 struct FastTile {
@@ -635,10 +556,17 @@ struct FastArgs {
   int slope_unit;
   const FastTile* tiles;
   int ntiles, total_units;
-  unsigned char* unit_flags;  // 1: a pixel's stencil reaches NoData; 2: the unit touches a window edge
+  unsigned* fix_list;   // units for the fix-up pass: index | FIX_EDGE when the unit touches a window edge
+  unsigned* fix_count;  // number of entries in fix_list
   FF gw[5];                   // Gaussian fill weights (float-float)
   PlaneK planes[FSG_STENCIL_NOUT];
 };
+
+constexpr unsigned FIX_EDGE = 0x80000000u;
+__device__ __forceinline__ void push_fix(const FastArgs& A, int u, bool edge) {
+  const unsigned i = atomicAdd(A.fix_count, 1u);
+  A.fix_list[i] = (unsigned)u | (edge ? FIX_EDGE : 0u);
+}
 
 __device__ __forceinline__ float shfl_up1(float v) { return __shfl_up_sync(0xffffffffu, v, 1); }
 __device__ __forceinline__ float shfl_dn1(float v) { return __shfl_down_sync(0xffffffffu, v, 1); }
@@ -687,7 +615,7 @@ __device__ __forceinline__ void store_pixel(const FastArgs& A, unsigned om, bool
 // shared memory, no barriers.  Row groups of G are loaded one group ahead.  A
 // warp ballot per group tells whether any NoData feeds it; only then are the
 // per-pixel checks evaluated.  Units touching a window edge, and units with a
-// valid pixel whose stencil reaches NoData, are flagged for the fix-up pass.
+// valid pixel whose stencil reaches NoData, are listed for the fix-up pass.
 // DIV: derivatives use the correctly rounded division (bit-exact np.gradient,
 // needed for the dx/dy planes); otherwise a multiply by the reciprocal.
 template <bool CURV, unsigned OM, bool ALLF32>
@@ -706,7 +634,7 @@ __global__ void __launch_bounds__(256) stencil_fast_kernel(const __grid_constant
     // the window, so every derivative is a central difference
     const bool interior = y0 - 2 >= T.wy0 && y1 + 2 <= T.wy1 && x0 - 2 >= T.wx0 && x0 + SW + 2 <= T.wx1;
     if (!interior) {
-      if (lane == 0) A.unit_flags[u] = 2;
+      if (lane == 0) push_fix(A, u, true);
       continue;
     }
     const int x = x0 - 2 + lane;
@@ -813,126 +741,220 @@ __global__ void __launch_bounds__(256) stencil_fast_kernel(const __grid_constant
 #pragma unroll
       for (int k = 0; k < G; ++k) cur[k] = nxt[k];
     }
-    if (__ballot_sync(0xffffffffu, bad) && lane == 0) A.unit_flags[u] = 1;
+    if (__ballot_sync(0xffffffffu, bad) && lane == 0) push_fix(A, u, false);
   }
 }
 
 // ------------------------------------------------------------- fix-up pass
-// NaN-aware Gaussian fill value of window cell (gy, gx): separable 9x9
-// normalised convolution with 'nearest' clamping at the window edges, in
-// float-float (_nan_utils.py:18-31 with the axis order of scipy).
-__device__ float fill_value(const FastArgs& A, const FastTile& T, int gy, int gx) {
-  const bool hn = A.has_nodata != 0;
-  float vv[9], vw[9];
-#pragma unroll 1
-  for (int j = 0; j < 9; ++j) {
-    const int xx = min(max(gx + j - 4, T.wx0), T.wx1 - 1);
-    float xv[9], xw[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) {
-      const int yy = min(max(gy + i - 4, T.wy0), T.wy1 - 1);
-      float v = __ldg(A.raster + (long long)yy * A.ld + xx);
-      const bool ok = !is_nodata(v, A.ndf, hn);
-      xv[i] = ok ? v : 0.f;
-      xw[i] = ok ? 1.f : 0.f;
-    }
-    vv[j] = gsum_ff(A.gw, xv);
-    vw[j] = gsum_ff(A.gw, xw);
+// One CTA per listed unit recomputes all of its pixels with the full
+// reference semantics in shared memory: NoData cells within reach of a valid
+// output pixel get the NaN-aware Gaussian fill (_nan_utils.py:18-31: separable
+// sigma = 1, radius 4, 'nearest' at the window edges, axis 0 then axis 1 with a
+// float32 intermediate, sums in float-float), then np.gradient with the
+// window's edge rules and the second derivatives on the signed steps.
+// Regions, relative to the unit origin (y0, x0):
+//   S  source values        rows -8 .. SH+8, cols -8 .. SW+8 (NaN outside the window)
+//   E  filled values        rows -4 .. SH+4, cols -4 .. SW+4
+//   D  first derivatives    rows -2 .. SH+2, cols -2 .. SW+2 (curvature only)
+constexpr int XS_R = SH + 16, XS_C = SW + 16;  // 80 x 44
+constexpr int XE_R = SH + 8, XE_C = SW + 8;    // 72 x 36
+constexpr int XD_R = SH + 4, XD_C = SW + 4;    // 68 x 32
+constexpr int XNT = 256;
+constexpr size_t FIX_SMEM = sizeof(float) * (XS_R * XS_C + XE_R * XE_C) +
+                            sizeof(float) * 2 * XE_R * XS_C +            // axis-0 sums (aliases D)
+                            sizeof(unsigned long long) * 4 * XE_R;        // row bitmasks
+static_assert(2 * XD_R * XD_C <= 2 * XE_R * XS_C, "derivative planes alias the axis-0 sums");
+static_assert(XE_C <= 64 && XS_C <= 64, "row bitmasks are 64 bits");
+
+template <bool DIV, class Fn>
+__device__ __forceinline__ float deriv_d(const Axis& a, int k, int lo, int hi, Fn f) {
+  if (k > lo && k < hi - 1) {
+    const float num = fsub(f(1), f(-1));
+    return DIV ? div_by(num, a.d2, a.rcp) : fmul(num, a.rcp);
   }
-  const float sv = gsum_ff(A.gw, vv), sw = gsum_ff(A.gw, vw);
-  return sw > 0.0f ? __fdiv_rn(sv, sw) : 0.0f;
+  if (k == lo) return fadd(fadd(fmul(a.fa, f(0)), fmul(a.fb, f(1))), fmul(a.fc, f(2)));
+  return fadd(fadd(fmul(a.ba, f(-2)), fmul(a.bb, f(-1))), fmul(a.bc, f(0)));
 }
 
-// Outputs of one valid pixel with the full reference semantics: the filled
-// values of its 9 x 9 neighbourhood (fills only for the NaN cells the formulas
-// read), np.gradient with the window's edge rules, second derivatives on the
-// signed steps.
-template <unsigned OM>
-__device__ void exact_pixel(const FastArgs& A, const FastTile& T, int gy, int gx, float* o) {
-  constexpr bool CURV = (OM & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) |
-                               (1u << FSG_OUT_CURV_PLANFORM) | (1u << FSG_OUT_CURV_PROFILE))) != 0;
-  const bool hn = A.has_nodata != 0;
-  float f[9][9];
-#pragma unroll 1
-  for (int r = 0; r < 9; ++r)
-#pragma unroll 1
-    for (int c = 0; c < 9; ++c) {
-      const int yy = gy + r - 4, xx = gx + c - 4;
-      // cells the derivative formulas can read: |dr| + |dc| <= 4 (central
-      // differences reach 2, one-sided edge formulas one more step)
-      const bool used = (abs(r - 4) + abs(c - 4)) <= (CURV ? 4 : 2) && (CURV || abs(r - 4) <= 2) &&
-                        (CURV || abs(c - 4) <= 2);
-      float v = __int_as_float(0x7fc00000);
-      if (used && yy >= T.wy0 && yy < T.wy1 && xx >= T.wx0 && xx < T.wx1) {
-        v = __ldg(A.raster + (long long)yy * A.ld + xx);
-        if (is_nodata(v, A.ndf, hn)) v = fill_value(A, T, yy, xx);
-      }
-      f[r][c] = v;
-    }
-  auto dx_at = [&](int r, int c) {
-    return deriv(T.g1x, gx + c, T.wx0, T.wx1, [&](int k) { return f[r + 4][c + 4 + k]; });
-  };
-  auto dy_at = [&](int r, int c) {
-    return deriv(T.g1y, gy + r, T.wy0, T.wy1, [&](int k) { return f[r + 4 + k][c + 4]; });
-  };
-  const float p = dx_at(0, 0), q = dy_at(0, 0);
-  float dxx = 0.f, dxy = 0.f, dyy = 0.f, dyx = 0.f;
-  if (CURV) {
-    dxx = deriv(T.c2x, gx, T.wx0, T.wx1, [&](int k) { return dx_at(0, k); });
-    dxy = deriv(T.c2y, gy, T.wy0, T.wy1, [&](int k) { return dx_at(k, 0); });
-    dyy = deriv(T.c2y, gy, T.wy0, T.wy1, [&](int k) { return dy_at(k, 0); });
-    if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = deriv(T.c2x, gx, T.wx0, T.wx1, [&](int k) { return dy_at(0, k); });
-  }
-  float pz = p, qz = q;
-  if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) {
-    const float zf = A.z;
-    pz = deriv(T.g1x, gx, T.wx0, T.wx1, [&](int k) { return fmul(f[4][4 + k], zf); });
-    qz = deriv(T.g1y, gy, T.wy0, T.wy1, [&](int k) { return fmul(f[4 + k][4], zf); });
-  }
-  const Light L{A.lx, A.ly, A.lz, A.slope_unit};
-  pixel_products(L, T.sx, T.sy, OM, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
-}
-
-// Recomputes the pixels of flagged units that the fast pass could not produce
-// exactly: every pixel of a unit touching a window edge, and in the other
-// flagged units the valid pixels whose stencil footprint holds NoData.
 template <unsigned OM, bool ALLF32>
-__global__ void __launch_bounds__(128) stencil_fixup_kernel(const __grid_constant__ FastArgs A) {
+__global__ void __launch_bounds__(XNT) stencil_fixup_kernel(const __grid_constant__ FastArgs A) {
   constexpr bool CURV = (OM & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) |
                                (1u << FSG_OUT_CURV_PLANFORM) | (1u << FSG_OUT_CURV_PROFILE))) != 0;
-  const int lane = threadIdx.x & 31;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  constexpr bool DIV = (OM & ((1u << FSG_OUT_DX) | (1u << FSG_OUT_DY))) != 0;
+  extern __shared__ __align__(16) unsigned char fix_smem[];
+  float* Sv = reinterpret_cast<float*>(fix_smem);
+  float* Fv = Sv + XS_R * XS_C;
+  float* VV = Fv + XE_R * XE_C;
+  float* VW = VV + XE_R * XS_C;
+  float* DX = VV;  // reused once the fills are done
+  float* DY = DX + XD_R * XD_C;
+  unsigned long long* VO = reinterpret_cast<unsigned long long*>(VW + XE_R * XS_C);  // valid output pixels
+  unsigned long long* NB = VO + XE_R;   // NoData cells inside the window
+  unsigned long long* ND = NB + XE_R;   // cells to fill (E columns)
+  unsigned long long* NV = ND + XE_R;   // axis-0 sums to form (S columns)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const bool hn = A.has_nodata != 0;
-  const int reach = CURV ? 2 : 1;
-  for (int u = warp; u < A.total_units; u += nwarps) {
-    const int flag = A.unit_flags[u];
-    if (!flag) continue;
-    const UnitGeom g = unit_geom(A, u);
+  const float qnan = __int_as_float(0x7fc00000);
+  const unsigned count = *A.fix_count;
+  for (unsigned it = blockIdx.x; it < count; it += gridDim.x) {
+    const unsigned e = A.fix_list[it];
+    const bool edge = (e & FIX_EDGE) != 0;
+    const UnitGeom g = unit_geom(A, (int)(e & ~FIX_EDGE));
     const FastTile& T = A.tiles[g.t];
-    const int x = g.x0 + lane;
-    if (lane >= SW || x >= g.xo) continue;
-    for (int y = g.y0; y < g.y1; ++y) {
-      float zc = __ldg(A.raster + (long long)y * A.ld + x);
-      const bool valid = !is_nodata(zc, A.ndf, hn);
-      bool need = flag == 2;
-      if (!need && valid) {
-        for (int dr = -reach; dr <= reach && !need; ++dr)
-          for (int dc = -reach; dc <= reach; ++dc) {
-            const float v = __ldg(A.raster + (long long)(y + dr) * A.ld + x + dc);
-            if (is_nodata(v, A.ndf, hn)) {
-              need = true;
-              break;
-            }
-          }
+    const int x0 = g.x0, y0 = g.y0, y1 = g.y1, xo = g.xo;
+    // (a) source region, NoData -> NaN, outside the window -> NaN (never read)
+    for (int i = tid; i < XS_R * XS_C; i += XNT) {
+      const int r = i / XS_C, c = i - (i / XS_C) * XS_C;
+      const int gy = y0 - 8 + r, gx = x0 - 8 + c;
+      float v = qnan;
+      if (gy >= T.wy0 && gy < T.wy1 && gx >= T.wx0 && gx < T.wx1) {
+        v = __ldg(A.raster + (long long)gy * A.ld + gx);
+        if (is_nodata(v, A.ndf, hn)) v = qnan;
       }
-      if (!need) continue;
+      Sv[i] = v;
+    }
+    __syncthreads();
+    // (b) row bitmasks of valid output pixels and of in-window NoData cells;
+    //     E starts as a copy of the source values
+    for (int r = warp; r < XE_R; r += XNT / 32) {
+      const int gy = y0 - 4 + r;
+      const bool row_out = gy >= y0 && gy < y1, row_win = gy >= T.wy0 && gy < T.wy1;
+      unsigned long long vo = 0, nb = 0;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int c = h * 32 + lane;
+        bool o = false, n = false;
+        if (c < XE_C) {
+          const float v = Sv[(r + 4) * XS_C + c + 4];
+          Fv[r * XE_C + c] = v;
+          const int gx = x0 - 4 + c;
+          o = row_out && gx >= x0 && gx < xo && v == v;
+          n = row_win && gx >= T.wx0 && gx < T.wx1 && v != v;
+        }
+        vo |= (unsigned long long)__ballot_sync(0xffffffffu, o) << (32 * h);
+        nb |= (unsigned long long)__ballot_sync(0xffffffffu, n) << (32 * h);
+      }
+      if (lane == 0) {
+        VO[r] = vo;
+        NB[r] = nb;
+      }
+    }
+    __syncthreads();
+    // (c) NoData cells within the derivative reach of a valid output pixel:
+    //     2 for central differences, 3 where one-sided edge formulas occur
+    const int R = edge ? 3 : 2;
+    bool any = false;
+    if (tid < XE_R) {
+      unsigned long long v = 0;
+      for (int k = -R; k <= R; ++k)
+        if (tid + k >= 0 && tid + k < XE_R) v |= VO[tid + k];
+      unsigned long long d = v;
+      for (int k = 1; k <= R; ++k) d |= (v << k) | (v >> k);
+      const unsigned long long need = d & NB[tid];
+      ND[tid] = need;
+      any = need != 0;
+    }
+    if (__syncthreads_or(any)) {
+      // (d) axis-0 sums needed by the axis-1 pass: S columns within 4 of a
+      //     cell to fill, inside the window
+      if (tid < XE_R) {
+        const unsigned long long n = ND[tid] << 4;
+        unsigned long long d = n;
+#pragma unroll
+        for (int k = 1; k <= 4; ++k) d |= (n << k) | (n >> k);
+        const int c_lo = max(T.wx0 - (x0 - 8), 0), c_hi = min(T.wx1 - (x0 - 8), XS_C);
+        const unsigned long long win =
+            c_hi > c_lo ? (((c_hi - c_lo) >= 64 ? ~0ull : ((1ull << (c_hi - c_lo)) - 1ull)) << c_lo) : 0ull;
+        NV[tid] = d & win;
+      }
+      __syncthreads();
+      FF gw[5];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) gw[j] = A.gw[j];
+      for (int i = tid; i < XE_R * XS_C; i += XNT) {
+        const int r = i / XS_C, sc = i - (i / XS_C) * XS_C;
+        if (!((NV[r] >> sc) & 1ull)) continue;
+        const int gy = y0 - 4 + r;
+        float xv[9], xw[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+          const int yy = min(max(gy + j - 4, T.wy0), T.wy1 - 1);
+          const float v = Sv[(yy - (y0 - 8)) * XS_C + sc];
+          const bool ok = v == v;
+          xv[j] = ok ? v : 0.f;
+          xw[j] = ok ? 1.f : 0.f;
+        }
+        VV[i] = gsum_ff(gw, xv);
+        VW[i] = gsum_ff(gw, xw);
+      }
+      __syncthreads();
+      // (e) axis-1 pass and the normalised fill value of each cell to fill
+      for (int i = tid; i < XE_R * XE_C; i += XNT) {
+        const int r = i / XE_C, c = i - (i / XE_C) * XE_C;
+        if (!((ND[r] >> c) & 1ull)) continue;
+        const int gx = x0 - 4 + c;
+        float xv[9], xw[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+          const int sc = min(max(gx + j - 4, T.wx0), T.wx1 - 1) - (x0 - 8);
+          xv[j] = VV[r * XS_C + sc];
+          xw[j] = VW[r * XS_C + sc];
+        }
+        const float sv = gsum_ff(gw, xv), sw = gsum_ff(gw, xw);
+        Fv[i] = sw > 0.0f ? __fdiv_rn(sv, sw) : 0.0f;
+      }
+      __syncthreads();
+    }
+    auto fe = [&](int gy, int gx) { return Fv[(gy - (y0 - 4)) * XE_C + (gx - (x0 - 4))]; };
+    // (f) first derivatives around the unit (curvature)
+    if (CURV) {
+      for (int i = tid; i < XD_R * XD_C; i += XNT) {
+        const int r = i / XD_C, c = i - (i / XD_C) * XD_C;
+        const int gy = y0 - 2 + r, gx = x0 - 2 + c;
+        float dx = qnan, dy = qnan;
+        if (gy >= T.wy0 && gy < T.wy1 && gx >= T.wx0 && gx < T.wx1) {
+          dx = deriv_d<DIV>(T.g1x, gx, T.wx0, T.wx1, [&](int k) { return fe(gy, gx + k); });
+          dy = deriv_d<DIV>(T.g1y, gy, T.wy0, T.wy1, [&](int k) { return fe(gy + k, gx); });
+        }
+        DX[i] = dx;
+        DY[i] = dy;
+      }
+      __syncthreads();
+    }
+    // (g) outputs of every pixel of the unit
+    const Light L{A.lx, A.ly, A.lz, A.slope_unit};
+    for (int i = tid; i < SH * SW; i += XNT) {
+      const int r = i / SW, c = i - (i / SW) * SW;
+      const int gy = y0 + r, gx = x0 + c;
+      if (gy >= y1 || gx >= xo) continue;
       float o[FSG_STENCIL_NOUT];
-      if (valid) {
-        exact_pixel<OM>(A, T, y, x, o);
+      const float z0 = Sv[(r + 8) * XS_C + c + 8];
+      if (z0 == z0) {
+        float p, q, dxx = 0.f, dxy = 0.f, dyy = 0.f, dyx = 0.f;
+        if (CURV) {
+          auto dxa = [&](int yy, int xx) { return DX[(yy - (y0 - 2)) * XD_C + (xx - (x0 - 2))]; };
+          auto dya = [&](int yy, int xx) { return DY[(yy - (y0 - 2)) * XD_C + (xx - (x0 - 2))]; };
+          p = dxa(gy, gx);
+          q = dya(gy, gx);
+          dxx = deriv_d<DIV>(T.c2x, gx, T.wx0, T.wx1, [&](int k) { return dxa(gy, gx + k); });
+          dxy = deriv_d<DIV>(T.c2y, gy, T.wy0, T.wy1, [&](int k) { return dxa(gy + k, gx); });
+          dyy = deriv_d<DIV>(T.c2y, gy, T.wy0, T.wy1, [&](int k) { return dya(gy + k, gx); });
+          if (OM & (1u << FSG_OUT_CURV_MEAN))
+            dyx = deriv_d<DIV>(T.c2x, gx, T.wx0, T.wx1, [&](int k) { return dya(gy, gx + k); });
+        } else {
+          p = deriv_d<DIV>(T.g1x, gx, T.wx0, T.wx1, [&](int k) { return fe(gy, gx + k); });
+          q = deriv_d<DIV>(T.g1y, gy, T.wy0, T.wy1, [&](int k) { return fe(gy + k, gx); });
+        }
+        float pz = p, qz = q;
+        if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) {
+          const float zf = A.z;
+          pz = deriv_d<DIV>(T.g1x, gx, T.wx0, T.wx1, [&](int k) { return fmul(fe(gy, gx + k), zf); });
+          qz = deriv_d<DIV>(T.g1y, gy, T.wy0, T.wy1, [&](int k) { return fmul(fe(gy + k, gx), zf); });
+        }
+        pixel_products(L, T.sx, T.sy, OM, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
       } else {
 #pragma unroll
-        for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) o[kk] = __int_as_float(0x7fc00000);
+        for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) o[kk] = qnan;
       }
       char* optr[FSG_STENCIL_NOUT];
 #pragma unroll
@@ -940,10 +962,11 @@ __global__ void __launch_bounds__(128) stencil_fixup_kernel(const __grid_constan
         if (!(OM & (1u << k))) continue;
         const PlaneK& P = A.planes[k];
         const int esz = ALLF32 ? 4 : (P.dtype == FSG_F32 ? 4 : (P.dtype == FSG_I16 ? 2 : 1));
-        optr[k] = static_cast<char*>(P.ptr) + ((long long)(T.oy0 + y - T.cy0) * P.ld + (T.ox0 + x - T.cx0)) * esz;
+        optr[k] = static_cast<char*>(P.ptr) + ((long long)(T.oy0 + gy - T.cy0) * P.ld + (T.ox0 + gx - T.cx0)) * esz;
       }
       store_pixel(A, OM, ALLF32, optr, o);
     }
+    __syncthreads();
   }
 }
 
@@ -1154,11 +1177,11 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
     }
     StreamScratch fscr;
     const size_t tiles_bytes = (sizeof(FastTile) * ft.size() + 255) & ~(size_t)255;
-    st = fscr.alloc(tiles_bytes + (size_t)units, s);
+    st = fscr.alloc(tiles_bytes + sizeof(unsigned) * ((size_t)units + 1), s);
     if (st) return st;
-    unsigned char* uflags = static_cast<unsigned char*>(fscr.ptr) + tiles_bytes;
+    unsigned* fix = reinterpret_cast<unsigned*>(static_cast<unsigned char*>(fscr.ptr) + tiles_bytes);
     FSG_CUDA(cudaMemcpyAsync(fscr.ptr, ft.data(), sizeof(FastTile) * ft.size(), cudaMemcpyHostToDevice, s));
-    FSG_CUDA(cudaMemsetAsync(uflags, 0, (size_t)units, s));
+    FSG_CUDA(cudaMemsetAsync(fix, 0, sizeof(unsigned), s));
     FastArgs F;
     std::memset(&F, 0, sizeof(F));
     F.raster = A.raster;
@@ -1171,7 +1194,8 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
     F.tiles = static_cast<const FastTile*>(fscr.ptr);
     F.ntiles = (int)ft.size();
     F.total_units = units;
-    F.unit_flags = uflags;
+    F.fix_count = fix;
+    F.fix_list = fix + 1;
     for (int j = 0; j < 5; ++j) F.gw[j] = {A.gw_hi[j], A.gw_lo[j]};
     std::copy(A.planes, A.planes + FSG_STENCIL_NOUT, F.planes);
     int fper = 0;
@@ -1179,10 +1203,11 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
     const int fgrid = std::min((units + 7) / 8, di.sms * std::max(1, fper));
     fast<<<fgrid, 256, 0, s>>>(F);
     FSG_LAUNCHED(1);
+    FSG_CUDA(cudaFuncSetAttribute(fixup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FIX_SMEM));
     int xper = 0;
-    FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&xper, fixup, 128, 0));
-    const int xgrid = std::min((units + 3) / 4, di.sms * std::max(1, xper));
-    fixup<<<xgrid, 128, 0, s>>>(F);
+    FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&xper, fixup, XNT, FIX_SMEM));
+    const int xgrid = std::min(units, di.sms * std::max(1, xper));
+    fixup<<<xgrid, XNT, FIX_SMEM, s>>>(F);
     FSG_LAUNCHED(1);
     return FSG_OK;
   }
