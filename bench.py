@@ -75,6 +75,15 @@ class ClockSampler:
                  "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+        # wait for the first sample: nvidia-smi's NVML start-up must not overlap the timed region
+        t0 = time.time()
+        while self.proc is not None and time.time() - t0 < 10.0:
+            try:
+                if os.path.getsize(self.path) > 0:
+                    break
+            except OSError:
+                pass
+            time.sleep(0.05)
         time.sleep(0.3)
 
     def stop(self):
@@ -246,7 +255,13 @@ def stencil_workload(args, rank, world):
     host_dem.copy_(dem)
     host_out = {n: torch.empty((H, W), dtype=torch.float32, pin_memory=True) for n in names}
     hplanes = {S.OUTPUT_INDEX[n]: S.host_plane(host_out[n]) for n in names}
-    h2d_bytes = sum(int(t.win_h) * int(t.win_w) * 4 for t in tiles)
+    # the host loop copies each row band's window union once (one block per band)
+    bands = {}
+    for t in tiles:
+        k = (int(t.core_y0), int(t.win_y0), int(t.win_h))
+        x0, x1 = bands.get(k, (1 << 30, -1))
+        bands[k] = (min(x0, int(t.win_x0)), max(x1, int(t.win_x0) + int(t.win_w)))
+    h2d_bytes = sum(k[2] * (x1 - x0) * 4 for k, (x0, x1) in bands.items())
     d2h_bytes = px * 4 * len(names)
 
     def e2e_step():
@@ -289,12 +304,12 @@ def stencil_workload(args, rank, world):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "peak_kind": peak_kind + " (burst copy)",
                      "algorithmic_bytes_per_px": ALG_BYTES_STENCIL_F32,
-                     "traffic": profiled_traffic("stencil", px)},
+                     "traffic": profiled_traffic("stencil_fast_kernel_fused4_f32", px)},
         "e2e": {"value": round(world * px / (e2e_ms * 1e-3) / 1e6, 1), "unit": "Mpix/s",
                 "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                 "ms_per_step": round(e2e_ms, 3), "matches_device_path": bool(ok),
-                "path": "fsg_stencil_host (C ABI): pinned host DEM and planes, per-tile H2D/compute/D2H "
-                        "overlapped on 3 streams"},
+                "path": "fsg_stencil_host (C ABI): pinned host DEM and planes; per row band of tiles one "
+                        "H2D block, one kernel call, one D2H block per plane, overlapped on 3 streams"},
         "gpu_launches": int(launches),
         "clocks": clk,
     }
@@ -302,13 +317,16 @@ def stencil_workload(args, rank, world):
 
 
 def profiled_traffic(kind: str, px: int):
-    """dram read+write bytes per launch from the committed ncu summary, scaled by pixels."""
-    p = os.path.join(ROOT, "profiles", f"{kind}_traffic.json")
+    """DRAM read+write bytes of the dominant kernel's launch, scaled to ``px`` pixels from
+    the ``dram_bytes_per_px:`` line of the committed ncu summary (None if absent)."""
+    p = os.path.join(ROOT, "profiles", f"{kind}.txt")
     if not os.path.exists(p):
         return None
     with open(p) as f:
-        d = json.load(f)
-    return int(round(d["dram_bytes_per_px"] * px))
+        for line in f:
+            if line.strip().startswith("dram_bytes_per_px:"):
+                return int(round(float(line.split(":", 1)[1].split()[0]) * px))
+    return None
 
 
 # ------------------------------------------------------------ extra sections

@@ -120,6 +120,19 @@ _SIGNATURES = {
                                        C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32]),
     "fsg_affine": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32,
                              C.POINTER(Plane), C.c_void_p]),
+    "fsg_smooth": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double,
+                             C.c_void_p, C.c_int64, C.c_void_p]),
+    "fsg_pad_reflect": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                  C.c_int32, C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]),
+    "fsg_accumulate": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_int32, C.c_void_p,
+                                 C.c_int64, C.c_void_p]),
+    "fsg_sample_coarse_accumulate": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
+                                               C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                               C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_int32,
+                                               C.c_float, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]),
+    "fsg_masked_store": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                   C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(Plane),
+                                   C.c_void_p]),
 }
 
 

@@ -265,8 +265,24 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
         params["radii"] = r
         if not params.get("weights"):
             params["weights"] = auto_spatial_weights(len(r))
-    if mode == "spatial" and algorithm in ("hillshade", "slope", "curvature", "openness"):
-        raise NotImplementedError("spatial mode of %s is not available in this build; use mode='local'" % algorithm)
+    if mode == "spatial" and algorithm == "openness":
+        raise NotImplementedError("spatial mode of openness is not available in this build; use mode='local'")
+    spatial = mode == "spatial" and algorithm in ("hillshade", "slope", "curvature")
+    if spatial:
+        # _sanitize_spatial_radii_weights_for_tile (core/tile_processor.py:100-127): integer
+        # radii >= 1, duplicates merged with their weights
+        ints = []
+        for r in params.get("radii") or []:
+            try:
+                fv = float(r)
+            except (TypeError, ValueError):
+                continue
+            if fv > 0:
+                ints.append(max(1, int(round(fv))))
+        if ints:
+            dr, dw = deduplicate_radii_weights(ints, params.get("weights"))
+            params["radii"] = dr
+            params["weights"] = dw
 
     # topousm_fast large-radius overview split (tile_processor.py:1236-1281)
     if algorithm == "topousm_fast":
@@ -295,7 +311,9 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
     out.fill_(fill)  # tiles skipped for NoData keep the NoData value
     res = LoopResult(out, output_dtype, qp, len(tiles), pad)
 
-    if algorithm in ("hillshade", "slope", "curvature"):
+    if spatial:
+        _spatial_loop(v, infos, tiles, algorithm, params, px, nodata, out, output_dtype, qp)
+    elif algorithm in ("hillshade", "slope", "curvature"):
         name = {"hillshade": "hillshade", "slope": "slope"}.get(algorithm)
         if algorithm == "curvature":
             ct = params.get("curvature_type", "mean")
@@ -324,3 +342,25 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
                             sampling=params.get("sampling", "reference"), nodata=nodata, stretch=stats)
         OP.run_openness(v, tiles, op, S.make_plane(out, output_dtype, qp))
     return res
+
+
+def _spatial_loop(v, infos, tiles, algorithm, params, px, nodata, out, output_dtype, qp):
+    """Spatial mode of a stencil product over the tile grid (one spatial_tile per tile;
+    large radii from one shared overview)."""
+    from ..algorithms import _spatial as SP
+    from ..common.spatial_mode import resolve_spatial_radii_weights
+    radii, weights = resolve_spatial_radii_weights(params.get("radii"), params.get("weights"), px)
+    if algorithm == "hillshade" and params.get("weights") is not None:
+        weights = params.get("weights")   # _impl_hillshade.py:84-87 keeps the caller's weights
+    kw = SP._product_kwargs(algorithm, params)
+    overview = None
+    if radii and max(int(round(float(r))) for r in radii) > 256:
+        overview = SP.Overview(v, nodata=nodata)
+    scratch: dict = {}
+    for info, t in zip(infos, tiles):
+        plane = S.make_plane(out[info.core_y:info.core_y + info.core_h, info.core_x:info.core_x + info.core_w],
+                             output_dtype, qp)
+        SP.spatial_tile(v, (info.win_y, info.win_x, info.win_h, info.win_w),
+                        (info.core_y, info.core_x, info.core_h, info.core_w), algorithm, radii, weights, kw,
+                        pixel_size=px, psx=float(t.pixel_scale_x), psy=float(t.pixel_scale_y), nodata=nodata,
+                        overview=overview, plane=plane, scratch=scratch)

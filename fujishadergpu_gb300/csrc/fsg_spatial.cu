@@ -1,0 +1,542 @@
+// Spatial mode of the stencil products: the per-radius smoothing
+// _smooth_for_radius (algorithms/_nan_utils.py:527-552) and the pieces of the
+// tile backend's per-radius response and weighted combination
+// (multiscale_response_fields, _nan_utils.py:441-524).
+//
+// The smoothing reproduces scipy's arithmetic closely enough that the
+// derivative products computed from it stay within float32 rounding of the
+// reference (derivatives of a smoothed DEM amplify any error of the
+// smoothing):
+//   * gaussian_filter: per axis, correlate1d with float64 weights and a
+//     float64 accumulator, rounded to float32 after each axis.  Here the
+//     accumulation is float-float (~48 bits) on the FP32 pipes and each axis
+//     output is rounded once to float32.
+//   * the block mean of _downsample_nan_aware sums in NumPy's float32 order:
+//     for each row of a cell, NumPy's pairwise sum of the row, added to the
+//     running cell total (the reduction over axes (1, 3) of a C-contiguous
+//     (oh, f, ow, f) array).
+//   * the corner-aligned order-1 zoom interpolates in float64 (as scipy
+//     does), summing the four corner terms in scipy's order, then rounds.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fsg_filters.cuh"
+
+namespace fsg {
+namespace {
+
+constexpr int NT = 256;
+constexpr float kQNaN = __builtin_nanf("");
+
+// ------------------------------------------------------------ Gaussian
+// x * w for a float x and a float-float weight.
+__device__ __forceinline__ FF ff_scale(float x, FF w) {
+  const float p = __fmul_rn(x, w.hi);
+  float e = __fmaf_rn(x, w.hi, -p);
+  e = __fmaf_rn(x, w.lo, e);
+  return fast_two_sum(p, e);
+}
+
+// Symmetric correlate1d at one output: x(0) * w0, then the pairs from the
+// outermost inwards, (x(-k) + x(k)) * wk, the order of scipy's symmetric
+// branch.  The pair sum is exact as a float-float.
+template <class Fn>
+__device__ __forceinline__ float corr_ff(const FF* __restrict__ g, int R, Fn x) {
+  FF acc = ff_scale(x(0), g[0]);
+  for (int k = R; k >= 1; --k) acc = ff_add(acc, ff_mul(two_sum(x(-k), x(k)), g[k]));
+  return __fadd_rn(acc.hi, acc.lo);
+}
+
+// Axis-0 pass ('nearest').  Channel v: the values (NaN -> 0 when two
+// channels are formed); channel w: the valid mask.  Two channels are formed
+// when `two` is set, or when *nan_flag is nonzero.
+__global__ void __launch_bounds__(NT) gauss_axis0(const float* __restrict__ src, long long ld, int h, int w,
+                                                  const FF* __restrict__ g, int R, int two, const int* nan_flag,
+                                                  float* v, float* wt, long long old, int rows_per_block) {
+  const int x = blockIdx.x * NT + threadIdx.x;
+  if (x >= w) return;
+  const bool pair = two || (nan_flag != nullptr && *nan_flag != 0);
+  const int y0 = blockIdx.y * rows_per_block, y1 = min(h, y0 + rows_per_block);
+  for (int y = y0; y < y1; ++y) {
+    auto val = [&](int k) {
+      const float a = __ldg(src + (long long)clamp_idx(y + k, h) * ld + x);
+      return pair ? (a == a ? a : 0.f) : a;
+    };
+    v[(long long)y * old + x] = corr_ff(g, R, val);
+    if (pair) {
+      auto ok = [&](int k) {
+        const float a = __ldg(src + (long long)clamp_idx(y + k, h) * ld + x);
+        return a == a ? 1.f : 0.f;
+      };
+      wt[(long long)y * old + x] = corr_ff(g, R, ok);
+    }
+  }
+}
+
+enum Axis1Mode { AX1_SMOOTH = 0, AX1_PAIR = 1 };
+
+// Axis-1 pass ('nearest').  AX1_SMOOTH: without NaN in the source (flag 0)
+// the filtered values; otherwise where(den > 0, num / den, 0)
+// (_nan_utils.py:18-31).  AX1_PAIR: both filtered channels (the void fill).
+__global__ void __launch_bounds__(NT) gauss_axis1(const float* __restrict__ v, const float* __restrict__ wt,
+                                                  long long ld, int h, int w, const FF* __restrict__ g, int R,
+                                                  int mode, const int* nan_flag, float* out, float* out2,
+                                                  long long old) {
+  const int x = blockIdx.x * NT + threadIdx.x;
+  if (x >= w) return;
+  const bool pair = mode == AX1_PAIR || (nan_flag != nullptr && *nan_flag != 0);
+  for (int y = blockIdx.y; y < h; y += gridDim.y) {
+    const float* rv = v + (long long)y * ld;
+    const float num = corr_ff(g, R, [&](int k) { return __ldg(rv + clamp_idx(x + k, w)); });
+    if (!pair) {
+      out[(long long)y * old + x] = num;
+      continue;
+    }
+    const float* rw = wt + (long long)y * ld;
+    const float den = corr_ff(g, R, [&](int k) { return __ldg(rw + clamp_idx(x + k, w)); });
+    if (mode == AX1_PAIR) {
+      out[(long long)y * old + x] = num;
+      out2[(long long)y * old + x] = den;
+    } else {
+      out[(long long)y * old + x] = den > 0.f ? __fdiv_rn(num, den) : 0.f;
+    }
+  }
+}
+
+// flag |= any NaN in the h x w array.
+__global__ void any_nan(const float* __restrict__ a, long long ld, int h, int w, int* flag) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= w) return;
+  bool n = false;
+  for (int y = blockIdx.y; y < h; y += gridDim.y) {
+    const float v = __ldg(a + (long long)y * ld + x);
+    n |= v != v;
+  }
+  if (__any_sync(__activemask(), n) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+// --------------------------------------------------------- decimation
+// NumPy's pairwise float32 sum of n (<= 16) values x(0..n-1).
+template <class Fn>
+__device__ __forceinline__ float np_pairwise(int n, Fn x) {
+  if (n < 8) {
+    float r = 0.f;
+    for (int i = 0; i < n; ++i) r = __fadd_rn(r, x(i));
+    return r;
+  }
+  float r[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) r[j] = x(j);
+  int i = 8;
+  for (; i < n - (n % 8); i += 8)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) r[j] = __fadd_rn(r[j], x(i + j));
+  float res = __fadd_rn(__fadd_rn(__fadd_rn(r[0], r[1]), __fadd_rn(r[2], r[3])),
+                        __fadd_rn(__fadd_rn(r[4], r[5]), __fadd_rn(r[6], r[7])));
+  for (; i < n; ++i) res = __fadd_rn(res, x(i));
+  return res;
+}
+
+// _downsample_nan_aware's cell mean (_nan_utils.py:629-641): cells padded
+// with NaN at the ragged edge, tot / max(cnt, 1) where cnt > 0 else NaN.
+__global__ void block_mean_np(const float* __restrict__ src, long long ld, int h, int w, int f, float* out,
+                              long long old, int oh, int ow, int* flag) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= oh || j >= ow) return;
+  float tot = 0.f;
+  int cnt = 0;
+  for (int a = 0; a < f; ++a) {
+    const int y = i * f + a;
+    const float* row = src + (long long)min(y, h - 1) * ld;
+    auto x = [&](int b) {
+      const int xx = j * f + b;
+      if (y >= h || xx >= w) return 0.f;
+      const float v = __ldg(row + xx);
+      return isfinite(v) ? v : 0.f;
+    };
+    tot = __fadd_rn(tot, np_pairwise(f, x));
+    if (y < h)
+      for (int b = 0; b < f; ++b) {
+        const int xx = j * f + b;
+        if (xx < w && isfinite(__ldg(row + xx))) ++cnt;
+      }
+  }
+  const float m = cnt > 0 ? __fdiv_rn(tot, (float)max(cnt, 1)) : kQNaN;
+  out[(long long)i * old + j] = m;
+  if (m != m) atomicOr(flag, 1);
+}
+
+// Enclosed coarse voids: where(nan & sw > 0.5, sv / max(sw, 1e-6), coarse)
+// (_nan_utils.py:655-667).
+__global__ void void_fill(float* coarse, long long ld, int h, int w, const float* sv, const float* sw,
+                          long long sld, const int* flag) {
+  if (*flag == 0) return;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= h || j >= w) return;
+  float& c = coarse[(long long)i * ld + j];
+  const float ww = sw[(long long)i * sld + j];
+  if (c != c && ww > 0.5f) c = __fdiv_rn(sv[(long long)i * sld + j], fmaxf(ww, 1e-6f));
+}
+
+// ------------------------------------------------------------ zoom
+// scipy.ndimage.zoom(order=1, mode='nearest', grid_mode=False) of a NaN-free
+// array to zh x zw, written into the target region [0, th) x [0, tw) with the
+// last row / column repeated where the zoom is smaller
+// (_upsample_to_shape, _nan_utils.py:671-698).  Coordinates and the four-term
+// sum are float64 as in scipy, without fused multiply-adds.
+__global__ void zoom_linear(const float* __restrict__ a, long long ld, int h, int w, int zh, int zw, double fy,
+                            double fx, float* out, long long old, int th, int tw) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= tw || y >= th) return;
+  const int zy = min(y, zh - 1), zx = min(x, zw - 1);
+  const double cy = __dmul_rn((double)zy, fy), cx = __dmul_rn((double)zx, fx);
+  const double sy = floor(cy), sx = floor(cx);
+  const double ty = __dsub_rn(cy, sy), tx = __dsub_rn(cx, sx);
+  const int y0 = clamp_idx((int)sy, h), y1 = clamp_idx((int)sy + 1, h);
+  const int x0 = clamp_idx((int)sx, w), x1 = clamp_idx((int)sx + 1, w);
+  const double wy0 = __dsub_rn(1.0, ty), wx0 = __dsub_rn(1.0, tx);
+  const double a00 = (double)__ldg(a + (long long)y0 * ld + x0), a01 = (double)__ldg(a + (long long)y0 * ld + x1);
+  const double a10 = (double)__ldg(a + (long long)y1 * ld + x0), a11 = (double)__ldg(a + (long long)y1 * ld + x1);
+  double t = __dmul_rn(__dmul_rn(a00, wy0), wx0);
+  t = __dadd_rn(t, __dmul_rn(__dmul_rn(a01, wy0), tx));
+  t = __dadd_rn(t, __dmul_rn(__dmul_rn(a10, ty), wx0));
+  t = __dadd_rn(t, __dmul_rn(__dmul_rn(a11, ty), tx));
+  out[(long long)y * old + x] = __double2float_rn(t);
+}
+
+// ------------------------------------------------------ tile pieces
+// dask's 'reflect' boundary (the edge sample repeated): index k of a line of
+// n samples extended by at most n on each side.
+__device__ __forceinline__ int sym_idx(int k, int n) {
+  if (k < 0) return -k - 1;
+  if (k >= n) return 2 * n - 1 - k;
+  return k;
+}
+
+__global__ void pad_reflect(ZView z, int y0, int x0, int h, int w, int d, float* dst, long long dld) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= w + 2 * d || y >= h + 2 * d) return;
+  dst[(long long)y * dld + x] = z.at(y0 + sym_idx(y - d, h), x0 + sym_idx(x - d, w));
+}
+
+__global__ void accumulate(const float* __restrict__ src, long long ld, int h, int w, float weight, int first,
+                           float* acc, long long ald) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= w || y >= h) return;
+  const float t = __fmul_rn(__ldg(src + (long long)y * ld + x), weight);
+  float& o = acc[(long long)y * ald + x];
+  o = first ? t : __fadd_rn(o, t);
+}
+
+struct SampleArgs {
+  const float* coarse;
+  long long cld;
+  int ch, cw;
+  ZView z;           // raster (NoData mask)
+  int y0, x0, h, w;  // region in the raster
+  int gy0, gx0;      // global pixel coordinates of the region's first pixel
+  float sy, sx;      // f32(ch / full_h), f32(cw / full_w)
+  float weight;
+  int first;
+  float* acc;
+  long long ald;
+};
+
+// _bilinear_sample_coarse (_nan_utils.py:255-281): float32 coordinates,
+// map_coordinates(order=1, mode='nearest') evaluated in float64 and rounded;
+// NaN where the raster is NoData (_nan_utils.py:395), then accumulated.
+__global__ void sample_coarse(const __grid_constant__ SampleArgs A) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= A.w || y >= A.h) return;
+  const int gy = A.gy0 + y, gx = A.gx0 + x;
+  const float zv = A.z.at(A.y0 + y, A.x0 + x);
+  float v;
+  if (zv != zv) {
+    v = kQNaN;
+  } else {
+    const float cy = __fsub_rn(__fmul_rn(__fadd_rn((float)gy, 0.5f), A.sy), 0.5f);
+    const float cx = __fsub_rn(__fmul_rn(__fadd_rn((float)gx, 0.5f), A.sx), 0.5f);
+    const double dy = (double)cy, dx = (double)cx;
+    const double sy = floor(dy), sx = floor(dx);
+    const double ty = __dsub_rn(dy, sy), tx = __dsub_rn(dx, sx);
+    const int y0 = clamp_idx((int)sy, A.ch), y1 = clamp_idx((int)sy + 1, A.ch);
+    const int x0 = clamp_idx((int)sx, A.cw), x1 = clamp_idx((int)sx + 1, A.cw);
+    const double wy0 = __dsub_rn(1.0, ty), wx0 = __dsub_rn(1.0, tx);
+    const float* C = A.coarse;
+    double t = __dmul_rn(__dmul_rn((double)__ldg(C + y0 * A.cld + x0), wy0), wx0);
+    t = __dadd_rn(t, __dmul_rn(__dmul_rn((double)__ldg(C + y0 * A.cld + x1), wy0), tx));
+    t = __dadd_rn(t, __dmul_rn(__dmul_rn((double)__ldg(C + y1 * A.cld + x0), ty), wx0));
+    t = __dadd_rn(t, __dmul_rn(__dmul_rn((double)__ldg(C + y1 * A.cld + x1), ty), tx));
+    v = __double2float_rn(t);
+  }
+  const float tt = __fmul_rn(v, A.weight);
+  float& o = A.acc[(long long)y * A.ald + x];
+  o = A.first ? tt : __fadd_rn(o, tt);
+}
+
+struct StoreArgs {
+  const float* acc;
+  long long ald;
+  ZView z;
+  int gy0, gx0, h, w;
+  void* out;
+  long long old;
+  int dtype;
+  float qa, qb;
+  int qmin, qmax;
+};
+
+// NaN at the raster's NoData (apply_nodata_mask, core/tile_compute.py:132-152),
+// then the plane's encoding.
+__global__ void masked_store(const __grid_constant__ StoreArgs A) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= A.w || y >= A.h) return;
+  const float zv = A.z.at(A.gy0 + y, A.gx0 + x);
+  const float v = zv != zv ? kQNaN : A.acc[(long long)y * A.ald + x];
+  const long long off = (long long)y * A.old + x;
+  if (A.dtype == FSG_F32) static_cast<float*>(A.out)[off] = v;
+  else if (A.dtype == FSG_U8) static_cast<uint8_t*>(A.out)[off] = (uint8_t)(int)quantize(v, A.qa, A.qb, A.qmin, A.qmax);
+  else static_cast<int16_t*>(A.out)[off] = (int16_t)(int)quantize(v, A.qa, A.qb, A.qmin, A.qmax);
+}
+
+// ------------------------------------------------------------ host
+dim3 blocks2d(int h, int w) { return dim3((w + 31) / 32, (h + 7) / 8); }
+
+// scipy.ndimage._gaussian_kernel1d(sigma, 0, int(4 sigma + 0.5)) normalised in
+// float64, as float-float pairs [0..R] (0 = centre).
+std::vector<FF> ff_gaussian(double sigma, int* radius) {
+  const int R = (int)(4.0 * sigma + 0.5);
+  std::vector<double> phi(2 * R + 1);
+  const double c = -0.5 / (sigma * sigma);
+  double s = 0.0;
+  for (int k = -R; k <= R; ++k) {
+    phi[k + R] = std::exp(c * (double)((long long)k * k));
+    s += phi[k + R];
+  }
+  std::vector<FF> g(R + 1);
+  for (int k = 0; k <= R; ++k) {
+    const double v = phi[k + R] / s;
+    g[k].hi = (float)v;
+    g[k].lo = (float)(v - (double)g[k].hi);
+  }
+  *radius = R;
+  return g;
+}
+
+constexpr size_t kMaxTable = 1 << 16;  // Gaussian weight table bytes (radius <= 8191)
+
+struct Arena {
+  char* p;
+  char* end;
+  void* take(size_t n) {
+    char* q = p;
+    p += (n + 255) & ~(size_t)255;
+    return p <= end ? q : nullptr;
+  }
+};
+
+// Gaussian of an h x w array (source and destination may not alias).
+// mode AX1_SMOOTH: NaN-aware (checked on the device); AX1_PAIR: the two raw
+// channels of where(nan, 0, a) and the valid mask, into dst / dst2.
+int gaussian(const float* src, long long ld, int h, int w, double sigma, int mode, float* dst, float* dst2,
+             long long dld, Arena& ar, cudaStream_t s) {
+  int R;
+  std::vector<FF> g = ff_gaussian(sigma, &R);
+  if (sizeof(FF) * g.size() > kMaxTable) return fail(FSG_ERR_UNSUPPORTED, "Gaussian radius %d too large", R);
+  FF* gd = static_cast<FF*>(ar.take(sizeof(FF) * g.size()));
+  float* v = static_cast<float*>(ar.take(sizeof(float) * (size_t)h * w));
+  float* wt = static_cast<float*>(ar.take(sizeof(float) * (size_t)h * w));
+  int* flag = static_cast<int*>(ar.take(sizeof(int)));
+  if (!gd || !v || !wt || !flag) return fail(FSG_ERR_WORKSPACE, "smoothing scratch exhausted");
+  FSG_CUDA(cudaMemcpyAsync(gd, g.data(), sizeof(FF) * g.size(), cudaMemcpyHostToDevice, s));
+  const int* nan_flag = nullptr;
+  if (mode == AX1_SMOOTH) {
+    FSG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+    any_nan<<<dim3((w + 255) / 256, std::min(h, 1024)), 256, 0, s>>>(src, ld, h, w, flag);
+    FSG_LAUNCHED(1);
+    nan_flag = flag;
+  }
+  const int rpb = 16;
+  gauss_axis0<<<dim3((w + NT - 1) / NT, (h + rpb - 1) / rpb), NT, 0, s>>>(
+      src, ld, h, w, gd, R, mode == AX1_PAIR ? 1 : 0, nan_flag, v, wt, w, rpb);
+  FSG_LAUNCHED(1);
+  gauss_axis1<<<dim3((w + NT - 1) / NT, std::min(h, 65535)), NT, 0, s>>>(v, wt, w, h, w, gd, R, mode, nan_flag, dst, dst2, dld);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+// _radius_to_downsample_factor (_nan_utils.py:555-601).
+int downsample_factor(double radius, double pixel_size, double algo_factor) {
+  const double r = std::max(1.0, radius);
+  const double px = std::max(1e-3, pixel_size != 0.0 ? pixel_size : 1.0);
+  const double score = (r / 24.0) * algo_factor * 1.0 * std::pow(std::max(1.0, 1.0 / px), 0.35);
+  if (score <= 1.0) return 1;
+  const double f = std::pow(2.0, std::floor(std::log2(score)));
+  return (int)std::max(1.0, std::min(f, 16.0));
+}
+
+size_t smooth_scratch_bytes(int h, int w, int f) {
+  const size_t full = (size_t)h * w;
+  const int hs = (h + f - 1) / f, ws = (w + f - 1) / f;
+  const size_t sm = (size_t)hs * ws;
+  const size_t gmax = kMaxTable;
+  if (f <= 1) return 2 * full * 4 + gmax + 4096;
+  return 8 * sm * 4 + 2 * gmax + 8192;
+}
+
+}  // namespace
+}  // namespace fsg
+
+using namespace fsg;
+
+extern "C" int fsg_smooth(const float* src, int64_t ld, int32_t h, int32_t w, double radius, double pixel_size,
+                          double algorithm_factor, float* dst, int64_t dst_ld, void* stream) {
+  if (!src || !dst) return fail(FSG_ERR_INVALID, "null array");
+  if (h < 0 || w < 0 || ld < w || dst_ld < w) return fail(FSG_ERR_SHAPE, "bad shape %d x %d", h, w);
+  if (!(radius == radius) || !(algorithm_factor > 0.0)) return fail(FSG_ERR_INVALID, "bad radius / factor");
+  if (h == 0 || w == 0) return FSG_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const double r = std::max(1.0, radius);
+  if (r <= 1.0) {
+    if (src != dst)
+      FSG_CUDA(cudaMemcpy2DAsync(dst, dst_ld * 4, src, ld * 4, (size_t)w * 4, h, cudaMemcpyDeviceToDevice, s));
+    return FSG_OK;
+  }
+  const int f = downsample_factor(r, pixel_size, algorithm_factor);
+  StreamScratch scratch;
+  const size_t bytes = smooth_scratch_bytes(h, w, f);
+  int st = scratch.alloc(bytes, s);
+  if (st) return st;
+  Arena ar{static_cast<char*>(scratch.ptr), static_cast<char*>(scratch.ptr) + bytes};
+  if (f <= 1) return gaussian(src, ld, h, w, std::max(0.5, r / 2.0), AX1_SMOOTH, dst, nullptr, dst_ld, ar, s);
+  // decimated: NaN-aware block mean (+ enclosed-void fill), Gaussian at the
+  // coarse resolution, bilinear zoom back to the block
+  const int hs = std::max(1, (h + f - 1) / f), ws = std::max(1, (w + f - 1) / f);
+  float* small = static_cast<float*>(ar.take(sizeof(float) * (size_t)hs * ws));
+  float* sv = static_cast<float*>(ar.take(sizeof(float) * (size_t)hs * ws));
+  float* sw = static_cast<float*>(ar.take(sizeof(float) * (size_t)hs * ws));
+  float* sm = static_cast<float*>(ar.take(sizeof(float) * (size_t)hs * ws));
+  int* flag = static_cast<int*>(ar.take(sizeof(int)));
+  if (!small || !sv || !sw || !sm || !flag) return fail(FSG_ERR_WORKSPACE, "smoothing scratch exhausted");
+  FSG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+  block_mean_np<<<blocks2d(hs, ws), dim3(32, 8), 0, s>>>(src, ld, h, w, f, small, ws, hs, ws, flag);
+  FSG_LAUNCHED(1);
+  // void fill: sigma = max(1, min(shape) / 64); the kernels are cheap when no void exists
+  st = gaussian(small, ws, hs, ws, std::max(1.0, (double)std::min(hs, ws) / 64.0), AX1_PAIR, sv, sw, ws, ar, s);
+  if (st) return st;
+  void_fill<<<blocks2d(hs, ws), dim3(32, 8), 0, s>>>(small, ws, hs, ws, sv, sw, ws, flag);
+  FSG_LAUNCHED(1);
+  st = gaussian(small, ws, hs, ws, std::max(0.5, (r / f) / 2.0), AX1_SMOOTH, sm, nullptr, ws, ar, s);
+  if (st) return st;
+  // zoom to round(n * (target / n)) samples per axis, grid_mode=False factors
+  const int zh = (int)std::nearbyint((double)hs * ((double)h / (double)hs));
+  const int zw = (int)std::nearbyint((double)ws * ((double)w / (double)ws));
+  const double fy = zh > 1 ? (double)(hs - 1) / (double)(zh - 1) : 1.0;
+  const double fx = zw > 1 ? (double)(ws - 1) / (double)(zw - 1) : 1.0;
+  zoom_linear<<<blocks2d(h, w), dim3(32, 8), 0, s>>>(sm, ws, hs, ws, zh, zw, fy, fx, dst, dst_ld, h, w);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+extern "C" int fsg_pad_reflect(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w, int32_t y0,
+                               int32_t x0, int32_t h, int32_t w, int32_t depth, double nodata, int32_t has_nodata,
+                               float* dst, int64_t dst_ld, void* stream) {
+  if (!raster_dev || !dst) return fail(FSG_ERR_INVALID, "null array");
+  if (h <= 0 || w <= 0 || y0 < 0 || x0 < 0 || y0 + h > raster_h || x0 + w > raster_w || ld < raster_w)
+    return fail(FSG_ERR_SHAPE, "window [%d, %d) x [%d, %d) outside the %d x %d raster", y0, y0 + h, x0, x0 + w,
+                raster_h, raster_w);
+  if (depth < 0 || depth > std::min(h, w))
+    return fail(FSG_ERR_SHAPE, "reflect depth %d exceeds the window (%d x %d)", depth, h, w);
+  if (dst_ld < (int64_t)w + 2 * depth) return fail(FSG_ERR_SHAPE, "destination row too short");
+  ZView z{raster_dev, (long long)ld, raster_h, raster_w, (float)nodata, has_nodata};
+  pad_reflect<<<blocks2d(h + 2 * depth, w + 2 * depth), dim3(32, 8), 0, (cudaStream_t)stream>>>(
+      z, y0, x0, h, w, depth, dst, dst_ld);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+extern "C" int fsg_accumulate(const float* src, int64_t ld, int32_t h, int32_t w, float weight, int32_t first,
+                              float* acc, int64_t acc_ld, void* stream) {
+  if (!src || !acc) return fail(FSG_ERR_INVALID, "null array");
+  if (h < 0 || w < 0 || ld < w || acc_ld < w) return fail(FSG_ERR_SHAPE, "bad shape %d x %d", h, w);
+  if (h == 0 || w == 0) return FSG_OK;
+  accumulate<<<blocks2d(h, w), dim3(32, 8), 0, (cudaStream_t)stream>>>(src, ld, h, w, weight, first, acc, acc_ld);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+extern "C" int fsg_sample_coarse_accumulate(const float* coarse, int64_t cld, int32_t ch, int32_t cw,
+                                            const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                                            int32_t y0, int32_t x0, int32_t h, int32_t w, int64_t gy0, int64_t gx0,
+                                            int64_t full_h, int64_t full_w, double nodata, int32_t has_nodata,
+                                            float weight, int32_t first, float* acc, int64_t acc_ld, void* stream) {
+  if (!coarse || !raster_dev || !acc) return fail(FSG_ERR_INVALID, "null array");
+  if (ch <= 0 || cw <= 0 || cld < cw || full_h <= 0 || full_w <= 0) return fail(FSG_ERR_SHAPE, "bad coarse shape");
+  if (h < 0 || w < 0 || y0 < 0 || x0 < 0 || y0 + h > raster_h || x0 + w > raster_w || acc_ld < w ||
+      ld < raster_w)
+    return fail(FSG_ERR_SHAPE, "region outside the raster");
+  if (gy0 < 0 || gx0 < 0 || gy0 + h > full_h || gx0 + w > full_w || full_h >= (1 << 24) || full_w >= (1 << 24))
+    return fail(FSG_ERR_SHAPE, "global region outside the %lld x %lld raster", (long long)full_h,
+                (long long)full_w);
+  if (h == 0 || w == 0) return FSG_OK;
+  SampleArgs A;
+  A.coarse = coarse;
+  A.cld = cld;
+  A.ch = ch;
+  A.cw = cw;
+  A.z = ZView{raster_dev, (long long)ld, raster_h, raster_w, (float)nodata, has_nodata};
+  A.y0 = y0;
+  A.x0 = x0;
+  A.gy0 = (int)gy0;
+  A.gx0 = (int)gx0;
+  A.h = h;
+  A.w = w;
+  A.sy = (float)((double)ch / (double)full_h);
+  A.sx = (float)((double)cw / (double)full_w);
+  A.weight = weight;
+  A.first = first;
+  A.acc = acc;
+  A.ald = acc_ld;
+  sample_coarse<<<blocks2d(h, w), dim3(32, 8), 0, (cudaStream_t)stream>>>(A);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+extern "C" int fsg_masked_store(const float* acc, int64_t acc_ld, const float* raster_dev, int64_t ld,
+                                int32_t raster_h, int32_t raster_w, int32_t gy0, int32_t gx0, int32_t h, int32_t w,
+                                double nodata, int32_t has_nodata, const fsg_plane* out, void* stream) {
+  if (!acc || !raster_dev || !out || !out->ptr) return fail(FSG_ERR_INVALID, "null array");
+  if (h < 0 || w < 0 || gy0 < 0 || gx0 < 0 || gy0 + h > raster_h || gx0 + w > raster_w || acc_ld < w ||
+      out->ld < w)
+    return fail(FSG_ERR_SHAPE, "region outside the raster");
+  if (out->dtype != FSG_F32 && out->dtype != FSG_U8 && out->dtype != FSG_I16)
+    return fail(FSG_ERR_DTYPE, "unsupported plane dtype %d", out->dtype);
+  if (h == 0 || w == 0) return FSG_OK;
+  StoreArgs A;
+  A.acc = acc;
+  A.ald = acc_ld;
+  A.z = ZView{raster_dev, (long long)ld, raster_h, raster_w, (float)nodata, has_nodata};
+  A.gy0 = gy0;
+  A.gx0 = gx0;
+  A.h = h;
+  A.w = w;
+  A.out = out->ptr;
+  A.old = out->ld;
+  A.dtype = out->dtype;
+  A.qa = out->q_a;
+  A.qb = out->q_b;
+  A.qmin = out->q_min;
+  A.qmax = out->q_max;
+  masked_store<<<blocks2d(h, w), dim3(32, 8), 0, (cudaStream_t)stream>>>(A);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}

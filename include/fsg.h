@@ -258,6 +258,53 @@ int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t 
 int fsg_openness_offsets(int32_t num_directions, int32_t max_distance, int32_t mode, int32_t* ox, int32_t* oy,
                          int32_t* ray_len, int32_t capacity);
 
+/* ------------------------------------------------------------- spatial mode */
+/* _smooth_for_radius(block, radius, pixel_size, algorithm)
+ * (algorithms/_nan_utils.py:527-552): identity for radius <= 1, else the
+ * NaN-aware Gaussian (sigma = max(0.5, r/2), 'nearest'), or for large radii the
+ * NaN-aware f x f block mean, Gaussian at that resolution and bilinear zoom
+ * back.  algorithm_factor is the per-algorithm factor of the decimation rule
+ * (_nan_utils.py:571-581): 1.0 hillshade and slope, 1.1 curvature, 1.15
+ * topousm_fast, 1.4 openness.  src and dst are h x w float32 device arrays
+ * (NaN = NoData) that must not overlap. */
+int fsg_smooth(const float* src, int64_t ld, int32_t h, int32_t w, double radius, double pixel_size,
+               double algorithm_factor, float* dst, int64_t dst_ld, void* stream);
+
+/* The raster window [y0, y0+h) x [x0, x0+w) mirrored by `depth` samples on
+ * every side, repeating the edge sample (dask map_overlap boundary='reflect',
+ * as the Dask branch of the spatial products uses it,
+ * algorithms/_nan_utils.py:500-512), NoData -> NaN.  dst is
+ * (h + 2 depth) x (w + 2 depth); depth <= min(h, w). */
+int fsg_pad_reflect(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w, int32_t y0,
+                    int32_t x0, int32_t h, int32_t w, int32_t depth, double nodata, int32_t has_nodata,
+                    float* dst, int64_t dst_ld, void* stream);
+
+/* acc = src * weight (first != 0) or acc + src * weight, float32 without a fused
+ * multiply-add: one step of the weighted combination of per-radius responses
+ * (_combine_multiscale_dask, algorithms/_nan_utils.py:182-213). */
+int fsg_accumulate(const float* src, int64_t ld, int32_t h, int32_t w, float weight, int32_t first,
+                   float* acc, int64_t acc_ld, void* stream);
+
+/* One large-radius response of a tile: the coarse (overview) response sampled
+ * bilinearly at global pixel centres (_bilinear_sample_coarse,
+ * algorithms/_nan_utils.py:255-281) for the raster region
+ * [y0, y0+h) x [x0, x0+w), whose first pixel has the global coordinates
+ * (gy0, gx0) in a full_h x full_w raster (full sizes < 2^24); NaN where the
+ * raster region is NoData (:395); accumulated into acc as fsg_accumulate does. */
+int fsg_sample_coarse_accumulate(const float* coarse_dev, int64_t cld, int32_t ch, int32_t cw,
+                                 const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                                 int32_t y0, int32_t x0, int32_t h, int32_t w, int64_t gy0, int64_t gx0,
+                                 int64_t full_h, int64_t full_w, double nodata, int32_t has_nodata, float weight,
+                                 int32_t first, float* acc, int64_t acc_ld, void* stream);
+
+/* Store of a combined tile core: NaN where the raster region
+ * [gy0, gy0+h) x [gx0, gx0+w) is NoData (apply_nodata_mask,
+ * core/tile_compute.py:132-152), then the plane's encoding; `out` addresses the
+ * region's first pixel. */
+int fsg_masked_store(const float* acc, int64_t acc_ld, const float* raster_dev, int64_t ld, int32_t raster_h,
+                     int32_t raster_w, int32_t gy0, int32_t gx0, int32_t h, int32_t w, double nodata,
+                     int32_t has_nodata, const fsg_plane* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

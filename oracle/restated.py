@@ -273,6 +273,142 @@ def smooth_for_radius(block, radius, *, pixel_size=1.0, algorithm="default"):
 
 
 # =============================================================================
+# Spatial mode of the stencil products
+# =============================================================================
+SPATIAL_PRODUCTS = ("hillshade", "slope", "curvature")
+
+
+def stencil_product(block, product, *, pixel_size=1.0, psx=None, psy=None, azimuth=DEFAULT_AZIMUTH,
+                    altitude=DEFAULT_ALTITUDE, z_factor=1.0, unit="degree", curvature_type="mean"):
+    """The local block function of one stencil product."""
+    if product == "hillshade":
+        return hillshade(block, azimuth=azimuth, altitude=altitude, z_factor=z_factor, pixel_size=pixel_size,
+                         psx=psx, psy=psy)
+    if product == "slope":
+        return slope(block, unit=unit, pixel_size=pixel_size, psx=psx, psy=psy)
+    return curvature(block, curvature_type=curvature_type, pixel_size=pixel_size, psx=psx, psy=psy)
+
+
+def spatial_block(block, product, radius, *, pixel_size=1.0, **kw):
+    """compute_hillshade_spatial_block (_impl_hillshade.py:57-67), compute_slope_spatial_block
+    (_impl_slope.py:38-45), _curv_spatial (_impl_curvature.py:72-78): smooth, then the product."""
+    sm = smooth_for_radius(block, radius, pixel_size=pixel_size, algorithm=product)
+    return stencil_product(sm, product, pixel_size=pixel_size, **kw)
+
+
+def spatial_depth(product, radius):
+    """depth_for_scale of the spatial branches (_impl_hillshade.py:98, _impl_slope.py:62,
+    _impl_curvature.py:85)."""
+    r = float(radius)
+    if product == "curvature":
+        return max(3, int(r * 2 + 2))
+    return max(2, int(r * 2 + 1))
+
+
+def map_overlap_reflect(fn, block, depth):
+    """dask ``map_overlap(fn, depth, boundary='reflect')`` on a one-chunk array, with the
+    depth cap of _nan_utils.py:502-503 (``max(1, min(depth, min_chunk - 1))``).
+
+    dask's 'reflect' boundary mirrors the array including its edge sample (NumPy's
+    'symmetric' pad); the block function runs on the padded chunk and the depth is
+    trimmed from every side.
+    """
+    d = max(1, min(int(depth), min(block.shape) - 1))
+    out = fn(np.pad(block, d, mode="symmetric"))
+    return out[d:-d, d:-d]
+
+
+def spatial_large_threshold(window_shape):
+    """large_radius_threshold (_nan_utils.py:219-228) of a one-chunk window."""
+    return int(max(256, int(min(window_shape)) // 16))
+
+
+def overview_decimation(full_h, full_w, oh, ow):
+    """read_overview_coarse_dem's decimation (_nan_utils.py:862-864)."""
+    return 0.5 * (full_w / float(ow) + full_h / float(oh))
+
+
+def overview_shape(full_h, full_w, sample_max=2048):
+    """read_overview_coarse_dem's overview size (_nan_utils.py:846-852)."""
+    scale = max(full_w / sample_max, full_h / sample_max, 1.0)
+    return max(1, int(round(full_h / scale))), max(1, int(round(full_w / scale)))
+
+
+def coarse_spatial_response(coarse_dem, product, radius, decimation, *, pixel_size=1.0, psx=None, psy=None, **kw):
+    """The overview branch of coarse_large_radius_response (_nan_utils.py:366-395): the block
+    function once on the whole overview, radius and pixel scales scaled by the decimation."""
+    fac = float(decimation)
+    rc = max(1, int(round(float(radius) / fac)))
+    return spatial_block(coarse_dem, product, rc, pixel_size=float(pixel_size) * fac,
+                         psx=None if psx is None else float(psx) * fac,
+                         psy=None if psy is None else float(psy) * fac, **kw).astype(np.float32)
+
+
+def combine_responses(responses, weights, product):
+    """The weighted mean of the spatial branches.
+
+    hillshade (_impl_hillshade.py:113-128): float32 weights normalised in float32;
+    slope / curvature (_combine_multiscale_dask, _nan_utils.py:182-213): weights
+    L1-normalised in float64.  Either way ``out = r0*w0; out = out + ri*wi`` in float32.
+    """
+    if len(responses) == 1 and product != "hillshade":
+        return responses[0]
+    if product == "hillshade":
+        w = np.asarray(weights, dtype=np.float32)
+        if not (np.isfinite(w).all() and float(w.sum()) > 0):
+            return np.mean(np.stack(responses, 0), axis=0)
+        w = w / w.sum()
+        ws = [np.float32(float(x)) for x in w]
+    else:
+        c = clean_normalized_weights(weights)
+        if c is None:
+            return np.mean(np.stack(responses, 0), axis=0)
+        ws = [np.float32(x) for x in c]
+    out = responses[0] * ws[0]
+    for r, w in zip(responses[1:], ws[1:]):
+        out = out + r * w
+    return out.astype(np.float32)
+
+
+def direct_multiscale(block, product, radii, weights, **kw):
+    """_direct_hillshade's local multi-radius branch (tile/dask_bridge.py:72-108 with
+    _combine_direct :28-69): per radius the spatial block, float32-normalised weights."""
+    rr = [max(1.0, float(r)) for r in radii]
+    resp = [spatial_block(block, product, r, **kw) for r in rr]
+    if len(resp) == 1:
+        return resp[0]
+    return combine_responses(resp, weights, "hillshade")
+
+
+def spatial_window(window, product, radii, weights, *, origin=(0, 0), full_shape=None, coarse_dem=None,
+                   decimation=None, pixel_size=1.0, psx=None, psy=None, return_responses=False, **kw):
+    """One tile window of a spatial-mode stencil product on the tile backend
+    (dask_bridge.py:334-346 falls back to the product's Dask ``process`` on the window as one
+    chunk; multiscale_response_fields, _nan_utils.py:441-524).
+
+    Radii above the window's large-radius threshold come from the overview (``coarse_dem``):
+    the product of the whole overview sampled at the window's global pixel centres, NaN at
+    the window's NaN; the others are ``map_overlap(spatial_block, depth, 'reflect')``.
+    """
+    h, w = window.shape
+    thr = spatial_large_threshold(window.shape)
+    H, W = full_shape if full_shape is not None else window.shape
+    out = []
+    for r in radii:
+        if int(round(float(r))) > thr and coarse_dem is not None:
+            cr = coarse_spatial_response(coarse_dem, product, r, decimation, pixel_size=pixel_size,
+                                         psx=psx, psy=psy, **kw)
+            up = bilinear_sample_coarse(cr, origin[0], origin[0] + h, origin[1], origin[1] + w, H, W)
+            out.append(np.where(np.isnan(window), np.float32(np.nan), up).astype(np.float32))
+        else:
+            fn = (lambda b, rr=float(r): spatial_block(b, product, rr, pixel_size=pixel_size, psx=psx, psy=psy,
+                                                       **kw))
+            out.append(map_overlap_reflect(fn, window, spatial_depth(product, r)).astype(np.float32))
+    comb = combine_responses(out, weights, product)
+    return (comb, out) if return_responses else comb
+
+
+# =============================================================================
 # topousm_fast
 # =============================================================================
 def local_mean_for_radius(block, radius, *, pixel_size=1.0):

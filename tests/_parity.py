@@ -9,6 +9,9 @@ Tolerances (stated once, used everywhere):
     of tanh there; NumPy's and CUDA's float32 tanh differ in that bit), the
     pre-gamma value (tanh+1)/2 agrees to 4 ulps of tanh (2^-23).
   * exact openness: mean angle within 0.01 degree.
+  * a weighted combination of curvature displays (spatial mode): 1e-5 plus
+    the sum over responses of weight x that response's own allowance (1e-5,
+    or in its tail the display change of 2^-23 in the pre-gamma value).
 """
 from __future__ import annotations
 
@@ -70,6 +73,29 @@ def assert_curvature_close(got, ref, what=""):
     assert not bad.any(), (f"{what}: {int(bad.sum())} cells off; worst display diff "
                            f"{float(d[bad].max()):.3e}")
     return int(tail.sum())
+
+
+def curvature_allowance(ref):
+    """Per-cell display allowance of one curvature response (the rule of assert_curvature_close)."""
+    r = to_np(ref).astype(np.float64)
+    u = r ** 2.2
+    tail = np.abs((u + CURV_TAIL_TOL) ** (1 / 2.2) - r)
+    return np.where(u < 1e-4, np.maximum(tail, 1e-5), 1e-5)
+
+
+def assert_curvature_combined_close(got, ref, responses, weights, what=""):
+    """A weighted sum of curvature displays against the oracle's, each response allowed its own error."""
+    got = to_np(got).astype(np.float64)
+    ref = to_np(ref).astype(np.float64)
+    assert_same_nan(got, ref, what)
+    allow = np.full(ref.shape, 1e-5)
+    for resp, w in zip(responses, weights):
+        allow = allow + float(w) * np.nan_to_num(curvature_allowance(resp), nan=0.0)
+    m = ~np.isnan(ref)
+    d = np.abs(got - ref)
+    bad = m & (d > allow)
+    assert not bad.any(), (f"{what}: {int(bad.sum())} cells off; worst excess "
+                           f"{float((d - allow)[bad].max()):.3e}")
 
 
 def assert_codes_close(got, ref, what="", lsb=1):

@@ -28,6 +28,9 @@ import reference_shim  # noqa: E402
 from fujishadergpu_gb300 import synth  # noqa: E402
 
 
+SPATIAL_BLOCK_RADII = (1.0, 3.0, 12.0, 40.0)
+
+
 def _stub_rasterio():
     import types
     if "rasterio" not in sys.modules:
@@ -127,6 +130,27 @@ def main():
             out = nu._smooth_for_radius(d.copy(), r, pixel_size=5.0, algorithm_name=algo)
             arrays[f"{dn}/smooth_{algo}_{int(r)}"] = np.asarray(out, np.float32)
     np.savez_compressed(os.path.join(HERE, "smooth.npz"), **arrays)
+
+    # ------------------------------------------------ spatial-mode block functions
+    arrays = {}
+    sp = synth.fbm(80, 96, hurst=0.8, seed=19, lo=0.0, hi=2500.0)
+    sp_nan = _with_disks(sp, 3, 20, 3.0, 8.0)
+    for dn, d in (("clean", sp), ("nan", sp_nan)):
+        arrays[f"{dn}/dem"] = d
+        kw = dict(pixel_size=5.0, pixel_scale_x=5.0, pixel_scale_y=-5.0)
+        for r in SPATIAL_BLOCK_RADII:
+            arrays[f"{dn}/hillshade_{int(r)}"] = hs_mod.compute_hillshade_spatial_block(
+                d.copy(), radius=r, azimuth=300.0, altitude=40.0, **kw)
+            arrays[f"{dn}/slope_{int(r)}"] = sl_mod.compute_slope_spatial_block(d.copy(), radius=r, **kw)
+            # _curv_spatial (_impl_curvature.py:72-78) is a closure inside process(): the same two calls
+            smc = nu._smooth_for_radius(d.copy(), r, pixel_size=5.0, algorithm_name="curvature")
+            arrays[f"{dn}/curvature_profile_{int(r)}"] = cv_mod.compute_curvature_block(
+                smc, curvature_type="profile", **kw)
+        db = importlib.import_module("FujiShaderGPU.algorithms.tile.dask_bridge")
+        arrays[f"{dn}/direct_hillshade_multiscale"] = db._direct_hillshade(
+            d.copy(), dict(radii=[1, 4, 16], weights=[0.5, 0.3, 0.2], pixel_size=5.0,
+                           pixel_scale_x=5.0, pixel_scale_y=-5.0))
+    np.savez_compressed(os.path.join(HERE, "spatial.npz"), **arrays)
 
     # ---------------------------------------------------------------- topousm
     arrays = {}

@@ -71,6 +71,38 @@ def test_spatial_smoothing_bit_exact(golden_dir, variant):
             g[f"{variant}/smooth_{algo}_{int(r)}"])
 
 
+@pytest.mark.parametrize("variant", ["clean", "nan"])
+def test_spatial_block_functions_bit_exact(golden_dir, variant):
+    """compute_*_spatial_block and the multi-radius _direct_hillshade (smoothing + product)."""
+    g = _load(golden_dir, "spatial")
+    dem = g[f"{variant}/dem"]
+    kw = dict(pixel_size=5.0, psx=5.0, psy=-5.0)
+    for r in (1.0, 3.0, 12.0, 40.0):
+        _eq(R.spatial_block(dem.copy(), "hillshade", r, azimuth=300.0, altitude=40.0, **kw),
+            g[f"{variant}/hillshade_{int(r)}"])
+        _eq(R.spatial_block(dem.copy(), "slope", r, **kw), g[f"{variant}/slope_{int(r)}"])
+        _eq(R.spatial_block(dem.copy(), "curvature", r, curvature_type="profile", **kw),
+            g[f"{variant}/curvature_profile_{int(r)}"])
+    _eq(R.direct_multiscale(dem.copy(), "hillshade", [1, 4, 16], [0.5, 0.3, 0.2], **kw),
+        g[f"{variant}/direct_hillshade_multiscale"])
+
+
+def test_map_overlap_reflect_is_symmetric_padding():
+    """dask's 'reflect' boundary repeats the edge sample; the depth is capped below the chunk."""
+    b = np.arange(12, dtype=np.float32).reshape(3, 4)
+    seen = {}
+
+    def fn(x):
+        seen["p"] = x.copy()
+        return x
+
+    out = R.map_overlap_reflect(fn, b, 2)
+    assert np.array_equal(out, b)
+    assert np.array_equal(seen["p"][2, :], np.array([1, 0, 0, 1, 2, 3, 3, 2], np.float32))
+    R.map_overlap_reflect(fn, b, 50)
+    assert seen["p"].shape == (3 + 4, 4 + 4)
+
+
 @pytest.mark.parametrize("case", ["t1_clean", "t2_nan", "t3_halfmetre", "t4_nan_r2"])
 def test_topousm_block_bit_exact(golden_dir, case):
     g = _load(golden_dir, "topousm")
