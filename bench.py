@@ -423,7 +423,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["stencil"], default="stencil")
+    ap.add_argument("--workload", choices=["stencil", "topousm", "openness"], default="stencil",
+                    help="stencil: the headline line; topousm / openness: that section alone (profiling)")
     ap.add_argument("--size", type=int, default=32768)
     ap.add_argument("--tile", type=int, default=4096)
     ap.add_argument("--halo", type=int, default=8)
@@ -439,6 +440,11 @@ def main():
         return reference_arm(args)
 
     rank, world, _ = dist_setup(args.gpus)
+    if args.workload != "stencil":
+        sec = topousm_section(args) if args.workload == "topousm" else openness_section(args)
+        if rank == 0:
+            print(json.dumps({"section": args.workload, **sec}))
+        return
     line = stencil_workload(args, rank, world)
     if not args.no_extra:
         import torch

@@ -529,15 +529,19 @@ __global__ void __launch_bounds__(NT, FSG_STENCIL_MINB) stencil_kernel(const __g
 
 
 // ------------------------------------------------------------ fast pass
-// Streaming kernel for the common case: a warp owns a strip of SW = 28 output
-// columns and SH rows; lane l holds column x0 - 2 + l, walks down the rows
-// keeping f, dx, dy of the neighbouring rows in registers, and takes the
-// horizontal neighbours from warp shuffles (lanes 2..29 emit outputs).  No
-// shared memory, no barriers.  A unit that touches a window edge, or holds a
-// valid pixel whose stencil reaches NoData (NaN propagates into its
+// Streaming kernel for the common case: a warp owns a strip of SW = 60 output
+// columns and SH rows; lane l holds the column pair (x0 - 2 + 2l, x0 - 1 + 2l)
+// as a float2, walks down the rows keeping f, dx, dy of the neighbouring rows
+// in registers, and takes the horizontal neighbours from one warp shuffle each
+// way per pair (lanes 1..30 emit outputs).  The arithmetic runs on both
+// columns at once with the paired FP32 instructions of sm_100+ (FADD2, FMUL2,
+// FFMA2: per component the same correctly rounded operation as the scalar
+// form).  No shared memory, no barriers.  A unit that touches a window edge,
+// or holds a valid pixel whose stencil reaches NoData (NaN propagates into its
 // derivatives), is appended to a list; the fix-up kernel recomputes every
-// listed unit exactly (NaN fill, one-sided edge formulas).
-constexpr int SW = 28, SH = 64;
+// listed unit exactly (NaN fill, one-sided edge formulas), as two halves of
+// FW = 30 columns.
+constexpr int SW = 60, SH = 64, FW = SW / 2;
 
 struct FastTile {
   int wy0, wx0, wy1, wx1, cy0, cx0, cy1, cx1, oy0, ox0;
@@ -568,8 +572,6 @@ __device__ __forceinline__ void push_fix(const FastArgs& A, int u, bool edge) {
   A.fix_list[i] = (unsigned)u | (edge ? FIX_EDGE : 0u);
 }
 
-__device__ __forceinline__ float shfl_up1(float v) { return __shfl_up_sync(0xffffffffu, v, 1); }
-__device__ __forceinline__ float shfl_dn1(float v) { return __shfl_down_sync(0xffffffffu, v, 1); }
 
 // Unit geometry shared by the fast pass and the fix-up pass.
 struct UnitGeom {
@@ -608,141 +610,298 @@ __device__ __forceinline__ void store_pixel(const FastArgs& A, unsigned om, bool
   }
 }
 
-// Fast streaming pass for the common case: a warp owns a strip of SW = 28
-// output columns and SH rows; lane l holds column x0 - 2 + l, walks down the
-// rows keeping f, dx, dy of the neighbouring rows in registers, and takes the
-// horizontal neighbours from warp shuffles (lanes 2..29 emit outputs).  No
-// shared memory, no barriers.  Row groups of G are loaded one group ahead.  A
-// warp ballot per group tells whether any NoData feeds it; only then are the
-// per-pixel checks evaluated.  Units touching a window edge, and units with a
-// valid pixel whose stencil reaches NoData, are listed for the fix-up pass.
-// DIV: derivatives use the correctly rounded division (bit-exact np.gradient,
-// needed for the dx/dy planes); otherwise a multiply by the reciprocal.
+// Paired FP32 helpers (float2 = the two columns of a lane).
+typedef float2 f2;
+__device__ __forceinline__ f2 P2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ f2 S2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ f2 add2(f2 a, f2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ bool nan2(f2 a) { return (a.x != a.x) | (a.y != a.y); }
+// div_by on both components (Markstein's correction, as div_by)
+__device__ __forceinline__ f2 div_by2(f2 a, float d, float r) {
+  const f2 q = mul2(a, S2(r));
+  const f2 e = fma2(P2(-q.x, -q.y), S2(d), a);
+  return fma2(e, S2(r), q);
+}
+__device__ __forceinline__ f2 gamma_display2(f2 k) {
+  const f2 t = mul2(k, S2(-288.53900817779268f));
+  const f2 e = P2(ex2_approx(t.x), ex2_approx(t.y));
+  const f2 l = add2(S2(1.0f), e);
+  const f2 m = mul2(S2(-0.45454545454545453f), P2(lg2_approx(l.x), lg2_approx(l.y)));
+  return P2(ex2_approx(m.x), ex2_approx(m.y));
+}
+// atan_poly on both components (x >= 0 or any sign; same steps as atan_poly)
+__device__ __forceinline__ f2 atan_poly2(f2 x) {
+  const float ax0 = fabsf(x.x), ax1 = fabsf(x.y);
+  const bool i0 = ax0 > 1.0f, i1 = ax1 > 1.0f;
+  const f2 a = P2(i0 ? rcp_approx(ax0) : ax0, i1 ? rcp_approx(ax1) : ax1);
+  const f2 a2 = mul2(a, a);
+  f2 p = S2(-0x1.09b3ep-8f);
+  p = fma2(a2, p, S2(0x1.662f9cp-6f));
+  p = fma2(a2, p, S2(-0x1.ca055ep-5f));
+  p = fma2(a2, p, S2(0x1.8af07cp-4f));
+  p = fma2(a2, p, S2(-0x1.1cd902p-3f));
+  p = fma2(a2, p, S2(0x1.988166p-3f));
+  p = fma2(a2, p, S2(-0x1.554c3ap-2f));
+  p = fma2(a2, p, S2(0x1.ffffeap-1f));
+  f2 r = mul2(a, p);
+  r.x = copysignf(i0 ? 1.57079632679489661923f - r.x : r.x, x.x);
+  r.y = copysignf(i1 ? 1.57079632679489661923f - r.y : r.y, x.y);
+  return r;
+}
+
+// pixel_products for two pixels at once.
+__device__ __forceinline__ void pixel_products2(const Light& L, float sign_x, float sign_y, unsigned om, f2 p, f2 q,
+                                                f2 pz, f2 qz, f2 dxx, f2 dxy, f2 dyy, f2 dyx, f2* o) {
+  if (om & (1u << FSG_OUT_HILLSHADE)) {
+    const f2 e = mul2(pz, S2(sign_x)), nn = mul2(qz, S2(sign_y));
+    const f2 t = sub2(S2(L.lz), add2(mul2(e, S2(L.lx)), mul2(nn, S2(L.ly))));
+    const f2 n2 = add2(add2(mul2(e, e), mul2(nn, nn)), S2(1.0f));
+    const f2 hs = mul2(t, P2(rsqrtf(n2.x), rsqrtf(n2.y)));
+    o[FSG_OUT_HILLSHADE] = P2(fminf(fmaxf(hs.x, 0.0f), 1.0f), fminf(fmaxf(hs.y, 0.0f), 1.0f));
+  }
+  if (om & (1u << FSG_OUT_SLOPE)) {
+    const f2 g2 = add2(mul2(p, p), mul2(q, q));
+    if (L.slope_unit == FSG_SLOPE_DEGREE) {
+      o[FSG_OUT_SLOPE] = mul2(atan_poly2(P2(sqrt_approx(g2.x), sqrt_approx(g2.y))), S2(57.295780181884765625f));
+    } else {
+      o[FSG_OUT_SLOPE] = P2(slope_value(p.x, q.x, L.slope_unit), slope_value(p.y, q.y, L.slope_unit));
+    }
+  }
+  if (om & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) | (1u << FSG_OUT_CURV_PLANFORM) |
+            (1u << FSG_OUT_CURV_PROFILE))) {
+    const f2 p2 = mul2(p, p), q2 = mul2(q, q), pq = mul2(p, q);
+    const f2 g2 = add2(p2, q2), one_g2 = add2(S2(1.0f), g2);
+    const f2 s15 = mul2(one_g2, P2(sqrt_approx(one_g2.x), sqrt_approx(one_g2.y)));  // (1 + p^2 + q^2)^1.5
+    const f2 pq2 = mul2(S2(2.0f), pq);
+    if (om & (1u << FSG_OUT_CURV_MEAN)) {
+      const f2 sm = mul2(add2(dxy, dyx), S2(0.5f));
+      const f2 num = fma2(add2(S2(1.0f), p2), dyy, sub2(mul2(add2(S2(1.0f), q2), dxx), mul2(pq2, sm)));
+      const f2 den = fma2(S2(2.0f), s15, S2(1e-10f));
+      o[FSG_OUT_CURV_MEAN] = gamma_display2(mul2(P2(-num.x, -num.y), P2(rcp_approx(den.x), rcp_approx(den.y))));
+    }
+    if (om & (1u << FSG_OUT_CURV_GAUSSIAN)) {
+      const f2 num = sub2(mul2(dxx, dyy), mul2(dxy, dxy));
+      const f2 den = mul2(one_g2, one_g2);
+      o[FSG_OUT_CURV_GAUSSIAN] = gamma_display2(mul2(num, P2(rcp_approx(den.x), rcp_approx(den.y))));
+    }
+    if (om & (1u << FSG_OUT_CURV_PLANFORM)) {
+      const f2 num = fma2(p2, dyy, sub2(mul2(q2, dxx), mul2(pq2, dxy)));
+      const f2 den = fma2(g2, P2(sqrt_approx(g2.x), sqrt_approx(g2.y)), S2(1e-10f));
+      o[FSG_OUT_CURV_PLANFORM] = gamma_display2(mul2(P2(-num.x, -num.y), P2(rcp_approx(den.x), rcp_approx(den.y))));
+    }
+    if (om & (1u << FSG_OUT_CURV_PROFILE)) {
+      const f2 num = fma2(q2, dyy, fma2(pq2, dxy, mul2(p2, dxx)));
+      const f2 den = fma2(g2, s15, S2(1e-10f));
+      o[FSG_OUT_CURV_PROFILE] = gamma_display2(mul2(P2(-num.x, -num.y), P2(rcp_approx(den.x), rcp_approx(den.y))));
+    }
+  }
+  o[FSG_OUT_DX] = p;
+  o[FSG_OUT_DY] = q;
+}
+
+// Fast streaming pass (see above).  Rows reach the warp through a ring of
+// RING rows in shared memory filled by cp.async (one 8-byte copy per lane and
+// row, RING-1 rows in flight ahead of the row being consumed), so the
+// prefetch depth costs no registers.  A warp vote per row tells whether any
+// NoData lies in the five rows feeding that output row; only then are the
+// per-pixel checks evaluated.  DIV: derivatives use the correctly rounded
+// division (bit-exact np.gradient, needed for the dx/dy planes); otherwise a
+// multiply by the reciprocal.
+#ifndef FSG_FAST_RING
+#define FSG_FAST_RING 16  // rows per warp ring (RING - 1 copies in flight)
+#endif
+#ifndef FSG_FAST_MINB
+#define FSG_FAST_MINB 3  // resident 256-thread blocks per SM the register budget must allow
+#endif
+constexpr int RING = FSG_FAST_RING;
+
+__device__ __forceinline__ void cp_async8(unsigned dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(unsigned dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 template <bool CURV, unsigned OM, bool ALLF32>
-__global__ void __launch_bounds__(256) stencil_fast_kernel(const __grid_constant__ FastArgs A) {
+__global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const __grid_constant__ FastArgs A) {
   constexpr bool DIV = (OM & ((1u << FSG_OUT_DX) | (1u << FSG_OUT_DY))) != 0;
+  constexpr int REACH = CURV ? 2 : 1;  // rows above / below an output row that feed it
+  __shared__ __align__(16) float2 ring_s[256 / 32][RING][32];
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  float2* ring = ring_s[threadIdx.x >> 5][0];
+  const unsigned sbase = (unsigned)__cvta_generic_to_shared(ring) + lane * 8;
   const bool hn = A.has_nodata != 0;
   const Light L{A.lx, A.ly, A.lz, A.slope_unit};
+  const float qnan = __int_as_float(0x7fc00000);
   for (int u = warp; u < A.total_units; u += nwarps) {
     const UnitGeom g = unit_geom(A, u);
     const FastTile& T = A.tiles[g.t];
     const int x0 = g.x0, y0 = g.y0, y1 = g.y1, xo = g.xo;
-    // stencil reach: rows y0-2 .. y1+1 and cols x0-2 .. x0+29 strictly inside
+    // stencil reach: rows y0-2 .. y1+1 and cols x0-2 .. x0+61 strictly inside
     // the window, so every derivative is a central difference
     const bool interior = y0 - 2 >= T.wy0 && y1 + 2 <= T.wy1 && x0 - 2 >= T.wx0 && x0 + SW + 2 <= T.wx1;
     if (!interior) {
       if (lane == 0) push_fix(A, u, true);
       continue;
     }
-    const int x = x0 - 2 + lane;
-    const bool out_lane = lane >= 2 && lane < 2 + SW && x < xo;
-    const float* rp = A.raster + (long long)(y0 - (CURV ? 2 : 1)) * A.ld + x;  // next row to read
-    auto ld_next = [&]() {
-      float v = __ldg(rp);
-      rp += A.ld;
-      return is_nodata(v, A.ndf, hn) ? __int_as_float(0x7fc00000) : v;
+    const int x = x0 - 2 + 2 * lane;  // first column of this lane's pair
+    const bool out0 = lane >= 1 && lane <= SW / 2 && x < xo, out1 = out0 && x + 1 < xo;
+    // 8-byte copies need an 8-byte aligned pair start (uniform per unit)
+    const bool vload = ((A.ld & 1) == 0) && ((((uintptr_t)A.raster >> 2) + (uintptr_t)x0) & 1) == 0;
+    const int nrows = (y1 - y0) + 2 * REACH;      // rows y0-REACH .. y1+REACH-1
+    const float* src0 = A.raster + (long long)(y0 - REACH) * A.ld + x;
+    // row k of the unit -> ring slot k % RING; RING-1 copy groups in flight
+    auto issue = [&](int k) {
+      if (k < nrows) {
+        const float* gp = src0 + (long long)k * A.ld;
+        const unsigned dst = sbase + (unsigned)((k % RING) * 256);
+        if (vload) {
+          cp_async8(dst, gp);
+        } else {
+          cp_async4(dst, gp);
+          cp_async4(dst + 4, gp + 1);
+        }
+      }
+      cp_async_commit();
     };
-    auto dv = [&](float num, const Axis& a) { return DIV ? div_by(num, a.d2, a.rcp) : fmul(num, a.rcp); };
+    int nan_left = 0;  // rows for which the NoData seen last still feeds an output
+    auto take = [&](int k) {
+      cp_async_wait<RING - 2>();
+      f2 v = ring[(k % RING) * 32 + lane];
+      issue(k + RING - 1);
+      if (hn) {
+        if (is_nodata(v.x, A.ndf, true)) v.x = qnan;
+        if (is_nodata(v.y, A.ndf, true)) v.y = qnan;
+      }
+      if (nan2(v)) nan_left = 2 * REACH + 1;
+      return v;
+    };
+#pragma unroll 1
+    for (int k = 0; k < RING - 1; ++k) issue(k);
+    auto dv = [&](f2 num, const Axis& a) { return DIV ? div_by2(num, a.d2, a.rcp) : mul2(num, S2(a.rcp)); };
+    // horizontal central difference of a row pair: (f(c+1) - f(c-1), f(c+2) - f(c))
+    auto hdiff = [&](f2 f) {
+      const float left = __shfl_up_sync(0xffffffffu, f.y, 1), right = __shfl_down_sync(0xffffffffu, f.x, 1);
+      return sub2(P2(f.y, right), P2(left, f.x));
+    };
     char* optr[FSG_STENCIL_NOUT];
     long long ostep[FSG_STENCIL_NOUT];
+    bool vstore[FSG_STENCIL_NOUT];
 #pragma unroll
     for (int k = 0; k < FSG_STENCIL_NOUT; ++k) {
       if (!(OM & (1u << k))) continue;
       const PlaneK& P = A.planes[k];
       const int esz = ALLF32 ? 4 : (P.dtype == FSG_F32 ? 4 : (P.dtype == FSG_I16 ? 2 : 1));
-      optr[k] = static_cast<char*>(P.ptr) + ((long long)(T.oy0 + y0 - T.cy0) * P.ld + (T.ox0 + x - T.cx0)) * esz;
+      const long long col = (long long)(T.ox0 + x - T.cx0);
+      optr[k] = static_cast<char*>(P.ptr) + ((long long)(T.oy0 + y0 - T.cy0) * P.ld + col) * esz;
       ostep[k] = P.ld * esz;
+      vstore[k] = esz == 4 && ((P.ld & 1) == 0) &&
+                  ((((uintptr_t)P.ptr >> 2) + (uintptr_t)(T.ox0 + x0 - 2 - T.cx0)) & 1) == 0 &&
+                  (((uintptr_t)P.ptr & 3) == 0);
     }
-    constexpr int G = 8;
-    const int last = CURV ? y1 + 1 : y1;  // last row read
-    int next_row = y0 - (CURV ? 2 : 1);
-    float fm2 = 0.f, fm1, f0, fp1, fp2 = 0.f;
-    if (CURV) fm2 = ld_next();
-    fm1 = ld_next();
-    f0 = ld_next();
-    fp1 = ld_next();
-    if (CURV) fp2 = ld_next();
-    next_row += CURV ? 5 : 3;
-    float cur[G];
-#pragma unroll
-    for (int k = 0; k < G; ++k) cur[k] = (next_row + k <= last) ? ld_next() : 0.f;
-    next_row += G;
-    auto dxof = [&](float f) { return dv(fsub(shfl_dn1(f), shfl_up1(f)), T.g1x); };
-    float dxm1 = 0.f, dym1 = 0.f, dx0 = 0.f, dy0 = 0.f;
+    int kr = 0;  // next unit row to take
+    f2 fm2 = S2(0.f), fm1, f0, fp1, fp2 = S2(0.f);
+    if (CURV) fm2 = take(kr++);
+    fm1 = take(kr++);
+    f0 = take(kr++);
+    fp1 = take(kr++);
+    if (CURV) fp2 = take(kr++);
+    f2 dxm1 = S2(0.f), dym1 = S2(0.f), dx0 = S2(0.f), dy0 = S2(0.f);
     if (CURV) {
-      dxm1 = dxof(fm1);
-      dym1 = dv(fsub(f0, fm2), T.g1y);
-      dx0 = dxof(f0);
-      dy0 = dv(fsub(fp1, fm1), T.g1y);
+      dxm1 = dv(hdiff(fm1), T.g1x);
+      dym1 = dv(sub2(f0, fm2), T.g1y);
+      dx0 = dv(hdiff(f0), T.g1x);
+      dy0 = dv(sub2(fp1, fm1), T.g1y);
     }
     bool bad = false;
-    for (int yb = y0; yb < y1; yb += G) {
-      float nxt[G];
+#pragma unroll 1
+    for (int y = y0; y < y1; ++y) {
+      // NoData in the 2*REACH+1 rows feeding this output row (any lane)?
+      const bool row_nan = __any_sync(0xffffffffu, nan_left > 0);
+      f2 p, q, dxx = S2(0.f), dxy = S2(0.f), dyy = S2(0.f), dyx = S2(0.f), dxp1 = S2(0.f), dyp1 = S2(0.f);
+      if (CURV) {
+        dxp1 = dv(hdiff(fp1), T.g1x);
+        dyp1 = dv(sub2(fp2, f0), T.g1y);
+        p = dx0;
+        q = dy0;
+        dxx = dv(hdiff(dx0), T.c2x);
+        dxy = dv(sub2(dxp1, dxm1), T.c2y);
+        dyy = dv(sub2(dyp1, dym1), T.c2y);
+        if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = dv(hdiff(dy0), T.c2x);
+      } else {
+        p = dv(hdiff(f0), T.g1x);
+        q = dv(sub2(fp1, fm1), T.g1y);
+      }
+      f2 pz = p, qz = q;
+      if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) {
+        const f2 zf = S2(A.z);
+        pz = dv(hdiff(mul2(f0, zf)), T.g1x);
+        qz = dv(sub2(mul2(fp1, zf), mul2(fm1, zf)), T.g1y);
+      }
+      const bool v0 = f0.x == f0.x, v1 = f0.y == f0.y;
+      if (row_nan) {
+        f2 chk = add2(p, q);
+        if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) chk = add2(chk, add2(pz, qz));
+        if (CURV) chk = add2(add2(chk, add2(dxx, dxy)), add2(dyy, dyx));
+        bad |= (out0 && v0 && chk.x != chk.x) || (out1 && v1 && chk.y != chk.y);
+      }
+      f2 o[FSG_STENCIL_NOUT];
+      pixel_products2(L, T.sx, T.sy, OM, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
+      if (!(v0 && v1)) {
 #pragma unroll
-      for (int k = 0; k < G; ++k) nxt[k] = (next_row + k <= last) ? ld_next() : 0.f;
-      next_row += G;
-      // NoData anywhere in the rows feeding this group (the window and the group buffer)?
-      bool gn = (fm2 != fm2) | (fm1 != fm1) | (f0 != f0) | (fp1 != fp1) | (fp2 != fp2);
-#pragma unroll
-      for (int k = 0; k < G; ++k) gn |= cur[k] != cur[k];
-      const bool group_nan = __any_sync(0xffffffffu, gn);
-#pragma unroll
-      for (int k = 0; k < G; ++k) {
-        const int y = yb + k;
-        if (y >= y1) break;
-        float p, q, dxx = 0.f, dxy = 0.f, dyy = 0.f, dyx = 0.f, dxp1 = 0.f, dyp1 = 0.f;
-        if (CURV) {
-          dxp1 = dxof(fp1);
-          dyp1 = dv(fsub(fp2, f0), T.g1y);
-          p = dx0;
-          q = dy0;
-          dxx = dv(fsub(shfl_dn1(dx0), shfl_up1(dx0)), T.c2x);
-          dxy = dv(fsub(dxp1, dxm1), T.c2y);
-          dyy = dv(fsub(dyp1, dym1), T.c2y);
-          if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = dv(fsub(shfl_dn1(dy0), shfl_up1(dy0)), T.c2x);
-        } else {
-          p = dxof(f0);
-          q = dv(fsub(fp1, fm1), T.g1y);
-        }
-        float pz = p, qz = q;
-        if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) {
-          const float zf = A.z;
-          pz = dv(fsub(shfl_dn1(fmul(f0, zf)), shfl_up1(fmul(f0, zf))), T.g1x);
-          qz = dv(fsub(fmul(fp1, zf), fmul(fm1, zf)), T.g1y);
-        }
-        const bool valid = f0 == f0;
-        if (group_nan) {
-          float chk = p + q;
-          if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) chk += pz + qz;
-          if (CURV) chk += dxx + dxy + dyy + dyx;
-          bad |= out_lane && valid && chk != chk;
-        }
-        float o[FSG_STENCIL_NOUT];
-        if (valid) {
-          pixel_products(L, T.sx, T.sy, OM, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
-        } else {
-#pragma unroll
-          for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) o[kk] = __int_as_float(0x7fc00000);
-        }
-        if (out_lane) store_pixel(A, OM, ALLF32, optr, o);
-#pragma unroll
-        for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) optr[kk] += ostep[kk];
-        // slide one row down
-        if (CURV) {
-          fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2; fp2 = cur[k];
-          dxm1 = dx0; dym1 = dy0; dx0 = dxp1; dy0 = dyp1;
-        } else {
-          fm1 = f0; f0 = fp1; fp1 = cur[k];
+        for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) {
+          if (!v0) o[kk].x = qnan;
+          if (!v1) o[kk].y = qnan;
         }
       }
 #pragma unroll
-      for (int k = 0; k < G; ++k) cur[k] = nxt[k];
+      for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) {
+        if (!(OM & (1u << kk))) continue;
+        char* dst = optr[kk];
+        if (ALLF32 || A.planes[kk].dtype == FSG_F32) {
+          if (vstore[kk] && out1) {
+            *reinterpret_cast<float2*>(dst) = o[kk];
+          } else {
+            if (out0) reinterpret_cast<float*>(dst)[0] = o[kk].x;
+            if (out1) reinterpret_cast<float*>(dst)[1] = o[kk].y;
+          }
+        } else {
+          const PlaneK& P = A.planes[kk];
+          const float c0 = quantize(o[kk].x, P.qa, P.qb, P.qmin, P.qmax);
+          const float c1 = quantize(o[kk].y, P.qa, P.qb, P.qmin, P.qmax);
+          if (P.dtype == FSG_U8) {
+            if (out0) reinterpret_cast<uint8_t*>(dst)[0] = (uint8_t)(int)c0;
+            if (out1) reinterpret_cast<uint8_t*>(dst)[1] = (uint8_t)(int)c1;
+          } else {
+            if (out0) reinterpret_cast<int16_t*>(dst)[0] = (int16_t)(int)c0;
+            if (out1) reinterpret_cast<int16_t*>(dst)[1] = (int16_t)(int)c1;
+          }
+        }
+        optr[kk] += ostep[kk];
+      }
+      // slide one row down
+      if (nan_left > 0) --nan_left;
+      if (y + 1 < y1) {
+        const f2 nx = take(kr++);
+        if (CURV) {
+          fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2; fp2 = nx;
+          dxm1 = dx0; dym1 = dy0; dx0 = dxp1; dy0 = dyp1;
+        } else {
+          fm1 = f0; f0 = fp1; fp1 = nx;
+        }
+      }
     }
     if (__ballot_sync(0xffffffffu, bad) && lane == 0) push_fix(A, u, false);
   }
+  cp_async_wait<0>();
 }
 
 // ------------------------------------------------------------- fix-up pass
@@ -753,12 +912,13 @@ __global__ void __launch_bounds__(256) stencil_fast_kernel(const __grid_constant
 // float32 intermediate, sums in float-float), then np.gradient with the
 // window's edge rules and the second derivatives on the signed steps.
 // Regions, relative to the unit origin (y0, x0):
-//   S  source values        rows -8 .. SH+8, cols -8 .. SW+8 (NaN outside the window)
-//   E  filled values        rows -4 .. SH+4, cols -4 .. SW+4
-//   D  first derivatives    rows -2 .. SH+2, cols -2 .. SW+2 (curvature only)
-constexpr int XS_R = SH + 16, XS_C = SW + 16;  // 80 x 44
-constexpr int XE_R = SH + 8, XE_C = SW + 8;    // 72 x 36
-constexpr int XD_R = SH + 4, XD_C = SW + 4;    // 68 x 32
+//   S  source values        rows -8 .. SH+8, cols -8 .. FW+8 (NaN outside the window)
+//   E  filled values        rows -4 .. SH+4, cols -4 .. FW+4
+//   D  first derivatives    rows -2 .. SH+2, cols -2 .. FW+2 (curvature only)
+// for each half (FW columns) of the unit.
+constexpr int XS_R = SH + 16, XS_C = FW + 16;  // 80 x 46
+constexpr int XE_R = SH + 8, XE_C = FW + 8;    // 72 x 38
+constexpr int XD_R = SH + 4, XD_C = FW + 4;    // 68 x 34
 constexpr int XNT = 256;
 constexpr size_t FIX_SMEM = sizeof(float) * (XS_R * XS_C + XE_R * XE_C) +
                             sizeof(float) * 2 * XE_R * XS_C +            // axis-0 sums (aliases D)
@@ -796,12 +956,13 @@ __global__ void __launch_bounds__(XNT) stencil_fixup_kernel(const __grid_constan
   const bool hn = A.has_nodata != 0;
   const float qnan = __int_as_float(0x7fc00000);
   const unsigned count = *A.fix_count;
-  for (unsigned it = blockIdx.x; it < count; it += gridDim.x) {
-    const unsigned e = A.fix_list[it];
+  for (unsigned it = blockIdx.x; it < 2 * count; it += gridDim.x) {
+    const unsigned e = A.fix_list[it >> 1];
     const bool edge = (e & FIX_EDGE) != 0;
     const UnitGeom g = unit_geom(A, (int)(e & ~FIX_EDGE));
     const FastTile& T = A.tiles[g.t];
-    const int x0 = g.x0, y0 = g.y0, y1 = g.y1, xo = g.xo;
+    const int x0 = g.x0 + (int)(it & 1) * FW, y0 = g.y0, y1 = g.y1, xo = min(x0 + FW, g.xo);
+    if (x0 >= xo) continue;
     // (a) source region, NoData -> NaN, outside the window -> NaN (never read)
     for (int i = tid; i < XS_R * XS_C; i += XNT) {
       const int r = i / XS_C, c = i - (i / XS_C) * XS_C;
@@ -923,8 +1084,8 @@ __global__ void __launch_bounds__(XNT) stencil_fixup_kernel(const __grid_constan
     }
     // (g) outputs of every pixel of the unit
     const Light L{A.lx, A.ly, A.lz, A.slope_unit};
-    for (int i = tid; i < SH * SW; i += XNT) {
-      const int r = i / SW, c = i - (i / SW) * SW;
+    for (int i = tid; i < SH * FW; i += XNT) {
+      const int r = i / FW, c = i - (i / FW) * FW;
       const int gy = y0 + r, gx = x0 + c;
       if (gy >= y1 || gx >= xo) continue;
       float o[FSG_STENCIL_NOUT];
@@ -1206,7 +1367,7 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
     FSG_CUDA(cudaFuncSetAttribute(fixup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FIX_SMEM));
     int xper = 0;
     FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&xper, fixup, XNT, FIX_SMEM));
-    const int xgrid = std::min(units, di.sms * std::max(1, xper));
+    const int xgrid = std::min(2 * units, di.sms * std::max(1, xper));
     fixup<<<xgrid, XNT, FIX_SMEM, s>>>(F);
     FSG_LAUNCHED(1);
     return FSG_OK;
