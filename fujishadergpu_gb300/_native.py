@@ -112,6 +112,8 @@ _SIGNATURES = {
     "fsg_percentile": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_double), C.c_int32,
                                  C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_void_p]),
     "fsg_std": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.c_void_p]),
+    "fsg_key_histogram": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_uint32, C.c_uint32, C.c_int32,
+                                    C.c_int32, C.POINTER(C.c_uint64), C.c_void_p]),
     "fsg_percentile_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_double), C.c_int32,
                                          C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_void_p]),
     "fsg_openness": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
@@ -133,6 +135,14 @@ _SIGNATURES = {
     "fsg_masked_store": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                    C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(Plane),
                                    C.c_void_p]),
+    "fsg_conv_pack_weights": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "fsg_conv3x3": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                              C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fsg_conv3x3_wgrad": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                    C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fsg_head_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_int64, C.c_void_p, C.c_void_p]),
+    "fsg_head_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 

@@ -63,11 +63,11 @@ def _scales(pixel_size, pixel_scale_x, pixel_scale_y):
 
 def openness_planes(block, *, openness_type="positive", num_directions=16, max_distance=50, pixel_size=1.0,
                     pixel_scale_x=None, pixel_scale_y=None, sampling="reference", display=True, raw=False,
-                    stretch=None, out_dtype="float32", qp=None):
+                    stretch=None, out_dtype="float32", qp=None, nodata=None):
     v = _arrays.as_device_f32_2d(block)
     sx, sy = _scales(pixel_size, pixel_scale_x, pixel_scale_y)
     params = make_params(openness_type=openness_type, num_directions=num_directions, max_distance=max_distance,
-                         pixel_size=pixel_size, sampling=sampling, stretch=stretch)
+                         pixel_size=pixel_size, sampling=sampling, stretch=stretch, nodata=nodata)
     disp = _arrays.empty(v.h, v.w, out_dtype, device=v.tensor.device) if display else None
     rawt = _arrays.empty(v.h, v.w, device=v.tensor.device) if raw else None
     if v.h * v.w:
@@ -86,11 +86,14 @@ def compute_openness_vectorized(block, *, openness_type: str = "positive", num_d
 
 
 def compute_openness_raw_degrees(block, *, openness_type="positive", num_directions=16, max_distance=50,
-                                 pixel_size=1.0, pixel_scale_x=None, pixel_scale_y=None, sampling="reference"):
-    """Directional mean zenith (positive) / nadir (negative) angle in degrees."""
+                                 pixel_size=1.0, pixel_scale_x=None, pixel_scale_y=None, sampling="reference",
+                                 nodata=None):
+    """Directional mean zenith (positive) / nadir (negative) angle in degrees (``nodata``: a
+    numeric sentinel treated as NoData, as the tile processor's mask)."""
     _, raw, v = openness_planes(block, openness_type=openness_type, num_directions=num_directions,
                                 max_distance=max_distance, pixel_size=pixel_size, pixel_scale_x=pixel_scale_x,
-                                pixel_scale_y=pixel_scale_y, sampling=sampling, display=False, raw=True)
+                                pixel_scale_y=pixel_scale_y, sampling=sampling, display=False, raw=True,
+                                nodata=nodata)
     return _arrays.wrap_result(raw, v.origin)
 
 

@@ -28,7 +28,8 @@
 namespace fsg {
 namespace {
 
-constexpr int BX = 32, BY = 8, RPT = 4;  // block 32 x 8 threads, 4 rows per thread: 32 x 32 pixels
+constexpr int BX = 32, BY = 8, RPT = 4;  // block 32 x 8 threads; a thread: 4 rows x 2 columns
+constexpr int PW = 2 * BX, PH = BY * RPT;  // pixels per block: 64 x 32
 
 struct RaySample {
   short ox, oy;
@@ -43,9 +44,11 @@ struct OpenArgs {
   int has_nodata;
   int positive;
   int ndir;
+  int ns;                      // samples per tile (all directions)
   const int* ray_begin;        // [ntiles * (ndir + 1)] offsets into samples
   const RaySample* samples;    // per tile: its own distance table
   const int* tile_sample0;     // first sample index of each tile
+  const int* tile_reach;       // per tile: max |ox|, max |oy| of its samples
   const fsg_tile* tiles;       // device copy
   const int* block0;           // first block of each tile
   int ntiles, total_blocks;
@@ -66,7 +69,37 @@ __device__ __forceinline__ float load_z(const OpenArgs& A, int y, int x, const f
   return is_nodata(v, A.ndf, A.has_nodata != 0) ? __int_as_float(0x7fc00000) : v;
 }
 
+typedef float2 f2;
+__device__ __forceinline__ f2 S2(float a) { return make_float2(a, a); }
+// (v - z) / d per component, correctly rounded (Markstein's correction, as
+// div_by); nz = -z, nd = -d (q * -d == -(q * d) exactly)
+__device__ __forceinline__ f2 slope2(f2 v, f2 nz, float nd, float r) {
+  const f2 num = __fadd2_rn(v, nz);
+  const f2 q = __fmul2_rn(num, S2(r));
+  const f2 e = __ffma2_rn(q, S2(nd), num);
+  return __ffma2_rn(e, S2(r), q);
+}
+__device__ __forceinline__ float nd_nan(float v, const OpenArgs& A) {
+  return is_nodata(v, A.ndf, true) ? __int_as_float(0x7fc00000) : v;
+}
+
+// Per pixel pair (x, x+1) and row: the per-direction extreme slope ratio of
+// the valid samples (NaN samples drop out: fmaxf / fminf return the other
+// operand), atan of it once per direction, directional mean.  Blocks whose
+// rays stay inside the window (all but the window's outer ring) take the
+// interior path: one element offset per sample, no bounds checks.
+template <bool POS, bool HN>
 __global__ void __launch_bounds__(BX * BY) openness_kernel(const __grid_constant__ OpenArgs A) {
+  extern __shared__ unsigned char osm[];
+  int* soff = reinterpret_cast<int*>(osm);             // [ns] element offset oy * ld + ox
+  float* sd = reinterpret_cast<float*>(soff + A.ns);   // [ns] distance
+  float* sr = sd + A.ns;                               // [ns] RN(1/d)
+  short* sox = reinterpret_cast<short*>(sr + A.ns);    // [ns]
+  short* soy = sox + A.ns;                             // [ns]
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  int loaded = -1;
+  const float init = POS ? -INFINITY : INFINITY;
+  const float half_pi = 1.57079637050628662109375f;  // f32(pi/2)
   for (int blk = blockIdx.x; blk < A.total_blocks; blk += gridDim.x) {
     int lo = 0, hi = A.ntiles - 1;
     while (lo < hi) {
@@ -74,68 +107,118 @@ __global__ void __launch_bounds__(BX * BY) openness_kernel(const __grid_constant
       if (A.block0[mid] <= blk) lo = mid; else hi = mid - 1;
     }
     const fsg_tile T = A.tiles[lo];
-    const int nbx = (T.core_w + BX - 1) / BX;
+    if (lo != loaded) {  // stage this tile's sample table
+      __syncthreads();
+      const RaySample* S = A.samples + A.tile_sample0[lo];
+      for (int i = tid; i < A.ns; i += BX * BY) {
+        const RaySample rs = S[i];
+        soff[i] = (int)rs.oy * (int)A.ld + (int)rs.ox;
+        sd[i] = rs.d;
+        sr[i] = rs.r;
+        sox[i] = rs.ox;
+        soy[i] = rs.oy;
+      }
+      loaded = lo;
+      __syncthreads();
+    }
+    const int* rb = A.ray_begin + lo * (A.ndir + 1);
+    const int nbx = (T.core_w + PW - 1) / PW;
     const int lb = blk - A.block0[lo];
     const int by = lb / nbx, bx = lb - by * nbx;
-    const int x = T.core_x0 + bx * BX + threadIdx.x;
-    const int yb = T.core_y0 + by * (BY * RPT) + threadIdx.y * RPT;
-    const RaySample* S = A.samples + A.tile_sample0[lo];
-    const int* rb = A.ray_begin + lo * (A.ndir + 1);
-    float z[RPT], sum[RPT], cnt[RPT];
+    const int bx0 = T.core_x0 + bx * PW, by0 = T.core_y0 + by * PH;
+    const int x = bx0 + 2 * threadIdx.x;
+    const int yb = by0 + threadIdx.y * RPT;
+    const int rx = A.tile_reach[2 * lo], ry = A.tile_reach[2 * lo + 1];
+    const bool interior = bx0 - rx >= T.win_x0 && bx0 + PW + rx <= T.win_x0 + T.win_w && by0 - ry >= T.win_y0 &&
+                          by0 + PH + ry <= T.win_y0 + T.win_h;
+    const bool cx0 = x < T.core_x0 + T.core_w, cx1 = x + 1 < T.core_x0 + T.core_w;
+    f2 z[RPT], sum[RPT], cnt[RPT];
 #pragma unroll
     for (int k = 0; k < RPT; ++k) {
-      z[k] = (x < T.core_x0 + T.core_w && yb + k < T.core_y0 + T.core_h) ? load_z(A, yb + k, x, T)
-                                                                          : __int_as_float(0x7fc00000);
-      sum[k] = 0.f;
-      cnt[k] = 0.f;
+      const bool row = yb + k < T.core_y0 + T.core_h;
+      z[k].x = (row && cx0) ? load_z(A, yb + k, x, T) : __int_as_float(0x7fc00000);
+      z[k].y = (row && cx1) ? load_z(A, yb + k, x + 1, T) : __int_as_float(0x7fc00000);
+      sum[k] = S2(0.f);
+      cnt[k] = S2(0.f);
     }
-    const float half_pi = 1.57079637050628662109375f;  // f32(pi/2)
+    const float* base = A.raster + (long long)yb * A.ld + x;
+    f2 nz[RPT];
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) nz[k] = make_float2(-z[k].x, -z[k].y);
     for (int d = 0; d < A.ndir; ++d) {
-      float ext[RPT];
+      f2 ext[RPT];
 #pragma unroll
-      for (int k = 0; k < RPT; ++k) ext[k] = A.positive ? -INFINITY : INFINITY;
-      for (int s = rb[d]; s < rb[d + 1]; ++s) {
-        const RaySample rs = S[s];
+      for (int k = 0; k < RPT; ++k) ext[k] = S2(init);
+      if (interior) {
+        for (int s = rb[d]; s < rb[d + 1]; ++s) {
+          const float* ps = base + soff[s];
+          const float nd = -sd[s], rr = sr[s];
 #pragma unroll
-        for (int k = 0; k < RPT; ++k) {
-          float v = load_z(A, yb + k + rs.oy, x + rs.ox, T);
-          if (v == v) {
-            float t = div_by(__fsub_rn(v, z[k]), rs.d, rs.r);
-            ext[k] = A.positive ? fmaxf(ext[k], t) : fminf(ext[k], t);
+          for (int k = 0; k < RPT; ++k) {
+            f2 v = make_float2(__ldg(ps + (long long)k * A.ld), __ldg(ps + (long long)k * A.ld + 1));
+            if (HN) v = make_float2(nd_nan(v.x, A), nd_nan(v.y, A));
+            const f2 t = slope2(v, nz[k], nd, rr);
+            ext[k].x = POS ? fmaxf(ext[k].x, t.x) : fminf(ext[k].x, t.x);
+            ext[k].y = POS ? fmaxf(ext[k].y, t.y) : fminf(ext[k].y, t.y);
+          }
+        }
+      } else {
+        for (int s = rb[d]; s < rb[d + 1]; ++s) {
+          const int ox = sox[s], oy = soy[s];
+          const float nd = -sd[s], rr = sr[s];
+#pragma unroll
+          for (int k = 0; k < RPT; ++k) {
+            const f2 v = make_float2(load_z(A, yb + k + oy, x + ox, T), load_z(A, yb + k + oy, x + 1 + ox, T));
+            const f2 t = slope2(v, nz[k], nd, rr);
+            ext[k].x = POS ? fmaxf(ext[k].x, t.x) : fminf(ext[k].x, t.x);
+            ext[k].y = POS ? fmaxf(ext[k].y, t.y) : fminf(ext[k].y, t.y);
           }
         }
       }
 #pragma unroll
       for (int k = 0; k < RPT; ++k) {
-        if (ext[k] != (A.positive ? -INFINITY : INFINITY)) {
-          float a = atanf(ext[k]);
-          sum[k] = __fadd_rn(sum[k], A.positive ? __fsub_rn(half_pi, a) : __fadd_rn(half_pi, a));
-          cnt[k] = __fadd_rn(cnt[k], 1.0f);
+        // atan of the extreme ratio once per direction; directions without a valid sample drop out
+        if (ext[k].x != init) {
+          const float a = atanf(ext[k].x);
+          sum[k].x = __fadd_rn(sum[k].x, POS ? __fsub_rn(half_pi, a) : __fadd_rn(half_pi, a));
+          cnt[k].x = __fadd_rn(cnt[k].x, 1.0f);
+        }
+        if (ext[k].y != init) {
+          const float a = atanf(ext[k].y);
+          sum[k].y = __fadd_rn(sum[k].y, POS ? __fsub_rn(half_pi, a) : __fadd_rn(half_pi, a));
+          cnt[k].y = __fadd_rn(cnt[k].y, 1.0f);
         }
       }
     }
 #pragma unroll
     for (int k = 0; k < RPT; ++k) {
       const int y = yb + k;
-      if (x >= T.core_x0 + T.core_w || y >= T.core_y0 + T.core_h) continue;
-      float mean = __fdiv_rn(sum[k], fmaxf(cnt[k], 1.0f));
-      float disp, rawd;
-      if (z[k] != z[k]) {
-        disp = rawd = __int_as_float(0x7fc00000);
-      } else {
-        float op = fminf(fmaxf(__fdiv_rn(mean, half_pi), 0.0f), 1.0f);
-        disp = op > 0.f ? exp2f(0.45454545454545453f * __log2f(op)) : 0.0f;
-        if (A.scale > 0.f) disp = fmaxf(__fdiv_rn(__fsub_rn(disp, A.lo), A.scale), 0.0f);
-        rawd = mean * 57.295780181884765625f;
+      if (y >= T.core_y0 + T.core_h) continue;
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int xx = x + c;
+        if (xx >= T.core_x0 + T.core_w) continue;
+        const float zz = c ? z[k].y : z[k].x;
+        const float sm = c ? sum[k].y : sum[k].x, cn = c ? cnt[k].y : cnt[k].x;
+        float mean = __fdiv_rn(sm, fmaxf(cn, 1.0f));
+        float disp, rawd;
+        if (zz != zz) {
+          disp = rawd = __int_as_float(0x7fc00000);
+        } else {
+          float op = fminf(fmaxf(__fdiv_rn(mean, half_pi), 0.0f), 1.0f);
+          disp = op > 0.f ? exp2f(0.45454545454545453f * __log2f(op)) : 0.0f;
+          if (A.scale > 0.f) disp = fmaxf(__fdiv_rn(__fsub_rn(disp, A.lo), A.scale), 0.0f);
+          rawd = mean * 57.295780181884765625f;
+        }
+        const long long py = T.out_y0 + (y - T.core_y0), px = T.out_x0 + (xx - T.core_x0);
+        if (A.disp) {
+          long long o = py * A.dld + px;
+          if (A.ddtype == FSG_F32) static_cast<float*>(A.disp)[o] = disp;
+          else if (A.ddtype == FSG_U8) static_cast<uint8_t*>(A.disp)[o] = (uint8_t)(int)quantize(disp, A.qa, A.qb, A.qmin, A.qmax);
+          else static_cast<int16_t*>(A.disp)[o] = (int16_t)(int)quantize(disp, A.qa, A.qb, A.qmin, A.qmax);
+        }
+        if (A.raw) A.raw[py * A.rld + px] = rawd;
       }
-      const long long py = T.out_y0 + (y - T.core_y0), px = T.out_x0 + (x - T.core_x0);
-      if (A.disp) {
-        long long o = py * A.dld + px;
-        if (A.ddtype == FSG_F32) static_cast<float*>(A.disp)[o] = disp;
-        else if (A.ddtype == FSG_U8) static_cast<uint8_t*>(A.disp)[o] = (uint8_t)(int)quantize(disp, A.qa, A.qb, A.qmin, A.qmax);
-        else static_cast<int16_t*>(A.disp)[o] = (int16_t)(int)quantize(disp, A.qa, A.qb, A.qmin, A.qmax);
-      }
-      if (A.raw) A.raw[py * A.rld + px] = rawd;
     }
   }
 }
@@ -218,7 +301,7 @@ extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_
   for (auto& r : rays) per_tile += (int)r.size();
   // Host tables: per tile its distance table (pixel scales may differ per tile).
   std::vector<RaySample> samples;
-  std::vector<int> ray_begin, tile_sample0, block0;
+  std::vector<int> ray_begin, tile_sample0, block0, reach;
   samples.reserve((size_t)per_tile * ntiles);
   int total = 0;
   for (int t = 0; t < ntiles; ++t) {
@@ -229,7 +312,7 @@ extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_
     if (sx < 1e-9) sx = fb;
     if (sy < 1e-9) sy = fb;
     tile_sample0.push_back((int)samples.size());
-    int acc = 0;
+    int acc = 0, rx = 0, ry = 0;
     for (int d = 0; d < ndir; ++d) {
       ray_begin.push_back(acc);
       for (auto& o : rays[d]) {
@@ -240,21 +323,25 @@ extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_
         rs.d = (float)dist;
         rs.r = 1.0f / rs.d;
         samples.push_back(rs);
+        rx = std::max(rx, std::abs(o.first));
+        ry = std::max(ry, std::abs(o.second));
         ++acc;
       }
     }
     ray_begin.push_back(acc);
+    reach.push_back(rx);
+    reach.push_back(ry);
     block0.push_back(total);
-    if (T.core_h > 0 && T.core_w > 0)
-      total += ((T.core_w + BX - 1) / BX) * ((T.core_h + BY * RPT - 1) / (BY * RPT));
+    if (T.core_h > 0 && T.core_w > 0) total += ((T.core_w + PW - 1) / PW) * ((T.core_h + PH - 1) / PH);
   }
   if (total == 0) return FSG_OK;
   cudaStream_t s = (cudaStream_t)stream;
   size_t b_samples = samples.size() * sizeof(RaySample), b_rb = ray_begin.size() * sizeof(int);
   size_t b_ts = tile_sample0.size() * sizeof(int), b_b0 = block0.size() * sizeof(int);
+  size_t b_re = reach.size() * sizeof(int);
   size_t b_tiles = (size_t)ntiles * sizeof(fsg_tile);
   auto al = [](size_t n) { return (n + 255) & ~(size_t)255; };
-  size_t bytes = al(b_samples) + al(b_rb) + al(b_ts) + al(b_b0) + al(b_tiles);
+  size_t bytes = al(b_samples) + al(b_rb) + al(b_ts) + al(b_b0) + al(b_tiles) + al(b_re);
   std::vector<char> host(bytes);
   size_t off = 0;
   auto put = [&](const void* src, size_t n) {
@@ -265,6 +352,7 @@ extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_
   };
   size_t o_s = put(samples.data(), b_samples), o_rb = put(ray_begin.data(), b_rb);
   size_t o_ts = put(tile_sample0.data(), b_ts), o_b0 = put(block0.data(), b_b0), o_t = put(tiles, b_tiles);
+  size_t o_re = put(reach.data(), b_re);
   StreamScratch scratch;
   st = scratch.alloc(bytes, s);
   if (st) return st;
@@ -280,6 +368,8 @@ extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_
   A.has_nodata = p->has_nodata != 0;
   A.positive = p->openness_type == 0;
   A.ndir = ndir;
+  A.ns = per_tile;
+  A.tile_reach = reinterpret_cast<const int*>(base + o_re);
   A.samples = reinterpret_cast<const RaySample*>(base + o_s);
   A.ray_begin = reinterpret_cast<const int*>(base + o_rb);
   A.tile_sample0 = reinterpret_cast<const int*>(base + o_ts);
@@ -303,10 +393,17 @@ extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_
   DeviceInfo di;
   st = device_info(&di);
   if (st) return st;
+  if ((long long)p->max_distance * ld >= (1LL << 31))
+    return fail(FSG_ERR_UNSUPPORTED, "max_distance %d x row pitch %lld exceeds 32-bit offsets", p->max_distance,
+                (long long)ld);
+  void (*kern)(OpenArgs) = A.positive ? (A.has_nodata ? openness_kernel<true, true> : openness_kernel<true, false>)
+                                      : (A.has_nodata ? openness_kernel<false, true> : openness_kernel<false, false>);
+  const size_t smem = (size_t)per_tile * (3 * sizeof(float) + 2 * sizeof(short)) + 16;
+  if (smem > 48 * 1024) FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, openness_kernel, BX * BY, 0));
+  FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BX * BY, smem));
   int grid = std::min(total, di.sms * std::max(1, per_sm));
-  openness_kernel<<<grid, dim3(BX, BY), 0, s>>>(A);
+  kern<<<grid, dim3(BX, BY), smem, s>>>(A);
   FSG_LAUNCHED(1);
   return FSG_OK;
 }

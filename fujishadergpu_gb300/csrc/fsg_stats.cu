@@ -7,7 +7,7 @@
 // per-pass bin choice runs on the device, so a percentile costs 1 + 3 * ranks
 // streaming passes and a single host synchronisation.  The linear
 // interpolation between neighbouring ranks follows numpy.percentile's
-// 'linear' method (virtual index n*q + (1 - q) - 1, _lerp), evaluated in FP64
+// 'linear' method (virtual index (n - 1) * q, _lerp), evaluated in FP64
 // (NumPy and CuPy interpolate float32 data in float32 for a scalar q; the two
 // differ by at most one float32 ulp of the result).
 #include <algorithm>
@@ -126,7 +126,7 @@ struct LinearPick {
 };
 static LinearPick linear_pick(long long n, double q) {
   double qq = q / 100.0;
-  double virt = (double)n * qq + (1.0 + qq * (1.0 - 1.0 - 1.0)) - 1.0;
+  double virt = (double)(n - 1) * qq;  // the 'linear' method's virtual index
   LinearPick p;
   double prev = std::floor(virt);
   p.gamma = virt - prev;
@@ -211,6 +211,51 @@ extern "C" int fsg_percentile(const float* values_dev, int64_t n, int32_t abs_va
     float a = value_of((unsigned long long)picks[i].lo), b = value_of((unsigned long long)picks[i].hi);
     out[i] = lerp_numpy(a, b, picks[i].gamma);
   }
+  return FSG_OK;
+}
+
+namespace fsg {
+namespace {
+// hist[(key >> shift) & (2^bits - 1)] += 1 for the valid keys with (key & mask) == prefix.
+__global__ void key_hist(const float* __restrict__ x, long long n, int absmode, unsigned prefix, unsigned mask,
+                         int shift, int bits, unsigned long long* hist) {
+  __shared__ unsigned h[BINS];
+  for (int i = threadIdx.x; i < BINS; i += NT) h[i] = 0;
+  __syncthreads();
+  const unsigned bm = (1u << bits) - 1u;
+  for (long long i = blockIdx.x * (long long)NT + threadIdx.x; i < n; i += (long long)gridDim.x * NT) {
+    unsigned k;
+    if (take(__ldg(x + i), absmode, &k) && (k & mask) == prefix) atomicAdd(&h[(k >> shift) & bm], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i <= (int)bm; i += NT)
+    if (h[i]) atomicAdd(&hist[i], (unsigned long long)h[i]);
+}
+}  // namespace
+}  // namespace fsg
+
+extern "C" int fsg_key_histogram(const float* values_dev, int64_t n, int32_t abs_values, uint32_t prefix,
+                                 uint32_t mask, int32_t shift, int32_t bits, uint64_t* hist_out, void* stream) {
+  if ((n > 0 && !values_dev) || !hist_out) return fail(FSG_ERR_INVALID, "null argument");
+  if (bits < 1 || bits > 11 || shift < 0 || shift + bits > 32)
+    return fail(FSG_ERR_INVALID, "bits %d / shift %d outside the 11-bit radix passes", bits, shift);
+  cudaStream_t s = (cudaStream_t)stream;
+  DeviceInfo di;
+  int st = device_info(&di);
+  if (st) return st;
+  const size_t nb = (size_t)1 << bits;
+  StreamScratch scratch;
+  st = scratch.alloc(nb * sizeof(unsigned long long), s);
+  if (st) return st;
+  unsigned long long* h = static_cast<unsigned long long*>(scratch.ptr);
+  FSG_CUDA(cudaMemsetAsync(h, 0, nb * sizeof(unsigned long long), s));
+  if (n > 0) {
+    const int grid = (int)std::max<long long>(1, std::min<long long>((n + NT - 1) / NT, (long long)di.sms * 8));
+    key_hist<<<grid, NT, 0, s>>>(values_dev, n, abs_values, prefix, mask, shift, bits, h);
+    FSG_LAUNCHED(1);
+  }
+  FSG_CUDA(cudaMemcpyAsync(hist_out, h, nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  FSG_CUDA(cudaStreamSynchronize(s));
   return FSG_OK;
 }
 

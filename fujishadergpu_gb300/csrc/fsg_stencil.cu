@@ -622,7 +622,7 @@ __device__ __forceinline__ bool nan2(f2 a) { return (a.x != a.x) | (a.y != a.y);
 // div_by on both components (Markstein's correction, as div_by)
 __device__ __forceinline__ f2 div_by2(f2 a, float d, float r) {
   const f2 q = mul2(a, S2(r));
-  const f2 e = fma2(P2(-q.x, -q.y), S2(d), a);
+  const f2 e = fma2(q, S2(-d), a);  // q * -d == -(q * d) exactly
   return fma2(e, S2(r), q);
 }
 __device__ __forceinline__ f2 gamma_display2(f2 k) {
@@ -743,15 +743,22 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
   const float qnan = __int_as_float(0x7fc00000);
   for (int u = warp; u < A.total_units; u += nwarps) {
     const UnitGeom g = unit_geom(A, u);
-    const FastTile& T = A.tiles[g.t];
+    const FastTile& TG = A.tiles[g.t];
     const int x0 = g.x0, y0 = g.y0, y1 = g.y1, xo = g.xo;
     // stencil reach: rows y0-2 .. y1+1 and cols x0-2 .. x0+61 strictly inside
     // the window, so every derivative is a central difference
-    const bool interior = y0 - 2 >= T.wy0 && y1 + 2 <= T.wy1 && x0 - 2 >= T.wx0 && x0 + SW + 2 <= T.wx1;
+    const bool interior = y0 - 2 >= TG.wy0 && y1 + 2 <= TG.wy1 && x0 - 2 >= TG.wx0 && x0 + SW + 2 <= TG.wx1;
     if (!interior) {
       if (lane == 0) push_fix(A, u, true);
       continue;
     }
+    // the tile's constants as values: the plane stores below could alias the
+    // tile table as far as the compiler knows, which would force reloads
+    struct {
+      Axis g1x, g1y, c2x, c2y;
+      float sx, sy;
+      int oy0, ox0, cy0, cx0;
+    } const T = {TG.g1x, TG.g1y, TG.c2x, TG.c2y, TG.sx, TG.sy, TG.oy0, TG.ox0, TG.cy0, TG.cx0};
     const int x = x0 - 2 + 2 * lane;  // first column of this lane's pair
     const bool out0 = lane >= 1 && lane <= SW / 2 && x < xo, out1 = out0 && x + 1 < xo;
     // 8-byte copies need an 8-byte aligned pair start (uniform per unit)

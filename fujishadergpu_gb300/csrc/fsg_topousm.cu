@@ -66,7 +66,8 @@ __global__ void __launch_bounds__(NT) box_cols(Src src, int r, int chunk, int na
 // Gaussian column pass (mode 'nearest'): weights g[0..R] (g[0] centre).
 template <class Src>
 __global__ void __launch_bounds__(NT) gauss_cols(Src src, const float* __restrict__ g, int R, int nan_aware,
-                                                 AView vm, AView wm) {
+                                                 AView vm, AView wm, const int* run_if) {
+  if (run_if && *run_if == 0) return;  // nothing to do (e.g. a void fill without voids)
   const int x = blockIdx.x * NT + threadIdx.x;
   if (x >= src.w) return;
   for (int y = blockIdx.y; y < src.h; y += gridDim.y) {
@@ -103,11 +104,13 @@ struct RowArgs {
   float weight;
   int first;
   int th, tw;          // tile of outputs per block (th * tw == NT * SEG)
+  const int* run_if;   // nullable: skip the pass when *run_if == 0
 };
 
 constexpr int SEG = 8;
 
 __global__ void __launch_bounds__(NT) row_pass(const __grid_constant__ RowArgs A) {
+  if (A.run_if && *A.run_if == 0) return;
   extern __shared__ float sm[];
   const int w = A.vm.w, h = A.vm.h;
   const int r = A.r;
@@ -361,6 +364,306 @@ __global__ void overview_kernel(ZView z, AView out) {
   out.ref(i, j) = cnt ? (float)(tot / (double)cnt) : kQNaN;
 }
 
+// ------------------------------------------------ fused full-resolution pass
+// All full-resolution box radii (downsample factor 1, r >= 2) of a tile in one
+// pass, then the rest of the output in the reference's order.  A CTA owns a
+// strip of TW = 256 - 2R output columns (R = largest such radius) and a chunk
+// of rows.  Each thread keeps one buffer column's running vertical sums
+// (compensated, per radius; 'reflect' rows) in registers and writes that
+// column's vertical means (the float32 intermediate of uniform_filter's first
+// axis) for G rows into shared memory; the horizontal means are running sums
+// over SEG-column segments of those rows (the buffer already holds the
+// reflected columns).  The epilogue adds the decimated radii (bilinear zoom of
+// their coarse means, as accum_upsample), the large-radius field, the scale and
+// the encoding, and stores each output pixel once.
+constexpr int ST_NT = 256, ST_G = 8, ST_SEG = 8, ST_MAXR = 64, ST_MAXN = 6, ST_MAXD = 4;
+// shared-memory row of ST_NT buffer columns; column c lives at c + c / 8 so
+// that threads walking 8-column segments hit distinct banks
+constexpr int ST_ROW = ST_NT + ST_NT / 8;
+__device__ __forceinline__ int sidx(int c) { return c + (c >> 3); }
+
+struct DecK {       // one decimated radius of a tile
+  const float* ms;  // its coarse mean (ROW_MEAN output), row pitch w
+  int h, w;
+  double zy, zx;    // corner-aligned zoom factors (in - 1) / (out - 1)
+  float weight;
+};
+
+struct TopoTileK {
+  ZView z;                 // the window
+  int cy0, cx0, ch, cw;    // core, window coordinates
+  int gy0, gx0;            // global coordinates of the window origin
+  char* out;               // output plane at the core origin
+  const int* nan_flag;     // NoData anywhere in the window
+  DecK dec[ST_MAXD];
+  int ndec;
+};
+
+struct StripItem {
+  int tile, x0, y0, y1;    // output columns [x0, x0 + TW) (window), rows [y0, y1)
+};
+
+struct StripArgs {
+  const TopoTileK* tiles;
+  const StripItem* items;
+  int nitems;
+  int nr, R, TW;
+  int radii[ST_MAXN];
+  float weights[ST_MAXN];
+  float fn[ST_MAXN], rn[ST_MAXN];  // box size 2r+1 and RN(1/(2r+1))
+  const float* field;      // large-radius field (nullable)
+  long long fld;
+  int fh, fw;
+  float sy, sx, w_large, scale;
+  long long old;
+  int dtype;
+  float qa, qb;
+  int qmin, qmax;
+  int have_small;
+};
+
+__device__ __forceinline__ float field_at(const StripArgs& A, int gy, int gx) {
+  // _nan_utils.py:276-281: coords in float32, map_coordinates order 1, 'nearest' (as field_sample).
+  float cy = __fsub_rn(__fmul_rn(__fadd_rn((float)gy, 0.5f), A.sy), 0.5f);
+  float cx = __fsub_rn(__fmul_rn(__fadd_rn((float)gx, 0.5f), A.sx), 0.5f);
+  float fy0 = floorf(cy), fx0 = floorf(cx);
+  float ty = cy - fy0, tx = cx - fx0;
+  int y0 = clamp_idx((int)fy0, A.fh), y1 = clamp_idx((int)fy0 + 1, A.fh);
+  int x0 = clamp_idx((int)fx0, A.fw), x1 = clamp_idx((int)fx0 + 1, A.fw);
+  const float* F = A.field;
+  float a = __ldg(F + y0 * A.fld + x0), b = __ldg(F + y0 * A.fld + x1);
+  float c = __ldg(F + y1 * A.fld + x0), d = __ldg(F + y1 * A.fld + x1);
+  float top = fmaf(tx, b - a, a);
+  float bot = fmaf(tx, d - c, c);
+  return fmaf(ty, bot - top, top);
+}
+
+
+
+// Shared memory of the strip kernel (floats):
+//   V  [G][nr][2][ST_ROW]  vertical means (values, valid fraction), padded columns
+//   M  [G][nr][TW + TW/16 + 1] horizontal means per radius, padded columns
+//   DY [ST_MAXD][G] (int y0, int y1, float fy)   decimated-grid row coordinates of the G rows
+//   DX [ST_MAXD][TW] (int x0, int x1, float fx)  decimated-grid column coordinates of the strip
+struct StripSmem {
+  static size_t floats(int nr, int TW) {
+    return (size_t)ST_G * nr * 2 * ST_ROW + (size_t)ST_G * nr * (TW + TW / 16 + 1) + 3 * (size_t)ST_MAXD * ST_G +
+           3 * (size_t)ST_MAXD * TW;
+  }
+};
+
+constexpr int ST_HSEG = 16;  // columns per horizontal running-sum segment
+// horizontal-mean row: column j at j + j / 16 (segment walks hit distinct banks)
+__device__ __forceinline__ int midx(int j) { return j + (j >> 4); }
+
+template <int NR>
+__global__ void __launch_bounds__(ST_NT) topousm_strip(const __grid_constant__ StripArgs A) {
+  extern __shared__ float smem[];
+  constexpr int nr = NR;
+  const int TW = A.TW;
+  const int MROW = TW + TW / ST_HSEG + 1;
+  float* V = smem;
+  float* M = V + (size_t)ST_G * nr * 2 * ST_ROW;
+  int* DYi = reinterpret_cast<int*>(M + (size_t)ST_G * nr * MROW);  // [ST_MAXD][G][2]
+  float* DYf = reinterpret_cast<float*>(DYi + 2 * ST_MAXD * ST_G);  // [ST_MAXD][G]
+  int* DXi = reinterpret_cast<int*>(DYf + ST_MAXD * ST_G);          // [ST_MAXD][TW][2]
+  float* DXf = reinterpret_cast<float*>(DXi + 2 * ST_MAXD * TW);    // [ST_MAXD][TW]
+  const int b = threadIdx.x;  // buffer column of the vertical pass
+  // the item's tile descriptor, staged in shared memory: the output stores
+  // could alias a global copy as far as the compiler knows
+  __shared__ TopoTileK Ts;
+  const TopoTileK& T = Ts;
+  for (int it = blockIdx.x; it < A.nitems; it += gridDim.x) {
+    const StripItem I = A.items[it];
+    __syncthreads();
+    for (int k = threadIdx.x; k < (int)(sizeof(TopoTileK) / 4); k += ST_NT)
+      reinterpret_cast<int*>(&Ts)[k] = reinterpret_cast<const int*>(A.tiles + I.tile)[k];
+    __syncthreads();
+    const bool nanw = *T.nan_flag != 0;
+    const ZView& z = T.z;
+    const int xc = reflect_idx(I.x0 - A.R + b, z.w);  // window column of this buffer column
+    const int xend = min(I.x0 + TW, T.cx0 + T.cw);     // end of the strip's outputs
+    // every row the vertical sums enter or leave lies inside the window
+    const bool rows_inside = I.y0 - A.R >= 0 && I.y1 + A.R < z.h;
+    // decimated-grid column coordinates of the strip (accum_upsample's zoom)
+    for (int d = 0; d < T.ndec; ++d)
+      for (int j = threadIdx.x; j < TW; j += ST_NT) {
+        const DecK& D = T.dec[d];
+        const double c = (double)(I.x0 + j) * D.zx;
+        const int sx = (int)floor(c);
+        DXi[(d * TW + j) * 2] = clamp_idx(sx, D.w);
+        DXi[(d * TW + j) * 2 + 1] = clamp_idx(sx + 1, D.w);
+        DXf[d * TW + j] = (float)(c - (double)sx);
+      }
+    CSum vs[NR > 0 ? NR : 1];
+    int vc[NR > 0 ? NR : 1];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      vc[q] = 0;
+      const int r = A.radii[q];
+      for (int k = -r; k <= r; ++k) {
+        const float v = z.at(reflect_idx(I.y0 + k, z.h), xc);
+        const bool ok = v == v;
+        vs[q].add(ok ? v : 0.f);
+        vc[q] += ok;
+      }
+    }
+    for (int yg = I.y0; yg < I.y1; yg += ST_G) {
+      const int gn = min(ST_G, I.y1 - yg);
+      // (1) vertical means of the group's rows, then slide the sums; the rows
+      //     entering and leaving the windows are loaded for the whole group first
+      if (NR > 0) {
+        float za[ST_G][NR > 0 ? NR : 1], zc[ST_G][NR > 0 ? NR : 1];
+        if (rows_inside) {  // no reflection anywhere in this chunk (uniform branch)
+          const float* col = z.p + xc;
+#pragma unroll
+          for (int i = 0; i < ST_G; ++i)
+#pragma unroll
+            for (int q = 0; q < NR; ++q) {
+              const int r = A.radii[q];
+              const int y = min(yg + i, I.y1 - 1);
+              float a = __ldg(col + (long long)(y + r + 1) * z.ld), c = __ldg(col + (long long)(y - r) * z.ld);
+              if (z.has_nodata) {
+                if (is_nodata(a, z.ndf, true)) a = kQNaN;
+                if (is_nodata(c, z.ndf, true)) c = kQNaN;
+              }
+              za[i][q] = a;
+              zc[i][q] = c;
+            }
+        } else {
+#pragma unroll
+          for (int i = 0; i < ST_G; ++i)
+#pragma unroll
+            for (int q = 0; q < NR; ++q) {
+              const int r = A.radii[q];
+              const int y = min(yg + i, I.y1 - 1);
+              za[i][q] = z.at(reflect_idx(y + r + 1, z.h), xc);
+              zc[i][q] = z.at(reflect_idx(y - r, z.h), xc);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < ST_G; ++i) {
+          if (i >= gn) break;
+#pragma unroll
+          for (int q = 0; q < NR; ++q) {
+            float* vrow = V + ((i * nr + q) * 2) * ST_ROW;
+            vrow[sidx(b)] = div_by(vs[q].value(), A.fn[q], A.rn[q]);
+            if (nanw) vrow[ST_ROW + sidx(b)] = div_by((float)vc[q], A.fn[q], A.rn[q]);
+            const float a = za[i][q], c = zc[i][q];
+            const bool oa = a == a, oc = c == c;
+            vs[q].add(oa ? a : 0.f);
+            vs[q].add(oc ? -c : -0.f);
+            vc[q] += (int)oa - (int)oc;
+          }
+        }
+      }
+      if (threadIdx.x < T.ndec * ST_G) {  // decimated-grid row coordinates of the group
+        const int d = threadIdx.x / ST_G, i = threadIdx.x - (threadIdx.x / ST_G) * ST_G;
+        const DecK& D = T.dec[d];
+        const double c = (double)(yg + i) * D.zy;
+        const int sy = (int)floor(c);
+        DYi[(d * ST_G + i) * 2] = clamp_idx(sy, D.h);
+        DYi[(d * ST_G + i) * 2 + 1] = clamp_idx(sy + 1, D.h);
+        DYf[d * ST_G + i] = (float)(c - (double)sy);
+      }
+      __syncthreads();
+      // (2) horizontal means: task = (row, radius, 16-column segment)
+      const int nseg = (TW + ST_HSEG - 1) / ST_HSEG;
+      // radius slowest, so that a warp's tasks share r (the initial sum's trip count)
+      for (int task = threadIdx.x; task < gn * nr * nseg; task += ST_NT) {
+        const int sg = task % nseg;
+        const int iq = task / nseg;
+        const int i = iq % gn, q = iq / gn;
+        const int r = A.radii[q];
+        const float fn = A.fn[q], rn = A.rn[q];
+        const float* vv = V + ((i * nr + q) * 2) * ST_ROW;
+        const float* vw = vv + ST_ROW;
+        float* mrow = M + (i * nr + q) * MROW;
+        const int c0 = A.R + sg * ST_HSEG;
+        CSum hv, hw;
+        for (int k = c0 - r; k <= c0 + r; ++k) {
+          hv.add(vv[sidx(k)]);
+          if (nanw) hw.add(vw[sidx(k)]);
+        }
+        const int jn = min(ST_HSEG, TW - sg * ST_HSEG);
+        for (int j = 0; j < jn; ++j) {
+          const float num = div_by(hv.value(), fn, rn);
+          float mean = num;
+          if (nanw) {
+            const float den = div_by(hw.value(), fn, rn);
+            mean = den > 0.f ? __fdiv_rn(num, den) : 0.f;
+          }
+          mrow[midx(sg * ST_HSEG + j)] = mean;
+          if (j + 1 < jn) {
+            hv.add(vv[sidx(c0 + j + r + 1)]);
+            hv.add(-vv[sidx(c0 + j - r)]);
+            if (nanw) {
+              hw.add(vw[sidx(c0 + j + r + 1)]);
+              hw.add(-vw[sidx(c0 + j - r)]);
+            }
+          }
+        }
+      }
+      __syncthreads();
+      // (3) per pixel: radii in order, decimated radii, large field, scale, encoding
+      for (int p = threadIdx.x; p < gn * TW; p += ST_NT) {
+        const int i = p / TW, j = p - (p / TW) * TW;
+        const int y = yg + i, x = I.x0 + j;
+        if (x >= xend) continue;
+        const float zv = z.at(y, x);
+        float a = 0.f;
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+          const float d = __fmul_rn(A.weights[q], __fsub_rn(zv, M[(i * nr + q) * MROW + midx(j)]));
+          a = q == 0 ? d : __fadd_rn(a, d);
+        }
+        for (int dd = 0; dd < T.ndec; ++dd) {
+          const DecK& D = T.dec[dd];
+          const int y0 = DYi[(dd * ST_G + i) * 2], y1 = DYi[(dd * ST_G + i) * 2 + 1];
+          const int x0 = DXi[(dd * TW + j) * 2], x1 = DXi[(dd * TW + j) * 2 + 1];
+          const float fy = DYf[dd * ST_G + i], fx = DXf[dd * TW + j];
+          const float* m = D.ms;
+          const float ma = __ldg(m + (long long)y0 * D.w + x0), mb = __ldg(m + (long long)y0 * D.w + x1);
+          const float mc = __ldg(m + (long long)y1 * D.w + x0), md = __ldg(m + (long long)y1 * D.w + x1);
+          const float top = fmaf(fx, mb - ma, ma), bot = fmaf(fx, md - mc, mc);
+          const float mean = fmaf(fy, bot - top, top);
+          const float t = __fmul_rn(D.weight, __fsub_rn(zv, mean));
+          a = (nr == 0 && dd == 0) ? t : __fadd_rn(a, t);
+        }
+        float v;
+        if (zv != zv) {
+          v = kQNaN;
+        } else {
+          const bool have_large = A.field != nullptr;
+          float large = 0.f;
+          if (have_large) large = __fsub_rn(__fmul_rn(A.w_large, zv), field_at(A, T.gy0 + y, T.gx0 + x));
+          if (A.have_small) v = have_large ? __fadd_rn(a, large) : a;
+          else v = large;
+          if (A.scale > 0.f) v = __fdiv_rn(v, A.scale);
+        }
+        const long long off = (long long)(y - T.cy0) * A.old + (x - T.cx0);
+        if (A.dtype == FSG_F32) reinterpret_cast<float*>(T.out)[off] = v;
+        else if (A.dtype == FSG_U8) reinterpret_cast<uint8_t*>(T.out)[off] = (uint8_t)(int)quantize(v, A.qa, A.qb, A.qmin, A.qmax);
+        else reinterpret_cast<int16_t*>(T.out)[off] = (int16_t)(int)quantize(v, A.qa, A.qb, A.qmin, A.qmax);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// flag[t] = any NoData in window t (ZView per tile); blockIdx.y = tile.
+__global__ void window_nan_flags(const TopoTileK* tiles, int* flags) {
+  const TopoTileK& T = tiles[blockIdx.y];
+  const ZView& z = T.z;
+  bool n = false;
+  for (int y = blockIdx.x; y < z.h; y += gridDim.x)
+    for (int x = threadIdx.x; x < z.w; x += blockDim.x) {
+      const float v = z.at(y, x);
+      n |= v != v;
+    }
+  if (__syncthreads_or(n) && threadIdx.x == 0) atomicOr(flags + blockIdx.y, 1);
+}
+
 // ------------------------------------------------------------------- host
 struct Grid2 {
   dim3 g, b;
@@ -420,7 +723,7 @@ static void row_geometry(int r, int nan_aware, int w, int* th, int* tw, size_t* 
 
 template <class Src>
 static int launch_box(const Src& src, int r, int nan_aware, AView vm, AView wm, RowArgs ra, cudaStream_t s) {
-  int chunk = std::max(64, 2 * r);
+  const int chunk = 128;  // rows per block: (2r+1)/128 extra adds per row buys enough blocks for large r
   dim3 g((src.w + NT - 1) / NT, (src.h + chunk - 1) / chunk);
   box_cols<Src><<<g, NT, 0, s>>>(src, r, chunk, nan_aware, vm, wm);
   FSG_LAUNCHED(1);
@@ -446,7 +749,7 @@ template <class Src>
 static int launch_gauss(const Src& src, const float* g, int R, int nan_aware, AView vm, AView wm, RowArgs ra,
                         cudaStream_t s) {
   dim3 gg((src.w + NT - 1) / NT, std::min(src.h, 65535));
-  gauss_cols<Src><<<gg, NT, 0, s>>>(src, g, R, nan_aware, vm, wm);
+  gauss_cols<Src><<<gg, NT, 0, s>>>(src, g, R, nan_aware, vm, wm, ra.run_if);
   FSG_LAUNCHED(1);
   ra.vm = vm;
   ra.wm = wm;
@@ -556,6 +859,7 @@ static int topousm_window(const ZView& z, const std::vector<int>& radii, const s
         ra.mode = ROW_PAIR;
         ra.out = resize(S.ssv, hs, ws);
         ra.out2 = resize(S.ssw, hs, ws);
+        ra.run_if = S.flag;
         st = launch_gauss(small, S.gv, R, 1, resize(S.svm, hs, ws), resize(S.swm, hs, ws), ra, s);
         if (st) return st;
         voidfill_combine<<<gd.g, gd.b, 0, s>>>(small, resize(S.ssv, hs, ws), resize(S.ssw, hs, ws), S.flag);
@@ -591,6 +895,199 @@ int prepare_g1(TopoScratch& S, cudaStream_t s) {
   return upload(S.g1, g, s);
 }
 
+// The fused strip path applies when the radii ascend, the factor-1 radii come
+// first (each 2..ST_MAXR, at most ST_MAXN of them) and at most ST_MAXD radii
+// are decimated.
+static bool strip_path_ok(const std::vector<int>& radii, double pixel_size, int* nfull) {
+  int nf = 0, nd = 0;
+  for (size_t i = 0; i < radii.size(); ++i) {
+    if (i > 0 && radii[i] < radii[i - 1]) return false;
+    if (topousm_downsample_factor((double)radii[i], pixel_size) == 1) {
+      if (nd > 0 || radii[i] < 2 || radii[i] > ST_MAXR) return false;
+      ++nf;
+    } else {
+      ++nd;
+    }
+  }
+  if (nf > ST_MAXN || nd > ST_MAXD) return false;
+  *nfull = nf;
+  return true;
+}
+
+// Coarse mean of one decimated radius of a window (the f > 1 branch of
+// topousm_window up to, not including, the zoom), into `ms` (hs x ws).
+static int decimated_mean(const ZView& z, int r, int f, TopoScratch& S, float* ms, cudaStream_t s) {
+  const int hs = std::max(1, (z.h + f - 1) / f), ws = std::max(1, (z.w + f - 1) / f);
+  AView small = resize(S.small, hs, ws);
+  FSG_CUDA(cudaMemsetAsync(S.flag, 0, sizeof(int), s));
+  Grid2 gd = grid2d(hs, ws);
+  downsample_kernel<<<gd.g, gd.b, 0, s>>>(z, f, small, S.flag);
+  FSG_LAUNCHED(1);
+  double sigma = std::max(1.0, (double)std::min(hs, ws) / 64.0);
+  int R;
+  std::vector<float> gw = gaussian_weights(sigma, &R);
+  if (R + 1 > 4096) return fail(FSG_ERR_UNSUPPORTED, "void-fill Gaussian radius %d too large", R);
+  int st = upload(S.gv, gw, s);
+  if (st) return st;
+  RowArgs ra;
+  std::memset(&ra, 0, sizeof(ra));
+  ra.mode = ROW_PAIR;
+  ra.out = resize(S.ssv, hs, ws);
+  ra.out2 = resize(S.ssw, hs, ws);
+  ra.run_if = S.flag;
+  st = launch_gauss(small, S.gv, R, 1, resize(S.svm, hs, ws), resize(S.swm, hs, ws), ra, s);
+  if (st) return st;
+  voidfill_combine<<<gd.g, gd.b, 0, s>>>(small, resize(S.ssv, hs, ws), resize(S.ssw, hs, ws), S.flag);
+  FSG_LAUNCHED(1);
+  const int rs = std::max(1, (int)std::nearbyint((double)r / f));
+  AView out{ms, ws, hs, ws};
+  return mean_for_radius(small, rs, S, out, s);
+}
+
+static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_tile* tiles, int32_t ntiles,
+                              const fsg_topousm_params* p, const fsg_plane* out, int nfull, cudaStream_t s) {
+  const std::vector<int> radii(p->radii, p->radii + p->nradii);
+  int maxh = 1, maxw = 1;
+  for (int t = 0; t < ntiles; ++t) {
+    maxh = std::max(maxh, tiles[t].win_h);
+    maxw = std::max(maxw, tiles[t].win_w);
+  }
+  std::vector<int> dec_idx;
+  for (int i = nfull; i < p->nradii; ++i) dec_idx.push_back(i);
+  // scratch: decimation pipeline (one window at a time) + per-tile coarse means + tables
+  size_t dec_bytes = 0;
+  std::vector<size_t> dec_off((size_t)ntiles * dec_idx.size());
+  for (int t = 0; t < ntiles; ++t)
+    for (size_t d = 0; d < dec_idx.size(); ++d) {
+      const int f = topousm_downsample_factor((double)radii[dec_idx[d]], p->pixel_size);
+      const size_t n = (size_t)std::max(1, (tiles[t].win_h + f - 1) / f) * std::max(1, (tiles[t].win_w + f - 1) / f);
+      dec_off[(size_t)t * dec_idx.size() + d] = dec_bytes;
+      dec_bytes += (n * sizeof(float) + 255) & ~(size_t)255;
+    }
+  int R = 0;
+  for (int i = 0; i < nfull; ++i) R = std::max(R, radii[i]);
+  const int TW = ((ST_NT - 2 * R) / ST_SEG) * ST_SEG;
+  constexpr int CHUNK = 512;
+  std::vector<StripItem> items;
+  for (int t = 0; t < ntiles; ++t) {
+    const fsg_tile& T = tiles[t];
+    if (T.core_h == 0 || T.core_w == 0) continue;
+    const int cy0 = T.core_y0 - T.win_y0, cx0 = T.core_x0 - T.win_x0;
+    for (int x = cx0; x < cx0 + T.core_w; x += TW)
+      for (int y = cy0; y < cy0 + T.core_h; y += CHUNK) items.push_back({t, x, y, std::min(y + CHUNK, cy0 + T.core_h)});
+  }
+  if (items.empty()) return FSG_OK;
+  const size_t topo_bytes = dec_idx.empty() ? 0 : TopoScratch::bytes(maxh, maxw);
+  const size_t tiles_off = (topo_bytes + dec_bytes + 255) & ~(size_t)255;
+  const size_t items_off = tiles_off + ((sizeof(TopoTileK) * ntiles + 255) & ~(size_t)255);
+  const size_t flags_off = items_off + ((sizeof(StripItem) * items.size() + 255) & ~(size_t)255);
+  const size_t total = flags_off + sizeof(int) * ntiles + 256;
+  StreamScratch scratch;
+  int st = scratch.alloc(total, s);
+  if (st) return st;
+  char* base = static_cast<char*>(scratch.ptr);
+  TopoScratch S;
+  if (!dec_idx.empty()) {
+    S.carve(base, maxh, maxw);
+    st = prepare_g1(S, s);
+    if (st) return st;
+  }
+  float* dec_base = reinterpret_cast<float*>(base + topo_bytes);
+  TopoTileK* tiles_dev = reinterpret_cast<TopoTileK*>(base + tiles_off);
+  StripItem* items_dev = reinterpret_cast<StripItem*>(base + items_off);
+  int* flags = reinterpret_cast<int*>(base + flags_off);
+  const size_t esz = out->dtype == FSG_F32 ? 4 : (out->dtype == FSG_I16 ? 2 : 1);
+  std::vector<TopoTileK> tk(ntiles);
+  for (int t = 0; t < ntiles; ++t) {
+    const fsg_tile& T = tiles[t];
+    TopoTileK& k = tk[t];
+    std::memset(&k, 0, sizeof(k));
+    k.z = ZView{raster_dev + (long long)T.win_y0 * ld + T.win_x0, ld, T.win_h, T.win_w, (float)p->nodata,
+                p->has_nodata != 0};
+    k.cy0 = T.core_y0 - T.win_y0;
+    k.cx0 = T.core_x0 - T.win_x0;
+    k.ch = T.core_h;
+    k.cw = T.core_w;
+    k.gy0 = T.win_y0;
+    k.gx0 = T.win_x0;
+    k.out = static_cast<char*>(out->ptr) + ((long long)T.out_y0 * out->ld + T.out_x0) * esz;
+    k.nan_flag = flags + t;
+    k.ndec = (int)dec_idx.size();
+    for (size_t d = 0; d < dec_idx.size(); ++d) {
+      const int r = radii[dec_idx[d]];
+      const int f = topousm_downsample_factor((double)r, p->pixel_size);
+      const int hs = std::max(1, (T.win_h + f - 1) / f), ws = std::max(1, (T.win_w + f - 1) / f);
+      float* ms = reinterpret_cast<float*>(reinterpret_cast<char*>(dec_base) + dec_off[(size_t)t * dec_idx.size() + d]);
+      if (T.core_h > 0 && T.core_w > 0) {
+        st = decimated_mean(k.z, r, f, S, ms, s);
+        if (st) return st;
+      }
+      k.dec[d].ms = ms;
+      k.dec[d].h = hs;
+      k.dec[d].w = ws;
+      k.dec[d].zy = T.win_h > 1 ? (double)(hs - 1) / (double)(T.win_h - 1) : 1.0;
+      k.dec[d].zx = T.win_w > 1 ? (double)(ws - 1) / (double)(T.win_w - 1) : 1.0;
+      k.dec[d].weight = (float)p->weights[dec_idx[d]];
+    }
+  }
+  FSG_CUDA(cudaMemcpyAsync(tiles_dev, tk.data(), sizeof(TopoTileK) * ntiles, cudaMemcpyHostToDevice, s));
+  FSG_CUDA(cudaMemcpyAsync(items_dev, items.data(), sizeof(StripItem) * items.size(), cudaMemcpyHostToDevice, s));
+  FSG_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * ntiles, s));
+  window_nan_flags<<<dim3(256, ntiles), 256, 0, s>>>(tiles_dev, flags);
+  FSG_LAUNCHED(1);
+  StripArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.tiles = tiles_dev;
+  A.items = items_dev;
+  A.nitems = (int)items.size();
+  A.nr = nfull;
+  A.R = R;
+  A.TW = TW;
+  for (int i = 0; i < nfull; ++i) {
+    A.radii[i] = radii[i];
+    A.weights[i] = (float)p->weights[i];
+    A.fn[i] = (float)(2 * radii[i] + 1);
+    A.rn[i] = 1.0f / A.fn[i];
+  }
+  A.field = p->coarse_dev;
+  A.fld = p->coarse_ld;
+  A.fh = p->coarse_h;
+  A.fw = p->coarse_w;
+  A.sy = p->coarse_dev ? (float)((double)p->coarse_h / (double)p->full_h) : 0.f;
+  A.sx = p->coarse_dev ? (float)((double)p->coarse_w / (double)p->full_w) : 0.f;
+  A.w_large = (float)p->w_large;
+  A.scale = (float)p->scale;
+  A.old = out->ld;
+  A.dtype = out->dtype;
+  A.qa = out->q_a;
+  A.qb = out->q_b;
+  A.qmin = out->q_min;
+  A.qmax = out->q_max;
+  A.have_small = p->nradii > 0;
+  const size_t smem = StripSmem::floats(std::max(1, nfull), TW) * sizeof(float);
+  void (*kern)(StripArgs) = nullptr;
+  switch (nfull) {
+    case 0: kern = topousm_strip<0>; break;
+    case 1: kern = topousm_strip<1>; break;
+    case 2: kern = topousm_strip<2>; break;
+    case 3: kern = topousm_strip<3>; break;
+    case 4: kern = topousm_strip<4>; break;
+    case 5: kern = topousm_strip<5>; break;
+    default: kern = topousm_strip<6>; break;
+  }
+  if (smem > 48 * 1024) FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  DeviceInfo di;
+  st = device_info(&di);
+  if (st) return st;
+  int per_sm = 0;
+  FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ST_NT, smem));
+  const int grid = std::min((int)items.size(), di.sms * std::max(1, per_sm));
+  kern<<<grid, ST_NT, smem, s>>>(A);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+
 }  // namespace fsg
 
 using namespace fsg;
@@ -613,6 +1110,11 @@ extern "C" int fsg_topousm(const float* raster_dev, int64_t ld, int32_t raster_h
   int st = validate_tiles(raster_h, raster_w, tiles, ntiles, 1);
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
+  {
+    const std::vector<int> rv(p->radii, p->radii + p->nradii);
+    int nfull = 0;
+    if (strip_path_ok(rv, p->pixel_size, &nfull)) return topousm_strip_path(raster_dev, ld, tiles, ntiles, p, out, nfull, s);
+  }
   int maxh = 1, maxw = 1;
   for (int t = 0; t < ntiles; ++t) {
     maxh = std::max(maxh, tiles[t].win_h);

@@ -194,6 +194,18 @@ int fsg_topousm_downsample_factor(double radius, double pixel_size);
 int fsg_percentile(const float* values_dev, int64_t n, int32_t abs_values, const double* q, int32_t nq,
                    double* out, int64_t* nvalid, void* stream);
 
+/* One pass of the radix select behind fsg_percentile, for statistics merged
+ * across devices (a raster sharded over GPUs): the histogram of the
+ * order-preserving uint32 keys of the valid float32 values (|v| when
+ * abs_values != 0) whose bits under `mask` equal `prefix`, binned by
+ * (key >> shift) & (2^bits - 1), bits <= 11.  Writes 2^bits counts to host
+ * `hist_out`; synchronises `stream`.  Summing the histograms of all shards
+ * and picking bins identically on every rank selects the exact order
+ * statistics of the union (no counterpart in the reference, which runs the
+ * statistics on one device). */
+int fsg_key_histogram(const float* values_dev, int64_t n, int32_t abs_values, uint32_t prefix, uint32_t mask,
+                      int32_t shift, int32_t bits, uint64_t* hist_out, void* stream);
+
 /* Population standard deviation of the valid (non-NaN) values, FP64
  * (the fallback scale of _normalization.py:30).  Synchronises `stream`. */
 int fsg_std(const float* values_dev, int64_t n, double* out, void* stream);
@@ -304,6 +316,35 @@ int fsg_sample_coarse_accumulate(const float* coarse_dev, int64_t cld, int32_t c
 int fsg_masked_store(const float* acc, int64_t acc_ld, const float* raster_dev, int64_t ld, int32_t raster_h,
                      int32_t raster_w, int32_t gy0, int32_t gx0, int32_t h, int32_t w, double nodata,
                      int32_t has_nodata, const fsg_plane* out, void* stream);
+
+/* ------------------------------------------------------ openness surrogate */
+/* Kernels of the convolutional openness surrogate (no counterpart in the
+ * reference, which runs the exact ray-march only).  Feature maps are float32
+ * [batch][h][w][channels], channels fastest; w a multiple of 16.  Weights of a
+ * 3x3 layer are float32 w[9][cin][32] (tap = 3*ky + kx), packed once into a
+ * BF16 table of 9 * cin_pad/16 * 256 uint32 (cin_pad = 16 for cin <= 16, else
+ * 32); `transpose` packs the table of the data gradient (cin == 32). */
+int fsg_conv_pack_weights(const float* w_dev, int32_t cin, int32_t transpose, uint32_t* wb_dev, void* stream);
+
+/* y = relu?(conv3x3_dil(x) + bias) (+ res): implicit GEMM on the tensor cores
+ * (BF16 operands, FP32 accumulation).  flip mirrors the taps (with a transposed
+ * table: the data gradient).  bias and res may be NULL. */
+int fsg_conv3x3(const float* x_dev, int32_t cin_pad, int32_t batch, int32_t h, int32_t w, int32_t dil,
+                const uint32_t* wb_dev, const float* bias_dev, int32_t relu, int32_t flip, const float* res_dev,
+                float* y_dev, void* stream);
+
+/* dw[9][cin][32] += sum over pixels of x(p + tap*dil)[ci] * gz(p)[co] (atomic; zero dw first). */
+int fsg_conv3x3_wgrad(const float* x_dev, int32_t cin, int32_t cin_pad, int32_t batch, int32_t h, int32_t w,
+                      int32_t dil, const float* gz_dev, float* dw_dev, void* stream);
+
+/* 1x1 head over 32 channels: out[p] = sum_c h[p][c] w[c] + bias. */
+int fsg_head_forward(const float* h_dev, const float* w_dev, float bias, int64_t npix, float* out_dev,
+                     void* stream);
+
+/* Head gradients: gh = gout * w (+ gres); gw[c] += sum_p h[p][c] gout[p]; gb += sum_p gout[p]
+ * (gw, gb accumulated atomically; gres may be NULL). */
+int fsg_head_backward(const float* h_dev, const float* w_dev, const float* gout_dev, const float* gres_dev,
+                      int64_t npix, float* gh_dev, float* gw_dev, float* gb_dev, void* stream);
 
 #ifdef __cplusplus
 }

@@ -126,3 +126,20 @@ def test_tiled_openness_per_tile_pixel_scales(op):
         g = got[cy:cy + ch, cx:cx + cw]
         assert np.array_equal(np.isnan(g), np.isnan(ref))
         assert float(np.nanmax(np.abs(g.astype(np.float64) - ref))) <= 0.01
+
+
+@pytest.mark.parametrize("otype", ["positive", "negative"])
+def test_interior_fast_path_with_numeric_nodata(op, otype):
+    """A window much wider than the rays: most blocks take the interior path (no bounds
+    checks); NoData given as a numeric sentinel on both sides of the comparison."""
+    from fujishadergpu_gb300 import synth
+    dem = synth.fbm(400, 420, hurst=0.7, seed=87, lo=0.0, hi=800.0)
+    dem[synth.nodata_disks(400, 420, count=6, seed=88, rmin=3.0, rmax=12.0)] = -9999.0
+    kw = dict(openness_type=otype, num_directions=16, max_distance=16, pixel_size=5.0, pixel_scale_x=5.0,
+              pixel_scale_y=-5.0)
+    raw = to_np(op.compute_openness_raw_degrees(torch.from_numpy(dem).cuda(), nodata=-9999.0, **kw))
+    clean = np.where(R.nodata_mask(dem, -9999.0), np.nan, dem).astype(np.float32)
+    ref = R.openness(clean, openness_type=otype, num_directions=16, max_distance=16, pixel_size=5.0, psx=5.0,
+                     psy=-5.0, raw_degrees=True)
+    assert np.array_equal(np.isnan(raw), np.isnan(ref))
+    assert float(np.nanmax(np.abs(raw.astype(np.float64) - ref))) <= 0.01
