@@ -416,6 +416,53 @@ def openness_section(args):
     return {"workload": f"openness positive, 16 dirs, R=256, 5 m, {n}x{n} (reference sampling)", **res}
 
 
+def surrogate_section(args):
+    """Openness (positive, 16 dirs, R = 256, 5 m) on a 16384^2 fBm+ridged DEM three ways over the
+    same 4096^2 tiles (halo 288): exact reference sampling, exact dense ray-march, and the CNN
+    surrogate with its exact check block per tile (tiles over 2 degrees MAE redone exactly)."""
+    import torch
+    from fujishadergpu_gb300 import synth
+    from fujishadergpu_gb300.algorithms import _impl_openness as OP
+    from fujishadergpu_gb300.core import tile_loop
+    from fujishadergpu_gb300.surrogate import openness_cnn as S
+    n = args.openness_size
+    model = S.load_default()
+    if model is None:
+        return {"unavailable": "no trained surrogate weights (fujishadergpu_gb300/surrogate/openness_r256.npz)"}
+    dem = synth.fbm_ridged_device(n, n, hurst=0.7, seed_fbm=5, seed_ridged=6, lo=0.0, hi=3000.0)
+    pad = tile_loop.required_padding("openness", {"mode": "local", "max_distance": 256}, 10.0, 4096)
+    infos = tile_loop.tile_grid(n, n, 4096, pad)
+    tiles = tile_loop.make_tiles(infos, pixel_scale_x=5.0, pixel_scale_y=-5.0)
+    from fujishadergpu_gb300 import _arrays
+    v = _arrays.as_device_f32_2d(dem)
+    res = {"workload": f"openness positive, 16 dirs, R=256, 5 m, {n}x{n}, 4096^2 tiles, halo {pad}",
+           "params": model.n_params()}
+    exact = {}
+    for mode in ("reference", "dense"):
+        raw = torch.empty((n, n), device="cuda")
+        params = OP.make_params(max_distance=256, pixel_size=5.0, sampling=mode)
+        stream = torch.cuda.current_stream()
+        ms = _time_ms(lambda: OP.run_openness(v, tiles, params, None, raw, stream=int(stream.cuda_stream)), 1, 1,
+                      stream)
+        exact[mode] = raw
+        res[f"exact_{mode}"] = {"value": round(n * n / (ms * 1e-3) / 1e6, 1), "unit": "Mpix/s",
+                                "ms_per_step": round(ms, 2)}
+    stream = torch.cuda.current_stream()
+    out = {}
+    ms = _time_ms(lambda: out.update(S.surrogate_tile_loop(dem, infos, model, pixel_size=5.0)), 1, 1, stream)
+    plane = out["plane"]
+    d = (plane - exact["reference"]).abs()
+    mae = float(d[torch.isfinite(d)].mean().item())
+    res["surrogate"] = {"value": round(n * n / (ms * 1e-3) / 1e6, 1), "unit": "Mpix/s", "ms_per_step": round(ms, 2),
+                        "mae_vs_exact_reference_deg": round(mae, 3), "tiles": out["tiles"],
+                        "tiles_redone_exactly": out["exact_redone"],
+                        "check_block_mae_deg": out["check_mae_deg"],
+                        "speedup_vs_exact_dense": round(res["exact_dense"]["ms_per_step"] / ms, 2),
+                        "speedup_vs_exact_reference": round(res["exact_reference"]["ms_per_step"] / ms, 3)}
+    del dem, plane, exact
+    return res
+
+
 # --------------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -423,7 +470,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["stencil", "topousm", "openness"], default="stencil",
+    ap.add_argument("--workload", choices=["stencil", "topousm", "openness", "surrogate"], default="stencil",
                     help="stencil: the headline line; topousm / openness: that section alone (profiling)")
     ap.add_argument("--size", type=int, default=32768)
     ap.add_argument("--tile", type=int, default=4096)
@@ -441,7 +488,8 @@ def main():
 
     rank, world, _ = dist_setup(args.gpus)
     if args.workload != "stencil":
-        sec = topousm_section(args) if args.workload == "topousm" else openness_section(args)
+        sec = {"topousm": topousm_section, "openness": openness_section,
+               "surrogate": surrogate_section}[args.workload](args)
         if rank == 0:
             print(json.dumps({"section": args.workload, **sec}))
         return
@@ -452,6 +500,8 @@ def main():
         line["extra"] = {"topousm_fast": topousm_section(args)}
         torch.cuda.empty_cache()
         line["extra"]["openness"] = openness_section(args)
+        torch.cuda.empty_cache()
+        line["extra"]["openness_surrogate"] = surrogate_section(args)
     if rank == 0:
         if not args.no_cpu_baseline and world == 1:
             procs = max(1, os.cpu_count() or 1)
