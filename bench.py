@@ -416,6 +416,33 @@ def openness_section(args):
     return {"workload": f"openness positive, 16 dirs, R=256, 5 m, {n}x{n} (reference sampling)", **res}
 
 
+def spatial_section(args):
+    """Spatial (multi-radius) mode on an 8192^2 fBm+ridged DEM (5 m, 4096^2 tiles): hillshade,
+    slope and curvature with radii 2, 8, 32, 128 and openness with distances 4, 16, 64, 256
+    (decimated 1x, 1x, 2x, 8x), weights 0.4, 0.3, 0.2, 0.1.  One step = the whole tile loop:
+    per tile and radius the reflect-padded window, the smoothing / decimated ray-march, the
+    product, the weighted combination and the masked store."""
+    import torch
+    from fujishadergpu_gb300 import synth
+    from fujishadergpu_gb300.core import tile_loop
+    n = args.spatial_size
+    dem = synth.fbm_ridged_device(n, n, hurst=0.75, seed_fbm=7, seed_ridged=8, lo=0.0, hi=2500.0)
+    stream = torch.cuda.current_stream()
+    w = [0.4, 0.3, 0.2, 0.1]
+    res = {}
+    for algo, radii, extra in (("hillshade", [2, 8, 32, 128], {}), ("slope", [2, 8, 32, 128], {}),
+                               ("curvature", [2, 8, 32, 128], {"curvature_type": "profile"}),
+                               ("openness", [4, 16, 64, 256], {"global_stats": (0.5, 0.4)})):
+        kw = dict(tile_size=4096, pixel_size=5.0, pixel_scale_x=5.0, pixel_scale_y=-5.0, mode="spatial",
+                  radii=radii, weights=w, **extra)
+        ms = _time_ms(lambda: tile_loop.process_dem_array(dem, algo, **kw), max(1, args.extra_steps // 2), 1,
+                      stream)
+        res[algo] = {"radii": radii, "value": round(n * n / (ms * 1e-3) / 1e6, 1), "unit": "Mpix/s",
+                     "ms_per_step": round(ms, 3)}
+    del dem
+    return {"workload": f"spatial mode, {n}x{n} fBm+ridged, 5 m, 4096^2 tiles, weights {w}", **res}
+
+
 def surrogate_section(args):
     """Openness (positive, 16 dirs, R = 256, 5 m) on a 16384^2 fBm+ridged DEM three ways over the
     same 4096^2 tiles (halo 288): exact reference sampling, exact dense ray-march, and the CNN
@@ -470,7 +497,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["stencil", "topousm", "openness", "surrogate"], default="stencil",
+    ap.add_argument("--workload", choices=["stencil", "topousm", "openness", "surrogate", "spatial"],
+                    default="stencil",
                     help="stencil: the headline line; topousm / openness: that section alone (profiling)")
     ap.add_argument("--size", type=int, default=32768)
     ap.add_argument("--tile", type=int, default=4096)
@@ -479,6 +507,7 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the topousm / openness sections")
     ap.add_argument("--topousm-size", type=int, default=32768)
     ap.add_argument("--openness-size", type=int, default=16384)
+    ap.add_argument("--spatial-size", type=int, default=8192)
     ap.add_argument("--extra-steps", type=int, default=4)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -488,8 +517,8 @@ def main():
 
     rank, world, _ = dist_setup(args.gpus)
     if args.workload != "stencil":
-        sec = {"topousm": topousm_section, "openness": openness_section,
-               "surrogate": surrogate_section}[args.workload](args)
+        sec = {"topousm": topousm_section, "openness": openness_section, "surrogate": surrogate_section,
+               "spatial": spatial_section}[args.workload](args)
         if rank == 0:
             print(json.dumps({"section": args.workload, **sec}))
         return
@@ -502,6 +531,8 @@ def main():
         line["extra"]["openness"] = openness_section(args)
         torch.cuda.empty_cache()
         line["extra"]["openness_surrogate"] = surrogate_section(args)
+        torch.cuda.empty_cache()
+        line["extra"]["spatial"] = spatial_section(args)
     if rank == 0:
         if not args.no_cpu_baseline and world == 1:
             procs = max(1, os.cpu_count() or 1)

@@ -82,6 +82,14 @@ class TopoUSMParams(C.Structure):
                 ("scale", C.c_double)]
 
 
+class StoreFinish(C.Structure):
+    _fields_ = [("divisor", C.c_float), ("stretch_lo", C.c_float), ("stretch_scale", C.c_float),
+                ("keep_nodata_values", C.c_int32)]
+
+
+COMBINE_WSUM, COMBINE_MAX, COMBINE_MIN = 0, 1, 2
+
+
 class OpennessParams(C.Structure):
     _fields_ = [("openness_type", C.c_int32), ("num_directions", C.c_int32), ("max_distance", C.c_int32),
                 ("mode", C.c_int32), ("pixel_size", C.c_double), ("nodata", C.c_double),
@@ -132,9 +140,16 @@ _SIGNATURES = {
                                                C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                                C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_int32,
                                                C.c_float, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]),
+    "fsg_combine": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_int32,
+                              C.c_void_p, C.c_int64, C.c_void_p]),
     "fsg_masked_store": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
-                                   C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(Plane),
-                                   C.c_void_p]),
+                                   C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(StoreFinish),
+                                   C.POINTER(Plane), C.c_void_p]),
+    "fsg_downsample_nan_aware": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                           C.c_int64, C.c_void_p]),
+    "fsg_upsample_to_shape": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                        C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
+                                        C.c_void_p]),
     "fsg_conv_pack_weights": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "fsg_conv3x3": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                               C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -1,11 +1,15 @@
-"""Spatial (multi-radius) mode of the stencil products.
+"""Spatial (multi-radius) mode of the stencil products and of openness.
 
-Reference behaviour, per product (hillshade, slope, curvature):
+Reference behaviour, per product (hillshade, slope, curvature, openness):
 
 * ``_smooth_for_radius`` (algorithms/_nan_utils.py:527-552) -> ``fsg_smooth``;
   ``compute_hillshade_spatial_block`` (_impl_hillshade.py:57-67),
   ``compute_slope_spatial_block`` (_impl_slope.py:38-45) and curvature's
   ``_curv_spatial`` (_impl_curvature.py:72-78) smooth, then run the product.
+* ``compute_openness_spatial_block`` (_impl_openness.py:135-164): openness
+  of the NaN-aware f x f decimation (``fsg_downsample_nan_aware``) with the
+  distance divided and the pixel scales multiplied by f, zoomed back to the
+  block (``fsg_upsample_to_shape``, evaluated only over the window's core).
 * The local multi-radius branch of ``_direct_hillshade``
   (algorithms/tile/dask_bridge.py:72-108, ``_combine_direct`` :28-69): the
   spatial block per radius on the whole window, float32-normalised weights.
@@ -17,9 +21,10 @@ Reference behaviour, per product (hillshade, slope, curvature):
   (radius and pixel scales divided / multiplied by its decimation) sampled at
   the window's global pixel centres and NaN at NoData (:366-395); the others
   are ``map_overlap(spatial_block, depth, boundary='reflect')``.  The
-  responses are combined with the product's weights (_impl_hillshade.py:113-128;
-  ``_combine_multiscale_dask`` :182-213) and the tile processor restores NaN at
-  the NoData footprint of the core (core/tile_processor.py:973-980).
+  responses are combined as the product's ``agg`` says (_impl_hillshade.py:109-131;
+  ``_combine_multiscale_dask`` :182-213), openness is display-stretched with the
+  global statistics (_impl_openness.py:216) and the tile processor restores NaN
+  at the NoData footprint of the core (core/tile_processor.py:973-980).
 """
 from __future__ import annotations
 
@@ -33,8 +38,9 @@ from .. import _arrays
 from .. import _native as N
 from . import _stencil as S
 
-ALGO_FACTOR = {"hillshade": 1.0, "slope": 1.0, "curvature": 1.1}   # _nan_utils.py:571-581
+ALGO_FACTOR = {"hillshade": 1.0, "slope": 1.0, "curvature": 1.1, "openness": 1.4}   # _nan_utils.py:571-581
 PRODUCTS = tuple(ALGO_FACTOR)
+STENCIL_PRODUCTS = ("hillshade", "slope", "curvature")
 
 
 def smooth_for_radius(block, radius, *, pixel_size: float = 1.0, algorithm_name: str = "default"):
@@ -50,6 +56,17 @@ def _algo_factor(name: str) -> float:
     return {"topousm_fast": 1.15, "hillshade": 1.0, "slope": 1.0, "specular": 1.4,
             "atmospheric_scattering": 1.05, "curvature": 1.1, "ambient_occlusion": 1.5,
             "openness": 1.4, "multi_light_uncertainty": 1.25}.get(str(name), 1.0)
+
+
+def downsample_factor(radius, pixel_size=1.0, algorithm_name="default", base_radius=24.0, max_factor=16) -> int:
+    """``_radius_to_downsample_factor`` (_nan_utils.py:555-601): a power of two from the radius,
+    the algorithm's factor and the resolution (the block shape does not enter)."""
+    r = max(1.0, float(radius))
+    px = max(1e-3, float(pixel_size) if pixel_size else 1.0)
+    score = (r / max(1.0, base_radius)) * _algo_factor(algorithm_name) * 1.0 * (max(1.0, 1.0 / px) ** 0.35)
+    if score <= 1.0:
+        return 1
+    return int(max(1, min(2 ** int(math.floor(math.log2(score))), max_factor)))
 
 
 def _smooth_into(ptr, ld, h, w, radius, pixel_size, algorithm_name, out, stream=None):
@@ -89,9 +106,67 @@ def _run_product(src_ptr, src_ld, src_h, src_w, core, product, kw, pixel_size, p
                                 arr, C.c_void_p(_arrays.current_stream_handle())))
 
 
+def _openness_spatial_into(src_ptr, src_ld, src_h, src_w, core, max_distance, kw, pixel_size, psx, psy, out,
+                           buf=None):
+    """compute_openness_spatial_block (_impl_openness.py:135-164) of the array ``src``,
+    evaluated over ``core`` (y0, x0, h, w) of it into ``out`` (h x w, float32).
+
+    Factor 1: the openness kernel with the window = all of src.  Factor f > 1: the
+    f x f NaN-aware decimation, openness there with max(2, round(md / f)) and the
+    pixel scales x f, then the NaN-aware zoom back to src's shape over the core only.
+    """
+    from ._impl_openness import make_params, run_openness
+    from ._stencil import make_plane
+    torch = _arrays._torch()
+    lib = N.lib()
+    stream = C.c_void_p(_arrays.current_stream_handle())
+    f = downsample_factor(float(max_distance), pixel_size, "openness")
+    sx, sy = abs(float(psx)), abs(float(psy))
+    if buf is None:
+        def buf(name, n):
+            return torch.empty(int(n), device=out.device, dtype=torch.float32)
+    if f <= 1:
+        view = _arrays.DevView(None, int(src_ptr), int(src_h), int(src_w), int(src_ld), "torch")
+        t = N.Tile()
+        t.win_y0, t.win_x0, t.win_h, t.win_w = 0, 0, src_h, src_w
+        t.core_y0, t.core_x0, t.core_h, t.core_w = core
+        t.out_y0, t.out_x0 = 0, 0
+        t.pixel_scale_x, t.pixel_scale_y = sx, sy
+        p = make_params(openness_type=kw.get("openness_type", "positive"),
+                        num_directions=kw.get("num_directions", 16), max_distance=int(max_distance),
+                        pixel_size=pixel_size)
+        run_openness(view, [t], p, make_plane(out))
+        return
+    hs, ws = (src_h + f - 1) // f, (src_w + f - 1) // f
+    small = buf("os_small", hs * ws)[: hs * ws].view(hs, ws)
+    N.check(lib.fsg_downsample_nan_aware(C.c_void_p(src_ptr), int(src_ld), int(src_h), int(src_w), int(f),
+                                         C.c_void_p(small.data_ptr()), ws, stream))
+    rsmall = buf("os_resp", hs * ws)[: hs * ws].view(hs, ws)
+    sview = _arrays.DevView(small, small.data_ptr(), hs, ws, ws, "torch")
+    md = max(2, int(round(float(max_distance) / float(f))))
+    p = make_params(openness_type=kw.get("openness_type", "positive"), num_directions=kw.get("num_directions", 16),
+                    max_distance=md, pixel_size=float(pixel_size) * f)
+    t = N.Tile()
+    t.win_y0, t.win_x0, t.win_h, t.win_w = 0, 0, hs, ws
+    t.core_y0, t.core_x0, t.core_h, t.core_w = 0, 0, hs, ws
+    t.out_y0, t.out_x0 = 0, 0
+    t.pixel_scale_x, t.pixel_scale_y = sx * f, sy * f
+    run_openness(sview, [t], p, make_plane(rsmall))
+    N.check(lib.fsg_upsample_to_shape(C.c_void_p(rsmall.data_ptr()), ws, hs, ws, int(src_h), int(src_w),
+                                      int(core[0]), int(core[1]), int(core[2]), int(core[3]),
+                                      C.c_void_p(out.data_ptr()), int(out.stride(0)), stream))
+
+
 def spatial_block(block, product: str, radius, *, pixel_size=1.0, pixel_scale_x=None, pixel_scale_y=None, **kw):
-    """The spatial block function of ``product`` (smoothing, then the product)."""
+    """The spatial block function of ``product`` (smoothing, then the product; openness:
+    compute_openness_spatial_block with ``radius`` as the maximum distance)."""
     v = _arrays.as_device_f32_2d(block)
+    if product == "openness":
+        out = _arrays.empty(v.h, v.w, device=v.tensor.device)
+        psx, psy = S.resolve_scales(pixel_size, pixel_scale_x, pixel_scale_y)
+        if v.h * v.w:
+            _openness_spatial_into(v.ptr, v.ld, v.h, v.w, (0, 0, v.h, v.w), radius, kw, pixel_size, psx, psy, out)
+        return _arrays.wrap_result(out, v.origin)
     sm = _arrays.empty(v.h, v.w, device=v.tensor.device)
     _smooth_into(v.ptr, v.ld, v.h, v.w, radius, pixel_size, product, sm)
     out = _arrays.empty(v.h, v.w, device=v.tensor.device)
@@ -123,6 +198,14 @@ def compute_curvature_spatial_block(block, *, curvature_type="mean", pixel_size=
                          pixel_scale_y=pixel_scale_y, curvature_type=curvature_type)
 
 
+def compute_openness_spatial_block(block, *, openness_type="positive", num_directions=16, max_distance=50,
+                                   pixel_size=1.0, pixel_scale_x=None, pixel_scale_y=None):
+    """_impl_openness.py:135-164."""
+    return spatial_block(block, "openness", max_distance, pixel_size=pixel_size, pixel_scale_x=pixel_scale_x,
+                         pixel_scale_y=pixel_scale_y, openness_type=openness_type,
+                         num_directions=int(num_directions))
+
+
 # ------------------------------------------------------------ weights
 def clean_normalized_weights(weights) -> Optional[List[float]]:
     """_clean_normalized_weights (_nan_utils.py:142-154)."""
@@ -139,32 +222,88 @@ def clean_normalized_weights(weights) -> Optional[List[float]]:
     return [v / s for v in out]
 
 
-def combine_weights(weights, n: int, product: str) -> List[float]:
-    """The float32 weight of each response.
+def _count_matches(weights, n: int) -> bool:
+    """_weight_count_matches (_nan_utils.py:132-139)."""
+    if weights is None or isinstance(weights, (str, bytes)):
+        return False
+    try:
+        return len(weights) == n
+    except TypeError:
+        return False
 
-    hillshade (_impl_hillshade.py:113-123) normalises float32 weights in float32;
-    slope / curvature (_combine_multiscale_dask, _nan_utils.py:203-208)
-    L1-normalise in float64 (cast to float32 by the multiply).  Weights of the
-    wrong length or without a positive sum fall back to the plain mean, taken
-    here as weights 1/n.
+
+class CombinePlan:
+    """How per-radius responses become one: ``op`` (N.COMBINE_*), the float32 weight of
+    each response (1 for max / min / sum) and the divisor applied at the store (n for the
+    plain mean, else 1); ``stack`` keeps the responses as bands."""
+
+    def __init__(self, op: int, weights: List[float], divisor: float = 1.0, stack: bool = False):
+        self.op, self.weights, self.divisor, self.stack = op, weights, float(divisor), stack
+
+
+def combine_plan(product: str, agg, weights, n: int, *, direct: bool = False) -> CombinePlan:
+    """The combination of the spatial branches.
+
+    ``direct``: the local multi-radius hillshade (``_combine_direct``,
+    algorithms/tile/dask_bridge.py:28-69): max / min / sum, a float32-normalised
+    weighted mean, else the mean as a sum of r * f32(1/n).
+    hillshade (_impl_hillshade.py:109-131): 'mean' with float32-normalised weights
+    (even for one radius), 'min', 'max', anything else the plain mean.
+    slope / curvature / openness (``_combine_multiscale_dask``, _nan_utils.py:182-213):
+    one response as it is, 'max' / 'min' / 'sum', 'mean' with weights L1-normalised in
+    float64, else the plain mean.  The plain mean is the float32 sum divided by n.
     """
-    if weights is not None and not isinstance(weights, (str, bytes)) and len(weights) == n:
+    a = str(agg or "mean").lower()
+    ones = [1.0] * n
+    if a == "stack":
+        return CombinePlan(N.COMBINE_WSUM, ones, stack=True)
+    if product != "hillshade" and n == 1:
+        return CombinePlan(N.COMBINE_WSUM, ones)
+    if a == "max":
+        return CombinePlan(N.COMBINE_MAX, ones)
+    if a == "min":
+        return CombinePlan(N.COMBINE_MIN, ones)
+    if a == "sum" and (direct or product != "hillshade"):
+        return CombinePlan(N.COMBINE_WSUM, ones)
+    if a == "mean":
         if product == "hillshade":
-            w = np.asarray(weights, dtype=np.float32)
-            if np.isfinite(w).all() and float(w.sum()) > 0:
-                w = w / w.sum()
-                return [float(np.float32(x)) for x in w]
-        else:
+            if isinstance(weights, (list, tuple)) and len(weights) == n:
+                w = np.asarray(weights, dtype=np.float32)
+                if np.isfinite(w).all() and float(w.sum()) > 0:
+                    w = w / w.sum()
+                    return CombinePlan(N.COMBINE_WSUM, [float(np.float32(x)) for x in w])
+        elif _count_matches(weights, n):
             c = clean_normalized_weights(weights)
             if c is not None:
-                return [float(np.float32(x)) for x in c]
-    return [float(np.float32(1.0 / n))] * n
+                return CombinePlan(N.COMBINE_WSUM, [float(np.float32(x)) for x in c])
+    if direct:
+        return CombinePlan(N.COMBINE_WSUM, [float(np.float32(1.0 / float(n)))] * n)
+    return CombinePlan(N.COMBINE_WSUM, ones, divisor=float(n))
 
 
 def spatial_depth(product: str, radius) -> int:
-    """depth_for_scale (_impl_hillshade.py:98, _impl_slope.py:62, _impl_curvature.py:85)."""
+    """depth_for_scale (_impl_hillshade.py:98, _impl_slope.py:62, _impl_curvature.py:85,
+    _impl_openness.py:196)."""
     r = float(radius)
+    if product == "openness":
+        return int(r) + 1
     return max(3, int(r * 2 + 2)) if product == "curvature" else max(2, int(r * 2 + 1))
+
+
+def spatial_scales(product: str, radii) -> List[float]:
+    """The scale handed to the block function per radius; openness takes
+    ``float(int(max(2, round(r))))`` as its maximum distance (_impl_openness.py:193)."""
+    if product == "openness":
+        return [float(int(max(2, round(float(r))))) for r in radii]
+    return [float(r) for r in radii]
+
+
+def spatial_is_large(product: str, scale, threshold: int) -> bool:
+    """is_large: ``int(round(r)) > thr`` (_impl_hillshade.py:103), ``int(md) > thr`` for
+    openness (_impl_openness.py:197)."""
+    if product == "openness":
+        return int(scale) > threshold
+    return int(round(float(scale))) > threshold
 
 
 def large_radius_threshold(win_h: int, win_w: int) -> int:
@@ -203,11 +342,14 @@ class Overview:
 def spatial_tile(raster: _arrays.DevView, win: Tuple[int, int, int, int], core: Tuple[int, int, int, int],
                  product: str, radii: Sequence[float], weights: Sequence[float], kw: dict, *, pixel_size: float,
                  psx: float, psy: float, nodata, overview: Optional[Overview], plane: N.Plane,
-                 scratch: dict, global_offset: Tuple[int, int] = (0, 0)) -> None:
+                 scratch: dict, global_offset: Tuple[int, int] = (0, 0), agg="mean", stretch=None,
+                 mask_nodata: bool = True) -> None:
     """One tile of the spatial product: window (y0, x0, h, w) and core (y0, x0, h, w) in
     raster coordinates; the combined core is stored into ``plane`` (addressing the core's
     first pixel).  ``global_offset`` is added to raster coordinates to give the global
-    pixel coordinates the overview is sampled at."""
+    pixel coordinates the overview is sampled at.  ``stretch``: openness' (p1, p99 - p1).
+    ``mask_nodata``: NaN at the raster's NoData (the tile processor's mask); the
+    window-level ``process`` returns the combination unmasked."""
     torch = _arrays._torch()
     lib = N.lib()
     stream = C.c_void_p(_arrays.current_stream_handle())
@@ -225,36 +367,66 @@ def spatial_tile(raster: _arrays.DevView, win: Tuple[int, int, int, int], core: 
             scratch[name] = b
         return b
 
+    scales = spatial_scales(product, radii)
+    plan = combine_plan(product, agg, weights, len(scales))
+    if plan.stack:
+        raise NotImplementedError("agg='stack' yields one band per radius; the tile loop writes one plane")
     acc = buf("acc", ch * cw)[: ch * cw].view(ch, cw)
     resp = buf("resp", ch * cw)[: ch * cw].view(ch, cw)
-    ws = combine_weights(weights, len(radii), product)
-    for i, (r, w) in enumerate(zip(radii, ws)):
+    for i, (r, w) in enumerate(zip(scales, plan.weights)):
         first = 1 if i == 0 else 0
-        if int(round(float(r))) > thr and overview is not None:
+        direct = plan.op == N.COMBINE_WSUM   # responses of a weighted sum go straight into acc
+        if spatial_is_large(product, r, thr) and overview is not None:
             cr = overview.response(product, r, kw, pixel_size, psx, psy)
+            tgt, tw_, tf = (acc, w, first) if direct else (resp, 1.0, 1)
             N.check(lib.fsg_sample_coarse_accumulate(
                 C.c_void_p(cr.ptr), cr.ld, cr.h, cr.w, C.c_void_p(raster.ptr), raster.ld, raster.h, raster.w,
                 cy, cx, ch, cw, cy + int(global_offset[0]), cx + int(global_offset[1]), overview.full[0],
-                overview.full[1], ndv, has_nd, C.c_float(w), first, C.c_void_p(acc.data_ptr()), acc.stride(0),
+                overview.full[1], ndv, has_nd, C.c_float(tw_), tf, C.c_void_p(tgt.data_ptr()), tgt.stride(0),
                 stream))
-            continue
-        d = max(1, min(spatial_depth(product, r), min(wh, ww) - 1))
-        ph, pw = wh + 2 * d, ww + 2 * d
-        padded = buf("pad", ph * pw)[: ph * pw].view(ph, pw)
-        smooth = buf("smooth", ph * pw)[: ph * pw].view(ph, pw)
-        N.check(lib.fsg_pad_reflect(C.c_void_p(raster.ptr), raster.ld, raster.h, raster.w, wy, wx, wh, ww, d, ndv,
-                                    has_nd, C.c_void_p(padded.data_ptr()), pw, stream))
-        _smooth_into(padded.data_ptr(), pw, ph, pw, r, pixel_size, product, smooth)
-        _run_product(smooth.data_ptr(), pw, ph, pw, (d + cy - wy, d + cx - wx, ch, cw), product, kw, pixel_size,
-                     psx, psy, resp)
-        N.check(lib.fsg_accumulate(C.c_void_p(resp.data_ptr()), cw, ch, cw, C.c_float(w), first,
-                                   C.c_void_p(acc.data_ptr()), cw, stream))
+        else:
+            d = max(1, min(spatial_depth(product, r), min(wh, ww) - 1))
+            ph, pw = wh + 2 * d, ww + 2 * d
+            padded = buf("pad", ph * pw)[: ph * pw].view(ph, pw)
+            N.check(lib.fsg_pad_reflect(C.c_void_p(raster.ptr), raster.ld, raster.h, raster.w, wy, wx, wh, ww, d,
+                                        ndv, has_nd, C.c_void_p(padded.data_ptr()), pw, stream))
+            pcore = (d + cy - wy, d + cx - wx, ch, cw)
+            if product == "openness":
+                _openness_spatial_into(padded.data_ptr(), pw, ph, pw, pcore, r, kw, pixel_size, psx, psy, resp,
+                                       buf=buf)
+            else:
+                smooth = buf("smooth", ph * pw)[: ph * pw].view(ph, pw)
+                _smooth_into(padded.data_ptr(), pw, ph, pw, r, pixel_size, product, smooth)
+                _run_product(smooth.data_ptr(), pw, ph, pw, pcore, product, kw, pixel_size, psx, psy, resp)
+        if not (direct and spatial_is_large(product, r, thr) and overview is not None):
+            N.check(lib.fsg_combine(C.c_void_p(resp.data_ptr()), cw, ch, cw, plan.op, C.c_float(w), first,
+                                    C.c_void_p(acc.data_ptr()), cw, stream))
+    fin = N.StoreFinish()
+    fin.divisor = plan.divisor
+    fin.stretch_lo, fin.stretch_scale = 0.0, 0.0
+    fin.keep_nodata_values = 0 if mask_nodata else 1
+    if product == "openness" and isinstance(stretch, (tuple, list)) and len(stretch) >= 2 \
+            and float(stretch[1]) > 1e-12:
+        fin.stretch_lo, fin.stretch_scale = float(stretch[0]), float(stretch[1])
     N.check(lib.fsg_masked_store(C.c_void_p(acc.data_ptr()), cw, C.c_void_p(raster.ptr), raster.ld, raster.h,
-                                 raster.w, cy, cx, ch, cw, ndv, has_nd, C.byref(plane), stream))
+                                 raster.w, cy, cx, ch, cw, ndv, has_nd, C.byref(fin), C.byref(plane), stream))
+
+
+def _stack_tile(v, name, radii, weights, kw, px, psx, psy, overview, origin, stretch):
+    """agg='stack': one band per radius, band-first (C, H, W)."""
+    torch = _arrays._torch()
+    bands = torch.empty((len(radii), v.h, v.w), device=v.tensor.device, dtype=torch.float32)
+    scratch: dict = {}
+    for k, r in enumerate(radii):
+        spatial_tile(v, (0, 0, v.h, v.w), (0, 0, v.h, v.w), name, [r], None, kw, pixel_size=px, psx=psx, psy=psy,
+                     nodata=None, overview=overview, plane=S.make_plane(bands[k]), scratch=scratch,
+                     global_offset=origin, stretch=stretch, mask_nodata=False)
+    return bands
 
 
 def spatial_stencil(name: str, dem_gpu, params: dict):
-    """``process(dem, mode='spatial' | multi-radius)`` of a stencil product on one window.
+    """``process(dem, mode='spatial' | multi-radius)`` of a stencil product or of openness
+    on one window.
 
     With ``mode='spatial'`` this is the tile backend's Dask fallback on the window as
     one chunk (large radii from ``_overview_coarse_dem`` when the params carry it,
@@ -268,24 +440,27 @@ def spatial_stencil(name: str, dem_gpu, params: dict):
     psx, psy = S.resolve_scales(px, p.get("pixel_scale_x"), p.get("pixel_scale_y"))
     kw = _product_kwargs(name, p)
     mode = str(p.get("mode", "local")).lower()
+    agg = p.get("agg", "mean")
+    stream = C.c_void_p(_arrays.current_stream_handle())
     out = _arrays.empty(v.h, v.w, device=v.tensor.device)
     if v.h * v.w == 0:
         return _arrays.wrap_result(out, v.origin)
     if mode != "spatial":
-        # _direct_hillshade local multi-radius branch
+        # _direct_hillshade local multi-radius branch (_combine_direct)
         radii = p.get("radii") or [1]
         radii = [max(1.0, float(r)) for r in radii]
-        ws = combine_weights(p.get("weights"), len(radii), "hillshade")
-        acc = _arrays.empty(v.h, v.w, device=v.tensor.device)
-        for i, (r, w) in enumerate(zip(radii, ws)):
-            resp = _arrays.as_device_f32_2d(spatial_block(v.tensor, name, r, pixel_size=px, pixel_scale_x=psx,
-                                                          pixel_scale_y=psy, **kw))
-            if len(radii) == 1:
-                return _arrays.wrap_result(resp.tensor, v.origin)
-            N.check(N.lib().fsg_accumulate(C.c_void_p(resp.ptr), resp.ld, v.h, v.w, C.c_float(w), 1 if i == 0 else 0,
-                                           C.c_void_p(acc.data_ptr()), acc.stride(0),
-                                           C.c_void_p(_arrays.current_stream_handle())))
-        return _arrays.wrap_result(acc, v.origin)
+        resp = [_arrays.as_device_f32_2d(spatial_block(v.tensor, name, r, pixel_size=px, pixel_scale_x=psx,
+                                                       pixel_scale_y=psy, **kw)) for r in radii]
+        plan = combine_plan("hillshade", agg, p.get("weights"), len(radii), direct=True)
+        if plan.stack:
+            torch = _arrays._torch()
+            return _arrays.wrap_result(torch.stack([x.tensor for x in resp], 0), v.origin)
+        if len(radii) == 1:
+            return _arrays.wrap_result(resp[0].tensor, v.origin)
+        for i, (x, w) in enumerate(zip(resp, plan.weights)):
+            N.check(N.lib().fsg_combine(C.c_void_p(x.ptr), x.ld, v.h, v.w, plan.op, C.c_float(w),
+                                        1 if i == 0 else 0, C.c_void_p(out.data_ptr()), out.stride(0), stream))
+        return _arrays.wrap_result(out, v.origin)
     radii, weights = resolve_spatial_radii_weights(p.get("radii"), p.get("weights"), px)
     if name == "hillshade" and p.get("weights") is not None:
         weights = p.get("weights")   # _impl_hillshade.py:84-87 keeps the caller's weights
@@ -294,11 +469,20 @@ def spatial_stencil(name: str, dem_gpu, params: dict):
     if cdem is not None and p.get("_overview_decimation") is not None and p.get("_tile_origin") is not None:
         overview = _GivenOverview(cdem, float(p["_overview_decimation"]), p.get("_tile_full_shape") or (v.h, v.w))
     origin = p.get("_tile_origin") or (0, 0)
-    plane = S.make_plane(out)
+    origin = (int(origin[0]), int(origin[1]))
+    stretch = p.get("global_stats") if name == "openness" else None
+    if str(agg or "mean").lower() == "stack":
+        return _arrays.wrap_result(_stack_tile(v, name, radii, weights, kw, px, psx, psy, overview, origin, stretch),
+                                   v.origin)
     spatial_tile(v, (0, 0, v.h, v.w), (0, 0, v.h, v.w), name, radii, weights, kw, pixel_size=px, psx=psx, psy=psy,
-                 nodata=None, overview=overview, plane=plane, scratch={},
-                 global_offset=(int(origin[0]), int(origin[1])))
+                 nodata=None, overview=overview, plane=S.make_plane(out), scratch={}, global_offset=origin, agg=agg,
+                 stretch=stretch, mask_nodata=False)
     return _arrays.wrap_result(out, v.origin)
+
+
+def spatial_openness(dem_gpu, params: dict):
+    """``OpennessAlgorithm.process(dem, mode='spatial')`` on one window (_impl_openness.py:188-216)."""
+    return spatial_stencil("openness", dem_gpu, params)
 
 
 def _product_kwargs(name: str, p: dict) -> dict:
@@ -307,6 +491,9 @@ def _product_kwargs(name: str, p: dict) -> dict:
                 "z_factor": 1.0 if p.get("z_factor") is None else float(p.get("z_factor", 1.0))}
     if name == "slope":
         return {"unit": str(p.get("unit", "degree"))}
+    if name == "openness":
+        return {"openness_type": str(p.get("openness_type", "positive")),
+                "num_directions": int(p.get("num_directions", 16))}
     return {"curvature_type": str(p.get("curvature_type", "mean"))}
 
 

@@ -265,24 +265,15 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
         params["radii"] = r
         if not params.get("weights"):
             params["weights"] = auto_spatial_weights(len(r))
-    if mode == "spatial" and algorithm == "openness":
-        raise NotImplementedError("spatial mode of openness is not available in this build; use mode='local'")
-    spatial = mode == "spatial" and algorithm in ("hillshade", "slope", "curvature")
+    spatial = mode == "spatial" and algorithm in ("hillshade", "slope", "curvature", "openness")
     if spatial:
-        # _sanitize_spatial_radii_weights_for_tile (core/tile_processor.py:100-127): integer
-        # radii >= 1, duplicates merged with their weights
-        ints = []
-        for r in params.get("radii") or []:
-            try:
-                fv = float(r)
-            except (TypeError, ValueError):
-                continue
-            if fv > 0:
-                ints.append(max(1, int(round(fv))))
-        if ints:
-            dr, dw = deduplicate_radii_weights(ints, params.get("weights"))
+        dr, dw = sanitize_spatial_radii_weights(algorithm, params.get("radii"), params.get("weights"))
+        if dr is not None:
             params["radii"] = dr
-            params["weights"] = dw
+            if dw is not None:
+                params["weights"] = dw
+            elif params.get("weights") is not None:
+                params["weights"] = None
 
     # topousm_fast large-radius overview split (tile_processor.py:1236-1281)
     if algorithm == "topousm_fast":
@@ -312,7 +303,16 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
     res = LoopResult(out, output_dtype, qp, len(tiles), pad)
 
     if spatial:
-        _spatial_loop(v, infos, tiles, algorithm, params, px, nodata, out, output_dtype, qp)
+        stretch = None
+        if algorithm == "openness":
+            # the openness stats describe the local display openness at max_distance in every
+            # mode (_norm_stats.py:45-46, :195-283)
+            stretch = params.get("global_stats")
+            if stretch is None:
+                stretch = global_stats_prepass(v.tensor, algorithm, dict(params, pixel_scale_x=psx,
+                                                                         pixel_scale_y=psy), nodata=nodata)
+            res.stats = stretch
+        _spatial_loop(v, infos, tiles, algorithm, params, px, nodata, out, output_dtype, qp, stretch)
     elif algorithm in ("hillshade", "slope", "curvature"):
         name = {"hillshade": "hillshade", "slope": "slope"}.get(algorithm)
         if algorithm == "curvature":
@@ -344,9 +344,50 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
     return res
 
 
-def _spatial_loop(v, infos, tiles, algorithm, params, px, nodata, out, output_dtype, qp):
-    """Spatial mode of a stencil product over the tile grid (one spatial_tile per tile;
-    large radii from one shared overview)."""
+def sanitize_spatial_radii_weights(algorithm: str, radii, weights):
+    """_sanitize_spatial_radii_weights_for_tile (core/tile_processor.py:102-172).
+
+    Stencil products: integer radii >= 1, duplicates merged with their weights.
+    openness: integer radii >= 2 (non-positive ones dropped with their weights),
+    weights kept only when every kept radius has one, then de-duplicated.
+    Returns (radii, weights) or (None, weights) when no radius survives.
+    """
+    if not isinstance(radii, (list, tuple)) or len(radii) == 0:
+        return None, weights
+    if algorithm != "openness":
+        ints = []
+        for r in radii:
+            try:
+                fv = float(r)
+            except (TypeError, ValueError):
+                continue
+            if fv > 0:
+                ints.append(max(1, int(round(fv))))
+        if not ints:
+            return None, weights
+        return deduplicate_radii_weights(ints, weights)
+    out_r, out_w = [], []
+    for i, rv in enumerate(radii):
+        try:
+            r = int(round(float(rv)))
+        except (TypeError, ValueError):
+            continue
+        if r <= 0:
+            continue
+        out_r.append(max(2, r))
+        if isinstance(weights, (list, tuple)) and i < len(weights):
+            try:
+                out_w.append(float(weights[i]))
+            except (TypeError, ValueError):
+                out_w.append(0.0)
+    if not out_r:
+        return None, None
+    return deduplicate_radii_weights(out_r, out_w if len(out_w) == len(out_r) else None)
+
+
+def _spatial_loop(v, infos, tiles, algorithm, params, px, nodata, out, output_dtype, qp, stretch=None):
+    """Spatial mode of a stencil product or of openness over the tile grid (one
+    spatial_tile per tile; large radii from one shared overview)."""
     from ..algorithms import _spatial as SP
     from ..common.spatial_mode import resolve_spatial_radii_weights
     radii, weights = resolve_spatial_radii_weights(params.get("radii"), params.get("weights"), px)
@@ -356,6 +397,7 @@ def _spatial_loop(v, infos, tiles, algorithm, params, px, nodata, out, output_dt
     overview = None
     if radii and max(int(round(float(r))) for r in radii) > 256:
         overview = SP.Overview(v, nodata=nodata)
+    agg = params.get("agg", "mean")
     scratch: dict = {}
     for info, t in zip(infos, tiles):
         plane = S.make_plane(out[info.core_y:info.core_y + info.core_h, info.core_x:info.core_x + info.core_w],
@@ -363,4 +405,4 @@ def _spatial_loop(v, infos, tiles, algorithm, params, px, nodata, out, output_dt
         SP.spatial_tile(v, (info.win_y, info.win_x, info.win_h, info.win_w),
                         (info.core_y, info.core_x, info.core_h, info.core_w), algorithm, radii, weights, kw,
                         pixel_size=px, psx=float(t.pixel_scale_x), psy=float(t.pixel_scale_y), nodata=nodata,
-                        overview=overview, plane=plane, scratch=scratch)
+                        overview=overview, plane=plane, scratch=scratch, agg=agg, stretch=stretch)

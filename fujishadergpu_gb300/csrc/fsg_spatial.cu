@@ -183,30 +183,47 @@ __global__ void void_fill(float* coarse, long long ld, int h, int w, const float
 }
 
 // ------------------------------------------------------------ zoom
-// scipy.ndimage.zoom(order=1, mode='nearest', grid_mode=False) of a NaN-free
-// array to zh x zw, written into the target region [0, th) x [0, tw) with the
-// last row / column repeated where the zoom is smaller
+// scipy.ndimage.zoom(order=1, mode='nearest', grid_mode=False) of an array to
+// zh x zw, evaluated over the region [y0, y0+oh) x [x0, x0+ow) of a th x tw
+// target with the last row / column repeated where the zoom is smaller
 // (_upsample_to_shape, _nan_utils.py:671-698).  Coordinates and the four-term
-// sum are float64 as in scipy, without fused multiply-adds.
+// sum are float64 as in scipy, without fused multiply-adds.  With NoData in
+// the source (*nan_flag != 0; NULL: none) the zoom is NaN-aware: the zooms of
+// the NaN -> 0 values and of the valid mask, each rounded to float32, then
+// num / max(den, 1e-6) where den > 1e-3, else NaN.
 __global__ void zoom_linear(const float* __restrict__ a, long long ld, int h, int w, int zh, int zw, double fy,
-                            double fx, float* out, long long old, int th, int tw) {
+                            double fx, const int* nan_flag, float* out, long long old, int y0, int x0, int oh,
+                            int ow) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= tw || y >= th) return;
-  const int zy = min(y, zh - 1), zx = min(x, zw - 1);
+  if (x >= ow || y >= oh) return;
+  const int zy = min(y0 + y, zh - 1), zx = min(x0 + x, zw - 1);
   const double cy = __dmul_rn((double)zy, fy), cx = __dmul_rn((double)zx, fx);
   const double sy = floor(cy), sx = floor(cx);
   const double ty = __dsub_rn(cy, sy), tx = __dsub_rn(cx, sx);
-  const int y0 = clamp_idx((int)sy, h), y1 = clamp_idx((int)sy + 1, h);
-  const int x0 = clamp_idx((int)sx, w), x1 = clamp_idx((int)sx + 1, w);
+  const int iy0 = clamp_idx((int)sy, h), iy1 = clamp_idx((int)sy + 1, h);
+  const int ix0 = clamp_idx((int)sx, w), ix1 = clamp_idx((int)sx + 1, w);
   const double wy0 = __dsub_rn(1.0, ty), wx0 = __dsub_rn(1.0, tx);
-  const double a00 = (double)__ldg(a + (long long)y0 * ld + x0), a01 = (double)__ldg(a + (long long)y0 * ld + x1);
-  const double a10 = (double)__ldg(a + (long long)y1 * ld + x0), a11 = (double)__ldg(a + (long long)y1 * ld + x1);
-  double t = __dmul_rn(__dmul_rn(a00, wy0), wx0);
-  t = __dadd_rn(t, __dmul_rn(__dmul_rn(a01, wy0), tx));
-  t = __dadd_rn(t, __dmul_rn(__dmul_rn(a10, ty), wx0));
-  t = __dadd_rn(t, __dmul_rn(__dmul_rn(a11, ty), tx));
-  out[(long long)y * old + x] = __double2float_rn(t);
+  const float v00 = __ldg(a + (long long)iy0 * ld + ix0), v01 = __ldg(a + (long long)iy0 * ld + ix1);
+  const float v10 = __ldg(a + (long long)iy1 * ld + ix0), v11 = __ldg(a + (long long)iy1 * ld + ix1);
+  auto lerp4 = [&](double a00, double a01, double a10, double a11) {
+    double t = __dmul_rn(__dmul_rn(a00, wy0), wx0);
+    t = __dadd_rn(t, __dmul_rn(__dmul_rn(a01, wy0), tx));
+    t = __dadd_rn(t, __dmul_rn(__dmul_rn(a10, ty), wx0));
+    t = __dadd_rn(t, __dmul_rn(__dmul_rn(a11, ty), tx));
+    return __double2float_rn(t);
+  };
+  float r;
+  if (nan_flag == nullptr || *nan_flag == 0) {
+    r = lerp4(v00, v01, v10, v11);
+  } else {
+    auto fv = [](float v) { return v == v ? (double)v : 0.0; };
+    auto fw = [](float v) { return v == v ? 1.0 : 0.0; };
+    const float num = lerp4(fv(v00), fv(v01), fv(v10), fv(v11));
+    const float den = lerp4(fw(v00), fw(v01), fw(v10), fw(v11));
+    r = den > 1e-3f ? __fdiv_rn(num, fmaxf(den, 1e-6f)) : kQNaN;
+  }
+  out[(long long)y * old + x] = r;
 }
 
 // ------------------------------------------------------ tile pieces
@@ -233,6 +250,23 @@ __global__ void accumulate(const float* __restrict__ src, long long ld, int h, i
   const float t = __fmul_rn(__ldg(src + (long long)y * ld + x), weight);
   float& o = acc[(long long)y * ald + x];
   o = first ? t : __fadd_rn(o, t);
+}
+
+// Element-wise max / min of the stacked responses as NumPy's reductions take
+// them: NaN as soon as one operand is NaN.
+__global__ void combine_extreme(const float* __restrict__ src, long long ld, int h, int w, int is_max, int first,
+                                float* acc, long long ald) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= w || y >= h) return;
+  const float v = __ldg(src + (long long)y * ld + x);
+  float& o = acc[(long long)y * ald + x];
+  if (first) {
+    o = v;
+  } else {
+    const float a = o;
+    o = (a != a || v != v) ? kQNaN : (is_max ? fmaxf(a, v) : fminf(a, v));
+  }
 }
 
 struct SampleArgs {
@@ -287,6 +321,10 @@ struct StoreArgs {
   long long ald;
   ZView z;
   int gy0, gx0, h, w;
+  float divisor;            // 1: none
+  int mask;                 // NaN at the raster's NoData
+  int has_stretch;
+  float stretch_lo, stretch_scale;
   void* out;
   long long old;
   int dtype;
@@ -301,7 +339,10 @@ __global__ void masked_store(const __grid_constant__ StoreArgs A) {
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= A.w || y >= A.h) return;
   const float zv = A.z.at(A.gy0 + y, A.gx0 + x);
-  const float v = zv != zv ? kQNaN : A.acc[(long long)y * A.ald + x];
+  float v = (A.mask && zv != zv) ? kQNaN : A.acc[(long long)y * A.ald + x];
+  if (A.divisor != 1.0f) v = __fdiv_rn(v, A.divisor);
+  // apply_display_stretch_dask (_global_stats.py:173-174): max((v - lo) / scale, 0), NaN kept
+  if (A.has_stretch && v == v) v = fmaxf(__fdiv_rn(__fsub_rn(v, A.stretch_lo), A.stretch_scale), 0.0f);
   const long long off = (long long)y * A.old + x;
   if (A.dtype == FSG_F32) static_cast<float*>(A.out)[off] = v;
   else if (A.dtype == FSG_U8) static_cast<uint8_t*>(A.out)[off] = (uint8_t)(int)quantize(v, A.qa, A.qb, A.qmin, A.qmax);
@@ -442,7 +483,66 @@ extern "C" int fsg_smooth(const float* src, int64_t ld, int32_t h, int32_t w, do
   const int zw = (int)std::nearbyint((double)ws * ((double)w / (double)ws));
   const double fy = zh > 1 ? (double)(hs - 1) / (double)(zh - 1) : 1.0;
   const double fx = zw > 1 ? (double)(ws - 1) / (double)(zw - 1) : 1.0;
-  zoom_linear<<<blocks2d(h, w), dim3(32, 8), 0, s>>>(sm, ws, hs, ws, zh, zw, fy, fx, dst, dst_ld, h, w);
+  zoom_linear<<<blocks2d(h, w), dim3(32, 8), 0, s>>>(sm, ws, hs, ws, zh, zw, fy, fx, nullptr, dst, dst_ld, 0, 0, h,
+                                                     w);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+extern "C" int fsg_downsample_nan_aware(const float* src, int64_t ld, int32_t h, int32_t w, int32_t f, float* dst,
+                                        int64_t dst_ld, void* stream) {
+  if (!src || !dst) return fail(FSG_ERR_INVALID, "null array");
+  if (h <= 0 || w <= 0 || ld < w || f < 1) return fail(FSG_ERR_SHAPE, "bad shape %d x %d / factor %d", h, w, f);
+  const int hs = (h + f - 1) / f, ws = (w + f - 1) / f;
+  if (dst_ld < ws) return fail(FSG_ERR_SHAPE, "destination row too short");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (f == 1) {
+    FSG_CUDA(cudaMemcpy2DAsync(dst, dst_ld * 4, src, ld * 4, (size_t)w * 4, h, cudaMemcpyDeviceToDevice, s));
+    return FSG_OK;
+  }
+  StreamScratch scratch;
+  // sv, sw and the Gaussian's two intermediate planes, its table and flags
+  const size_t bytes = 6 * (size_t)hs * ws * 4 + 2 * kMaxTable + 8192;
+  int st = scratch.alloc(bytes, s);
+  if (st) return st;
+  Arena ar{static_cast<char*>(scratch.ptr), static_cast<char*>(scratch.ptr) + bytes};
+  float* sv = static_cast<float*>(ar.take(sizeof(float) * (size_t)hs * ws));
+  float* sw = static_cast<float*>(ar.take(sizeof(float) * (size_t)hs * ws));
+  int* flag = static_cast<int*>(ar.take(sizeof(int)));
+  if (!sv || !sw || !flag) return fail(FSG_ERR_WORKSPACE, "decimation scratch exhausted");
+  FSG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+  block_mean_np<<<blocks2d(hs, ws), dim3(32, 8), 0, s>>>(src, ld, h, w, f, dst, dst_ld, hs, ws, flag);
+  FSG_LAUNCHED(1);
+  st = gaussian(dst, dst_ld, hs, ws, std::max(1.0, (double)std::min(hs, ws) / 64.0), AX1_PAIR, sv, sw, ws, ar, s);
+  if (st) return st;
+  void_fill<<<blocks2d(hs, ws), dim3(32, 8), 0, s>>>(dst, dst_ld, hs, ws, sv, sw, ws, flag);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+extern "C" int fsg_upsample_to_shape(const float* src, int64_t ld, int32_t h, int32_t w, int32_t th, int32_t tw,
+                                     int32_t y0, int32_t x0, int32_t oh, int32_t ow, float* dst, int64_t dst_ld,
+                                     void* stream) {
+  if (!src || !dst) return fail(FSG_ERR_INVALID, "null array");
+  if (h <= 0 || w <= 0 || ld < w || th <= 0 || tw <= 0 || y0 < 0 || x0 < 0 || oh < 0 || ow < 0 || y0 + oh > th ||
+      x0 + ow > tw || dst_ld < ow)
+    return fail(FSG_ERR_SHAPE, "bad zoom shapes");
+  if (oh == 0 || ow == 0) return FSG_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  StreamScratch scratch;
+  int st = scratch.alloc(256, s);
+  if (st) return st;
+  int* flag = static_cast<int*>(scratch.ptr);
+  FSG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+  any_nan<<<dim3((w + 255) / 256, std::min(h, 1024)), 256, 0, s>>>(src, ld, h, w, flag);
+  FSG_LAUNCHED(1);
+  // zoom output size round(n * (target / n)) per axis; grid_mode=False factors
+  const int zh = (int)std::nearbyint((double)h * ((double)th / (double)h));
+  const int zw = (int)std::nearbyint((double)w * ((double)tw / (double)w));
+  const double fy = zh > 1 ? (double)(h - 1) / (double)(zh - 1) : 1.0;
+  const double fx = zw > 1 ? (double)(w - 1) / (double)(zw - 1) : 1.0;
+  zoom_linear<<<blocks2d(oh, ow), dim3(32, 8), 0, s>>>(src, ld, h, w, zh, zw, fy, fx, flag, dst, dst_ld, y0, x0, oh,
+                                                       ow);
   FSG_LAUNCHED(1);
   return FSG_OK;
 }
@@ -470,6 +570,22 @@ extern "C" int fsg_accumulate(const float* src, int64_t ld, int32_t h, int32_t w
   if (h < 0 || w < 0 || ld < w || acc_ld < w) return fail(FSG_ERR_SHAPE, "bad shape %d x %d", h, w);
   if (h == 0 || w == 0) return FSG_OK;
   accumulate<<<blocks2d(h, w), dim3(32, 8), 0, (cudaStream_t)stream>>>(src, ld, h, w, weight, first, acc, acc_ld);
+  FSG_LAUNCHED(1);
+  return FSG_OK;
+}
+
+extern "C" int fsg_combine(const float* src, int64_t ld, int32_t h, int32_t w, int32_t op, float weight,
+                           int32_t first, float* acc, int64_t acc_ld, void* stream) {
+  if (!src || !acc) return fail(FSG_ERR_INVALID, "null array");
+  if (h < 0 || w < 0 || ld < w || acc_ld < w) return fail(FSG_ERR_SHAPE, "bad shape %d x %d", h, w);
+  if (op < FSG_COMBINE_WSUM || op > FSG_COMBINE_MIN) return fail(FSG_ERR_INVALID, "unknown combine op %d", op);
+  if (h == 0 || w == 0) return FSG_OK;
+  if (op == FSG_COMBINE_WSUM)
+    accumulate<<<blocks2d(h, w), dim3(32, 8), 0, (cudaStream_t)stream>>>(src, ld, h, w, weight, first, acc, acc_ld);
+  else
+    combine_extreme<<<blocks2d(h, w), dim3(32, 8), 0, (cudaStream_t)stream>>>(src, ld, h, w,
+                                                                              op == FSG_COMBINE_MAX ? 1 : 0, first,
+                                                                              acc, acc_ld);
   FSG_LAUNCHED(1);
   return FSG_OK;
 }
@@ -513,8 +629,10 @@ extern "C" int fsg_sample_coarse_accumulate(const float* coarse, int64_t cld, in
 
 extern "C" int fsg_masked_store(const float* acc, int64_t acc_ld, const float* raster_dev, int64_t ld,
                                 int32_t raster_h, int32_t raster_w, int32_t gy0, int32_t gx0, int32_t h, int32_t w,
-                                double nodata, int32_t has_nodata, const fsg_plane* out, void* stream) {
+                                double nodata, int32_t has_nodata, const fsg_store_finish* finish,
+                                const fsg_plane* out, void* stream) {
   if (!acc || !raster_dev || !out || !out->ptr) return fail(FSG_ERR_INVALID, "null array");
+  if (finish && !(finish->divisor > 0.0f)) return fail(FSG_ERR_INVALID, "divisor %g", (double)finish->divisor);
   if (h < 0 || w < 0 || gy0 < 0 || gx0 < 0 || gy0 + h > raster_h || gx0 + w > raster_w || acc_ld < w ||
       out->ld < w)
     return fail(FSG_ERR_SHAPE, "region outside the raster");
@@ -536,6 +654,11 @@ extern "C" int fsg_masked_store(const float* acc, int64_t acc_ld, const float* r
   A.qb = out->q_b;
   A.qmin = out->q_min;
   A.qmax = out->q_max;
+  A.divisor = finish ? finish->divisor : 1.0f;
+  A.mask = finish ? (finish->keep_nodata_values ? 0 : 1) : 1;
+  A.has_stretch = finish && finish->stretch_scale > 1e-12f ? 1 : 0;
+  A.stretch_lo = finish ? finish->stretch_lo : 0.0f;
+  A.stretch_scale = finish ? finish->stretch_scale : 1.0f;
   masked_store<<<blocks2d(h, w), dim3(32, 8), 0, (cudaStream_t)stream>>>(A);
   FSG_LAUNCHED(1);
   return FSG_OK;

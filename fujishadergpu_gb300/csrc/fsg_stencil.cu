@@ -713,10 +713,17 @@ __device__ __forceinline__ void pixel_products2(const Light& L, float sign_x, fl
 #ifndef FSG_FAST_RING
 #define FSG_FAST_RING 16  // rows per warp ring (RING - 1 copies in flight)
 #endif
+#ifndef FSG_FAST_PRODUCTS
+#define FSG_FAST_PRODUCTS 2  // 2: products on column pairs (paired FP32); 1: per column (scalar)
+#endif
+#ifndef FSG_FAST_ROW_UNROLL
+#define FSG_FAST_ROW_UNROLL 1  // output rows per loop body (register renaming instead of moves)
+#endif
 #ifndef FSG_FAST_MINB
 #define FSG_FAST_MINB 3  // resident 256-thread blocks per SM the register budget must allow
 #endif
 constexpr int RING = FSG_FAST_RING;
+constexpr int ROW_UNROLL = FSG_FAST_ROW_UNROLL;
 
 __device__ __forceinline__ void cp_async8(unsigned dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
@@ -754,11 +761,15 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
     }
     // the tile's constants as values: the plane stores below could alias the
     // tile table as far as the compiler knows, which would force reloads
+    struct Step {
+      float d2, rcp;
+    };
     struct {
-      Axis g1x, g1y, c2x, c2y;
+      Step g1x, g1y, c2x, c2y;
       float sx, sy;
       int oy0, ox0, cy0, cx0;
-    } const T = {TG.g1x, TG.g1y, TG.c2x, TG.c2y, TG.sx, TG.sy, TG.oy0, TG.ox0, TG.cy0, TG.cx0};
+    } const T = {{TG.g1x.d2, TG.g1x.rcp}, {TG.g1y.d2, TG.g1y.rcp}, {TG.c2x.d2, TG.c2x.rcp},
+                 {TG.c2y.d2, TG.c2y.rcp}, TG.sx, TG.sy, TG.oy0, TG.ox0, TG.cy0, TG.cx0};
     const int x = x0 - 2 + 2 * lane;  // first column of this lane's pair
     const bool out0 = lane >= 1 && lane <= SW / 2 && x < xo, out1 = out0 && x + 1 < xo;
     // 8-byte copies need an 8-byte aligned pair start (uniform per unit)
@@ -793,7 +804,8 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
     };
 #pragma unroll 1
     for (int k = 0; k < RING - 1; ++k) issue(k);
-    auto dv = [&](f2 num, const Axis& a) { return DIV ? div_by2(num, a.d2, a.rcp) : mul2(num, S2(a.rcp)); };
+    // by value: a reference would give the steps an address (a stack slot and a local load per use)
+    auto dv = [](f2 num, Step a) { return DIV ? div_by2(num, a.d2, a.rcp) : mul2(num, S2(a.rcp)); };
     // horizontal central difference of a row pair: (f(c+1) - f(c-1), f(c+2) - f(c))
     auto hdiff = [&](f2 f) {
       const float left = __shfl_up_sync(0xffffffffu, f.y, 1), right = __shfl_down_sync(0xffffffffu, f.x, 1);
@@ -829,7 +841,7 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
       dy0 = dv(sub2(fp1, fm1), T.g1y);
     }
     bool bad = false;
-#pragma unroll 1
+#pragma unroll ROW_UNROLL
     for (int y = y0; y < y1; ++y) {
       // NoData in the 2*REACH+1 rows feeding this output row (any lane)?
       const bool row_nan = __any_sync(0xffffffffu, nan_left > 0);
@@ -861,7 +873,17 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
         bad |= (out0 && v0 && chk.x != chk.x) || (out1 && v1 && chk.y != chk.y);
       }
       f2 o[FSG_STENCIL_NOUT];
+#if FSG_FAST_PRODUCTS == 1
+      {
+        float ox[FSG_STENCIL_NOUT], oy[FSG_STENCIL_NOUT];
+        pixel_products(L, T.sx, T.sy, OM, p.x, q.x, pz.x, qz.x, dxx.x, dxy.x, dyy.x, dyx.x, ox);
+        pixel_products(L, T.sx, T.sy, OM, p.y, q.y, pz.y, qz.y, dxx.y, dxy.y, dyy.y, dyx.y, oy);
+#pragma unroll
+        for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) o[kk] = P2(ox[kk], oy[kk]);
+      }
+#else
       pixel_products2(L, T.sx, T.sy, OM, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
+#endif
       if (!(v0 && v1)) {
 #pragma unroll
         for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) {

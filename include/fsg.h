@@ -282,6 +282,19 @@ int fsg_openness_offsets(int32_t num_directions, int32_t max_distance, int32_t m
 int fsg_smooth(const float* src, int64_t ld, int32_t h, int32_t w, double radius, double pixel_size,
                double algorithm_factor, float* dst, int64_t dst_ld, void* stream);
 
+/* _downsample_nan_aware(block, f) (algorithms/_nan_utils.py:604-668): the
+ * NaN-aware f x f block mean summed in NumPy's float32 order, enclosed voids
+ * filled by the normalised Gaussian; dst is ceil(h/f) x ceil(w/f). */
+int fsg_downsample_nan_aware(const float* src, int64_t ld, int32_t h, int32_t w, int32_t f, float* dst,
+                             int64_t dst_ld, void* stream);
+
+/* _upsample_to_shape(block, (th, tw)) (algorithms/_nan_utils.py:671-698):
+ * scipy's zoom(order=1, mode='nearest') in float64, NaN-aware when the source
+ * holds NaN, last row / column repeated where the zoom is smaller; writes the
+ * target region [y0, y0+oh) x [x0, x0+ow) to dst. */
+int fsg_upsample_to_shape(const float* src, int64_t ld, int32_t h, int32_t w, int32_t th, int32_t tw, int32_t y0,
+                          int32_t x0, int32_t oh, int32_t ow, float* dst, int64_t dst_ld, void* stream);
+
 /* The raster window [y0, y0+h) x [x0, x0+w) mirrored by `depth` samples on
  * every side, repeating the edge sample (dask map_overlap boundary='reflect',
  * as the Dask branch of the spatial products uses it,
@@ -297,6 +310,15 @@ int fsg_pad_reflect(const float* raster_dev, int64_t ld, int32_t raster_h, int32
 int fsg_accumulate(const float* src, int64_t ld, int32_t h, int32_t w, float weight, int32_t first,
                    float* acc, int64_t acc_ld, void* stream);
 
+/* Combination step of per-radius responses (_combine_multiscale_dask,
+ * algorithms/_nan_utils.py:182-213; _impl_hillshade.py:109-131):
+ * FSG_COMBINE_WSUM as fsg_accumulate (weight 1: the plain sum), FSG_COMBINE_MAX /
+ * FSG_COMBINE_MIN the element-wise extreme with NaN propagating as in NumPy's
+ * max / min over the stack; first != 0 starts the combination with src. */
+enum fsg_combine_op { FSG_COMBINE_WSUM = 0, FSG_COMBINE_MAX = 1, FSG_COMBINE_MIN = 2 };
+int fsg_combine(const float* src, int64_t ld, int32_t h, int32_t w, int32_t op, float weight, int32_t first,
+                float* acc, int64_t acc_ld, void* stream);
+
 /* One large-radius response of a tile: the coarse (overview) response sampled
  * bilinearly at global pixel centres (_bilinear_sample_coarse,
  * algorithms/_nan_utils.py:255-281) for the raster region
@@ -309,13 +331,28 @@ int fsg_sample_coarse_accumulate(const float* coarse_dev, int64_t cld, int32_t c
                                  int64_t full_h, int64_t full_w, double nodata, int32_t has_nodata, float weight,
                                  int32_t first, float* acc, int64_t acc_ld, void* stream);
 
+/* The last steps of a combined response before its store: divided by
+ * `divisor` (the plain mean's count; 1 for none), then, with
+ * stretch_scale > 1e-12, the display stretch max((v - stretch_lo) /
+ * stretch_scale, 0) of apply_display_stretch_dask
+ * (algorithms/_global_stats.py:156-178), NaN kept.  keep_nodata_values != 0
+ * skips the NoData mask (the window-level process() of the reference returns
+ * the combined responses unmasked). */
+typedef struct fsg_store_finish {
+  float divisor;
+  float stretch_lo;
+  float stretch_scale;
+  int32_t keep_nodata_values;
+} fsg_store_finish;
+
 /* Store of a combined tile core: NaN where the raster region
  * [gy0, gy0+h) x [gx0, gx0+w) is NoData (apply_nodata_mask,
- * core/tile_compute.py:132-152), then the plane's encoding; `out` addresses the
- * region's first pixel. */
+ * core/tile_compute.py:132-152) unless finish says otherwise, the finishing
+ * steps (finish may be NULL: mask only), then the plane's encoding; `out`
+ * addresses the region's first pixel. */
 int fsg_masked_store(const float* acc, int64_t acc_ld, const float* raster_dev, int64_t ld, int32_t raster_h,
                      int32_t raster_w, int32_t gy0, int32_t gx0, int32_t h, int32_t w, double nodata,
-                     int32_t has_nodata, const fsg_plane* out, void* stream);
+                     int32_t has_nodata, const fsg_store_finish* finish, const fsg_plane* out, void* stream);
 
 /* ------------------------------------------------------ openness surrogate */
 /* Kernels of the convolutional openness surrogate (no counterpart in the

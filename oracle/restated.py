@@ -275,7 +275,7 @@ def smooth_for_radius(block, radius, *, pixel_size=1.0, algorithm="default"):
 # =============================================================================
 # Spatial mode of the stencil products
 # =============================================================================
-SPATIAL_PRODUCTS = ("hillshade", "slope", "curvature")
+SPATIAL_PRODUCTS = ("hillshade", "slope", "curvature", "openness")
 
 
 def stencil_product(block, product, *, pixel_size=1.0, psx=None, psy=None, azimuth=DEFAULT_AZIMUTH,
@@ -289,20 +289,59 @@ def stencil_product(block, product, *, pixel_size=1.0, psx=None, psy=None, azimu
     return curvature(block, curvature_type=curvature_type, pixel_size=pixel_size, psx=psx, psy=psy)
 
 
+def openness_spatial_block(block, *, openness_type="positive", num_directions=16, max_distance=50,
+                           pixel_size=1.0, psx=None, psy=None):
+    """_impl_openness.py:135-164 (compute_openness_spatial_block): openness of the NaN-aware
+    f x f decimated block (f from the radius, algorithm factor 1.4) with the distance divided
+    and the pixel scales multiplied by f, zoomed back to the block's shape."""
+    f = downsample_factor(float(max_distance), pixel_size=pixel_size, algorithm="openness")
+    if f <= 1:
+        return openness(block, openness_type=openness_type, num_directions=num_directions,
+                        max_distance=max_distance, pixel_size=pixel_size, psx=psx, psy=psy)
+    small = downsample_nan_aware(block, f)
+    res = openness(small, openness_type=openness_type, num_directions=num_directions,
+                   max_distance=max(2, int(round(float(max_distance) / float(f)))),
+                   pixel_size=float(pixel_size) * float(f),
+                   psx=None if psx is None else abs(float(psx)) * f,
+                   psy=None if psy is None else abs(float(psy)) * f)
+    return upsample_to_shape(res, block.shape)
+
+
 def spatial_block(block, product, radius, *, pixel_size=1.0, **kw):
     """compute_hillshade_spatial_block (_impl_hillshade.py:57-67), compute_slope_spatial_block
-    (_impl_slope.py:38-45), _curv_spatial (_impl_curvature.py:72-78): smooth, then the product."""
+    (_impl_slope.py:38-45), _curv_spatial (_impl_curvature.py:72-78): smooth, then the product;
+    openness: compute_openness_spatial_block with ``radius`` as the maximum distance."""
+    if product == "openness":
+        return openness_spatial_block(block, max_distance=radius, pixel_size=pixel_size, **kw)
     sm = smooth_for_radius(block, radius, pixel_size=pixel_size, algorithm=product)
     return stencil_product(sm, product, pixel_size=pixel_size, **kw)
 
 
 def spatial_depth(product, radius):
     """depth_for_scale of the spatial branches (_impl_hillshade.py:98, _impl_slope.py:62,
-    _impl_curvature.py:85)."""
+    _impl_curvature.py:85, _impl_openness.py:196)."""
     r = float(radius)
+    if product == "openness":
+        return int(r) + 1
     if product == "curvature":
         return max(3, int(r * 2 + 2))
     return max(2, int(r * 2 + 1))
+
+
+def spatial_scales(product, radii):
+    """The per-radius scale handed to the block function: the radius itself, for openness
+    ``float(int(max(2, round(r))))`` (_impl_openness.py:193)."""
+    if product == "openness":
+        return [float(int(max(2, round(float(r))))) for r in radii]
+    return [float(r) for r in radii]
+
+
+def spatial_is_large(product, scale, threshold):
+    """is_large of the spatial branches: ``int(round(r)) > thr`` (_impl_hillshade.py:103,
+    _impl_slope.py:63, _impl_curvature.py:86), ``int(md) > thr`` for openness (:197)."""
+    if product == "openness":
+        return int(scale) > threshold
+    return int(round(float(scale))) > threshold
 
 
 def map_overlap_reflect(fn, block, depth):
@@ -344,25 +383,48 @@ def coarse_spatial_response(coarse_dem, product, radius, decimation, *, pixel_si
                          psy=None if psy is None else float(psy) * fac, **kw).astype(np.float32)
 
 
-def combine_responses(responses, weights, product):
-    """The weighted mean of the spatial branches.
+def _plain_mean(responses):
+    """da.mean(stack, axis=0) of float32 responses: the float32 sum in order, / float32(n)."""
+    out = responses[0].astype(np.float32)
+    for r in responses[1:]:
+        out = out + r
+    return (out / np.float32(len(responses))).astype(np.float32)
 
-    hillshade (_impl_hillshade.py:113-128): float32 weights normalised in float32;
-    slope / curvature (_combine_multiscale_dask, _nan_utils.py:182-213): weights
-    L1-normalised in float64.  Either way ``out = r0*w0; out = out + ri*wi`` in float32.
+
+def combine_responses(responses, weights, product, agg="mean"):
+    """The combination of the spatial branches' per-radius responses.
+
+    hillshade (_impl_hillshade.py:109-131): 'mean' with float32 weights normalised in
+    float32, 'min', 'max', anything else the plain mean; slope / curvature / openness
+    (_combine_multiscale_dask, _nan_utils.py:182-213): one response returned as it is,
+    'max' / 'min' / 'sum' over the stack (NaN propagating), 'mean' with weights
+    L1-normalised in float64.  A weighted mean is ``out = r0*w0; out = out + ri*wi`` in
+    float32; weights of the wrong length or without a positive sum give the plain mean.
     """
-    if len(responses) == 1 and product != "hillshade":
+    agg = str(agg or "mean").lower()
+    if product != "hillshade" and len(responses) == 1:
         return responses[0]
+    if agg == "max":
+        return np.max(np.stack(responses, 0), axis=0).astype(np.float32)
+    if agg == "min":
+        return np.min(np.stack(responses, 0), axis=0).astype(np.float32)
+    if agg == "sum" and product != "hillshade":
+        out = responses[0].astype(np.float32)
+        for r in responses[1:]:
+            out = out + r
+        return out
+    if agg != "mean" or weights is None or isinstance(weights, (str, bytes)) or len(weights) != len(responses):
+        return _plain_mean(responses)
     if product == "hillshade":
         w = np.asarray(weights, dtype=np.float32)
         if not (np.isfinite(w).all() and float(w.sum()) > 0):
-            return np.mean(np.stack(responses, 0), axis=0)
+            return _plain_mean(responses)
         w = w / w.sum()
         ws = [np.float32(float(x)) for x in w]
     else:
         c = clean_normalized_weights(weights)
         if c is None:
-            return np.mean(np.stack(responses, 0), axis=0)
+            return _plain_mean(responses)
         ws = [np.float32(x) for x in c]
     out = responses[0] * ws[0]
     for r, w in zip(responses[1:], ws[1:]):
@@ -381,7 +443,8 @@ def direct_multiscale(block, product, radii, weights, **kw):
 
 
 def spatial_window(window, product, radii, weights, *, origin=(0, 0), full_shape=None, coarse_dem=None,
-                   decimation=None, pixel_size=1.0, psx=None, psy=None, return_responses=False, **kw):
+                   decimation=None, pixel_size=1.0, psx=None, psy=None, return_responses=False, agg="mean",
+                   stretch=None, **kw):
     """One tile window of a spatial-mode stencil product on the tile backend
     (dask_bridge.py:334-346 falls back to the product's Dask ``process`` on the window as one
     chunk; multiscale_response_fields, _nan_utils.py:441-524).
@@ -394,8 +457,8 @@ def spatial_window(window, product, radii, weights, *, origin=(0, 0), full_shape
     thr = spatial_large_threshold(window.shape)
     H, W = full_shape if full_shape is not None else window.shape
     out = []
-    for r in radii:
-        if int(round(float(r))) > thr and coarse_dem is not None:
+    for r in spatial_scales(product, radii):
+        if spatial_is_large(product, r, thr) and coarse_dem is not None:
             cr = coarse_spatial_response(coarse_dem, product, r, decimation, pixel_size=pixel_size,
                                          psx=psx, psy=psy, **kw)
             up = bilinear_sample_coarse(cr, origin[0], origin[0] + h, origin[1], origin[1] + w, H, W)
@@ -404,7 +467,10 @@ def spatial_window(window, product, radii, weights, *, origin=(0, 0), full_shape
             fn = (lambda b, rr=float(r): spatial_block(b, product, rr, pixel_size=pixel_size, psx=psx, psy=psy,
                                                        **kw))
             out.append(map_overlap_reflect(fn, window, spatial_depth(product, r)).astype(np.float32))
-    comb = combine_responses(out, weights, product)
+    comb = combine_responses(out, weights, product, agg)
+    if product == "openness":
+        # apply_display_stretch_dask after the combination (_impl_openness.py:216)
+        comb = apply_stretch(comb, stretch)
     return (comb, out) if return_responses else comb
 
 

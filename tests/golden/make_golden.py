@@ -29,6 +29,9 @@ from fujishadergpu_gb300 import synth  # noqa: E402
 
 
 SPATIAL_BLOCK_RADII = (1.0, 3.0, 12.0, 40.0)
+OPENNESS_SPATIAL_FACTORS = (2, 4, 8)
+OPENNESS_ODD_TARGET = (131, 97)
+OPENNESS_SPATIAL_DISTANCES = (12, 40, 80, 150)   # decimation factors 1, 2, 4, 8 at 5 m
 
 
 def _stub_rasterio():
@@ -151,6 +154,25 @@ def main():
             d.copy(), dict(radii=[1, 4, 16], weights=[0.5, 0.3, 0.2], pixel_size=5.0,
                            pixel_scale_x=5.0, pixel_scale_y=-5.0))
     np.savez_compressed(os.path.join(HERE, "spatial.npz"), **arrays)
+
+    # ------------------------------------------------- openness spatial-mode block
+    arrays = {}
+    ob = synth.fbm(120, 136, hurst=0.8, seed=23, lo=0.0, hi=2500.0)
+    ob_nan = _with_disks(ob, 4, 24, 6.0, 14.0)
+    ob_nan[:, :20] = np.nan  # exterior strip: border-connected coarse voids stay NaN
+    for dn, d in (("clean", ob), ("nan", ob_nan)):
+        arrays[f"{dn}/dem"] = d
+        for f in OPENNESS_SPATIAL_FACTORS:
+            arrays[f"{dn}/down_{f}"] = np.asarray(nu._downsample_nan_aware(d.copy(), f), np.float32)
+        small = arrays[f"{dn}/down_4"]
+        arrays[f"{dn}/up_4"] = np.asarray(nu._upsample_to_shape(small, d.shape), np.float32)
+        arrays[f"{dn}/up_4_odd"] = np.asarray(nu._upsample_to_shape(small, OPENNESS_ODD_TARGET), np.float32)
+        for md in OPENNESS_SPATIAL_DISTANCES:
+            for ot in ("positive", "negative"):
+                arrays[f"{dn}/openness_{ot}_{md}"] = op_mod.compute_openness_spatial_block(
+                    d.copy(), openness_type=ot, num_directions=16, max_distance=md, pixel_size=5.0,
+                    pixel_scale_x=5.0, pixel_scale_y=-5.0)
+    np.savez_compressed(os.path.join(HERE, "openness_spatial.npz"), **arrays)
 
     # ---------------------------------------------------------------- topousm
     arrays = {}

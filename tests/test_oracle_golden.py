@@ -164,6 +164,48 @@ def test_openness_bit_exact(golden_dir, case):
         _eq(out, g[f"{case}/{ot}"])
 
 
+@pytest.mark.parametrize("variant", ["clean", "nan"])
+def test_openness_spatial_pieces_bit_exact(golden_dir, variant):
+    """_downsample_nan_aware (block mean, enclosed voids filled, exterior kept NaN),
+    _upsample_to_shape (NaN-aware zoom, odd target) and compute_openness_spatial_block at
+    decimation factors 1, 2, 4 and 8."""
+    g = _load(golden_dir, "openness_spatial")
+    dem = g[f"{variant}/dem"]
+    for f in (2, 4, 8):
+        _eq(R.downsample_nan_aware(dem.copy(), f), g[f"{variant}/down_{f}"])
+    small = g[f"{variant}/down_4"]
+    _eq(R.upsample_to_shape(small, dem.shape), g[f"{variant}/up_4"])
+    _eq(R.upsample_to_shape(small, (131, 97)), g[f"{variant}/up_4_odd"])
+    for md in (12, 40, 80, 150):
+        for ot in ("positive", "negative"):
+            _eq(R.openness_spatial_block(dem.copy(), openness_type=ot, max_distance=md, pixel_size=5.0, psx=5.0,
+                                         psy=-5.0), g[f"{variant}/openness_{ot}_{md}"])
+    if variant == "nan":
+        # the exterior strip keeps its NaN coarse cells; some empty interior cells are filled
+        assert np.isnan(g["nan/down_8"][:, :2]).all()
+        empty = np.isnan(dem).reshape(30, 4, 34, 4).all(axis=(1, 3))
+        assert np.isnan(g["nan/down_4"][:, 5:]).sum() < empty[:, 5:].sum()
+
+
+def test_spatial_combination_modes():
+    """_combine_multiscale_dask / the hillshade branch: max / min propagate NaN, 'sum' and the
+    plain mean add in order, invalid weights fall back to the plain mean."""
+    a = np.asarray([[1.0, np.nan, 3.0]], np.float32)
+    b = np.asarray([[2.0, 5.0, 1.0]], np.float32)
+    c = np.asarray([[0.5, 1.0, 7.0]], np.float32)
+    rs = [a, b, c]
+    assert np.array_equal(R.combine_responses(rs, None, "slope", "max"), np.asarray([[2.0, np.nan, 7.0]], np.float32),
+                          equal_nan=True)
+    assert np.array_equal(R.combine_responses(rs, None, "openness", "min"),
+                          np.asarray([[0.5, np.nan, 1.0]], np.float32), equal_nan=True)
+    assert np.array_equal(R.combine_responses(rs, None, "curvature", "sum"), (a + b) + c, equal_nan=True)
+    mean = ((a + b) + c) / np.float32(3)
+    assert np.array_equal(R.combine_responses(rs, [1, -1, float("nan")] * 0 + [0, 0, 0], "slope"), mean,
+                          equal_nan=True)
+    assert np.array_equal(R.combine_responses(rs, [1, 2], "hillshade"), mean, equal_nan=True)
+    assert np.array_equal(R.combine_responses([a], [3.0], "openness", "max"), a, equal_nan=True)
+
+
 def test_openness_reference_known_answers(golden_dir):
     """reference tests/test_openness_yokoyama.py:1-47 on the oracle."""
     g = _load(golden_dir, "openness")
