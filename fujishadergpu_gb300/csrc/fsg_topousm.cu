@@ -18,8 +18,10 @@
 // accumulation, consumes them.  Running sums are error-free (TwoSum) so long
 // windows do not drift.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "fsg_filters.cuh"
@@ -415,11 +417,14 @@ struct StripArgs {
   long long fld;
   int fh, fw;
   float sy, sx, w_large, scale;
+  float rscale;            // RN(1 / scale)
   long long old;
   int dtype;
   float qa, qb;
   int qmin, qmax;
   int have_small;
+  int ring;                // topousm_fixed: rows of the prefix ring (2R + 2G + 1)
+  const unsigned* zmax;    // topousm_fixed: max |z| over the windows (float bits)
 };
 
 __device__ __forceinline__ float field_at(const StripArgs& A, int gy, int gx) {
@@ -651,6 +656,346 @@ __global__ void __launch_bounds__(ST_NT) topousm_strip(const __grid_constant__ S
   }
 }
 
+// ------------------------------------ fused full-resolution pass, exact sums
+// The same work as topousm_strip with every box sum computed exactly in 64-bit
+// fixed point.  A cell contributes q = (rint(z * 2^k) << FX_CB) + valid (0 for
+// NoData), so one integer sum carries both the value sum and the valid count
+// of a box; the count stays below 2^FX_CB and the value part below 2^63, so
+// the low FX_CB bits of any box sum are its count and the rest its value sum,
+// even though the running sums themselves wrap modulo 2^64 (unsigned).  k is
+// chosen per launch from max |z| over the windows.  The box mean is then
+// sum * 2^-k / count, rounded once: the reference's separable float32 means
+// (uniform_filter per axis, float32 intermediate; NaN-aware num/den) agree with
+// it to within two float32 ulps, and no running sum drifts.
+//
+// Per strip of FX_NT buffer columns (window columns x0-R .. x0-R+255, 'reflect'
+// at the window edges) and per row t of the window (rows 'reflect'ed too):
+//   E[t][j] = sum_{b < j} q[t][b]                  (row prefix, j = 0..256)
+// is kept in a ring of 2R+2G+1 rows in shared memory, so one row prefix serves
+// every radius.  Thread c owns output column c (buffer column b = R + c) and
+// keeps, per radius, the box sum of its pixel as a running sum over rows:
+//   D_r(y) = sum_{t = y-r}^{y+r} (E[t][b+r+1] - E[t][b-r]).
+// Rows go in groups of G: while the threads walk the group's rows (four ring
+// reads per radius and row), each warp prefix-sums one row of the next group
+// into the ring; one barrier per group.  The coarse-field and decimated-grid
+// corner values a thread needs change only every few rows and stay in
+// registers.
+constexpr int FX_NT = 256, FX_CB = 15, FX_G = 8, FX_MAXNR = 4;
+constexpr int FX_EP = 257 + 16;  // padded pitch of a 257-entry row: entry j at j + j / 16
+__device__ __forceinline__ int fx_idx(int j) { return j + (j >> 4); }
+typedef unsigned long long u64;
+
+// max |z| over the valid cells of every window, as float bits (atomicMax on
+// the bit pattern orders non-negative floats); blockIdx.y = tile.
+__global__ void window_absmax(const TopoTileK* tiles, unsigned* zmax) {
+  const TopoTileK& T = tiles[blockIdx.y];
+  const ZView& z = T.z;
+  float m = 0.f;
+  for (int y = blockIdx.x; y < z.h; y += gridDim.x) {
+    const float* row = z.p + (long long)y * z.ld;
+#pragma unroll 4
+    for (int x = threadIdx.x; x < z.w; x += blockDim.x) {
+      const float v = __ldg(row + x);
+      if (!is_nodata(v, z.ndf, z.has_nodata != 0)) m = fmaxf(m, fabsf(v));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ float wm[32];
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, wm[w]);
+    m = fmaxf(m, wm[0]);
+    if (isfinite(m)) atomicMax(zmax, __float_as_uint(m));
+  }
+}
+
+// Shared memory of topousm_fixed (bytes): the prefix ring, the per-group table
+// of ring-row offsets (entering / leaving row of each radius) and the
+// decimated grids' row coordinates of a group.
+struct FxSmem {
+  static size_t bytes(int ring) {
+    return sizeof(u64) * FX_EP * (size_t)ring + sizeof(int2) * FX_G * FX_MAXNR + 3 * sizeof(float) * ST_MAXD * FX_G;
+  }
+};
+
+template <int NR>
+__global__ void __launch_bounds__(FX_NT, 1) topousm_fixed(const __grid_constant__ StripArgs A) {
+  extern __shared__ __align__(16) u64 fsm[];
+  constexpr int G = FX_G;
+  constexpr int ROWB = FX_EP * 8;  // bytes per ring row
+  const int RING = A.ring, TW = A.TW, R = A.R;
+  u64* ring = fsm;
+  int2* OFF = reinterpret_cast<int2*>(ring + (size_t)RING * FX_EP);  // [G][FX_MAXNR] byte offsets
+  int* DYi = reinterpret_cast<int*>(OFF + G * FX_MAXNR);             // [ST_MAXD][G][2]
+  float* DYf = reinterpret_cast<float*>(DYi + 2 * ST_MAXD * G);      // [ST_MAXD][G]
+  const char* ringb = reinterpret_cast<const char*>(ring);
+  __shared__ TopoTileK Ts;
+  const TopoTileK& T = Ts;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // warps 0 .. ncons-1 own the strip's output columns; the others prefix-sum rows
+  const int ncons = min(FX_NT / 32, (TW + 31) / 32);
+  const int nprod = FX_NT / 32 - ncons;
+  // fixed-point scale 2^k: |z| < 2^e for every valid z, and e + k = 33 keeps
+  // every box's value sum below 2^(33 + log2(129^2) + FX_CB) < 2^63
+  const unsigned mb = *A.zmax;
+  const int e = mb ? (int)((mb >> 23) & 0xFF) - 126 : 0;
+  const int k = max(-100, min(100, 33 - e));
+  const float sk = ldexpf(1.0f, k), isk = ldexpf(1.0f, -k);
+  // entry 0 of every prefix row is 0 and never written again
+  for (int r = tid; r < RING; r += FX_NT) ring[(size_t)r * FX_EP] = 0ull;
+  const int c = tid;               // output column of this thread within the strip
+  const int b = R + c;             // its buffer column
+  // per-radius constants: prefix-column byte offsets, weight, full box count and RN(1/count)
+  int ja[NR], jb[NR], n2[NR];
+  float wq[NR], n2f[NR], rn2[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    const int r = A.radii[q];
+    ja[q] = c < TW ? fx_idx(b + r + 1) * 8 : 0;
+    jb[q] = c < TW ? fx_idx(b - r) * 8 : 0;
+    n2[q] = (2 * r + 1) * (2 * r + 1);
+    n2f[q] = (float)n2[q];
+    rn2[q] = 1.0f / n2f[q];
+    wq[q] = A.weights[q];
+  }
+  for (int it = blockIdx.x; it < A.nitems; it += gridDim.x) {
+    const StripItem I = A.items[it];
+    __syncthreads();
+    for (int q = tid; q < (int)(sizeof(TopoTileK) / 4); q += FX_NT)
+      reinterpret_cast<int*>(&Ts)[q] = reinterpret_cast<const int*>(A.tiles + I.tile)[q];
+    __syncthreads();
+    const ZView z = T.z;
+    const int y0 = I.y0, y1 = I.y1, x0 = I.x0;
+    const int xb = x0 - R;                          // window column of buffer column 0
+    const int x = x0 + c;
+    const bool active = c < TW && x < min(x0 + TW, T.cx0 + T.cw);
+    const int tbase = y0 - R;                       // ring slot of row t: (t - tbase) % RING
+    const bool vec = xb >= 0 && xb + FX_NT <= z.w && (z.ld & 3) == 0 &&
+                     ((reinterpret_cast<uintptr_t>(z.p + xb) & 15) == 0);
+    // one row of the window (reflected) -> this lane's 8 buffer columns 8*lane .. 8*lane+7
+    auto load_row = [&](int t, float (&v)[8]) {
+      const float* row = z.p + (long long)reflect_idx(t, z.h) * z.ld;
+      if (vec) {
+        const float4* p4 = reinterpret_cast<const float4*>(row + xb + 8 * lane);
+        const float4 a4 = __ldg(p4), b4 = __ldg(p4 + 1);
+        v[0] = a4.x; v[1] = a4.y; v[2] = a4.z; v[3] = a4.w;
+        v[4] = b4.x; v[5] = b4.y; v[6] = b4.z; v[7] = b4.w;
+      } else {
+#pragma unroll
+        for (int m = 0; m < 8; ++m) v[m] = __ldg(row + reflect_idx(xb + 8 * lane + m, z.w));
+      }
+    };
+    // fixed-point cells, warp-wide prefix, store E[t][1..256] into the ring
+    auto scan_store = [&](int t, const float (&v)[8]) {
+      u64 pm[8];
+      u64 acc = 0ull;
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const float xv = v[m];
+        const bool ok = !is_nodata(xv, z.ndf, z.has_nodata != 0);
+        const u64 q = ok ? ((u64)__float2ll_rn(__fmul_rn(xv, sk)) << FX_CB) + 1ull : 0ull;
+        acc += q;
+        pm[m] = acc;
+      }
+      u64 incl = acc;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const u64 n = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += n;
+      }
+      const u64 excl = incl - acc;
+      u64* row = ring + (size_t)((t - tbase) % RING) * FX_EP;
+#pragma unroll
+      for (int m = 0; m < 8; ++m) row[fx_idx(8 * lane + m + 1)] = excl + pm[m];
+    };
+    // prologue: rows tbase .. y0 + G + R - 1 (those the first group needs)
+    {
+      const int tend = min(y0 + G + R, y1 + R);
+      for (int t = tbase + warp; t < tend; t += FX_NT / 32) {
+        float v[8];
+        load_row(t, v);
+        scan_store(t, v);
+      }
+    }
+    // column coordinates of the coarse field and of the decimated grids (fixed per item)
+    const bool have_large = A.field != nullptr;
+    int fxa = 0, fxb = 0;
+    float ftx = 0.f;
+    if (have_large) {
+      const float cx = __fsub_rn(__fmul_rn(__fadd_rn((float)(T.gx0 + x), 0.5f), A.sx), 0.5f);
+      const float f0 = floorf(cx);
+      ftx = cx - f0;
+      fxa = clamp_idx((int)f0, A.fw);
+      fxb = clamp_idx((int)f0 + 1, A.fw);
+    }
+    int dxa[ST_MAXD], dxb[ST_MAXD], dya[ST_MAXD];
+    float dfx[ST_MAXD], dm[ST_MAXD][4];
+#pragma unroll
+    for (int d = 0; d < ST_MAXD; ++d) {
+      dxa[d] = dxb[d] = 0;
+      dya[d] = -1;
+      dfx[d] = 0.f;
+      if (d < T.ndec) {
+        const DecK& D = T.dec[d];
+        const double cc = (double)x * D.zx;
+        const int sx = (int)floor(cc);
+        dxa[d] = clamp_idx(sx, D.w);
+        dxb[d] = clamp_idx(sx + 1, D.w);
+        dfx[d] = (float)(cc - (double)sx);
+      }
+      dm[d][0] = dm[d][1] = dm[d][2] = dm[d][3] = 0.f;
+    }
+    int fya = INT_MIN;
+    float fa = 0.f, fb = 0.f, fc = 0.f, fd = 0.f;
+    const float* zp = z.p + (long long)y0 * z.ld + x;   // this column, current row
+    const size_t esz = A.dtype == FSG_F32 ? 4 : (A.dtype == FSG_I16 ? 2 : 1);
+    char* op = T.out + ((long long)(y0 - T.cy0) * A.old + (x - T.cx0)) * (long long)esz;
+    const long long ostep = A.old * (long long)esz;
+    __syncthreads();
+    // the box sums of row y0 (2r+1 rows of the ring per radius)
+    u64 D[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      const int r = A.radii[q];
+      u64 s = 0ull;
+      if (active)
+        for (int t = y0 - r; t <= y0 + r; ++t) {
+          const char* row = ringb + (size_t)((t - tbase) % RING) * ROWB;
+          s += *reinterpret_cast<const u64*>(row + ja[q]) - *reinterpret_cast<const u64*>(row + jb[q]);
+        }
+      D[q] = s;
+    }
+    float zn = active ? __ldg(zp) : 0.f;  // z of the next row (prefetched)
+    for (int yg = y0; yg < y1; yg += G) {
+      const int gn = min(G, y1 - yg);
+      // ring-row byte offsets of the group: entering row y + r, leaving row y - 1 - r
+      if (tid < G * NR) {
+        const int i = tid / NR, q = tid - (tid / NR) * NR;
+        const int r = A.radii[q];
+        const int y = yg + i;
+        int se = (y + r - tbase) % RING;
+        int sl = y - 1 - r - tbase;
+        sl = sl < 0 ? 0 : sl % RING;  // (row y0's sums are built directly)
+        OFF[i * FX_MAXNR + q] = make_int2(se * ROWB, sl * ROWB);
+      } else if (tid >= 64 && tid < 64 + T.ndec * G) {  // decimated-grid row coordinates
+        const int d = (tid - 64) / G, i = (tid - 64) - ((tid - 64) / G) * G;
+        const DecK& Dk = T.dec[d];
+        const double cc = (double)(yg + i) * Dk.zy;
+        const int sy2 = (int)floor(cc);
+        DYi[(d * G + i) * 2] = clamp_idx(sy2, Dk.h);
+        DYi[(d * G + i) * 2 + 1] = clamp_idx(sy2 + 1, Dk.h);
+        DYf[d * G + i] = (float)(cc - (double)sy2);
+      }
+      const bool more = yg + G < y1;  // a next group exists: its rows go into the ring now
+      float nv[8];
+      const int tn1 = yg + G + R + warp;
+      const bool scan1 = nprod == 0 && more && tn1 < y1 + R;
+      if (scan1) load_row(tn1, nv);
+      __syncthreads();  // tables
+      if (warp < ncons && active) {
+#pragma unroll 2
+        for (int i = 0; i < gn; ++i) {
+          const int y = yg + i;
+          const float zv = zn;
+          if (y + 1 < y1) zn = __ldg(zp + z.ld);
+          zp += z.ld;
+          float a = 0.f;
+#pragma unroll
+          for (int q = 0; q < NR; ++q) {
+            if (y > y0) {
+              const int2 o = OFF[i * FX_MAXNR + q];
+              const u64 ea = *reinterpret_cast<const u64*>(ringb + o.x + ja[q]);
+              const u64 eb = *reinterpret_cast<const u64*>(ringb + o.x + jb[q]);
+              const u64 la = *reinterpret_cast<const u64*>(ringb + o.y + ja[q]);
+              const u64 lb = *reinterpret_cast<const u64*>(ringb + o.y + jb[q]);
+              D[q] += (ea - eb) - (la - lb);
+            }
+            const long long S = (long long)D[q];
+            const int cnt = (int)S & ((1 << FX_CB) - 1);
+            const float num = __fmul_rn(__ll2float_rn(S >> FX_CB), isk);
+            float mean;
+            if (cnt == n2[q]) {  // no NoData in the box: divide by the fixed count (Markstein)
+              const float qq = __fmul_rn(num, rn2[q]);
+              mean = __fmaf_rn(__fmaf_rn(-qq, n2f[q], num), rn2[q], qq);
+            } else if (cnt > 0) {
+              const float dn = (float)cnt, rr = rcp_approx(dn);
+              const float qq = __fmul_rn(num, rr);
+              mean = __fmaf_rn(__fmaf_rn(-qq, dn, num), rr, qq);
+            } else {
+              mean = 0.f;
+            }
+            const float dq = __fmul_rn(wq[q], __fsub_rn(zv, mean));
+            a = q == 0 ? dq : __fadd_rn(a, dq);
+          }
+#pragma unroll
+          for (int dd = 0; dd < ST_MAXD; ++dd) {
+            if (dd >= T.ndec) break;
+            const DecK& Dk = T.dec[dd];
+            const int ya = DYi[(dd * G + i) * 2];
+            if (ya != dya[dd]) {  // new decimated row pair (uniform across the block)
+              const int yb = DYi[(dd * G + i) * 2 + 1];
+              const float* m = Dk.ms;
+              dm[dd][0] = __ldg(m + (long long)ya * Dk.w + dxa[dd]);
+              dm[dd][1] = __ldg(m + (long long)ya * Dk.w + dxb[dd]);
+              dm[dd][2] = __ldg(m + (long long)yb * Dk.w + dxa[dd]);
+              dm[dd][3] = __ldg(m + (long long)yb * Dk.w + dxb[dd]);
+              dya[dd] = ya;
+            }
+            const float fy = DYf[dd * G + i], fx = dfx[dd];
+            const float top = fmaf(fx, dm[dd][1] - dm[dd][0], dm[dd][0]);
+            const float bot = fmaf(fx, dm[dd][3] - dm[dd][2], dm[dd][2]);
+            const float mean = fmaf(fy, bot - top, top);
+            const float t = __fmul_rn(Dk.weight, __fsub_rn(zv, mean));
+            a = (NR == 0 && dd == 0) ? t : __fadd_rn(a, t);
+          }
+          const bool nan = is_nodata(zv, z.ndf, z.has_nodata != 0);
+          float v;
+          if (nan) {
+            v = kQNaN;
+          } else {
+            float large = 0.f;
+            if (have_large) {
+              // _nan_utils.py:276-281 (as field_at), with the column part fixed per item
+              const float cy = __fsub_rn(__fmul_rn(__fadd_rn((float)(T.gy0 + y), 0.5f), A.sy), 0.5f);
+              const float f0 = floorf(cy);
+              const float ty = cy - f0;
+              if ((int)f0 != fya) {  // keyed on the unclamped row: both rows clamp at the top edge
+                const int ya = clamp_idx((int)f0, A.fh), yb = clamp_idx((int)f0 + 1, A.fh);
+                const float* F = A.field;
+                fa = __ldg(F + ya * A.fld + fxa);
+                fb = __ldg(F + ya * A.fld + fxb);
+                fc = __ldg(F + yb * A.fld + fxa);
+                fd = __ldg(F + yb * A.fld + fxb);
+                fya = (int)f0;
+              }
+              const float top = fmaf(ftx, fb - fa, fa);
+              const float bot = fmaf(ftx, fd - fc, fc);
+              large = __fsub_rn(__fmul_rn(A.w_large, zv), fmaf(ty, bot - top, top));
+            }
+            if (A.have_small) v = have_large ? __fadd_rn(a, large) : a;
+            else v = large;
+            if (A.scale > 0.f) v = div_by(v, A.scale, A.rscale);
+          }
+          if (A.dtype == FSG_F32) *reinterpret_cast<float*>(op) = v;
+          else if (A.dtype == FSG_U8) *reinterpret_cast<uint8_t*>(op) = (uint8_t)(int)quantize(v, A.qa, A.qb, A.qmin, A.qmax);
+          else *reinterpret_cast<int16_t*>(op) = (int16_t)(int)quantize(v, A.qa, A.qb, A.qmin, A.qmax);
+          op += ostep;
+        }
+      } else if (warp >= ncons && more) {
+        // producer warps: the next group's rows into the ring
+        for (int tn = yg + G + R + (warp - ncons); tn < min(yg + 2 * G + R, y1 + R); tn += nprod) {
+          float v[8];
+          load_row(tn, v);
+          scan_store(tn, v);
+        }
+      }
+      if (scan1) scan_store(tn1, nv);
+      __syncthreads();  // ring rows of the next group; tables free
+    }
+  }
+}
+
 // flag[t] = any NoData in window t (ZView per tile); blockIdx.y = tile.
 __global__ void window_nan_flags(const TopoTileK* tiles, int* flags) {
   const TopoTileK& T = tiles[blockIdx.y];
@@ -789,6 +1134,27 @@ struct TopoScratch {
   static size_t bytes(int h, int w) {
     size_t full = (size_t)h * w, sm = (size_t)((h + 1) / 2) * ((w + 1) / 2);
     return (3 * full + 6 * sm) * sizeof(float) + 256 + 8 * 1024 + 16 * 1024 + 6 * 256;
+  }
+  // decimation pipeline only (no full-size buffers)
+  static size_t bytes_small(int h, int w) {
+    size_t sm = (size_t)((h + 1) / 2) * ((w + 1) / 2);
+    return 6 * ((sm * sizeof(float) + 255) & ~(size_t)255) + 256 + 8 * 1024 + 16 * 1024 + 6 * 256;
+  }
+  void carve_small(void* base, int h, int w) {
+    char* p = static_cast<char*>(base);
+    auto take = [&](size_t n) {
+      char* q = p;
+      p += (n + 255) & ~(size_t)255;
+      return q;
+    };
+    int hs = (h + 1) / 2, ws = (w + 1) / 2;
+    size_t sm = (size_t)hs * ws;
+    acc = vm = wm = AView{nullptr, 0, 0, 0};
+    AView* smalls[] = {&small, &svm, &swm, &smean, &ssv, &ssw};
+    for (AView* a : smalls) *a = {reinterpret_cast<float*>(take(sm * 4)), ws, hs, ws};
+    flag = reinterpret_cast<int*>(take(256));
+    g1 = reinterpret_cast<float*>(take(8 * 1024));
+    gv = reinterpret_cast<float*>(take(16 * 1024));
   }
   void carve(void* base, int h, int w) {
     char* p = static_cast<char*>(base);
@@ -944,6 +1310,35 @@ static int decimated_mean(const ZView& z, int r, int f, TopoScratch& S, float* m
   return mean_for_radius(small, rs, S, out, s);
 }
 
+// Streams on which the per-window decimation pipelines of one call run side
+// by side (each window's pipeline is a chain of small launches); created once
+// per device, joined back into the caller's stream with events.
+constexpr int AUX_STREAMS = 8;
+struct AuxStreams {
+  int device = -1;
+  cudaStream_t st[AUX_STREAMS];
+  cudaEvent_t fork, join[AUX_STREAMS];
+};
+static int aux_streams(AuxStreams** out) {
+  static std::mutex mu;
+  static AuxStreams pool[64];
+  int dev = 0;
+  FSG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(FSG_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(mu);
+  AuxStreams& a = pool[dev];
+  if (a.device != dev) {
+    for (int i = 0; i < AUX_STREAMS; ++i) {
+      FSG_CUDA(cudaStreamCreateWithFlags(&a.st[i], cudaStreamNonBlocking));
+      FSG_CUDA(cudaEventCreateWithFlags(&a.join[i], cudaEventDisableTiming));
+    }
+    FSG_CUDA(cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming));
+    a.device = dev;
+  }
+  *out = &a;
+  return FSG_OK;
+}
+
 static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_tile* tiles, int32_t ntiles,
                               const fsg_topousm_params* p, const fsg_plane* out, int nfull, cudaStream_t s) {
   const std::vector<int> radii(p->radii, p->radii + p->nradii);
@@ -966,8 +1361,15 @@ static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_til
     }
   int R = 0;
   for (int i = 0; i < nfull; ++i) R = std::max(R, radii[i]);
-  const int TW = ((ST_NT - 2 * R) / ST_SEG) * ST_SEG;
-  constexpr int CHUNK = 512;
+  DeviceInfo di;
+  int st = device_info(&di);
+  if (st) return st;
+  // exact fixed-point kernel when its ring fits in shared memory, else the compensated one
+  const int fx_ring = 2 * R + 2 * FX_G + 1;
+  const bool fixed = nfull >= 1 && nfull <= FX_MAXNR && 2 * R < FX_NT - 32 &&
+                     FxSmem::bytes(fx_ring) <= di.smem_optin;
+  const int TW = fixed ? FX_NT - 2 * R : ((ST_NT - 2 * R) / ST_SEG) * ST_SEG;
+  const int CHUNK = fixed ? 1024 : 512;
   std::vector<StripItem> items;
   for (int t = 0; t < ntiles; ++t) {
     const fsg_tile& T = tiles[t];
@@ -977,21 +1379,33 @@ static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_til
       for (int y = cy0; y < cy0 + T.core_h; y += CHUNK) items.push_back({t, x, y, std::min(y + CHUNK, cy0 + T.core_h)});
   }
   if (items.empty()) return FSG_OK;
-  const size_t topo_bytes = dec_idx.empty() ? 0 : TopoScratch::bytes(maxh, maxw);
+  int nwork = 0;
+  for (int t = 0; t < ntiles; ++t) nwork += tiles[t].core_h > 0 && tiles[t].core_w > 0;
+  const int NS = dec_idx.empty() ? 0 : std::max(1, std::min(AUX_STREAMS, nwork));
+  const size_t one_small = (TopoScratch::bytes_small(maxh, maxw) + 255) & ~(size_t)255;
+  const size_t topo_bytes = (size_t)NS * one_small;
   const size_t tiles_off = (topo_bytes + dec_bytes + 255) & ~(size_t)255;
   const size_t items_off = tiles_off + ((sizeof(TopoTileK) * ntiles + 255) & ~(size_t)255);
   const size_t flags_off = items_off + ((sizeof(StripItem) * items.size() + 255) & ~(size_t)255);
-  const size_t total = flags_off + sizeof(int) * ntiles + 256;
+  const size_t total = flags_off + sizeof(int) * (ntiles + 1) + 256;
   StreamScratch scratch;
-  int st = scratch.alloc(total, s);
+  st = scratch.alloc(total, s);
   if (st) return st;
   char* base = static_cast<char*>(scratch.ptr);
-  TopoScratch S;
-  if (!dec_idx.empty()) {
-    S.carve(base, maxh, maxw);
-    st = prepare_g1(S, s);
+  TopoScratch SS[AUX_STREAMS];
+  AuxStreams* aux = nullptr;
+  if (NS > 0) {
+    for (int i = 0; i < NS; ++i) {
+      SS[i].carve_small(base + (size_t)i * one_small, maxh, maxw);
+      st = prepare_g1(SS[i], s);
+      if (st) return st;
+    }
+    st = aux_streams(&aux);
     if (st) return st;
+    FSG_CUDA(cudaEventRecord(aux->fork, s));
+    for (int i = 0; i < NS; ++i) FSG_CUDA(cudaStreamWaitEvent(aux->st[i], aux->fork, 0));
   }
+  int nlaunched = 0;
   float* dec_base = reinterpret_cast<float*>(base + topo_bytes);
   TopoTileK* tiles_dev = reinterpret_cast<TopoTileK*>(base + tiles_off);
   StripItem* items_dev = reinterpret_cast<StripItem*>(base + items_off);
@@ -1019,8 +1433,9 @@ static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_til
       const int hs = std::max(1, (T.win_h + f - 1) / f), ws = std::max(1, (T.win_w + f - 1) / f);
       float* ms = reinterpret_cast<float*>(reinterpret_cast<char*>(dec_base) + dec_off[(size_t)t * dec_idx.size() + d]);
       if (T.core_h > 0 && T.core_w > 0) {
-        st = decimated_mean(k.z, r, f, S, ms, s);
-        if (st) return st;
+        const int si = nlaunched % NS;
+        st = decimated_mean(k.z, r, f, SS[si], ms, aux->st[si]);
+        if (st) break;
       }
       k.dec[d].ms = ms;
       k.dec[d].h = hs;
@@ -1029,11 +1444,19 @@ static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_til
       k.dec[d].zx = T.win_w > 1 ? (double)(ws - 1) / (double)(T.win_w - 1) : 1.0;
       k.dec[d].weight = (float)p->weights[dec_idx[d]];
     }
+    if (k.ndec > 0 && T.core_h > 0 && T.core_w > 0) ++nlaunched;
+    if (st) break;
   }
+  for (int i = 0; i < NS; ++i) {  // join the decimation streams (also on error: the scratch is freed on s)
+    FSG_CUDA(cudaEventRecord(aux->join[i], aux->st[i]));
+    FSG_CUDA(cudaStreamWaitEvent(s, aux->join[i], 0));
+  }
+  if (st) return st;
   FSG_CUDA(cudaMemcpyAsync(tiles_dev, tk.data(), sizeof(TopoTileK) * ntiles, cudaMemcpyHostToDevice, s));
   FSG_CUDA(cudaMemcpyAsync(items_dev, items.data(), sizeof(StripItem) * items.size(), cudaMemcpyHostToDevice, s));
-  FSG_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * ntiles, s));
-  window_nan_flags<<<dim3(256, ntiles), 256, 0, s>>>(tiles_dev, flags);
+  FSG_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (ntiles + 1), s));
+  if (fixed) window_absmax<<<dim3(128, ntiles), 256, 0, s>>>(tiles_dev, reinterpret_cast<unsigned*>(flags + ntiles));
+  else window_nan_flags<<<dim3(256, ntiles), 256, 0, s>>>(tiles_dev, flags);
   FSG_LAUNCHED(1);
   StripArgs A;
   std::memset(&A, 0, sizeof(A));
@@ -1057,6 +1480,7 @@ static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_til
   A.sx = p->coarse_dev ? (float)((double)p->coarse_w / (double)p->full_w) : 0.f;
   A.w_large = (float)p->w_large;
   A.scale = (float)p->scale;
+  A.rscale = A.scale > 0.f ? 1.0f / A.scale : 0.f;
   A.old = out->ld;
   A.dtype = out->dtype;
   A.qa = out->q_a;
@@ -1064,6 +1488,25 @@ static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_til
   A.qmin = out->q_min;
   A.qmax = out->q_max;
   A.have_small = p->nradii > 0;
+  A.ring = fx_ring;
+  A.zmax = reinterpret_cast<const unsigned*>(flags + ntiles);
+  if (fixed) {
+    void (*fk)(StripArgs) = nullptr;
+    switch (nfull) {
+      case 1: fk = topousm_fixed<1>; break;
+      case 2: fk = topousm_fixed<2>; break;
+      case 3: fk = topousm_fixed<3>; break;
+      default: fk = topousm_fixed<4>; break;
+    }
+    const size_t fsmem = FxSmem::bytes(fx_ring);
+    FSG_CUDA(cudaFuncSetAttribute(fk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+    int per = 0;
+    FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fk, FX_NT, fsmem));
+    const int grid = std::min((int)items.size(), di.sms * std::max(1, per));
+    fk<<<grid, FX_NT, fsmem, s>>>(A);
+    FSG_LAUNCHED(1);
+    return FSG_OK;
+  }
   const size_t smem = StripSmem::floats(std::max(1, nfull), TW) * sizeof(float);
   void (*kern)(StripArgs) = nullptr;
   switch (nfull) {
@@ -1076,9 +1519,6 @@ static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_til
     default: kern = topousm_strip<6>; break;
   }
   if (smem > 48 * 1024) FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  DeviceInfo di;
-  st = device_info(&di);
-  if (st) return st;
   int per_sm = 0;
   FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ST_NT, smem));
   const int grid = std::min((int)items.size(), di.sms * std::max(1, per_sm));
