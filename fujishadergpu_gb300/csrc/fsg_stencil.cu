@@ -541,7 +541,8 @@ __global__ void __launch_bounds__(NT, FSG_STENCIL_MINB) stencil_kernel(const __g
 // derivatives), is appended to a list; the fix-up kernel recomputes every
 // listed unit exactly (NaN fill, one-sided edge formulas), as two halves of
 // FW = 30 columns.
-constexpr int SW = 60, SH = 64, FW = SW / 2;
+constexpr int SW = 128, SH = 64, FW = 32, NQ = SW / FW;  // unit 128 x 64; fix-up in quarters of 32 columns
+constexpr int RW = SW + 4;  // ring row: the unit's 128 columns, then x0-2, x0-1, x0+128, x0+129
 
 struct FastTile {
   int wy0, wx0, wy1, wx1, cy0, cx0, cy1, cx1, oy0, ox0;
@@ -588,9 +589,7 @@ __device__ __forceinline__ UnitGeom unit_geom(const FastArgs& A, int u) {
   const int cy = lu / T.nstrip, sx = lu - (lu / T.nstrip) * T.nstrip;
   UnitGeom g;
   g.t = lo;
-  // the last strip of a core is moved left to end at the core edge (it
-  // recomputes a few columns of its neighbour with identical values)
-  g.x0 = (T.cx1 - T.cx0 >= SW) ? min(T.cx0 + sx * SW, T.cx1 - SW) : T.cx0;
+  g.x0 = T.cx0 + sx * SW;  // the last strip of a core may be narrower
   g.y0 = T.cy0 + cy * SH;
   g.y1 = min(g.y0 + SH, T.cy1);
   g.xo = min(g.x0 + SW, T.cx1);
@@ -625,108 +624,112 @@ __device__ __forceinline__ f2 div_by2(f2 a, float d, float r) {
   const f2 e = fma2(q, S2(-d), a);  // q * -d == -(q * d) exactly
   return fma2(e, S2(r), q);
 }
-__device__ __forceinline__ f2 gamma_display2(f2 k) {
-  const f2 t = mul2(k, S2(-288.53900817779268f));
-  const f2 e = P2(ex2_approx(t.x), ex2_approx(t.y));
-  const f2 l = add2(S2(1.0f), e);
-  const f2 m = mul2(S2(-0.45454545454545453f), P2(lg2_approx(l.x), lg2_approx(l.y)));
-  return P2(ex2_approx(m.x), ex2_approx(m.y));
-}
-// atan_poly on both components (x >= 0 or any sign; same steps as atan_poly)
-__device__ __forceinline__ f2 atan_poly2(f2 x) {
-  const float ax0 = fabsf(x.x), ax1 = fabsf(x.y);
-  const bool i0 = ax0 > 1.0f, i1 = ax1 > 1.0f;
-  const f2 a = P2(i0 ? rcp_approx(ax0) : ax0, i1 ? rcp_approx(ax1) : ax1);
+// arctan in degrees of a non-negative x: 6-term odd polynomial in a = min(x, 1/x)
+// fitted (Lawson's iteratively reweighted least squares on Chebyshev nodes) to
+// degrees(atan(a)) on [0, 1], |error| <= 1.1e-4 degree, and 90 - atan(1/x) above 1.
+__device__ __forceinline__ f2 atan_deg_pos2(f2 x) {
+  const bool i0 = x.x > 1.0f, i1 = x.y > 1.0f;
+  const f2 a = P2(i0 ? rcp_approx(x.x) : x.x, i1 ? rcp_approx(x.y) : x.y);
   const f2 a2 = mul2(a, a);
-  f2 p = S2(-0x1.09b3ep-8f);
-  p = fma2(a2, p, S2(0x1.662f9cp-6f));
-  p = fma2(a2, p, S2(-0x1.ca055ep-5f));
-  p = fma2(a2, p, S2(0x1.8af07cp-4f));
-  p = fma2(a2, p, S2(-0x1.1cd902p-3f));
-  p = fma2(a2, p, S2(0x1.988166p-3f));
-  p = fma2(a2, p, S2(-0x1.554c3ap-2f));
-  p = fma2(a2, p, S2(0x1.ffffeap-1f));
+  f2 p = S2(-0x1.57c936p-1f);
+  p = fma2(a2, p, S2(0x1.821bb8p+1f));
+  p = fma2(a2, p, S2(-0x1.aaed80p+2f));
+  p = fma2(a2, p, S2(0x1.62d978p+3f));
+  p = fma2(a2, p, S2(-0x1.30ed18p+4f));
+  p = fma2(a2, p, S2(0x1.ca5b16p+5f));
   f2 r = mul2(a, p);
-  r.x = copysignf(i0 ? 1.57079632679489661923f - r.x : r.x, x.x);
-  r.y = copysignf(i1 ? 1.57079632679489661923f - r.y : r.y, x.y);
+  r.x = i0 ? 90.0f - r.x : r.x;
+  r.y = i1 ? 90.0f - r.y : r.y;
   return r;
 }
 
-// pixel_products for two pixels at once.
-__device__ __forceinline__ void pixel_products2(const Light& L, float sign_x, float sign_y, unsigned om, f2 p, f2 q,
-                                                f2 pz, f2 qz, f2 dxx, f2 dxy, f2 dyy, f2 dyx, f2* o) {
+// pixel_products for two pixels at once.  slx = sign_x * lx and sly =
+// sign_y * ly (exact: the signs are +-1).  zone: pz, qz are p, q (z factor 1),
+// so 1 + pz^2 + qz^2 is curvature's 1 + p^2 + q^2 and one rsqrt serves both.
+// Curvature displays use t = -288.54 k = num / (den / 288.54), the constant
+// folded into the denominators.
+__device__ __forceinline__ void pixel_products2(const Light& L, float slx, float sly, bool zone, unsigned om, f2 p,
+                                                f2 q, f2 pz, f2 qz, f2 dxx, f2 dxy, f2 dyy, f2 dyx, f2* o) {
+  constexpr unsigned CURVM = (1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) |
+                             (1u << FSG_OUT_CURV_PLANFORM) | (1u << FSG_OUT_CURV_PROFILE);
+  const f2 g2 = fma2(p, p, mul2(q, q));
+  const f2 one_g2 = add2(S2(1.0f), g2);
+  f2 rs1 = S2(0.f);  // rsqrt(1 + p^2 + q^2), when the hillshade computed it
   if (om & (1u << FSG_OUT_HILLSHADE)) {
-    const f2 e = mul2(pz, S2(sign_x)), nn = mul2(qz, S2(sign_y));
-    const f2 t = sub2(S2(L.lz), add2(mul2(e, S2(L.lx)), mul2(nn, S2(L.ly))));
-    const f2 n2 = add2(add2(mul2(e, e), mul2(nn, nn)), S2(1.0f));
-    const f2 hs = mul2(t, P2(rsqrtf(n2.x), rsqrtf(n2.y)));
-    o[FSG_OUT_HILLSHADE] = P2(fminf(fmaxf(hs.x, 0.0f), 1.0f), fminf(fmaxf(hs.y, 0.0f), 1.0f));
+    const f2 t = fma2(pz, S2(-slx), fma2(qz, S2(-sly), S2(L.lz)));
+    const f2 n2 = zone ? one_g2 : fma2(pz, pz, fma2(qz, qz, S2(1.0f)));
+    const f2 rs = P2(rsqrtf(n2.x), rsqrtf(n2.y));
+    rs1 = rs;
+    o[FSG_OUT_HILLSHADE] = P2(__saturatef(t.x * rs.x), __saturatef(t.y * rs.y));
   }
   if (om & (1u << FSG_OUT_SLOPE)) {
-    const f2 g2 = add2(mul2(p, p), mul2(q, q));
     if (L.slope_unit == FSG_SLOPE_DEGREE) {
-      o[FSG_OUT_SLOPE] = mul2(atan_poly2(P2(sqrt_approx(g2.x), sqrt_approx(g2.y))), S2(57.295780181884765625f));
+      o[FSG_OUT_SLOPE] = atan_deg_pos2(P2(sqrt_approx(g2.x), sqrt_approx(g2.y)));
     } else {
       o[FSG_OUT_SLOPE] = P2(slope_value(p.x, q.x, L.slope_unit), slope_value(p.y, q.y, L.slope_unit));
     }
   }
-  if (om & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) | (1u << FSG_OUT_CURV_PLANFORM) |
-            (1u << FSG_OUT_CURV_PROFILE))) {
+  if (om & CURVM) {
+    constexpr float C = 1.0f / 288.53900817779268f;  // den / 288.54: t = num / den'
     const f2 p2 = mul2(p, p), q2 = mul2(q, q), pq = mul2(p, q);
-    const f2 g2 = add2(p2, q2), one_g2 = add2(S2(1.0f), g2);
-    const f2 s15 = mul2(one_g2, P2(sqrt_approx(one_g2.x), sqrt_approx(one_g2.y)));  // (1 + p^2 + q^2)^1.5
+    // (1 + p^2 + q^2)^1.5
+    const f2 sq1 = (zone && (om & (1u << FSG_OUT_HILLSHADE))) ? mul2(one_g2, rs1)
+                                                              : P2(sqrt_approx(one_g2.x), sqrt_approx(one_g2.y));
+    const f2 s15 = mul2(one_g2, sq1);
     const f2 pq2 = mul2(S2(2.0f), pq);
+    const f2 g2c = mul2(g2, S2(C));
+    auto display = [](f2 num, f2 den) {  // ((tanh(100k) + 1) / 2)^(1/2.2), k = -num / (288.54 den)
+      const f2 t = mul2(num, P2(rcp_approx(den.x), rcp_approx(den.y)));
+      const f2 e = P2(ex2_approx(t.x), ex2_approx(t.y));
+      const f2 l = add2(S2(1.0f), e);
+      const f2 m = mul2(S2(-0.45454545454545453f), P2(lg2_approx(l.x), lg2_approx(l.y)));
+      return P2(ex2_approx(m.x), ex2_approx(m.y));
+    };
     if (om & (1u << FSG_OUT_CURV_MEAN)) {
       const f2 sm = mul2(add2(dxy, dyx), S2(0.5f));
       const f2 num = fma2(add2(S2(1.0f), p2), dyy, sub2(mul2(add2(S2(1.0f), q2), dxx), mul2(pq2, sm)));
-      const f2 den = fma2(S2(2.0f), s15, S2(1e-10f));
-      o[FSG_OUT_CURV_MEAN] = gamma_display2(mul2(P2(-num.x, -num.y), P2(rcp_approx(den.x), rcp_approx(den.y))));
+      o[FSG_OUT_CURV_MEAN] = display(num, fma2(S2(2.0f * C), s15, S2(1e-10f * C)));
     }
     if (om & (1u << FSG_OUT_CURV_GAUSSIAN)) {
       const f2 num = sub2(mul2(dxx, dyy), mul2(dxy, dxy));
       const f2 den = mul2(one_g2, one_g2);
-      o[FSG_OUT_CURV_GAUSSIAN] = gamma_display2(mul2(num, P2(rcp_approx(den.x), rcp_approx(den.y))));
+      o[FSG_OUT_CURV_GAUSSIAN] = display(P2(-num.x, -num.y), mul2(den, S2(C)));
     }
     if (om & (1u << FSG_OUT_CURV_PLANFORM)) {
       const f2 num = fma2(p2, dyy, sub2(mul2(q2, dxx), mul2(pq2, dxy)));
-      const f2 den = fma2(g2, P2(sqrt_approx(g2.x), sqrt_approx(g2.y)), S2(1e-10f));
-      o[FSG_OUT_CURV_PLANFORM] = gamma_display2(mul2(P2(-num.x, -num.y), P2(rcp_approx(den.x), rcp_approx(den.y))));
+      o[FSG_OUT_CURV_PLANFORM] = display(num, fma2(g2c, P2(sqrt_approx(g2.x), sqrt_approx(g2.y)), S2(1e-10f * C)));
     }
     if (om & (1u << FSG_OUT_CURV_PROFILE)) {
       const f2 num = fma2(q2, dyy, fma2(pq2, dxy, mul2(p2, dxx)));
-      const f2 den = fma2(g2, s15, S2(1e-10f));
-      o[FSG_OUT_CURV_PROFILE] = gamma_display2(mul2(P2(-num.x, -num.y), P2(rcp_approx(den.x), rcp_approx(den.y))));
+      o[FSG_OUT_CURV_PROFILE] = display(num, fma2(g2c, s15, S2(1e-10f * C)));
     }
   }
   o[FSG_OUT_DX] = p;
   o[FSG_OUT_DY] = q;
 }
 
-// Fast streaming pass (see above).  Rows reach the warp through a ring of
-// RING rows in shared memory filled by cp.async (one 8-byte copy per lane and
-// row, RING-1 rows in flight ahead of the row being consumed), so the
-// prefetch depth costs no registers.  A warp vote per row tells whether any
-// NoData lies in the five rows feeding that output row; only then are the
-// per-pixel checks evaluated.  DIV: derivatives use the correctly rounded
-// division (bit-exact np.gradient, needed for the dx/dy planes); otherwise a
-// multiply by the reciprocal.
+// Fast streaming pass (see above).  A warp owns a unit of SW = 128 columns and
+// SH = 64 rows; lane l holds columns x0+4l .. x0+4l+3 as two float2 pairs, so
+// every plane is written with one 16-byte store per lane (a 512-byte
+// contiguous row segment per warp).  Rows reach the warp through a ring of RING
+// rows in shared memory filled by cp.async (16 bytes per lane and row, plus the
+// four halo columns x0-2, x0-1, x0+128, x0+129 copied by lane 0), RING-1 rows
+// in flight.  Horizontal neighbours come from one shuffle each way per row and
+// quantity; lanes 0 and 31 take theirs from the halo columns.  A warp vote per
+// row tells whether any NoData lies in the rows feeding that output row; only
+// then are the per-pixel checks evaluated.  DIV: derivatives use the correctly
+// rounded division (bit-exact np.gradient, needed for the dx/dy planes);
+// otherwise a multiply by the reciprocal.
 #ifndef FSG_FAST_RING
-#define FSG_FAST_RING 16  // rows per warp ring (RING - 1 copies in flight)
-#endif
-#ifndef FSG_FAST_PRODUCTS
-#define FSG_FAST_PRODUCTS 2  // 2: products on column pairs (paired FP32); 1: per column (scalar)
-#endif
-#ifndef FSG_FAST_ROW_UNROLL
-#define FSG_FAST_ROW_UNROLL 1  // output rows per loop body (register renaming instead of moves)
+#define FSG_FAST_RING 11  // rows per warp ring (RING - 1 copies in flight; 8 x 11 x 528 B static)
 #endif
 #ifndef FSG_FAST_MINB
-#define FSG_FAST_MINB 3  // resident 256-thread blocks per SM the register budget must allow
+#define FSG_FAST_MINB 2  // resident 256-thread blocks per SM the register budget must allow
 #endif
 constexpr int RING = FSG_FAST_RING;
-constexpr int ROW_UNROLL = FSG_FAST_ROW_UNROLL;
 
-__device__ __forceinline__ void cp_async8(unsigned dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+__device__ __forceinline__ void cp_async16(unsigned dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async4(unsigned dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
@@ -735,26 +738,40 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// Four columns of a lane as two pairs, plus the lane's edge pair: lane 0 keeps
+// (f[x0-2], f[x0-1]) and lane 31 (f[x0+128], f[x0+129]) (unused elsewhere).
+struct Q4 {
+  f2 lo, hi;
+};
+__device__ __forceinline__ Q4 q4add(Q4 a, Q4 b) { return {add2(a.lo, b.lo), add2(a.hi, b.hi)}; }
+__device__ __forceinline__ Q4 q4sub(Q4 a, Q4 b) { return {sub2(a.lo, b.lo), sub2(a.hi, b.hi)}; }
+__device__ __forceinline__ Q4 q4mul(Q4 a, f2 s) { return {mul2(a.lo, s), mul2(a.hi, s)}; }
+// f(c+1) - f(c-1) for the four columns, left = f(x-1), right = f(x+4)
+__device__ __forceinline__ Q4 q4hdiff(Q4 f, float left, float right) {
+  return {sub2(P2(f.lo.y, f.hi.x), P2(left, f.lo.x)), sub2(P2(f.hi.y, right), P2(f.lo.y, f.hi.x))};
+}
+
 template <bool CURV, unsigned OM, bool ALLF32>
 __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const __grid_constant__ FastArgs A) {
   constexpr bool DIV = (OM & ((1u << FSG_OUT_DX) | (1u << FSG_OUT_DY))) != 0;
   constexpr int REACH = CURV ? 2 : 1;  // rows above / below an output row that feed it
-  __shared__ __align__(16) float2 ring_s[256 / 32][RING][32];
+  __shared__ __align__(16) float ring_s[256 / 32][RING][RW];
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  float2* ring = ring_s[threadIdx.x >> 5][0];
-  const unsigned sbase = (unsigned)__cvta_generic_to_shared(ring) + lane * 8;
+  float* ring = ring_s[threadIdx.x >> 5][0];
+  const unsigned sbase = (unsigned)__cvta_generic_to_shared(ring);
   const bool hn = A.has_nodata != 0;
   const Light L{A.lx, A.ly, A.lz, A.slope_unit};
   const float qnan = __int_as_float(0x7fc00000);
+  const bool e0lane = lane == 0, e31lane = lane == 31;
   for (int u = warp; u < A.total_units; u += nwarps) {
     const UnitGeom g = unit_geom(A, u);
     const FastTile& TG = A.tiles[g.t];
     const int x0 = g.x0, y0 = g.y0, y1 = g.y1, xo = g.xo;
-    // stencil reach: rows y0-2 .. y1+1 and cols x0-2 .. x0+61 strictly inside
+    // stencil reach: rows y0-2 .. y1+1 and cols x0-2 .. xo+1 strictly inside
     // the window, so every derivative is a central difference
-    const bool interior = y0 - 2 >= TG.wy0 && y1 + 2 <= TG.wy1 && x0 - 2 >= TG.wx0 && x0 + SW + 2 <= TG.wx1;
+    const bool interior = y0 - 2 >= TG.wy0 && y1 + 2 <= TG.wy1 && x0 - 2 >= TG.wx0 && xo + 2 <= TG.wx1;
     if (!interior) {
       if (lane == 0) push_fix(A, u, true);
       continue;
@@ -766,51 +783,78 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
     };
     struct {
       Step g1x, g1y, c2x, c2y;
-      float sx, sy;
-      int oy0, ox0, cy0, cx0;
+      float slx, sly;
+      int oy0, ox0, cy0, cx0, wx1;
     } const T = {{TG.g1x.d2, TG.g1x.rcp}, {TG.g1y.d2, TG.g1y.rcp}, {TG.c2x.d2, TG.c2x.rcp},
-                 {TG.c2y.d2, TG.c2y.rcp}, TG.sx, TG.sy, TG.oy0, TG.ox0, TG.cy0, TG.cx0};
-    const int x = x0 - 2 + 2 * lane;  // first column of this lane's pair
-    const bool out0 = lane >= 1 && lane <= SW / 2 && x < xo, out1 = out0 && x + 1 < xo;
-    // 8-byte copies need an 8-byte aligned pair start (uniform per unit)
-    const bool vload = ((A.ld & 1) == 0) && ((((uintptr_t)A.raster >> 2) + (uintptr_t)x0) & 1) == 0;
+                 {TG.c2y.d2, TG.c2y.rcp}, TG.sx * L.lx, TG.sy * L.ly, TG.oy0, TG.ox0, TG.cy0, TG.cx0, TG.wx1};
+    const int xl = x0 + 4 * lane;  // first column of this lane
+    // output columns of this lane: xl + m < xo
+    const int nout = min(4, max(0, xo - xl));
+    // 16-byte copies need a 16-byte aligned start for every row (uniform per unit)
+    const bool vload = ((A.ld & 3) == 0) && ((((uintptr_t)A.raster >> 2) + (uintptr_t)x0) & 3) == 0;
+    const bool lfull = xl + 3 < T.wx1;
     const int nrows = (y1 - y0) + 2 * REACH;      // rows y0-REACH .. y1+REACH-1
-    const float* src0 = A.raster + (long long)(y0 - REACH) * A.ld + x;
+    const float* src0 = A.raster + (long long)(y0 - REACH) * A.ld;
     // row k of the unit -> ring slot k % RING; RING-1 copy groups in flight
     auto issue = [&](int k) {
       if (k < nrows) {
         const float* gp = src0 + (long long)k * A.ld;
-        const unsigned dst = sbase + (unsigned)((k % RING) * 256);
-        if (vload) {
-          cp_async8(dst, gp);
+        const unsigned dst = sbase + (unsigned)((k % RING) * (RW * 4));
+        if (vload && lfull) {
+          cp_async16(dst + 16 * lane, gp + xl);
         } else {
-          cp_async4(dst, gp);
-          cp_async4(dst + 4, gp + 1);
+#pragma unroll
+          for (int m = 0; m < 4; ++m)
+            if (xl + m < T.wx1) cp_async4(dst + 4 * (4 * lane + m), gp + xl + m);
+        }
+        if (lane == 0) {
+          cp_async4(dst + 4 * SW, gp + x0 - 2);
+          cp_async4(dst + 4 * SW + 4, gp + x0 - 1);
+          if (x0 + SW + 1 < T.wx1) {
+            cp_async4(dst + 4 * SW + 8, gp + x0 + SW);
+            cp_async4(dst + 4 * SW + 12, gp + x0 + SW + 1);
+          }
         }
       }
       cp_async_commit();
     };
     int nan_left = 0;  // rows for which the NoData seen last still feeds an output
-    auto take = [&](int k) {
+    // take row k: the lane's four columns and its edge pair
+    auto take = [&](int k, Q4& f, f2& e) {
       cp_async_wait<RING - 2>();
-      f2 v = ring[(k % RING) * 32 + lane];
+      __syncwarp();
+      const float* rp = ring + (k % RING) * RW;
+      const float4 v = *reinterpret_cast<const float4*>(rp + 4 * lane);
+      const float4 h = *reinterpret_cast<const float4*>(rp + SW);
+      f = {P2(v.x, v.y), P2(v.z, v.w)};
+      e = e31lane ? P2(h.z, h.w) : P2(h.x, h.y);
+      __syncwarp();
       issue(k + RING - 1);
       if (hn) {
-        if (is_nodata(v.x, A.ndf, true)) v.x = qnan;
-        if (is_nodata(v.y, A.ndf, true)) v.y = qnan;
+        if (is_nodata(f.lo.x, A.ndf, true)) f.lo.x = qnan;
+        if (is_nodata(f.lo.y, A.ndf, true)) f.lo.y = qnan;
+        if (is_nodata(f.hi.x, A.ndf, true)) f.hi.x = qnan;
+        if (is_nodata(f.hi.y, A.ndf, true)) f.hi.y = qnan;
+        if (is_nodata(e.x, A.ndf, true)) e.x = qnan;
+        if (is_nodata(e.y, A.ndf, true)) e.y = qnan;
       }
-      if (nan2(v)) nan_left = 2 * REACH + 1;
-      return v;
+      if (nan2(f.lo) || nan2(f.hi) || ((e0lane || e31lane) && nan2(e))) nan_left = 2 * REACH + 1;
     };
 #pragma unroll 1
     for (int k = 0; k < RING - 1; ++k) issue(k);
     // by value: a reference would give the steps an address (a stack slot and a local load per use)
     auto dv = [](f2 num, Step a) { return DIV ? div_by2(num, a.d2, a.rcp) : mul2(num, S2(a.rcp)); };
-    // horizontal central difference of a row pair: (f(c+1) - f(c-1), f(c+2) - f(c))
-    auto hdiff = [&](f2 f) {
-      const float left = __shfl_up_sync(0xffffffffu, f.y, 1), right = __shfl_down_sync(0xffffffffu, f.x, 1);
-      return sub2(P2(f.y, right), P2(left, f.x));
+    auto dv4 = [&](Q4 num, Step a) { return Q4{dv(num.lo, a), dv(num.hi, a)}; };
+    auto dv1 = [](float num, Step a) { return DIV ? div_by(num, a.d2, a.rcp) : __fmul_rn(num, a.rcp); };
+    // horizontal central difference of a row: neighbours from the adjacent lanes or the edge pair
+    auto hdiff = [&](Q4 f, f2 e) {
+      float left = __shfl_up_sync(0xffffffffu, f.hi.y, 1), right = __shfl_down_sync(0xffffffffu, f.lo.x, 1);
+      if (e0lane) left = e.y;   // f[x0-1]
+      if (e31lane) right = e.x; // f[x0+128]
+      return q4hdiff(f, left, right);
     };
+    // the edge lanes' derivative one column outside the unit: lane 0 at x0-1, lane 31 at x0+128
+    auto edge_dx = [&](Q4 f, f2 e) { return e31lane ? __fsub_rn(e.y, f.hi.y) : __fsub_rn(f.lo.x, e.x); };
     char* optr[FSG_STENCIL_NOUT];
     long long ostep[FSG_STENCIL_NOUT];
     bool vstore[FSG_STENCIL_NOUT];
@@ -819,76 +863,81 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
       if (!(OM & (1u << k))) continue;
       const PlaneK& P = A.planes[k];
       const int esz = ALLF32 ? 4 : (P.dtype == FSG_F32 ? 4 : (P.dtype == FSG_I16 ? 2 : 1));
-      const long long col = (long long)(T.ox0 + x - T.cx0);
+      const long long col = (long long)(T.ox0 + xl - T.cx0);
       optr[k] = static_cast<char*>(P.ptr) + ((long long)(T.oy0 + y0 - T.cy0) * P.ld + col) * esz;
       ostep[k] = P.ld * esz;
-      vstore[k] = esz == 4 && ((P.ld & 1) == 0) &&
-                  ((((uintptr_t)P.ptr >> 2) + (uintptr_t)(T.ox0 + x0 - 2 - T.cx0)) & 1) == 0 &&
+      vstore[k] = esz == 4 && ((P.ld & 3) == 0) &&
+                  ((((uintptr_t)P.ptr >> 2) + (uintptr_t)(T.ox0 + x0 - T.cx0)) & 3) == 0 &&
                   (((uintptr_t)P.ptr & 3) == 0);
     }
     int kr = 0;  // next unit row to take
-    f2 fm2 = S2(0.f), fm1, f0, fp1, fp2 = S2(0.f);
-    if (CURV) fm2 = take(kr++);
-    fm1 = take(kr++);
-    f0 = take(kr++);
-    fp1 = take(kr++);
-    if (CURV) fp2 = take(kr++);
-    f2 dxm1 = S2(0.f), dym1 = S2(0.f), dx0 = S2(0.f), dy0 = S2(0.f);
+    Q4 fm2{}, fm1, f0, fp1, fp2{};
+    f2 em2 = S2(0.f), em1, e0, ep1, ep2 = S2(0.f);
+    if (CURV) take(kr++, fm2, em2);
+    take(kr++, fm1, em1);
+    take(kr++, f0, e0);
+    take(kr++, fp1, ep1);
+    if (CURV) take(kr++, fp2, ep2);
+    // first derivatives of rows -1 and 0 (curvature), with the edge lanes' outside column
+    Q4 dxm1{}, dym1{}, dx0{}, dy0{};
+    float xd0 = 0.f, yd0 = 0.f;  // edge-lane dx / dy of row 0 (outside column)
     if (CURV) {
-      dxm1 = dv(hdiff(fm1), T.g1x);
-      dym1 = dv(sub2(f0, fm2), T.g1y);
-      dx0 = dv(hdiff(f0), T.g1x);
-      dy0 = dv(sub2(fp1, fm1), T.g1y);
+      dxm1 = dv4(hdiff(fm1, em1), T.g1x);
+      dym1 = dv4(q4sub(f0, fm2), T.g1y);
+      dx0 = dv4(hdiff(f0, e0), T.g1x);
+      dy0 = dv4(q4sub(fp1, fm1), T.g1y);
+      xd0 = dv1(edge_dx(f0, e0), T.g1x);
+      yd0 = dv1(__fsub_rn(e31lane ? ep1.x : ep1.y, e31lane ? em1.x : em1.y), T.g1y);
     }
     bool bad = false;
-#pragma unroll ROW_UNROLL
+#pragma unroll 1
     for (int y = y0; y < y1; ++y) {
       // NoData in the 2*REACH+1 rows feeding this output row (any lane)?
       const bool row_nan = __any_sync(0xffffffffu, nan_left > 0);
-      f2 p, q, dxx = S2(0.f), dxy = S2(0.f), dyy = S2(0.f), dyx = S2(0.f), dxp1 = S2(0.f), dyp1 = S2(0.f);
+      Q4 p, q, dxx{}, dxy{}, dyy{}, dyx{}, dxp1{}, dyp1{};
+      float xp1 = 0.f, yp1 = 0.f;
       if (CURV) {
-        dxp1 = dv(hdiff(fp1), T.g1x);
-        dyp1 = dv(sub2(fp2, f0), T.g1y);
+        dxp1 = dv4(hdiff(fp1, ep1), T.g1x);
+        dyp1 = dv4(q4sub(fp2, f0), T.g1y);
+        xp1 = dv1(edge_dx(fp1, ep1), T.g1x);
+        yp1 = dv1(__fsub_rn(e31lane ? ep2.x : ep2.y, e31lane ? e0.x : e0.y), T.g1y);
         p = dx0;
         q = dy0;
-        dxx = dv(hdiff(dx0), T.c2x);
-        dxy = dv(sub2(dxp1, dxm1), T.c2y);
-        dyy = dv(sub2(dyp1, dym1), T.c2y);
-        if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = dv(hdiff(dy0), T.c2x);
+        dxx = dv4(hdiff(dx0, P2(xd0, xd0)), T.c2x);
+        dxy = dv4(q4sub(dxp1, dxm1), T.c2y);
+        dyy = dv4(q4sub(dyp1, dym1), T.c2y);
+        if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = dv4(hdiff(dy0, P2(yd0, yd0)), T.c2x);
       } else {
-        p = dv(hdiff(f0), T.g1x);
-        q = dv(sub2(fp1, fm1), T.g1y);
+        p = dv4(hdiff(f0, e0), T.g1x);
+        q = dv4(q4sub(fp1, fm1), T.g1y);
       }
-      f2 pz = p, qz = q;
+      Q4 pz = p, qz = q;
       if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) {
         const f2 zf = S2(A.z);
-        pz = dv(hdiff(mul2(f0, zf)), T.g1x);
-        qz = dv(sub2(mul2(fp1, zf), mul2(fm1, zf)), T.g1y);
+        pz = dv4(hdiff(q4mul(f0, zf), mul2(e0, zf)), T.g1x);
+        qz = dv4(q4sub(q4mul(fp1, zf), q4mul(fm1, zf)), T.g1y);
       }
-      const bool v0 = f0.x == f0.x, v1 = f0.y == f0.y;
       if (row_nan) {
-        f2 chk = add2(p, q);
-        if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) chk = add2(chk, add2(pz, qz));
-        if (CURV) chk = add2(add2(chk, add2(dxx, dxy)), add2(dyy, dyx));
-        bad |= (out0 && v0 && chk.x != chk.x) || (out1 && v1 && chk.y != chk.y);
+        Q4 chk = q4add(p, q);
+        if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) chk = q4add(chk, q4add(pz, qz));
+        if (CURV) chk = q4add(q4add(chk, q4add(dxx, dxy)), q4add(dyy, dyx));
+        bad |= (nout > 0 && f0.lo.x == f0.lo.x && chk.lo.x != chk.lo.x) ||
+               (nout > 1 && f0.lo.y == f0.lo.y && chk.lo.y != chk.lo.y) ||
+               (nout > 2 && f0.hi.x == f0.hi.x && chk.hi.x != chk.hi.x) ||
+               (nout > 3 && f0.hi.y == f0.hi.y && chk.hi.y != chk.hi.y);
       }
-      f2 o[FSG_STENCIL_NOUT];
-#if FSG_FAST_PRODUCTS == 1
-      {
-        float ox[FSG_STENCIL_NOUT], oy[FSG_STENCIL_NOUT];
-        pixel_products(L, T.sx, T.sy, OM, p.x, q.x, pz.x, qz.x, dxx.x, dxy.x, dyy.x, dyx.x, ox);
-        pixel_products(L, T.sx, T.sy, OM, p.y, q.y, pz.y, qz.y, dxx.y, dxy.y, dyy.y, dyx.y, oy);
-#pragma unroll
-        for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) o[kk] = P2(ox[kk], oy[kk]);
-      }
-#else
-      pixel_products2(L, T.sx, T.sy, OM, p, q, pz, qz, dxx, dxy, dyy, dyx, o);
-#endif
-      if (!(v0 && v1)) {
+      f2 olo[FSG_STENCIL_NOUT], ohi[FSG_STENCIL_NOUT];
+      pixel_products2(L, T.slx, T.sly, A.z_is_one != 0, OM, p.lo, q.lo, pz.lo, qz.lo, dxx.lo, dxy.lo, dyy.lo,
+                      dyx.lo, olo);
+      pixel_products2(L, T.slx, T.sly, A.z_is_one != 0, OM, p.hi, q.hi, pz.hi, qz.hi, dxx.hi, dxy.hi, dyy.hi,
+                      dyx.hi, ohi);
+      if (nan2(f0.lo) || nan2(f0.hi)) {
 #pragma unroll
         for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) {
-          if (!v0) o[kk].x = qnan;
-          if (!v1) o[kk].y = qnan;
+          if (f0.lo.x != f0.lo.x) olo[kk].x = qnan;
+          if (f0.lo.y != f0.lo.y) olo[kk].y = qnan;
+          if (f0.hi.x != f0.hi.x) ohi[kk].x = qnan;
+          if (f0.hi.y != f0.hi.y) ohi[kk].y = qnan;
         }
       }
 #pragma unroll
@@ -896,22 +945,29 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
         if (!(OM & (1u << kk))) continue;
         char* dst = optr[kk];
         if (ALLF32 || A.planes[kk].dtype == FSG_F32) {
-          if (vstore[kk] && out1) {
-            *reinterpret_cast<float2*>(dst) = o[kk];
+          if (vstore[kk] && nout == 4) {
+            *reinterpret_cast<float4*>(dst) = make_float4(olo[kk].x, olo[kk].y, ohi[kk].x, ohi[kk].y);
           } else {
-            if (out0) reinterpret_cast<float*>(dst)[0] = o[kk].x;
-            if (out1) reinterpret_cast<float*>(dst)[1] = o[kk].y;
+            float* d = reinterpret_cast<float*>(dst);
+            if (nout > 0) d[0] = olo[kk].x;
+            if (nout > 1) d[1] = olo[kk].y;
+            if (nout > 2) d[2] = ohi[kk].x;
+            if (nout > 3) d[3] = ohi[kk].y;
           }
         } else {
           const PlaneK& P = A.planes[kk];
-          const float c0 = quantize(o[kk].x, P.qa, P.qb, P.qmin, P.qmax);
-          const float c1 = quantize(o[kk].y, P.qa, P.qb, P.qmin, P.qmax);
+          const float c[4] = {quantize(olo[kk].x, P.qa, P.qb, P.qmin, P.qmax),
+                              quantize(olo[kk].y, P.qa, P.qb, P.qmin, P.qmax),
+                              quantize(ohi[kk].x, P.qa, P.qb, P.qmin, P.qmax),
+                              quantize(ohi[kk].y, P.qa, P.qb, P.qmin, P.qmax)};
           if (P.dtype == FSG_U8) {
-            if (out0) reinterpret_cast<uint8_t*>(dst)[0] = (uint8_t)(int)c0;
-            if (out1) reinterpret_cast<uint8_t*>(dst)[1] = (uint8_t)(int)c1;
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+              if (m < nout) reinterpret_cast<uint8_t*>(dst)[m] = (uint8_t)(int)c[m];
           } else {
-            if (out0) reinterpret_cast<int16_t*>(dst)[0] = (int16_t)(int)c0;
-            if (out1) reinterpret_cast<int16_t*>(dst)[1] = (int16_t)(int)c1;
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+              if (m < nout) reinterpret_cast<int16_t*>(dst)[m] = (int16_t)(int)c[m];
           }
         }
         optr[kk] += ostep[kk];
@@ -919,12 +975,17 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
       // slide one row down
       if (nan_left > 0) --nan_left;
       if (y + 1 < y1) {
-        const f2 nx = take(kr++);
+        Q4 nx;
+        f2 ne;
+        take(kr++, nx, ne);
         if (CURV) {
           fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2; fp2 = nx;
+          em2 = em1; em1 = e0; e0 = ep1; ep1 = ep2; ep2 = ne;
           dxm1 = dx0; dym1 = dy0; dx0 = dxp1; dy0 = dyp1;
+          xd0 = xp1; yd0 = yp1;
         } else {
           fm1 = f0; f0 = fp1; fp1 = nx;
+          em1 = e0; e0 = ep1; ep1 = ne;
         }
       }
     }
@@ -944,7 +1005,7 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
 //   S  source values        rows -8 .. SH+8, cols -8 .. FW+8 (NaN outside the window)
 //   E  filled values        rows -4 .. SH+4, cols -4 .. FW+4
 //   D  first derivatives    rows -2 .. SH+2, cols -2 .. FW+2 (curvature only)
-// for each half (FW columns) of the unit.
+// for each quarter (FW columns) of the unit.
 constexpr int XS_R = SH + 16, XS_C = FW + 16;  // 80 x 46
 constexpr int XE_R = SH + 8, XE_C = FW + 8;    // 72 x 38
 constexpr int XD_R = SH + 4, XD_C = FW + 4;    // 68 x 34
@@ -985,12 +1046,12 @@ __global__ void __launch_bounds__(XNT) stencil_fixup_kernel(const __grid_constan
   const bool hn = A.has_nodata != 0;
   const float qnan = __int_as_float(0x7fc00000);
   const unsigned count = *A.fix_count;
-  for (unsigned it = blockIdx.x; it < 2 * count; it += gridDim.x) {
-    const unsigned e = A.fix_list[it >> 1];
+  for (unsigned it = blockIdx.x; it < NQ * count; it += gridDim.x) {
+    const unsigned e = A.fix_list[it / NQ];
     const bool edge = (e & FIX_EDGE) != 0;
     const UnitGeom g = unit_geom(A, (int)(e & ~FIX_EDGE));
     const FastTile& T = A.tiles[g.t];
-    const int x0 = g.x0 + (int)(it & 1) * FW, y0 = g.y0, y1 = g.y1, xo = min(x0 + FW, g.xo);
+    const int x0 = g.x0 + (int)(it % NQ) * FW, y0 = g.y0, y1 = g.y1, xo = min(x0 + FW, g.xo);
     if (x0 >= xo) continue;
     // (a) source region, NoData -> NaN, outside the window -> NaN (never read)
     for (int i = tid; i < XS_R * XS_C; i += XNT) {
@@ -1390,13 +1451,13 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
     std::copy(A.planes, A.planes + FSG_STENCIL_NOUT, F.planes);
     int fper = 0;
     FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fper, fast, 256, 0));
-    const int fgrid = std::min((units + 7) / 8, di.sms * std::max(1, fper));
+    const int fgrid = std::min((units + 7) / 8, di.sms * std::max(1, fper));  // one unit per warp
     fast<<<fgrid, 256, 0, s>>>(F);
     FSG_LAUNCHED(1);
     FSG_CUDA(cudaFuncSetAttribute(fixup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FIX_SMEM));
     int xper = 0;
     FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&xper, fixup, XNT, FIX_SMEM));
-    const int xgrid = std::min(2 * units, di.sms * std::max(1, xper));
+    const int xgrid = std::min(NQ * units, di.sms * std::max(1, xper));
     fixup<<<xgrid, XNT, FIX_SMEM, s>>>(F);
     FSG_LAUNCHED(1);
     return FSG_OK;
