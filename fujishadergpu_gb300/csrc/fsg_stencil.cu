@@ -561,16 +561,19 @@ struct FastArgs {
   int slope_unit;
   const FastTile* tiles;
   int ntiles, total_units;
-  unsigned* fix_list;   // units for the fix-up pass: index | FIX_EDGE when the unit touches a window edge
+  unsigned* fix_list;   // unit quarters for the fix-up pass: unit | quarter << 28 | FIX_EDGE (touches a window edge)
   unsigned* fix_count;  // number of entries in fix_list
   FF gw[5];                   // Gaussian fill weights (float-float)
   PlaneK planes[FSG_STENCIL_NOUT];
 };
 
-constexpr unsigned FIX_EDGE = 0x80000000u;
-__device__ __forceinline__ void push_fix(const FastArgs& A, int u, bool edge) {
-  const unsigned i = atomicAdd(A.fix_count, 1u);
-  A.fix_list[i] = (unsigned)u | (edge ? FIX_EDGE : 0u);
+constexpr unsigned FIX_EDGE = 0x80000000u, FIX_QSHIFT = 28, FIX_UNIT = (1u << FIX_QSHIFT) - 1u;
+// queue the quarters of unit u whose bit is set in qmask (entry = unit | quarter << 28 | edge flag)
+__device__ __forceinline__ void push_fix(const FastArgs& A, int u, bool edge, unsigned qmask) {
+  const unsigned n = __popc(qmask);
+  unsigned i = atomicAdd(A.fix_count, n);
+  for (unsigned q = 0; q < NQ; ++q)
+    if ((qmask >> q) & 1u) A.fix_list[i++] = (unsigned)u | (q << FIX_QSHIFT) | (edge ? FIX_EDGE : 0u);
 }
 
 
@@ -773,7 +776,7 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
     // the window, so every derivative is a central difference
     const bool interior = y0 - 2 >= TG.wy0 && y1 + 2 <= TG.wy1 && x0 - 2 >= TG.wx0 && xo + 2 <= TG.wx1;
     if (!interior) {
-      if (lane == 0) push_fix(A, u, true);
+      if (lane == 0) push_fix(A, u, true, (1u << NQ) - 1u);
       continue;
     }
     // the tile's constants as values: the plane stores below could alias the
@@ -989,7 +992,13 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
         }
       }
     }
-    if (__ballot_sync(0xffffffffu, bad) && lane == 0) push_fix(A, u, false);
+    // quarters (eight lanes each) holding a pixel whose stencil reached NoData
+    const unsigned bb = __ballot_sync(0xffffffffu, bad);
+    if (bb && lane == 0) {
+      unsigned qm = 0;
+      for (unsigned qq = 0; qq < NQ; ++qq) qm |= ((bb >> (8 * qq)) & 0xffu) ? (1u << qq) : 0u;
+      push_fix(A, u, false, qm);
+    }
   }
   cp_async_wait<0>();
 }
@@ -1046,12 +1055,12 @@ __global__ void __launch_bounds__(XNT) stencil_fixup_kernel(const __grid_constan
   const bool hn = A.has_nodata != 0;
   const float qnan = __int_as_float(0x7fc00000);
   const unsigned count = *A.fix_count;
-  for (unsigned it = blockIdx.x; it < NQ * count; it += gridDim.x) {
-    const unsigned e = A.fix_list[it / NQ];
+  for (unsigned it = blockIdx.x; it < count; it += gridDim.x) {
+    const unsigned e = A.fix_list[it];
     const bool edge = (e & FIX_EDGE) != 0;
-    const UnitGeom g = unit_geom(A, (int)(e & ~FIX_EDGE));
+    const UnitGeom g = unit_geom(A, (int)(e & FIX_UNIT));
     const FastTile& T = A.tiles[g.t];
-    const int x0 = g.x0 + (int)(it % NQ) * FW, y0 = g.y0, y1 = g.y1, xo = min(x0 + FW, g.xo);
+    const int x0 = g.x0 + (int)((e >> FIX_QSHIFT) & (NQ - 1)) * FW, y0 = g.y0, y1 = g.y1, xo = min(x0 + FW, g.xo);
     if (x0 >= xo) continue;
     // (a) source region, NoData -> NaN, outside the window -> NaN (never read)
     for (int i = tid; i < XS_R * XS_C; i += XNT) {
@@ -1428,7 +1437,8 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
     }
     StreamScratch fscr;
     const size_t tiles_bytes = (sizeof(FastTile) * ft.size() + 255) & ~(size_t)255;
-    st = fscr.alloc(tiles_bytes + sizeof(unsigned) * ((size_t)units + 1), s);
+    if ((unsigned)units > FIX_UNIT) return fail(FSG_ERR_UNSUPPORTED, "%d stencil units exceed the fix-up list's index range", units);
+    st = fscr.alloc(tiles_bytes + sizeof(unsigned) * ((size_t)NQ * units + 1), s);
     if (st) return st;
     unsigned* fix = reinterpret_cast<unsigned*>(static_cast<unsigned char*>(fscr.ptr) + tiles_bytes);
     FSG_CUDA(cudaMemcpyAsync(fscr.ptr, ft.data(), sizeof(FastTile) * ft.size(), cudaMemcpyHostToDevice, s));
