@@ -1021,7 +1021,7 @@ constexpr int XD_R = SH + 4, XD_C = FW + 4;    // 68 x 34
 constexpr int XNT = 256;
 constexpr size_t FIX_SMEM = sizeof(float) * (XS_R * XS_C + XE_R * XE_C) +
                             sizeof(float) * 2 * XE_R * XS_C +            // axis-0 sums (aliases D)
-                            sizeof(unsigned long long) * 4 * XE_R;        // row bitmasks
+                            sizeof(unsigned long long) * 5 * XE_R;        // row bitmasks
 static_assert(2 * XD_R * XD_C <= 2 * XE_R * XS_C, "derivative planes alias the axis-0 sums");
 static_assert(XE_C <= 64 && XS_C <= 64, "row bitmasks are 64 bits");
 
@@ -1036,7 +1036,7 @@ __device__ __forceinline__ float deriv_d(const Axis& a, int k, int lo, int hi, F
 }
 
 template <unsigned OM, bool ALLF32>
-__global__ void __launch_bounds__(XNT) stencil_fixup_kernel(const __grid_constant__ FastArgs A) {
+__global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_constant__ FastArgs A) {
   constexpr bool CURV = (OM & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) |
                                (1u << FSG_OUT_CURV_PLANFORM) | (1u << FSG_OUT_CURV_PROFILE))) != 0;
   constexpr bool DIV = (OM & ((1u << FSG_OUT_DX) | (1u << FSG_OUT_DY))) != 0;
@@ -1051,6 +1051,7 @@ __global__ void __launch_bounds__(XNT) stencil_fixup_kernel(const __grid_constan
   unsigned long long* NB = VO + XE_R;   // NoData cells inside the window
   unsigned long long* ND = NB + XE_R;   // cells to fill (E columns)
   unsigned long long* NV = ND + XE_R;   // axis-0 sums to form (S columns)
+  unsigned long long* AF = NV + XE_R;   // valid outputs whose stencil holds NoData (the fast pass's others stand)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const bool hn = A.has_nodata != 0;
   const float qnan = __int_as_float(0x7fc00000);
@@ -1113,6 +1114,14 @@ __global__ void __launch_bounds__(XNT) stencil_fixup_kernel(const __grid_constan
       const unsigned long long need = d & NB[tid];
       ND[tid] = need;
       any = need != 0;
+      // outputs whose stencil footprint (a (2K+1)^2 box) contains a NoData cell
+      constexpr int K = CURV ? 2 : 1;
+      unsigned long long nbr = 0;
+      for (int k = -K; k <= K; ++k)
+        if (tid + k >= 0 && tid + k < XE_R) nbr |= NB[tid + k];
+      unsigned long long dil = nbr;
+      for (int k = 1; k <= K; ++k) dil |= (nbr << k) | (nbr >> k);
+      AF[tid] = VO[tid] & dil;
     }
     if (__syncthreads_or(any)) {
       // (d) axis-0 sums needed by the axis-1 pass: S columns within 4 of a
@@ -1187,6 +1196,8 @@ __global__ void __launch_bounds__(XNT) stencil_fixup_kernel(const __grid_constan
       const int r = i / FW, c = i - (i / FW) * FW;
       const int gy = y0 + r, gx = x0 + c;
       if (gy >= y1 || gx >= xo) continue;
+      // an interior unit's other pixels keep the fast pass's values (no NoData in their stencil)
+      if (!edge && !((AF[r + 4] >> (c + 4)) & 1ull)) continue;
       float o[FSG_STENCIL_NOUT];
       const float z0 = Sv[(r + 8) * XS_C + c + 8];
       if (z0 == z0) {
