@@ -103,6 +103,8 @@ _SIGNATURES = {
     "fsg_version": (C.c_char_p, []),
     "fsg_last_error": (C.c_char_p, []),
     "fsg_launch_count": (C.c_int64, []),
+    "fsg_timing_begin": (C.c_int, [C.c_int32]),
+    "fsg_timing_end": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "fsg_nodata_mask": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                   C.c_void_p, C.c_int64, C.c_void_p]),
     "fsg_stencil": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
@@ -200,3 +202,24 @@ def check(status: int) -> None:
 
 def launch_count() -> int:
     return int(lib().fsg_launch_count())
+
+
+class kernel_timer:
+    """Context manager timing the dominant kernel of each library call (CUDA events
+    recorded by the library around those launches); ``.ms`` = summed kernel time,
+    ``.launches`` = number of timed launches."""
+
+    def __init__(self, max_launches: int = 4096):
+        self.max_launches = int(max_launches)
+        self.ms = 0.0
+        self.launches = 0
+
+    def __enter__(self):
+        check(lib().fsg_timing_begin(self.max_launches))
+        return self
+
+    def __exit__(self, *exc):
+        tot, n = C.c_double(0.0), C.c_int32(0)
+        check(lib().fsg_timing_end(C.byref(tot), C.byref(n)))
+        self.ms, self.launches = float(tot.value), int(n.value)
+        return False

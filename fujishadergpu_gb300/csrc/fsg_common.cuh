@@ -18,6 +18,9 @@ void set_error(const char* fmt, ...);
 int fail(int code, const char* fmt, ...);
 int cuda_fail(cudaError_t e, const char* what);
 void count_launches(int64_t n);
+// Records a CUDA event on s around a marked kernel (start before the launch,
+// end after it) while fsg_timing_begin is active; no-op otherwise.
+void timing_mark(cudaStream_t s, bool start);
 
 #define FSG_CUDA(call)                                      \
   do {                                                      \

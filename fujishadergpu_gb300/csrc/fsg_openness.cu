@@ -403,7 +403,9 @@ extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_
   int per_sm = 0;
   FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BX * BY, smem));
   int grid = std::min(total, di.sms * std::max(1, per_sm));
+  timing_mark(s, true);
   kern<<<grid, dim3(BX, BY), smem, s>>>(A);
+  timing_mark(s, false);
   FSG_LAUNCHED(1);
   return FSG_OK;
 }

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "fsg_common.cuh"
 
@@ -15,7 +16,20 @@ thread_local std::string g_last_error;
 std::atomic<int64_t> g_launches{0};
 std::mutex g_dev_mutex;
 DeviceInfo g_dev_cache[64];
+// device-side timing of marked kernels (fsg_timing_begin / fsg_timing_end)
+std::mutex g_tmu;
+std::atomic<bool> g_timing{false};
+std::vector<cudaEvent_t> g_tev;
+int g_tn = 0;
 }  // namespace
+
+void timing_mark(cudaStream_t s, bool start) {
+  if (!g_timing.load(std::memory_order_relaxed)) return;
+  std::lock_guard<std::mutex> lk(g_tmu);
+  const int n = (int)g_tev.size();
+  if (start ? (g_tn % 2 != 0 || g_tn + 2 > n) : (g_tn % 2 != 1)) return;
+  if (cudaEventRecord(g_tev[g_tn], s) == cudaSuccess) ++g_tn;
+}
 
 void set_error(const char* fmt, ...) {
   char buf[1024];
@@ -83,6 +97,37 @@ const char* fsg_version(void) { return "fsg-gb300 0.1.0 (sm_103a)"; }
 const char* fsg_last_error(void) { return fsg::g_last_error.c_str(); }
 
 int64_t fsg_launch_count(void) { return fsg::g_launches.load(); }
+
+int fsg_timing_begin(int32_t max_launches) {
+  using namespace fsg;
+  if (max_launches < 1 || max_launches > 1 << 16) return fail(FSG_ERR_INVALID, "max_launches %d", max_launches);
+  std::lock_guard<std::mutex> lk(g_tmu);
+  for (cudaEvent_t e : g_tev) cudaEventDestroy(e);
+  g_tev.assign((size_t)2 * max_launches, nullptr);
+  for (auto& e : g_tev) FSG_CUDA(cudaEventCreate(&e));
+  g_tn = 0;
+  g_timing.store(true);
+  return FSG_OK;
+}
+
+int fsg_timing_end(double* total_ms, int32_t* launches) {
+  using namespace fsg;
+  if (!total_ms || !launches) return fail(FSG_ERR_INVALID, "null argument");
+  g_timing.store(false);
+  std::lock_guard<std::mutex> lk(g_tmu);
+  double tot = 0.0;
+  const int pairs = g_tn / 2;
+  for (int i = 0; i < pairs; ++i) {
+    FSG_CUDA(cudaEventSynchronize(g_tev[2 * i + 1]));
+    float ms = 0.f;
+    FSG_CUDA(cudaEventElapsedTime(&ms, g_tev[2 * i], g_tev[2 * i + 1]));
+    tot += ms;
+  }
+  *total_ms = tot;
+  *launches = pairs;
+  g_tn = 0;
+  return FSG_OK;
+}
 
 int fsg_nodata_mask(const float* raster_dev, int64_t ld, int32_t h, int32_t w, double nodata,
                     int32_t has_nodata, uint8_t* mask_dev, int64_t mask_ld, void* stream) {

@@ -1473,7 +1473,9 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
     int fper = 0;
     FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fper, fast, 256, 0));
     const int fgrid = std::min((units + 7) / 8, di.sms * std::max(1, fper));  // one unit per warp
+    timing_mark(s, true);
     fast<<<fgrid, 256, 0, s>>>(F);
+    timing_mark(s, false);
     FSG_LAUNCHED(1);
     FSG_CUDA(cudaFuncSetAttribute(fixup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FIX_SMEM));
     int xper = 0;

@@ -346,23 +346,44 @@ __global__ void field_accum(AView mean, float w, int first, AView field) {
 }
 
 // Overview decimation: NaN-aware mean of the source pixels whose centres fall
-// in each output cell (an exact f x f block mean for integer factors).
+// in each output cell (an exact f x f block mean for integer factors).  The
+// sum is float-float (about 48 significant bits; GB300's FP64 rate is a small
+// fraction of its FP32 rate) in four independent chains, the mean formed in
+// double once per cell.
 __global__ void overview_kernel(ZView z, AView out) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= out.h || j >= out.w) return;
-  long long ya = ((long long)i * z.h) / out.h, yb = ((long long)(i + 1) * z.h) / out.h;
-  long long xa = ((long long)j * z.w) / out.w, xb = ((long long)(j + 1) * z.w) / out.w;
-  double tot = 0.0;
-  long long cnt = 0;
-  for (long long y = ya; y < yb; ++y)
-    for (long long x = xa; x < xb; ++x) {
-      float v = z.at((int)y, (int)x);
-      if (v == v) {
-        tot += v;
+  const int ya = (int)(((long long)i * z.h) / out.h), yb = (int)(((long long)(i + 1) * z.h) / out.h);
+  const int xa = (int)(((long long)j * z.w) / out.w), xb = (int)(((long long)(j + 1) * z.w) / out.w);
+  FF acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  int cnt = 0;
+  for (int y = ya; y < yb; ++y) {
+    const float* row = z.p + (long long)y * z.ld;
+    int x = xa;
+    for (; x + 3 < xb; x += 4) {
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const float v = __ldg(row + x + m);
+        if (!is_nodata(v, z.ndf, z.has_nodata != 0)) {
+          const FF t = two_sum(acc[m].hi, v);
+          acc[m] = {t.hi, __fadd_rn(acc[m].lo, t.lo)};
+          ++cnt;
+        }
+      }
+    }
+    for (; x < xb; ++x) {
+      const float v = __ldg(row + x);
+      if (!is_nodata(v, z.ndf, z.has_nodata != 0)) {
+        const FF t = two_sum(acc[0].hi, v);
+        acc[0] = {t.hi, __fadd_rn(acc[0].lo, t.lo)};
         ++cnt;
       }
     }
+  }
+  double tot = 0.0;
+#pragma unroll
+  for (int m = 0; m < 4; ++m) tot += (double)acc[m].hi + (double)acc[m].lo;
   out.ref(i, j) = cnt ? (float)(tot / (double)cnt) : kQNaN;
 }
 
@@ -690,23 +711,45 @@ typedef unsigned long long u64;
 __global__ void window_absmax(const TopoTileK* tiles, unsigned* zmax) {
   const TopoTileK& T = tiles[blockIdx.y];
   const ZView& z = T.z;
-  float m = 0.f;
+  float m[4] = {0.f, 0.f, 0.f, 0.f};
   for (int y = blockIdx.x; y < z.h; y += gridDim.x) {
     const float* row = z.p + (long long)y * z.ld;
-#pragma unroll 4
-    for (int x = threadIdx.x; x < z.w; x += blockDim.x) {
+    // scalar head up to a 16-byte boundary, float4 body, scalar tail
+    const int head = min(z.w, (int)((16 - ((uintptr_t)row & 15)) & 15) / 4);
+    const int nv = (z.w - head) / 4;
+    for (int x = threadIdx.x; x < head; x += blockDim.x) {
       const float v = __ldg(row + x);
-      if (!is_nodata(v, z.ndf, z.has_nodata != 0)) m = fmaxf(m, fabsf(v));
+      if (!is_nodata(v, z.ndf, z.has_nodata != 0)) m[0] = fmaxf(m[0], fabsf(v));
+    }
+    if (((uintptr_t)row & 3) == 0) {
+      const float4* r4 = reinterpret_cast<const float4*>(row + head);
+      for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+        const float4 v = __ldg(r4 + k);
+        const float e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (!is_nodata(e[q], z.ndf, z.has_nodata != 0)) m[q] = fmaxf(m[q], fabsf(e[q]));
+      }
+    } else {
+      for (int x = head + threadIdx.x; x < head + 4 * nv; x += blockDim.x) {
+        const float v = __ldg(row + x);
+        if (!is_nodata(v, z.ndf, z.has_nodata != 0)) m[1] = fmaxf(m[1], fabsf(v));
+      }
+    }
+    for (int x = head + 4 * nv + threadIdx.x; x < z.w; x += blockDim.x) {
+      const float v = __ldg(row + x);
+      if (!is_nodata(v, z.ndf, z.has_nodata != 0)) m[2] = fmaxf(m[2], fabsf(v));
     }
   }
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  float mm = fmaxf(fmaxf(m[0], m[1]), fmaxf(m[2], m[3]));
+  for (int o = 16; o > 0; o >>= 1) mm = fmaxf(mm, __shfl_xor_sync(0xffffffffu, mm, o));
   __shared__ float wm[32];
-  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = mm;
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, wm[w]);
-    m = fmaxf(m, wm[0]);
-    if (isfinite(m)) atomicMax(zmax, __float_as_uint(m));
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) mm = fmaxf(mm, wm[w]);
+    mm = fmaxf(mm, wm[0]);
+    if (isfinite(mm)) atomicMax(zmax, __float_as_uint(mm));
   }
 }
 
@@ -1503,7 +1546,9 @@ static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_til
     int per = 0;
     FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fk, FX_NT, fsmem));
     const int grid = std::min((int)items.size(), di.sms * std::max(1, per));
+    timing_mark(s, true);
     fk<<<grid, FX_NT, fsmem, s>>>(A);
+    timing_mark(s, false);
     FSG_LAUNCHED(1);
     return FSG_OK;
   }

@@ -78,6 +78,14 @@ const char* fsg_version(void);
 const char* fsg_last_error(void);
 /* Number of kernels launched by this library on the calling process (all devices). */
 int64_t fsg_launch_count(void);
+/* Device-side timing of the dominant kernel of each call (the fused stencil's
+ * streaming pass, the topousm_fast strip pass, the openness ray-march): between
+ * fsg_timing_begin and fsg_timing_end, up to max_launches such launches are
+ * bracketed by CUDA events on their stream; fsg_timing_end synchronises those
+ * events and returns the summed kernel time.  No reference counterpart
+ * (measurement support for the roofline figures). */
+int fsg_timing_begin(int32_t max_launches);
+int fsg_timing_end(double* total_ms, int32_t* launches);
 
 /* NoData mask (core/tile_processor.py:185-196): mask_dev[i] = 1 where
  * isnan(v) or (has_nodata and (|v - nodata| <= 1e-6 in float32, or v == nodata)). */
