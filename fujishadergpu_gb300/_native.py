@@ -109,10 +109,16 @@ _SIGNATURES = {
                                   C.c_void_p, C.c_int64, C.c_void_p]),
     "fsg_stencil": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
                               C.POINTER(StencilParams), C.POINTER(Plane), C.c_void_p]),
+    "fsg_stencil_plan": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
+                                   C.POINTER(StencilParams), C.POINTER(Plane), C.POINTER(C.c_void_p)]),
+    "fsg_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fsg_plan_destroy": (None, [C.c_void_p]),
     "fsg_stencil_host": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
                                    C.POINTER(StencilParams), C.POINTER(Plane), C.c_void_p]),
     "fsg_topousm": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
                               C.POINTER(TopoUSMParams), C.POINTER(Plane), C.c_void_p]),
+    "fsg_topousm_plan": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
+                                   C.POINTER(TopoUSMParams), C.POINTER(Plane), C.POINTER(C.c_void_p)]),
     "fsg_topousm_coarse_field": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                            C.POINTER(C.c_double), C.c_int32, C.c_double, C.c_void_p, C.c_int64,
                                            C.c_void_p]),
@@ -128,6 +134,9 @@ _SIGNATURES = {
                                          C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_void_p]),
     "fsg_openness": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
                                C.POINTER(OpennessParams), C.POINTER(Plane), C.c_void_p, C.c_int64, C.c_void_p]),
+    "fsg_openness_plan": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
+                                    C.POINTER(OpennessParams), C.POINTER(Plane), C.c_void_p, C.c_int64,
+                                    C.POINTER(C.c_void_p)]),
     "fsg_openness_offsets": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                        C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32]),
     "fsg_affine": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32,

@@ -11,6 +11,14 @@
 
 #include "fsg.h"
 
+// A prepared launch (fsg_plan in include/fsg.h): owns the device tables of one
+// entry point's call; launch() issues only kernels, memsets and device-side
+// copies, so it can be captured in a CUDA graph.
+struct fsg_plan {
+  virtual ~fsg_plan() {}
+  virtual int launch(cudaStream_t s) = 0;
+};
+
 namespace fsg {
 
 // ------------------------------------------------------------------ errors

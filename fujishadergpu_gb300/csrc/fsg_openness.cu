@@ -282,9 +282,44 @@ extern "C" int fsg_openness_offsets(int32_t num_directions, int32_t max_distance
   return FSG_OK;
 }
 
-extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+namespace fsg {
+// One openness job: the packed device tables (host image), the kernel
+// arguments and the launch shape.  The eager entry point uploads the image
+// into stream-ordered scratch; a plan uploads it once into memory it owns.
+struct OpenJob {
+  bool empty = true;
+  std::vector<char> host;
+  size_t o_s = 0, o_rb = 0, o_ts = 0, o_b0 = 0, o_t = 0, o_re = 0;
+  OpenArgs A;
+  void (*kern)(OpenArgs) = nullptr;
+  int grid = 0;
+  size_t smem = 0;
+  void bind(void* dev) {
+    char* base = static_cast<char*>(dev);
+    A.tile_reach = reinterpret_cast<const int*>(base + o_re);
+    A.samples = reinterpret_cast<const RaySample*>(base + o_s);
+    A.ray_begin = reinterpret_cast<const int*>(base + o_rb);
+    A.tile_sample0 = reinterpret_cast<const int*>(base + o_ts);
+    A.block0 = reinterpret_cast<const int*>(base + o_b0);
+    A.tiles = reinterpret_cast<const fsg_tile*>(base + o_t);
+  }
+  int upload(void* dev, cudaStream_t s) const {
+    FSG_CUDA(cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, s));
+    return FSG_OK;
+  }
+  int enqueue(cudaStream_t s) const {
+    if (empty) return FSG_OK;
+    timing_mark(s, true);
+    kern<<<grid, dim3(BX, BY), smem, s>>>(A);
+    timing_mark(s, false);
+    FSG_LAUNCHED(1);
+    return FSG_OK;
+  }
+};
+
+static int openness_prepare(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
                             const fsg_tile* tiles, int32_t ntiles, const fsg_openness_params* p,
-                            const fsg_plane* display, float* raw_deg_dev, int64_t raw_ld, void* stream) {
+                            const fsg_plane* display, float* raw_deg_dev, int64_t raw_ld, OpenJob& J) {
   if (!p || (ntiles > 0 && !tiles)) return fail(FSG_ERR_INVALID, "null argument");
   if (ntiles < 0 || raster_h < 0 || raster_w < 0 || ld < raster_w) return fail(FSG_ERR_INVALID, "bad raster shape");
   if ((!display || !display->ptr) && !raw_deg_dev) return fail(FSG_ERR_INVALID, "no output requested");
@@ -334,15 +369,16 @@ extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_
     block0.push_back(total);
     if (T.core_h > 0 && T.core_w > 0) total += ((T.core_w + PW - 1) / PW) * ((T.core_h + PH - 1) / PH);
   }
-  if (total == 0) return FSG_OK;
-  cudaStream_t s = (cudaStream_t)stream;
+  J.empty = total == 0;
+  if (J.empty) return FSG_OK;
   size_t b_samples = samples.size() * sizeof(RaySample), b_rb = ray_begin.size() * sizeof(int);
   size_t b_ts = tile_sample0.size() * sizeof(int), b_b0 = block0.size() * sizeof(int);
   size_t b_re = reach.size() * sizeof(int);
   size_t b_tiles = (size_t)ntiles * sizeof(fsg_tile);
   auto al = [](size_t n) { return (n + 255) & ~(size_t)255; };
   size_t bytes = al(b_samples) + al(b_rb) + al(b_ts) + al(b_b0) + al(b_tiles) + al(b_re);
-  std::vector<char> host(bytes);
+  std::vector<char>& host = J.host;
+  host.assign(bytes, 0);
   size_t off = 0;
   auto put = [&](const void* src, size_t n) {
     std::memcpy(host.data() + off, src, n);
@@ -350,15 +386,13 @@ extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_
     off += al(n);
     return o;
   };
-  size_t o_s = put(samples.data(), b_samples), o_rb = put(ray_begin.data(), b_rb);
-  size_t o_ts = put(tile_sample0.data(), b_ts), o_b0 = put(block0.data(), b_b0), o_t = put(tiles, b_tiles);
-  size_t o_re = put(reach.data(), b_re);
-  StreamScratch scratch;
-  st = scratch.alloc(bytes, s);
-  if (st) return st;
-  FSG_CUDA(cudaMemcpyAsync(scratch.ptr, host.data(), bytes, cudaMemcpyHostToDevice, s));
-  char* base = static_cast<char*>(scratch.ptr);
-  OpenArgs A;
+  J.o_s = put(samples.data(), b_samples);
+  J.o_rb = put(ray_begin.data(), b_rb);
+  J.o_ts = put(tile_sample0.data(), b_ts);
+  J.o_b0 = put(block0.data(), b_b0);
+  J.o_t = put(tiles, b_tiles);
+  J.o_re = put(reach.data(), b_re);
+  OpenArgs& A = J.A;
   std::memset(&A, 0, sizeof(A));
   A.raster = raster_dev;
   A.ld = ld;
@@ -369,12 +403,6 @@ extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_
   A.positive = p->openness_type == 0;
   A.ndir = ndir;
   A.ns = per_tile;
-  A.tile_reach = reinterpret_cast<const int*>(base + o_re);
-  A.samples = reinterpret_cast<const RaySample*>(base + o_s);
-  A.ray_begin = reinterpret_cast<const int*>(base + o_rb);
-  A.tile_sample0 = reinterpret_cast<const int*>(base + o_ts);
-  A.block0 = reinterpret_cast<const int*>(base + o_b0);
-  A.tiles = reinterpret_cast<const fsg_tile*>(base + o_t);
   A.ntiles = ntiles;
   A.total_blocks = total;
   A.lo = (float)p->stretch_lo;
@@ -402,10 +430,65 @@ extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_
   if (smem > 48 * 1024) FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BX * BY, smem));
-  int grid = std::min(total, di.sms * std::max(1, per_sm));
-  timing_mark(s, true);
-  kern<<<grid, dim3(BX, BY), smem, s>>>(A);
-  timing_mark(s, false);
-  FSG_LAUNCHED(1);
+  J.kern = kern;
+  J.smem = smem;
+  J.grid = std::min(total, di.sms * std::max(1, per_sm));
+  return FSG_OK;
+}
+
+struct OpenPlan final : fsg_plan {
+  OpenJob J;
+  void* dev = nullptr;
+  ~OpenPlan() override {
+    if (dev) cudaFree(dev);
+  }
+  int launch(cudaStream_t s) override { return J.enqueue(s); }
+};
+}  // namespace fsg
+
+extern "C" int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                            const fsg_tile* tiles, int32_t ntiles, const fsg_openness_params* p,
+                            const fsg_plane* display, float* raw_deg_dev, int64_t raw_ld, void* stream) {
+  using namespace fsg;
+  OpenJob J;
+  int st = openness_prepare(raster_dev, ld, raster_h, raster_w, tiles, ntiles, p, display, raw_deg_dev, raw_ld, J);
+  if (st || J.empty) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  StreamScratch scratch;
+  st = scratch.alloc(J.host.size(), s);
+  if (st) return st;
+  J.bind(scratch.ptr);
+  st = J.upload(scratch.ptr, s);
+  if (st) return st;
+  return J.enqueue(s);
+}
+
+extern "C" int fsg_openness_plan(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                                 const fsg_tile* tiles, int32_t ntiles, const fsg_openness_params* p,
+                                 const fsg_plane* display, float* raw_deg_dev, int64_t raw_ld, fsg_plan** plan) {
+  using namespace fsg;
+  if (!plan) return fail(FSG_ERR_INVALID, "null plan pointer");
+  *plan = nullptr;
+  OpenPlan* P = new OpenPlan();
+  int st = openness_prepare(raster_dev, ld, raster_h, raster_w, tiles, ntiles, p, display, raw_deg_dev, raw_ld, P->J);
+  if (!st && !P->J.empty) {
+    cudaError_t e = cudaMalloc(&P->dev, P->J.host.size());
+    if (e != cudaSuccess) {
+      P->dev = nullptr;
+      st = cuda_fail(e, "cudaMalloc(plan)");
+    } else {
+      P->J.bind(P->dev);
+      st = P->J.upload(P->dev, nullptr);
+      if (!st) {
+        e = cudaStreamSynchronize(nullptr);
+        if (e != cudaSuccess) st = cuda_fail(e, "plan upload");
+      }
+    }
+  }
+  if (st) {
+    delete P;
+    return st;
+  }
+  *plan = P;
   return FSG_OK;
 }

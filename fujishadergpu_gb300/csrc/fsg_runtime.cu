@@ -98,6 +98,13 @@ const char* fsg_last_error(void) { return fsg::g_last_error.c_str(); }
 
 int64_t fsg_launch_count(void) { return fsg::g_launches.load(); }
 
+int fsg_plan_launch(fsg_plan* plan, void* stream) {
+  if (!plan) return fsg::fail(FSG_ERR_INVALID, "null plan");
+  return plan->launch((cudaStream_t)stream);
+}
+
+void fsg_plan_destroy(fsg_plan* plan) { delete plan; }
+
 int fsg_timing_begin(int32_t max_launches) {
   using namespace fsg;
   if (max_launches < 1 || max_launches > 1 << 16) return fail(FSG_ERR_INVALID, "max_launches %d", max_launches);

@@ -1302,10 +1302,66 @@ int validate_tiles(int32_t raster_h, int32_t raster_w, const fsg_tile* tiles, in
 
 }  // namespace fsg
 
-extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+namespace fsg {
+// One fused-stencil job: every table and launch parameter, built on the host.
+// The eager entry point uploads the tables into stream-ordered scratch and
+// launches; a plan uploads them once into memory it owns, and each launch
+// then only issues a memset and kernels (capturable in a CUDA graph).
+struct StencilJob {
+  bool empty = true, fast = false;
+  StencilArgs A;
+  std::vector<TileK> tk;
+  void (*kern)(StencilArgs) = nullptr;
+  int grid = 0;
+  FastArgs F;
+  std::vector<FastTile> ft;
+  int units = 0, fgrid = 0, xgrid = 0;
+  void (*fastk)(FastArgs) = nullptr;
+  void (*fixk)(FastArgs) = nullptr;
+  size_t tiles_bytes() const {
+    return fast ? (sizeof(FastTile) * ft.size() + 255) & ~(size_t)255
+                : (tk.size() > (size_t)INLINE_TILES ? (sizeof(TileK) * tk.size() + 255) & ~(size_t)255 : 0);
+  }
+  size_t device_bytes() const { return tiles_bytes() + (fast ? sizeof(unsigned) * ((size_t)NQ * units + 1) : 0); }
+  // point the kernel arguments at the tables / fix-up list in `dev`
+  void bind(void* dev) {
+    if (fast) {
+      unsigned* fix = reinterpret_cast<unsigned*>(static_cast<unsigned char*>(dev) + tiles_bytes());
+      F.tiles = static_cast<const FastTile*>(dev);
+      F.fix_count = fix;
+      F.fix_list = fix + 1;
+    } else if (tk.size() > (size_t)INLINE_TILES) {
+      A.tiles_dev = static_cast<const TileK*>(dev);
+    }
+  }
+  int upload(void* dev, cudaStream_t s) const {
+    if (fast) FSG_CUDA(cudaMemcpyAsync(dev, ft.data(), sizeof(FastTile) * ft.size(), cudaMemcpyHostToDevice, s));
+    else if (tk.size() > (size_t)INLINE_TILES)
+      FSG_CUDA(cudaMemcpyAsync(dev, tk.data(), sizeof(TileK) * tk.size(), cudaMemcpyHostToDevice, s));
+    return FSG_OK;
+  }
+  // launches only (no host memory involved)
+  int enqueue(cudaStream_t s) const {
+    if (empty) return FSG_OK;
+    if (fast) {
+      FSG_CUDA(cudaMemsetAsync(F.fix_count, 0, sizeof(unsigned), s));
+      timing_mark(s, true);
+      fastk<<<fgrid, 256, 0, s>>>(F);
+      timing_mark(s, false);
+      FSG_LAUNCHED(1);
+      fixk<<<xgrid, XNT, FIX_SMEM, s>>>(F);
+      FSG_LAUNCHED(1);
+      return FSG_OK;
+    }
+    kern<<<grid, NT, SMEM_BYTES, s>>>(A);
+    FSG_LAUNCHED(1);
+    return FSG_OK;
+  }
+};
+
+static int stencil_prepare(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
                            const fsg_tile* tiles, int32_t ntiles, const fsg_stencil_params* params,
-                           const fsg_plane* planes, void* stream) {
-  using namespace fsg;
+                           const fsg_plane* planes, StencilJob& J) {
   if (!params || !planes || (ntiles > 0 && !tiles)) return fail(FSG_ERR_INVALID, "null argument");
   if (ntiles < 0 || raster_h < 0 || raster_w < 0) return fail(FSG_ERR_INVALID, "negative size");
   if (ld < raster_w) return fail(FSG_ERR_INVALID, "row pitch %lld < width %d", (long long)ld, raster_w);
@@ -1322,7 +1378,7 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
   int st = validate_tiles(raster_h, raster_w, tiles, ntiles, 3);
   if (st) return st;
 
-  StencilArgs A;
+  StencilArgs& A = J.A;
   std::memset(&A, 0, sizeof(A));
   A.raster = raster_dev;
   A.ld = ld;
@@ -1352,7 +1408,8 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
     A.planes[o].qmin = planes[o].q_min;
     A.planes[o].qmax = planes[o].q_max;
   }
-  std::vector<TileK> tk;
+  std::vector<TileK>& tk = J.tk;
+  tk.clear();
   tk.reserve(ntiles);
   int total = 0;
   for (int t = 0; t < ntiles; ++t) {
@@ -1383,25 +1440,17 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
     k.sign_y = s.pixel_scale_y >= 0.0 ? 1.0f : -1.0f;
     tk.push_back(k);
   }
-  if (total == 0) return FSG_OK;
+  J.empty = total == 0;
+  if (J.empty) return FSG_OK;
   A.ntiles = (int)tk.size();
   A.total_blocks = total;
-  cudaStream_t s = (cudaStream_t)stream;
-  StreamScratch scratch;
-  if (A.ntiles <= INLINE_TILES) {
-    std::copy(tk.begin(), tk.end(), A.inl);
-  } else {
-    st = scratch.alloc(sizeof(TileK) * tk.size(), s);
-    if (st) return st;
-    FSG_CUDA(cudaMemcpyAsync(scratch.ptr, tk.data(), sizeof(TileK) * tk.size(), cudaMemcpyHostToDevice, s));
-    A.tiles_dev = static_cast<const TileK*>(scratch.ptr);
-  }
+  if (A.ntiles <= INLINE_TILES) std::copy(tk.begin(), tk.end(), A.inl);
   DeviceInfo di;
   st = device_info(&di);
   if (st) return st;
   const bool curv = (outmask & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) |
                                 (1u << FSG_OUT_CURV_PLANFORM) | (1u << FSG_OUT_CURV_PROFILE))) != 0;
-  auto kern = curv ? stencil_kernel<true, 0u> : stencil_kernel<false, 0u>;
+  J.kern = curv ? stencil_kernel<true, 0u> : stencil_kernel<false, 0u>;
   void (*fast)(FastArgs) = nullptr;
   void (*fixup)(FastArgs) = nullptr;
   constexpr unsigned HS = 1u << FSG_OUT_HILLSHADE, SL = 1u << FSG_OUT_SLOPE, CM = 1u << FSG_OUT_CURV_MEAN,
@@ -1429,9 +1478,10 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
 #undef FSG_CASE
     default: break;
   }
-  if (fast) {
-    // fast streaming pass over every tile, then the exact fix-up of the units it flagged
-    std::vector<FastTile> ft;
+  J.fast = fast != nullptr;
+  if (J.fast) {
+    // fast streaming pass over every tile, then the exact fix-up of the quarters it flagged
+    J.ft.clear();
     int units = 0;
     for (const TileK& k : tk) {
       FastTile f;
@@ -1444,17 +1494,10 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
       units += f.nstrip * ((ch + SH - 1) / SH);
       f.g1x = k.g1x; f.g1y = k.g1y; f.c2x = k.c2x; f.c2y = k.c2y;
       f.sx = k.sign_x; f.sy = k.sign_y;
-      ft.push_back(f);
+      J.ft.push_back(f);
     }
-    StreamScratch fscr;
-    const size_t tiles_bytes = (sizeof(FastTile) * ft.size() + 255) & ~(size_t)255;
     if ((unsigned)units > FIX_UNIT) return fail(FSG_ERR_UNSUPPORTED, "%d stencil units exceed the fix-up list's index range", units);
-    st = fscr.alloc(tiles_bytes + sizeof(unsigned) * ((size_t)NQ * units + 1), s);
-    if (st) return st;
-    unsigned* fix = reinterpret_cast<unsigned*>(static_cast<unsigned char*>(fscr.ptr) + tiles_bytes);
-    FSG_CUDA(cudaMemcpyAsync(fscr.ptr, ft.data(), sizeof(FastTile) * ft.size(), cudaMemcpyHostToDevice, s));
-    FSG_CUDA(cudaMemsetAsync(fix, 0, sizeof(unsigned), s));
-    FastArgs F;
+    FastArgs& F = J.F;
     std::memset(&F, 0, sizeof(F));
     F.raster = A.raster;
     F.ld = A.ld;
@@ -1463,35 +1506,89 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
     F.ndf = A.ndf;
     F.has_nodata = A.has_nodata;
     F.slope_unit = A.slope_unit;
-    F.tiles = static_cast<const FastTile*>(fscr.ptr);
-    F.ntiles = (int)ft.size();
+    F.ntiles = (int)J.ft.size();
     F.total_units = units;
-    F.fix_count = fix;
-    F.fix_list = fix + 1;
     for (int j = 0; j < 5; ++j) F.gw[j] = {A.gw_hi[j], A.gw_lo[j]};
     std::copy(A.planes, A.planes + FSG_STENCIL_NOUT, F.planes);
+    J.units = units;
+    J.fastk = fast;
+    J.fixk = fixup;
     int fper = 0;
     FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fper, fast, 256, 0));
-    const int fgrid = std::min((units + 7) / 8, di.sms * std::max(1, fper));  // one unit per warp
-    timing_mark(s, true);
-    fast<<<fgrid, 256, 0, s>>>(F);
-    timing_mark(s, false);
-    FSG_LAUNCHED(1);
+    J.fgrid = std::min((units + 7) / 8, di.sms * std::max(1, fper));  // one unit per warp
     FSG_CUDA(cudaFuncSetAttribute(fixup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FIX_SMEM));
     int xper = 0;
     FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&xper, fixup, XNT, FIX_SMEM));
-    const int xgrid = std::min(NQ * units, di.sms * std::max(1, xper));
-    fixup<<<xgrid, XNT, FIX_SMEM, s>>>(F);
-    FSG_LAUNCHED(1);
+    J.xgrid = std::min(NQ * units, di.sms * std::max(1, xper));
     return FSG_OK;
   }
-  FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
-  FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  FSG_CUDA(cudaFuncSetAttribute(J.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+  FSG_CUDA(cudaFuncSetAttribute(J.kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int per_sm = 0;
-  FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, SMEM_BYTES));
+  FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, J.kern, NT, SMEM_BYTES));
   if (per_sm < 1) per_sm = 1;
-  int grid = std::min(total, di.sms * per_sm);
-  kern<<<grid, NT, SMEM_BYTES, s>>>(A);
-  FSG_LAUNCHED(1);
+  J.grid = std::min(total, di.sms * per_sm);
+  return FSG_OK;
+}
+
+// A prepared fused-stencil launch over fixed buffers and tiles.
+struct StencilPlan final : fsg_plan {
+  StencilJob J;
+  void* dev = nullptr;
+  ~StencilPlan() override {
+    if (dev) cudaFree(dev);
+  }
+  int launch(cudaStream_t s) override { return J.enqueue(s); }
+};
+}  // namespace fsg
+
+extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                           const fsg_tile* tiles, int32_t ntiles, const fsg_stencil_params* params,
+                           const fsg_plane* planes, void* stream) {
+  using namespace fsg;
+  StencilJob J;
+  int st = stencil_prepare(raster_dev, ld, raster_h, raster_w, tiles, ntiles, params, planes, J);
+  if (st || J.empty) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  StreamScratch scratch;
+  const size_t bytes = J.device_bytes();
+  if (bytes) {
+    st = scratch.alloc(bytes, s);
+    if (st) return st;
+    J.bind(scratch.ptr);
+    st = J.upload(scratch.ptr, s);
+    if (st) return st;
+  }
+  return J.enqueue(s);
+}
+
+extern "C" int fsg_stencil_plan(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                                const fsg_tile* tiles, int32_t ntiles, const fsg_stencil_params* params,
+                                const fsg_plane* planes, fsg_plan** plan) {
+  using namespace fsg;
+  if (!plan) return fail(FSG_ERR_INVALID, "null plan pointer");
+  *plan = nullptr;
+  StencilPlan* P = new StencilPlan();
+  int st = stencil_prepare(raster_dev, ld, raster_h, raster_w, tiles, ntiles, params, planes, P->J);
+  const size_t bytes = st ? 0 : P->J.device_bytes();
+  if (!st && bytes) {
+    cudaError_t e = cudaMalloc(&P->dev, bytes);
+    if (e != cudaSuccess) {
+      P->dev = nullptr;
+      st = cuda_fail(e, "cudaMalloc(plan)");
+    } else {
+      P->J.bind(P->dev);
+      st = P->J.upload(P->dev, nullptr);
+      if (!st) {
+        e = cudaStreamSynchronize(nullptr);
+        if (e != cudaSuccess) st = cuda_fail(e, "plan upload");
+      }
+    }
+  }
+  if (st) {
+    delete P;
+    return st;
+  }
+  *plan = P;
   return FSG_OK;
 }

@@ -1323,36 +1323,6 @@ static bool strip_path_ok(const std::vector<int>& radii, double pixel_size, int*
   return true;
 }
 
-// Coarse mean of one decimated radius of a window (the f > 1 branch of
-// topousm_window up to, not including, the zoom), into `ms` (hs x ws).
-static int decimated_mean(const ZView& z, int r, int f, TopoScratch& S, float* ms, cudaStream_t s) {
-  const int hs = std::max(1, (z.h + f - 1) / f), ws = std::max(1, (z.w + f - 1) / f);
-  AView small = resize(S.small, hs, ws);
-  FSG_CUDA(cudaMemsetAsync(S.flag, 0, sizeof(int), s));
-  Grid2 gd = grid2d(hs, ws);
-  downsample_kernel<<<gd.g, gd.b, 0, s>>>(z, f, small, S.flag);
-  FSG_LAUNCHED(1);
-  double sigma = std::max(1.0, (double)std::min(hs, ws) / 64.0);
-  int R;
-  std::vector<float> gw = gaussian_weights(sigma, &R);
-  if (R + 1 > 4096) return fail(FSG_ERR_UNSUPPORTED, "void-fill Gaussian radius %d too large", R);
-  int st = upload(S.gv, gw, s);
-  if (st) return st;
-  RowArgs ra;
-  std::memset(&ra, 0, sizeof(ra));
-  ra.mode = ROW_PAIR;
-  ra.out = resize(S.ssv, hs, ws);
-  ra.out2 = resize(S.ssw, hs, ws);
-  ra.run_if = S.flag;
-  st = launch_gauss(small, S.gv, R, 1, resize(S.svm, hs, ws), resize(S.swm, hs, ws), ra, s);
-  if (st) return st;
-  voidfill_combine<<<gd.g, gd.b, 0, s>>>(small, resize(S.ssv, hs, ws), resize(S.ssw, hs, ws), S.flag);
-  FSG_LAUNCHED(1);
-  const int rs = std::max(1, (int)std::nearbyint((double)r / f));
-  AView out{ms, ws, hs, ws};
-  return mean_for_radius(small, rs, S, out, s);
-}
-
 // Streams on which the per-window decimation pipelines of one call run side
 // by side (each window's pipeline is a chain of small launches); created once
 // per device, joined back into the caller's stream with events.
@@ -1382,26 +1352,132 @@ static int aux_streams(AuxStreams** out) {
   return FSG_OK;
 }
 
-static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_tile* tiles, int32_t ntiles,
-                              const fsg_topousm_params* p, const fsg_plane* out, int nfull, cudaStream_t s) {
+// Coarse mean of one decimated radius of a window with its void-fill weights
+// already on the device (gv, radius R): the launches of decimated_mean only.
+static int decimated_mean_dev(const ZView& z, int r, int f, TopoScratch& S, const float* gv, int R, float* ms,
+                              cudaStream_t s) {
+  const int hs = std::max(1, (z.h + f - 1) / f), ws = std::max(1, (z.w + f - 1) / f);
+  AView small = resize(S.small, hs, ws);
+  FSG_CUDA(cudaMemsetAsync(S.flag, 0, sizeof(int), s));
+  Grid2 gd = grid2d(hs, ws);
+  downsample_kernel<<<gd.g, gd.b, 0, s>>>(z, f, small, S.flag);
+  FSG_LAUNCHED(1);
+  RowArgs ra;
+  std::memset(&ra, 0, sizeof(ra));
+  ra.mode = ROW_PAIR;
+  ra.out = resize(S.ssv, hs, ws);
+  ra.out2 = resize(S.ssw, hs, ws);
+  ra.run_if = S.flag;
+  int st = launch_gauss(small, gv, R, 1, resize(S.svm, hs, ws), resize(S.swm, hs, ws), ra, s);
+  if (st) return st;
+  voidfill_combine<<<gd.g, gd.b, 0, s>>>(small, resize(S.ssv, hs, ws), resize(S.ssw, hs, ws), S.flag);
+  FSG_LAUNCHED(1);
+  const int rs = std::max(1, (int)std::nearbyint((double)r / f));
+  AView out{ms, ws, hs, ws};
+  return mean_for_radius(small, rs, S, out, s);
+}
+
+// One topousm_fast strip-path job: host images of every device table (tile
+// descriptors, strip items, Gaussian weight tables), the layout of its device
+// buffer and the launch parameters.  The eager entry point uploads the images
+// into stream-ordered scratch; a plan uploads them once into memory it owns.
+// enqueue() issues only launches, memsets and event fork/join of the
+// per-window decimation pipelines on the auxiliary streams (capturable).
+struct TopoJob {
+  bool empty = true, fixed = false;
+  int ntiles = 0, nfull = 0, NS = 0, maxh = 1, maxw = 1, grid = 0;
+  std::vector<TopoTileK> tk;
+  std::vector<StripItem> items;
+  struct DecWork {
+    int t, r, f, R;
+    size_t ms_off, gv_off;  // bytes from the dec area / floats into the weight table
+  };
+  std::vector<DecWork> work;
+  std::vector<float> gv, g1;
+  std::vector<size_t> dec_ms;  // per (tile, dec), tile-major: byte offset of its coarse mean in the dec area
+  size_t one_small = 0, topo_bytes = 0, dec_bytes = 0, g1_off = 0, gv_off = 0, tiles_off = 0, items_off = 0,
+         flags_off = 0, total = 0;
+  StripArgs A;
+  void (*kern)(StripArgs) = nullptr;
+  size_t smem = 0;
+  // bound device state
+  char* base = nullptr;
+  TopoScratch SS[AUX_STREAMS];
+  AuxStreams* aux = nullptr;
+
+  void bind(void* dev) {
+    base = static_cast<char*>(dev);
+    float* g1d = reinterpret_cast<float*>(base + g1_off);
+    for (int i = 0; i < NS; ++i) {
+      SS[i].carve_small(base + (size_t)i * one_small, maxh, maxw);
+      SS[i].g1 = g1d;
+    }
+    int* flags = reinterpret_cast<int*>(base + flags_off);
+    for (int t = 0; t < ntiles; ++t) {
+      tk[t].nan_flag = flags + t;
+      for (int d = 0; d < tk[t].ndec; ++d) tk[t].dec[d].ms = nullptr;
+    }
+    // coarse means: per (tile, dec) in tile-major order
+    size_t k = 0;
+    for (int t = 0; t < ntiles; ++t)
+      for (int d = 0; d < tk[t].ndec; ++d) tk[t].dec[d].ms = reinterpret_cast<float*>(base + topo_bytes + dec_ms[k++]);
+    A.tiles = reinterpret_cast<const TopoTileK*>(base + tiles_off);
+    A.items = reinterpret_cast<const StripItem*>(base + items_off);
+    A.zmax = reinterpret_cast<const unsigned*>(flags + ntiles);
+  }
+  int upload(cudaStream_t s) const {
+    if (!g1.empty()) FSG_CUDA(cudaMemcpyAsync(base + g1_off, g1.data(), g1.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    if (!gv.empty()) FSG_CUDA(cudaMemcpyAsync(base + gv_off, gv.data(), gv.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    FSG_CUDA(cudaMemcpyAsync(base + tiles_off, tk.data(), sizeof(TopoTileK) * ntiles, cudaMemcpyHostToDevice, s));
+    FSG_CUDA(cudaMemcpyAsync(base + items_off, items.data(), sizeof(StripItem) * items.size(), cudaMemcpyHostToDevice, s));
+    return FSG_OK;
+  }
+
+  int enqueue(cudaStream_t s) const {
+    if (empty) return FSG_OK;
+    int st = FSG_OK;
+    if (NS > 0) {
+      FSG_CUDA(cudaEventRecord(aux->fork, s));
+      for (int i = 0; i < NS; ++i) FSG_CUDA(cudaStreamWaitEvent(aux->st[i], aux->fork, 0));
+      const float* gvd = reinterpret_cast<const float*>(base + gv_off);
+      for (size_t i = 0; i < work.size() && !st; ++i) {
+        const DecWork& w = work[i];
+        const int si = (int)(i % (size_t)NS);
+        TopoScratch S = SS[si];
+        st = decimated_mean_dev(tk[w.t].z, w.r, w.f, S, gvd + w.gv_off, w.R,
+                                reinterpret_cast<float*>(base + topo_bytes + w.ms_off), aux->st[si]);
+      }
+      for (int i = 0; i < NS; ++i) {  // join (also on error: the scratch is released on s)
+        FSG_CUDA(cudaEventRecord(aux->join[i], aux->st[i]));
+        FSG_CUDA(cudaStreamWaitEvent(s, aux->join[i], 0));
+      }
+      if (st) return st;
+    }
+    int* flags = reinterpret_cast<int*>(base + flags_off);
+    const TopoTileK* tiles_dev = reinterpret_cast<const TopoTileK*>(base + tiles_off);
+    FSG_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (ntiles + 1), s));
+    if (fixed) window_absmax<<<dim3(128, ntiles), 256, 0, s>>>(tiles_dev, reinterpret_cast<unsigned*>(flags + ntiles));
+    else window_nan_flags<<<dim3(256, ntiles), 256, 0, s>>>(tiles_dev, flags);
+    FSG_LAUNCHED(1);
+    if (fixed) timing_mark(s, true);
+    kern<<<grid, fixed ? FX_NT : ST_NT, smem, s>>>(A);
+    if (fixed) timing_mark(s, false);
+    FSG_LAUNCHED(1);
+    return FSG_OK;
+  }
+};
+
+static int topousm_strip_prepare(const float* raster_dev, int64_t ld, const fsg_tile* tiles, int32_t ntiles,
+                                 const fsg_topousm_params* p, const fsg_plane* out, int nfull, TopoJob& J) {
   const std::vector<int> radii(p->radii, p->radii + p->nradii);
-  int maxh = 1, maxw = 1;
+  J.ntiles = ntiles;
+  J.nfull = nfull;
   for (int t = 0; t < ntiles; ++t) {
-    maxh = std::max(maxh, tiles[t].win_h);
-    maxw = std::max(maxw, tiles[t].win_w);
+    J.maxh = std::max(J.maxh, tiles[t].win_h);
+    J.maxw = std::max(J.maxw, tiles[t].win_w);
   }
   std::vector<int> dec_idx;
   for (int i = nfull; i < p->nradii; ++i) dec_idx.push_back(i);
-  // scratch: decimation pipeline (one window at a time) + per-tile coarse means + tables
-  size_t dec_bytes = 0;
-  std::vector<size_t> dec_off((size_t)ntiles * dec_idx.size());
-  for (int t = 0; t < ntiles; ++t)
-    for (size_t d = 0; d < dec_idx.size(); ++d) {
-      const int f = topousm_downsample_factor((double)radii[dec_idx[d]], p->pixel_size);
-      const size_t n = (size_t)std::max(1, (tiles[t].win_h + f - 1) / f) * std::max(1, (tiles[t].win_w + f - 1) / f);
-      dec_off[(size_t)t * dec_idx.size() + d] = dec_bytes;
-      dec_bytes += (n * sizeof(float) + 255) & ~(size_t)255;
-    }
   int R = 0;
   for (int i = 0; i < nfull; ++i) R = std::max(R, radii[i]);
   DeviceInfo di;
@@ -1409,55 +1485,29 @@ static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_til
   if (st) return st;
   // exact fixed-point kernel when its ring fits in shared memory, else the compensated one
   const int fx_ring = 2 * R + 2 * FX_G + 1;
-  const bool fixed = nfull >= 1 && nfull <= FX_MAXNR && 2 * R < FX_NT - 32 &&
-                     FxSmem::bytes(fx_ring) <= di.smem_optin;
-  const int TW = fixed ? FX_NT - 2 * R : ((ST_NT - 2 * R) / ST_SEG) * ST_SEG;
-  const int CHUNK = fixed ? 1024 : 512;
-  std::vector<StripItem> items;
+  J.fixed = nfull >= 1 && nfull <= FX_MAXNR && 2 * R < FX_NT - 32 && FxSmem::bytes(fx_ring) <= di.smem_optin;
+  const int TW = J.fixed ? FX_NT - 2 * R : ((ST_NT - 2 * R) / ST_SEG) * ST_SEG;
+  const int CHUNK = J.fixed ? 1024 : 512;
   for (int t = 0; t < ntiles; ++t) {
     const fsg_tile& T = tiles[t];
     if (T.core_h == 0 || T.core_w == 0) continue;
     const int cy0 = T.core_y0 - T.win_y0, cx0 = T.core_x0 - T.win_x0;
     for (int x = cx0; x < cx0 + T.core_w; x += TW)
-      for (int y = cy0; y < cy0 + T.core_h; y += CHUNK) items.push_back({t, x, y, std::min(y + CHUNK, cy0 + T.core_h)});
+      for (int y = cy0; y < cy0 + T.core_h; y += CHUNK) J.items.push_back({t, x, y, std::min(y + CHUNK, cy0 + T.core_h)});
   }
-  if (items.empty()) return FSG_OK;
+  J.empty = J.items.empty();
+  if (J.empty) return FSG_OK;
   int nwork = 0;
   for (int t = 0; t < ntiles; ++t) nwork += tiles[t].core_h > 0 && tiles[t].core_w > 0;
-  const int NS = dec_idx.empty() ? 0 : std::max(1, std::min(AUX_STREAMS, nwork));
-  const size_t one_small = (TopoScratch::bytes_small(maxh, maxw) + 255) & ~(size_t)255;
-  const size_t topo_bytes = (size_t)NS * one_small;
-  const size_t tiles_off = (topo_bytes + dec_bytes + 255) & ~(size_t)255;
-  const size_t items_off = tiles_off + ((sizeof(TopoTileK) * ntiles + 255) & ~(size_t)255);
-  const size_t flags_off = items_off + ((sizeof(StripItem) * items.size() + 255) & ~(size_t)255);
-  const size_t total = flags_off + sizeof(int) * (ntiles + 1) + 256;
-  StreamScratch scratch;
-  st = scratch.alloc(total, s);
-  if (st) return st;
-  char* base = static_cast<char*>(scratch.ptr);
-  TopoScratch SS[AUX_STREAMS];
-  AuxStreams* aux = nullptr;
-  if (NS > 0) {
-    for (int i = 0; i < NS; ++i) {
-      SS[i].carve_small(base + (size_t)i * one_small, maxh, maxw);
-      st = prepare_g1(SS[i], s);
-      if (st) return st;
-    }
-    st = aux_streams(&aux);
-    if (st) return st;
-    FSG_CUDA(cudaEventRecord(aux->fork, s));
-    for (int i = 0; i < NS; ++i) FSG_CUDA(cudaStreamWaitEvent(aux->st[i], aux->fork, 0));
-  }
-  int nlaunched = 0;
-  float* dec_base = reinterpret_cast<float*>(base + topo_bytes);
-  TopoTileK* tiles_dev = reinterpret_cast<TopoTileK*>(base + tiles_off);
-  StripItem* items_dev = reinterpret_cast<StripItem*>(base + items_off);
-  int* flags = reinterpret_cast<int*>(base + flags_off);
+  J.NS = dec_idx.empty() ? 0 : std::max(1, std::min(AUX_STREAMS, nwork));
+  J.one_small = (TopoScratch::bytes_small(J.maxh, J.maxw) + 255) & ~(size_t)255;
+  J.topo_bytes = (size_t)J.NS * J.one_small;
+  // per (tile, dec) coarse means and void-fill weight tables
   const size_t esz = out->dtype == FSG_F32 ? 4 : (out->dtype == FSG_I16 ? 2 : 1);
-  std::vector<TopoTileK> tk(ntiles);
+  J.tk.assign(ntiles, TopoTileK{});
   for (int t = 0; t < ntiles; ++t) {
     const fsg_tile& T = tiles[t];
-    TopoTileK& k = tk[t];
+    TopoTileK& k = J.tk[t];
     std::memset(&k, 0, sizeof(k));
     k.z = ZView{raster_dev + (long long)T.win_y0 * ld + T.win_x0, ld, T.win_h, T.win_w, (float)p->nodata,
                 p->has_nodata != 0};
@@ -1468,44 +1518,46 @@ static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_til
     k.gy0 = T.win_y0;
     k.gx0 = T.win_x0;
     k.out = static_cast<char*>(out->ptr) + ((long long)T.out_y0 * out->ld + T.out_x0) * esz;
-    k.nan_flag = flags + t;
     k.ndec = (int)dec_idx.size();
     for (size_t d = 0; d < dec_idx.size(); ++d) {
       const int r = radii[dec_idx[d]];
       const int f = topousm_downsample_factor((double)r, p->pixel_size);
       const int hs = std::max(1, (T.win_h + f - 1) / f), ws = std::max(1, (T.win_w + f - 1) / f);
-      float* ms = reinterpret_cast<float*>(reinterpret_cast<char*>(dec_base) + dec_off[(size_t)t * dec_idx.size() + d]);
+      J.dec_ms.push_back(J.dec_bytes);
       if (T.core_h > 0 && T.core_w > 0) {
-        const int si = nlaunched % NS;
-        st = decimated_mean(k.z, r, f, SS[si], ms, aux->st[si]);
-        if (st) break;
+        double sigma = std::max(1.0, (double)std::min(hs, ws) / 64.0);
+        int Rg;
+        std::vector<float> gw = gaussian_weights(sigma, &Rg);
+        if (Rg + 1 > 4096) return fail(FSG_ERR_UNSUPPORTED, "void-fill Gaussian radius %d too large", Rg);
+        const size_t go = J.gv.size();
+        J.gv.insert(J.gv.end(), gw.begin(), gw.end());
+        J.gv.resize((J.gv.size() + 63) & ~(size_t)63);  // 256-byte aligned tables
+        J.work.push_back({t, r, f, Rg, J.dec_bytes, go});
       }
-      k.dec[d].ms = ms;
+      J.dec_bytes += ((size_t)hs * ws * sizeof(float) + 255) & ~(size_t)255;
       k.dec[d].h = hs;
       k.dec[d].w = ws;
       k.dec[d].zy = T.win_h > 1 ? (double)(hs - 1) / (double)(T.win_h - 1) : 1.0;
       k.dec[d].zx = T.win_w > 1 ? (double)(ws - 1) / (double)(T.win_w - 1) : 1.0;
       k.dec[d].weight = (float)p->weights[dec_idx[d]];
     }
-    if (k.ndec > 0 && T.core_h > 0 && T.core_w > 0) ++nlaunched;
-    if (st) break;
   }
-  for (int i = 0; i < NS; ++i) {  // join the decimation streams (also on error: the scratch is freed on s)
-    FSG_CUDA(cudaEventRecord(aux->join[i], aux->st[i]));
-    FSG_CUDA(cudaStreamWaitEvent(s, aux->join[i], 0));
+  if (J.NS > 0) {
+    int Rg;
+    J.g1 = gaussian_weights(1.0, &Rg);
+    st = aux_streams(&J.aux);  // created now, outside any stream capture
+    if (st) return st;
   }
-  if (st) return st;
-  FSG_CUDA(cudaMemcpyAsync(tiles_dev, tk.data(), sizeof(TopoTileK) * ntiles, cudaMemcpyHostToDevice, s));
-  FSG_CUDA(cudaMemcpyAsync(items_dev, items.data(), sizeof(StripItem) * items.size(), cudaMemcpyHostToDevice, s));
-  FSG_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (ntiles + 1), s));
-  if (fixed) window_absmax<<<dim3(128, ntiles), 256, 0, s>>>(tiles_dev, reinterpret_cast<unsigned*>(flags + ntiles));
-  else window_nan_flags<<<dim3(256, ntiles), 256, 0, s>>>(tiles_dev, flags);
-  FSG_LAUNCHED(1);
-  StripArgs A;
+  auto al = [](size_t n) { return (n + 255) & ~(size_t)255; };
+  J.g1_off = al(J.topo_bytes + J.dec_bytes);
+  J.gv_off = J.g1_off + al(J.g1.size() * sizeof(float) + 1);
+  J.tiles_off = J.gv_off + al(J.gv.size() * sizeof(float) + 1);
+  J.items_off = J.tiles_off + al(sizeof(TopoTileK) * ntiles);
+  J.flags_off = J.items_off + al(sizeof(StripItem) * J.items.size());
+  J.total = J.flags_off + sizeof(int) * (ntiles + 1) + 256;
+  StripArgs& A = J.A;
   std::memset(&A, 0, sizeof(A));
-  A.tiles = tiles_dev;
-  A.items = items_dev;
-  A.nitems = (int)items.size();
+  A.nitems = (int)J.items.size();
   A.nr = nfull;
   A.R = R;
   A.TW = TW;
@@ -1532,54 +1584,68 @@ static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_til
   A.qmax = out->q_max;
   A.have_small = p->nradii > 0;
   A.ring = fx_ring;
-  A.zmax = reinterpret_cast<const unsigned*>(flags + ntiles);
-  if (fixed) {
-    void (*fk)(StripArgs) = nullptr;
+  if (J.fixed) {
     switch (nfull) {
-      case 1: fk = topousm_fixed<1>; break;
-      case 2: fk = topousm_fixed<2>; break;
-      case 3: fk = topousm_fixed<3>; break;
-      default: fk = topousm_fixed<4>; break;
+      case 1: J.kern = topousm_fixed<1>; break;
+      case 2: J.kern = topousm_fixed<2>; break;
+      case 3: J.kern = topousm_fixed<3>; break;
+      default: J.kern = topousm_fixed<4>; break;
     }
-    const size_t fsmem = FxSmem::bytes(fx_ring);
-    FSG_CUDA(cudaFuncSetAttribute(fk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+    J.smem = FxSmem::bytes(fx_ring);
+    FSG_CUDA(cudaFuncSetAttribute(J.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)J.smem));
     int per = 0;
-    FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fk, FX_NT, fsmem));
-    const int grid = std::min((int)items.size(), di.sms * std::max(1, per));
-    timing_mark(s, true);
-    fk<<<grid, FX_NT, fsmem, s>>>(A);
-    timing_mark(s, false);
-    FSG_LAUNCHED(1);
+    FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, J.kern, FX_NT, J.smem));
+    J.grid = std::min((int)J.items.size(), di.sms * std::max(1, per));
     return FSG_OK;
   }
-  const size_t smem = StripSmem::floats(std::max(1, nfull), TW) * sizeof(float);
-  void (*kern)(StripArgs) = nullptr;
+  J.smem = StripSmem::floats(std::max(1, nfull), TW) * sizeof(float);
   switch (nfull) {
-    case 0: kern = topousm_strip<0>; break;
-    case 1: kern = topousm_strip<1>; break;
-    case 2: kern = topousm_strip<2>; break;
-    case 3: kern = topousm_strip<3>; break;
-    case 4: kern = topousm_strip<4>; break;
-    case 5: kern = topousm_strip<5>; break;
-    default: kern = topousm_strip<6>; break;
+    case 0: J.kern = topousm_strip<0>; break;
+    case 1: J.kern = topousm_strip<1>; break;
+    case 2: J.kern = topousm_strip<2>; break;
+    case 3: J.kern = topousm_strip<3>; break;
+    case 4: J.kern = topousm_strip<4>; break;
+    case 5: J.kern = topousm_strip<5>; break;
+    default: J.kern = topousm_strip<6>; break;
   }
-  if (smem > 48 * 1024) FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (J.smem > 48 * 1024) FSG_CUDA(cudaFuncSetAttribute(J.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)J.smem));
   int per_sm = 0;
-  FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ST_NT, smem));
-  const int grid = std::min((int)items.size(), di.sms * std::max(1, per_sm));
-  kern<<<grid, ST_NT, smem, s>>>(A);
-  FSG_LAUNCHED(1);
+  FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, J.kern, ST_NT, J.smem));
+  J.grid = std::min((int)J.items.size(), di.sms * std::max(1, per_sm));
   return FSG_OK;
 }
+
+static int topousm_strip_path(const float* raster_dev, int64_t ld, const fsg_tile* tiles, int32_t ntiles,
+                              const fsg_topousm_params* p, const fsg_plane* out, int nfull, cudaStream_t s) {
+  TopoJob J;
+  int st = topousm_strip_prepare(raster_dev, ld, tiles, ntiles, p, out, nfull, J);
+  if (st || J.empty) return st;
+  StreamScratch scratch;
+  st = scratch.alloc(J.total, s);
+  if (st) return st;
+  J.bind(scratch.ptr);
+  st = J.upload(s);
+  if (st) return st;
+  return J.enqueue(s);
+}
+
+struct TopoPlan final : fsg_plan {
+  TopoJob J;
+  void* dev = nullptr;
+  ~TopoPlan() override {
+    if (dev) cudaFree(dev);
+  }
+  int launch(cudaStream_t s) override { return J.enqueue(s); }
+};
+
 
 
 }  // namespace fsg
 
 using namespace fsg;
 
-extern "C" int fsg_topousm(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
-                           const fsg_tile* tiles, int32_t ntiles, const fsg_topousm_params* p,
-                           const fsg_plane* out, void* stream) {
+static int topousm_validate(int64_t ld, int32_t raster_h, int32_t raster_w, const fsg_tile* tiles, int32_t ntiles,
+                            const fsg_topousm_params* p, const fsg_plane* out) {
   if (!p || !out || (ntiles > 0 && !tiles)) return fail(FSG_ERR_INVALID, "null argument");
   if (ntiles < 0 || raster_h < 0 || raster_w < 0 || ld < raster_w) return fail(FSG_ERR_INVALID, "bad raster shape");
   if (!out->ptr) return fail(FSG_ERR_INVALID, "output plane is NULL");
@@ -1592,7 +1658,48 @@ extern "C" int fsg_topousm(const float* raster_dev, int64_t ld, int32_t raster_h
   if (p->coarse_dev && (p->coarse_h < 1 || p->coarse_w < 1 || p->coarse_ld < p->coarse_w || p->full_h < 1 ||
                         p->full_w < 1))
     return fail(FSG_ERR_INVALID, "coarse field shape");
-  int st = validate_tiles(raster_h, raster_w, tiles, ntiles, 1);
+  return validate_tiles(raster_h, raster_w, tiles, ntiles, 1);
+}
+
+extern "C" int fsg_topousm_plan(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                                const fsg_tile* tiles, int32_t ntiles, const fsg_topousm_params* p,
+                                const fsg_plane* out, fsg_plan** plan) {
+  if (!plan) return fail(FSG_ERR_INVALID, "null plan pointer");
+  *plan = nullptr;
+  int st = topousm_validate(ld, raster_h, raster_w, tiles, ntiles, p, out);
+  if (st) return st;
+  const std::vector<int> rv(p->radii, p->radii + p->nradii);
+  int nfull = 0;
+  if (!strip_path_ok(rv, p->pixel_size, &nfull))
+    return fail(FSG_ERR_UNSUPPORTED, "topousm plan: the radii must ascend with the full-resolution radii first");
+  TopoPlan* P = new TopoPlan();
+  st = topousm_strip_prepare(raster_dev, ld, tiles, ntiles, p, out, nfull, P->J);
+  if (!st && !P->J.empty) {
+    cudaError_t e = cudaMalloc(&P->dev, P->J.total);
+    if (e != cudaSuccess) {
+      P->dev = nullptr;
+      st = cuda_fail(e, "cudaMalloc(plan)");
+    } else {
+      P->J.bind(P->dev);
+      st = P->J.upload(nullptr);
+      if (!st) {
+        e = cudaStreamSynchronize(nullptr);
+        if (e != cudaSuccess) st = cuda_fail(e, "plan upload");
+      }
+    }
+  }
+  if (st) {
+    delete P;
+    return st;
+  }
+  *plan = P;
+  return FSG_OK;
+}
+
+extern "C" int fsg_topousm(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                           const fsg_tile* tiles, int32_t ntiles, const fsg_topousm_params* p,
+                           const fsg_plane* out, void* stream) {
+  int st = topousm_validate(ld, raster_h, raster_w, tiles, ntiles, p, out);
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
   {

@@ -72,6 +72,18 @@ typedef struct fsg_tile {
   double pixel_scale_x, pixel_scale_y;       /* signed metres per pixel (tile_processor.py:910-932) */
 } fsg_tile;
 
+/* ------------------------------------------------------------------ plans
+ * A plan is one entry point's call prepared once: its tile tables are
+ * uploaded into device memory the plan owns, so fsg_plan_launch issues only
+ * kernels, memsets and device-side copies on the given stream and can be
+ * captured into a CUDA graph (the core/ tile scheduler's persistent work
+ * queue, core/tile_processor.py:1629-1683, replayed as one graph launch).
+ * The buffers named at creation must stay valid while the plan is used.
+ * Creating and destroying a plan synchronise; launching does not. */
+typedef struct fsg_plan fsg_plan;
+int fsg_plan_launch(fsg_plan* plan, void* stream);
+void fsg_plan_destroy(fsg_plan* plan);
+
 /* ------------------------------------------------------------- utilities */
 int fsg_abi_version(void);
 const char* fsg_version(void);
@@ -127,6 +139,10 @@ typedef struct fsg_stencil_params {
 int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
                 const fsg_tile* tiles, int32_t ntiles, const fsg_stencil_params* params,
                 const fsg_plane* planes, void* stream);
+/* fsg_stencil prepared as a plan (same arguments, no stream). */
+int fsg_stencil_plan(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                     const fsg_tile* tiles, int32_t ntiles, const fsg_stencil_params* params,
+                     const fsg_plane* planes, fsg_plan** plan);
 
 /* The same fused pass over a raster and output planes in HOST memory (pinned
  * memory gives asynchronous copies): per tile, the window is copied to the
@@ -173,6 +189,12 @@ typedef struct fsg_topousm_params {
 int fsg_topousm(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
                 const fsg_tile* tiles, int32_t ntiles, const fsg_topousm_params* params,
                 const fsg_plane* out, void* stream);
+/* fsg_topousm prepared as a plan (same arguments, no stream); radius lists
+ * that take the fused strip pass only (ascending, full-resolution radii first),
+ * else FSG_ERR_UNSUPPORTED. */
+int fsg_topousm_plan(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                     const fsg_tile* tiles, int32_t ntiles, const fsg_topousm_params* p,
+                     const fsg_plane* out, fsg_plan** plan);
 
 /* Large-radius field on the overview grid: sum_i f32(w_i) * mean_{r_i}(coarse), r_i =
  * max(1, round(radius_i / decimation)) -- compute_topousm_fast_large_coarse_field
@@ -271,6 +293,10 @@ typedef struct fsg_openness_params {
 int fsg_openness(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
                  const fsg_tile* tiles, int32_t ntiles, const fsg_openness_params* params,
                  const fsg_plane* display, float* raw_deg_dev, int64_t raw_ld, void* stream);
+/* fsg_openness prepared as a plan (same arguments, no stream). */
+int fsg_openness_plan(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                      const fsg_tile* tiles, int32_t ntiles, const fsg_openness_params* params,
+                      const fsg_plane* display, float* raw_deg_dev, int64_t raw_ld, fsg_plan** plan);
 
 /* Host-only: the ray offsets the kernel uses (dx, dy per sample, directions in
  * order; ray_len[d] samples for direction d).  Returns FSG_ERR_WORKSPACE with
