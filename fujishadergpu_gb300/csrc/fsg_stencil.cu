@@ -661,7 +661,7 @@ __device__ __forceinline__ void pixel_products2(const Light& L, float slx, float
   if (om & (1u << FSG_OUT_HILLSHADE)) {
     const f2 t = fma2(pz, S2(-slx), fma2(qz, S2(-sly), S2(L.lz)));
     const f2 n2 = zone ? one_g2 : fma2(pz, pz, fma2(qz, qz, S2(1.0f)));
-    const f2 rs = P2(rsqrtf(n2.x), rsqrtf(n2.y));
+    const f2 rs = P2(rsqrt_approx(n2.x), rsqrt_approx(n2.y));
     rs1 = rs;
     o[FSG_OUT_HILLSHADE] = P2(__saturatef(t.x * rs.x), __saturatef(t.y * rs.y));
   }
@@ -727,9 +727,16 @@ __device__ __forceinline__ void pixel_products2(const Light& L, float slx, float
 #define FSG_FAST_RING 11  // rows per warp ring (RING - 1 copies in flight; 8 x 11 x 528 B static)
 #endif
 #ifndef FSG_FAST_MINB
-#define FSG_FAST_MINB 2  // resident 256-thread blocks per SM the register budget must allow
+#define FSG_FAST_MINB 2  // resident blocks per SM the register budget must allow
+#endif
+#ifndef FSG_FAST_NT
+#define FSG_FAST_NT 256  // threads per block of the streaming pass (one unit per warp)
 #endif
 constexpr int RING = FSG_FAST_RING;
+#ifndef FSG_FAST_ROW_UNROLL
+#define FSG_FAST_ROW_UNROLL 1  // output rows per loop body (register renaming instead of moves)
+#endif
+constexpr int ROW_UNROLL = FSG_FAST_ROW_UNROLL;
 
 __device__ __forceinline__ void cp_async16(unsigned dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
@@ -755,10 +762,10 @@ __device__ __forceinline__ Q4 q4hdiff(Q4 f, float left, float right) {
 }
 
 template <bool CURV, unsigned OM, bool ALLF32>
-__global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const __grid_constant__ FastArgs A) {
+__global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kernel(const __grid_constant__ FastArgs A) {
   constexpr bool DIV = (OM & ((1u << FSG_OUT_DX) | (1u << FSG_OUT_DY))) != 0;
   constexpr int REACH = CURV ? 2 : 1;  // rows above / below an output row that feed it
-  __shared__ __align__(16) float ring_s[256 / 32][RING][RW];
+  __shared__ __align__(16) float ring_s[FSG_FAST_NT / 32][RING][RW];
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -893,7 +900,7 @@ __global__ void __launch_bounds__(256, FSG_FAST_MINB) stencil_fast_kernel(const 
       yd0 = dv1(__fsub_rn(e31lane ? ep1.x : ep1.y, e31lane ? em1.x : em1.y), T.g1y);
     }
     bool bad = false;
-#pragma unroll 1
+#pragma unroll ROW_UNROLL
     for (int y = y0; y < y1; ++y) {
       // NoData in the 2*REACH+1 rows feeding this output row (any lane)?
       const bool row_nan = __any_sync(0xffffffffu, nan_left > 0);
@@ -1346,7 +1353,7 @@ struct StencilJob {
     if (fast) {
       FSG_CUDA(cudaMemsetAsync(F.fix_count, 0, sizeof(unsigned), s));
       timing_mark(s, true);
-      fastk<<<fgrid, 256, 0, s>>>(F);
+      fastk<<<fgrid, FSG_FAST_NT, 0, s>>>(F);
       timing_mark(s, false);
       FSG_LAUNCHED(1);
       fixk<<<xgrid, XNT, FIX_SMEM, s>>>(F);
@@ -1514,8 +1521,8 @@ static int stencil_prepare(const float* raster_dev, int64_t ld, int32_t raster_h
     J.fastk = fast;
     J.fixk = fixup;
     int fper = 0;
-    FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fper, fast, 256, 0));
-    J.fgrid = std::min((units + 7) / 8, di.sms * std::max(1, fper));  // one unit per warp
+    FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fper, fast, FSG_FAST_NT, 0));
+    J.fgrid = std::min((units + FSG_FAST_NT / 32 - 1) / (FSG_FAST_NT / 32), di.sms * std::max(1, fper));  // one unit per warp
     FSG_CUDA(cudaFuncSetAttribute(fixup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FIX_SMEM));
     int xper = 0;
     FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&xper, fixup, XNT, FIX_SMEM));
