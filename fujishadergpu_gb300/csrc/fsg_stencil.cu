@@ -1070,18 +1070,27 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
     const FastTile& T = A.tiles[g.t];
     const int x0 = g.x0 + (int)((e >> FIX_QSHIFT) & (NQ - 1)) * FW, y0 = g.y0, y1 = g.y1, xo = min(x0 + FW, g.xo);
     if (x0 >= xo) continue;
-    // (a) source region, NoData -> NaN, outside the window -> NaN (never read)
-    for (int i = tid; i < XS_R * XS_C; i += XNT) {
-      const int r = i / XS_C, c = i - (i / XS_C) * XS_C;
-      const int gy = y0 - 8 + r, gx = x0 - 8 + c;
-      float v = qnan;
-      if (gy >= T.wy0 && gy < T.wy1 && gx >= T.wx0 && gx < T.wx1) {
-        v = __ldg(A.raster + (long long)gy * A.ld + gx);
-        if (is_nodata(v, A.ndf, hn)) v = qnan;
+    // (a) source region: cells inside the window copied with cp.async (all in
+    //     flight at once), the rest NaN (never read); then NoData -> NaN
+    {
+      const unsigned sv0 = (unsigned)__cvta_generic_to_shared(Sv);
+      for (int i = tid; i < XS_R * XS_C; i += XNT) {
+        const int r = i / XS_C, c = i - (i / XS_C) * XS_C;
+        const int gy = y0 - 8 + r, gx = x0 - 8 + c;
+        if (gy >= T.wy0 && gy < T.wy1 && gx >= T.wx0 && gx < T.wx1)
+          cp_async4(sv0 + 4u * (unsigned)i, A.raster + (long long)gy * A.ld + gx);
+        else
+          Sv[i] = qnan;
       }
-      Sv[i] = v;
+      cp_async_commit();
+      cp_async_wait<0>();
+      __syncthreads();
+      if (hn) {
+        for (int i = tid; i < XS_R * XS_C; i += XNT)
+          if (is_nodata(Sv[i], A.ndf, true)) Sv[i] = qnan;
+        __syncthreads();
+      }
     }
-    __syncthreads();
     // (b) row bitmasks of valid output pixels and of in-window NoData cells;
     //     E starts as a copy of the source values
     for (int r = warp; r < XE_R; r += XNT / 32) {
