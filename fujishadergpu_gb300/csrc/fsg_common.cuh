@@ -48,6 +48,7 @@ struct DeviceInfo {
   int device = -1;
   int sms = 0;
   size_t smem_optin = 0;
+  size_t smem_per_sm = 0;
 };
 // Properties of the current device (cached per device).
 int device_info(DeviceInfo* out);

@@ -63,11 +63,13 @@ int device_info(DeviceInfo* out) {
   std::lock_guard<std::mutex> lk(g_dev_mutex);
   DeviceInfo& d = g_dev_cache[dev];
   if (d.device != dev) {
-    int sms = 0, optin = 0;
+    int sms = 0, optin = 0, per_sm = 0;
     FSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     FSG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    FSG_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
     d.sms = sms;
     d.smem_optin = (size_t)optin;
+    d.smem_per_sm = (size_t)per_sm;
     d.device = dev;
   }
   *out = d;

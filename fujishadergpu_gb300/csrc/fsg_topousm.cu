@@ -1039,6 +1039,291 @@ __global__ void __launch_bounds__(FX_NT, 1) topousm_fixed(const __grid_constant_
   }
 }
 
+// Hybrid variant for two or more full-resolution radii: the prefix ring holds
+// only the rows of the smaller radii (2 Rs + G + 1 rows, Rs = the second
+// largest radius), and the largest radius R takes, per group of G rows, its
+// entering rows y+R and leaving rows y-1-R from two G-row buffers that the warps
+// prefix-sum for that group (those rows are read again from L2).  With the
+// default radii (2, 8, 32) a CTA needs ~90 KB instead of 178 KB, so two CTAs
+// share an SM.  Each group runs a scan phase (all warps: the group's new ring
+// rows and its entering / leaving rows of R) and a pixel phase (output-column
+// warps), with a barrier after each; the other CTA of the SM fills the gaps.
+// The running sum of R for the first row of an item is built by adding its
+// 2R+1 rows through the entering buffer, G rows at a time.
+constexpr int HY_MAXNR = FX_MAXNR;
+struct HySmem {
+  static size_t bytes(int ring) {
+    return sizeof(u64) * FX_EP * ((size_t)ring + 2 * FX_G) + sizeof(int2) * FX_G * HY_MAXNR +
+           3 * sizeof(float) * ST_MAXD * FX_G;
+  }
+};
+
+template <int NR>
+__global__ void __launch_bounds__(FX_NT, 2) topousm_hybrid(const __grid_constant__ StripArgs A) {
+  static_assert(NR >= 2, "the hybrid kernel needs a ring radius and a large radius");
+  extern __shared__ __align__(16) u64 fsm[];
+  constexpr int G = FX_G;
+  constexpr int NS = NR - 1;  // radii served by the ring
+  const int RING = A.ring, TW = A.TW, R = A.R;
+  u64* ring = fsm;
+  u64* BE = ring + (size_t)RING * FX_EP;                     // [G][FX_EP] entering rows of R
+  u64* BL = BE + (size_t)G * FX_EP;                          // [G][FX_EP] leaving rows of R
+  int2* OFF = reinterpret_cast<int2*>(BL + (size_t)G * FX_EP);  // [G][HY_MAXNR] ring-row element offsets
+  int* DYi = reinterpret_cast<int*>(OFF + G * HY_MAXNR);     // [ST_MAXD][G][2]
+  float* DYf = reinterpret_cast<float*>(DYi + 2 * ST_MAXD * G);
+  __shared__ TopoTileK Ts;
+  const TopoTileK& T = Ts;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NW = FX_NT / 32;
+  const int ncons = min(NW, (TW + 31) / 32);
+  const unsigned mb = *A.zmax;
+  const int e = mb ? (int)((mb >> 23) & 0xFF) - 126 : 0;
+  const int k = max(-100, min(100, 33 - e));
+  const float sk = ldexpf(1.0f, k), isk = ldexpf(1.0f, -k);
+  for (int r = tid; r < RING; r += FX_NT) ring[(size_t)r * FX_EP] = 0ull;
+  for (int r = tid; r < 2 * G; r += FX_NT) BE[(size_t)r * FX_EP] = 0ull;
+  const int c = tid, b = R + c;
+  int ja[NR], jb[NR];
+  float wq[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    const int r = A.radii[q];
+    ja[q] = c < TW ? fx_idx(b + r + 1) : 0;
+    jb[q] = c < TW ? fx_idx(b - r) : 0;
+    wq[q] = A.weights[q];
+  }
+  const int Rs = A.radii[NS - 1];
+  for (int it = blockIdx.x; it < A.nitems; it += gridDim.x) {
+    const StripItem I = A.items[it];
+    __syncthreads();
+    for (int q = tid; q < (int)(sizeof(TopoTileK) / 4); q += FX_NT)
+      reinterpret_cast<int*>(&Ts)[q] = reinterpret_cast<const int*>(A.tiles + I.tile)[q];
+    __syncthreads();
+    const ZView z = T.z;
+    const int y0 = I.y0, y1 = I.y1, x0 = I.x0;
+    const int xb = x0 - R;
+    const int x = x0 + c;
+    const bool active = c < TW && x < min(x0 + TW, T.cx0 + T.cw);
+    const int tbase = y0 - Rs;  // ring slot of row t: (t - tbase) % RING
+    const bool vec = xb >= 0 && xb + FX_NT <= z.w && (z.ld & 3) == 0 &&
+                     ((reinterpret_cast<uintptr_t>(z.p + xb) & 15) == 0);
+    // row t of the window (reflected) -> prefix sums E[t][1..256] at dst
+    auto scan_row = [&](int t, u64* dst) {
+      float v[8];
+      const float* row = z.p + (long long)reflect_idx(t, z.h) * z.ld;
+      if (vec) {
+        const float4* p4 = reinterpret_cast<const float4*>(row + xb + 8 * lane);
+        const float4 a4 = __ldg(p4), b4 = __ldg(p4 + 1);
+        v[0] = a4.x; v[1] = a4.y; v[2] = a4.z; v[3] = a4.w;
+        v[4] = b4.x; v[5] = b4.y; v[6] = b4.z; v[7] = b4.w;
+      } else {
+#pragma unroll
+        for (int m = 0; m < 8; ++m) v[m] = __ldg(row + reflect_idx(xb + 8 * lane + m, z.w));
+      }
+      u64 pm[8];
+      u64 acc = 0ull;
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const float xv = v[m];
+        const bool ok = !is_nodata(xv, z.ndf, z.has_nodata != 0);
+        const u64 q = ok ? ((u64)__float2ll_rn(__fmul_rn(xv, sk)) << FX_CB) + 1ull : 0ull;
+        acc += q;
+        pm[m] = acc;
+      }
+      u64 incl = acc;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const u64 n = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += n;
+      }
+      const u64 excl = incl - acc;
+#pragma unroll
+      for (int m = 0; m < 8; ++m) dst[fx_idx(8 * lane + m + 1)] = excl + pm[m];
+    };
+    auto ring_row = [&](int t) { return ring + (size_t)((t - tbase) % RING) * FX_EP; };
+    // prologue: ring rows y0-Rs .. y0+Rs
+    for (int t = tbase + warp; t <= y0 + Rs; t += NW) scan_row(t, ring_row(t));
+    // columns of the coarse field and of the decimated grids (fixed per item)
+    const bool have_large = A.field != nullptr;
+    int fxa = 0, fxb = 0;
+    float ftx = 0.f;
+    if (have_large) {
+      const float cx = __fsub_rn(__fmul_rn(__fadd_rn((float)(T.gx0 + x), 0.5f), A.sx), 0.5f);
+      const float f0 = floorf(cx);
+      ftx = cx - f0;
+      fxa = clamp_idx((int)f0, A.fw);
+      fxb = clamp_idx((int)f0 + 1, A.fw);
+    }
+    int dxa[ST_MAXD], dxb[ST_MAXD], dya[ST_MAXD];
+    float dfx[ST_MAXD], dm[ST_MAXD][4];
+#pragma unroll
+    for (int d = 0; d < ST_MAXD; ++d) {
+      dxa[d] = dxb[d] = 0;
+      dya[d] = -1;
+      dfx[d] = 0.f;
+      if (d < T.ndec) {
+        const DecK& D = T.dec[d];
+        const double cc = (double)x * D.zx;
+        const int sx = (int)floor(cc);
+        dxa[d] = clamp_idx(sx, D.w);
+        dxb[d] = clamp_idx(sx + 1, D.w);
+        dfx[d] = (float)(cc - (double)sx);
+      }
+      dm[d][0] = dm[d][1] = dm[d][2] = dm[d][3] = 0.f;
+    }
+    int fya = INT_MIN;
+    float fa = 0.f, fb = 0.f, fc = 0.f, fd = 0.f;
+    const float* zp = z.p + (long long)y0 * z.ld + x;
+    const size_t esz = A.dtype == FSG_F32 ? 4 : (A.dtype == FSG_I16 ? 2 : 1);
+    char* op = T.out + ((long long)(y0 - T.cy0) * A.old + (x - T.cx0)) * (long long)esz;
+    const long long ostep = A.old * (long long)esz;
+    __syncthreads();
+    // running sums of row y0: ring radii from the ring, R by adding its 2R+1 rows G at a time
+    u64 D[NR];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+      const int r = A.radii[q];
+      u64 s = 0ull;
+      if (active)
+        for (int t = y0 - r; t <= y0 + r; ++t) {
+          const u64* row = ring_row(t);
+          s += row[ja[q]] - row[jb[q]];
+        }
+      D[q] = s;
+    }
+    D[NS] = 0ull;
+    for (int t0 = y0 - R; t0 <= y0 + R; t0 += G) {
+      const int tn = min(G, y0 + R + 1 - t0);
+      for (int i = warp; i < tn; i += NW) scan_row(t0 + i, BE + (size_t)i * FX_EP);
+      __syncthreads();
+      if (active)
+        for (int i = 0; i < tn; ++i) D[NS] += BE[(size_t)i * FX_EP + ja[NS]] - BE[(size_t)i * FX_EP + jb[NS]];
+      __syncthreads();
+    }
+    float zn = active ? __ldg(zp) : 0.f;  // z of the next row (prefetched)
+    int tring = y0 + Rs;                  // last ring row scanned
+    for (int yg = y0; yg < y1; yg += G) {
+      const int gn = min(G, y1 - yg);
+      // (scan phase) the group's new ring rows, its entering / leaving rows of R; tables
+      {
+        const int tr_end = min(yg + gn - 1 + Rs, y1 - 1 + Rs);
+        const int nring = max(0, tr_end - tring);
+        const int jobs = nring + 2 * gn;
+        for (int jdx = warp; jdx < jobs; jdx += NW) {
+          if (jdx < nring) {
+            const int t = tring + 1 + jdx;
+            scan_row(t, ring_row(t));
+          } else {
+            const int i = (jdx - nring) % gn, leave = (jdx - nring) / gn;
+            const int y = yg + i;
+            if (y > y0) scan_row(leave ? y - 1 - R : y + R, (leave ? BL : BE) + (size_t)i * FX_EP);
+          }
+        }
+        tring = max(tring, tr_end);
+        if (tid < G * NS) {
+          const int i = tid / NS, q = tid - (tid / NS) * NS;
+          const int r = A.radii[q];
+          const int y = yg + i;
+          const int se = (y + r - tbase) % RING;
+          int sl = y - 1 - r - tbase;
+          sl = sl < 0 ? 0 : sl % RING;
+          OFF[i * HY_MAXNR + q] = make_int2(se * FX_EP, sl * FX_EP);
+        } else if (tid >= 64 && tid < 64 + T.ndec * G) {
+          const int d = (tid - 64) / G, i = (tid - 64) - ((tid - 64) / G) * G;
+          const DecK& Dk = T.dec[d];
+          const double cc = (double)(yg + i) * Dk.zy;
+          const int sy2 = (int)floor(cc);
+          DYi[(d * G + i) * 2] = clamp_idx(sy2, Dk.h);
+          DYi[(d * G + i) * 2 + 1] = clamp_idx(sy2 + 1, Dk.h);
+          DYf[d * G + i] = (float)(cc - (double)sy2);
+        }
+      }
+      __syncthreads();
+      // (pixel phase)
+      if (warp < ncons && active) {
+        for (int i = 0; i < gn; ++i) {
+          const int y = yg + i;
+          const float zv = zn;
+          if (y + 1 < y1) zn = __ldg(zp + z.ld);
+          zp += z.ld;
+          float a = 0.f;
+#pragma unroll
+          for (int q = 0; q < NR; ++q) {
+            if (y > y0) {
+              if (q < NS) {
+                const int2 o = OFF[i * HY_MAXNR + q];
+                D[q] += (fsm[o.x + ja[q]] - fsm[o.x + jb[q]]) - (fsm[o.y + ja[q]] - fsm[o.y + jb[q]]);
+              } else {
+                const u64* be = BE + (size_t)i * FX_EP;
+                const u64* bl = BL + (size_t)i * FX_EP;
+                D[q] += (be[ja[q]] - be[jb[q]]) - (bl[ja[q]] - bl[jb[q]]);
+              }
+            }
+            const long long S = (long long)D[q];
+            const int cnt = (int)S & ((1 << FX_CB) - 1);
+            const float num = __fmul_rn(__ll2float_rn(S >> FX_CB), isk);
+            const float dn = (float)max(cnt, 1), rr = rcp_approx(dn);  // Markstein-corrected num / cnt
+            const float qq = __fmul_rn(num, rr);
+            const float mean = cnt > 0 ? __fmaf_rn(__fmaf_rn(-qq, dn, num), rr, qq) : 0.f;
+            const float dq = __fmul_rn(wq[q], __fsub_rn(zv, mean));
+            a = q == 0 ? dq : __fadd_rn(a, dq);
+          }
+#pragma unroll
+          for (int dd = 0; dd < ST_MAXD; ++dd) {
+            if (dd >= T.ndec) break;
+            const DecK& Dk = T.dec[dd];
+            const int ya = DYi[(dd * G + i) * 2];
+            if (ya != dya[dd]) {
+              const int yb = DYi[(dd * G + i) * 2 + 1];
+              const float* m = Dk.ms;
+              dm[dd][0] = __ldg(m + (long long)ya * Dk.w + dxa[dd]);
+              dm[dd][1] = __ldg(m + (long long)ya * Dk.w + dxb[dd]);
+              dm[dd][2] = __ldg(m + (long long)yb * Dk.w + dxa[dd]);
+              dm[dd][3] = __ldg(m + (long long)yb * Dk.w + dxb[dd]);
+              dya[dd] = ya;
+            }
+            const float fy = DYf[dd * G + i], fx = dfx[dd];
+            const float top = fmaf(fx, dm[dd][1] - dm[dd][0], dm[dd][0]);
+            const float bot = fmaf(fx, dm[dd][3] - dm[dd][2], dm[dd][2]);
+            const float mean = fmaf(fy, bot - top, top);
+            a = __fadd_rn(a, __fmul_rn(Dk.weight, __fsub_rn(zv, mean)));
+          }
+          float v;
+          if (is_nodata(zv, z.ndf, z.has_nodata != 0)) {
+            v = kQNaN;
+          } else {
+            float large = 0.f;
+            if (have_large) {
+              const float cy = __fsub_rn(__fmul_rn(__fadd_rn((float)(T.gy0 + y), 0.5f), A.sy), 0.5f);
+              const float f0 = floorf(cy);
+              const float ty = cy - f0;
+              if ((int)f0 != fya) {
+                const int ya = clamp_idx((int)f0, A.fh), yb = clamp_idx((int)f0 + 1, A.fh);
+                const float* F = A.field;
+                fa = __ldg(F + ya * A.fld + fxa);
+                fb = __ldg(F + ya * A.fld + fxb);
+                fc = __ldg(F + yb * A.fld + fxa);
+                fd = __ldg(F + yb * A.fld + fxb);
+                fya = (int)f0;
+              }
+              const float top = fmaf(ftx, fb - fa, fa);
+              const float bot = fmaf(ftx, fd - fc, fc);
+              large = __fsub_rn(__fmul_rn(A.w_large, zv), fmaf(ty, bot - top, top));
+            }
+            v = have_large ? __fadd_rn(a, large) : a;
+            if (A.scale > 0.f) v = div_by(v, A.scale, A.rscale);
+          }
+          if (A.dtype == FSG_F32) *reinterpret_cast<float*>(op) = v;
+          else if (A.dtype == FSG_U8) *reinterpret_cast<uint8_t*>(op) = (uint8_t)(int)quantize(v, A.qa, A.qb, A.qmin, A.qmax);
+          else *reinterpret_cast<int16_t*>(op) = (int16_t)(int)quantize(v, A.qa, A.qb, A.qmin, A.qmax);
+          op += ostep;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // flag[t] = any NoData in window t (ZView per tile); blockIdx.y = tile.
 __global__ void window_nan_flags(const TopoTileK* tiles, int* flags) {
   const TopoTileK& T = tiles[blockIdx.y];
@@ -1584,6 +1869,26 @@ static int topousm_strip_prepare(const float* raster_dev, int64_t ld, const fsg_
   A.qmax = out->q_max;
   A.have_small = p->nradii > 0;
   A.ring = fx_ring;
+  if (J.fixed && nfull >= 2) {
+    // hybrid: the ring holds the smaller radii only, the largest takes per-group row buffers
+    const int Rs = radii[nfull - 2];
+    const int hy_ring = 2 * Rs + FX_G + 1;
+    const size_t hsmem = HySmem::bytes(hy_ring);
+    if (2 * hsmem + 2 * 1024 <= (size_t)di.smem_per_sm) {
+      switch (nfull) {
+        case 2: J.kern = topousm_hybrid<2>; break;
+        case 3: J.kern = topousm_hybrid<3>; break;
+        default: J.kern = topousm_hybrid<4>; break;
+      }
+      A.ring = hy_ring;
+      J.smem = hsmem;
+      FSG_CUDA(cudaFuncSetAttribute(J.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)J.smem));
+      int per = 0;
+      FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, J.kern, FX_NT, J.smem));
+      J.grid = std::min((int)J.items.size(), di.sms * std::max(1, per));
+      return FSG_OK;
+    }
+  }
   if (J.fixed) {
     switch (nfull) {
       case 1: J.kern = topousm_fixed<1>; break;
