@@ -1052,17 +1052,17 @@ __global__ void __launch_bounds__(FX_NT, 1) topousm_fixed(const __grid_constant_
 // 2R+1 rows through the entering buffer, G rows at a time.
 constexpr int HY_MAXNR = FX_MAXNR;
 struct HySmem {
-  static size_t bytes(int ring) {
-    return sizeof(u64) * FX_EP * ((size_t)ring + 2 * FX_G) + sizeof(int2) * FX_G * HY_MAXNR +
-           3 * sizeof(float) * ST_MAXD * FX_G;
+  static size_t bytes(int ring, int G) {
+    return sizeof(u64) * FX_EP * ((size_t)ring + 2 * G) + sizeof(int2) * G * HY_MAXNR +
+           3 * sizeof(float) * ST_MAXD * G;
   }
 };
 
-template <int NR>
-__global__ void __launch_bounds__(FX_NT, 2) topousm_hybrid(const __grid_constant__ StripArgs A) {
+// HNT threads (>= the strip's output columns), G rows per group, MINB CTAs per SM.
+template <int NR, int HNT, int G, int MINB>
+__global__ void __launch_bounds__(HNT, MINB) topousm_hybrid(const __grid_constant__ StripArgs A) {
   static_assert(NR >= 2, "the hybrid kernel needs a ring radius and a large radius");
   extern __shared__ __align__(16) u64 fsm[];
-  constexpr int G = FX_G;
   constexpr int NS = NR - 1;  // radii served by the ring
   const int RING = A.ring, TW = A.TW, R = A.R;
   u64* ring = fsm;
@@ -1074,14 +1074,14 @@ __global__ void __launch_bounds__(FX_NT, 2) topousm_hybrid(const __grid_constant
   __shared__ TopoTileK Ts;
   const TopoTileK& T = Ts;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  constexpr int NW = FX_NT / 32;
+  constexpr int NW = HNT / 32;
   const int ncons = min(NW, (TW + 31) / 32);
   const unsigned mb = *A.zmax;
   const int e = mb ? (int)((mb >> 23) & 0xFF) - 126 : 0;
   const int k = max(-100, min(100, 33 - e));
   const float sk = ldexpf(1.0f, k), isk = ldexpf(1.0f, -k);
-  for (int r = tid; r < RING; r += FX_NT) ring[(size_t)r * FX_EP] = 0ull;
-  for (int r = tid; r < 2 * G; r += FX_NT) BE[(size_t)r * FX_EP] = 0ull;
+  for (int r = tid; r < RING; r += HNT) ring[(size_t)r * FX_EP] = 0ull;
+  for (int r = tid; r < 2 * G; r += HNT) BE[(size_t)r * FX_EP] = 0ull;
   const int c = tid, b = R + c;
   int ja[NR], jb[NR];
   float wq[NR];
@@ -1096,7 +1096,7 @@ __global__ void __launch_bounds__(FX_NT, 2) topousm_hybrid(const __grid_constant
   for (int it = blockIdx.x; it < A.nitems; it += gridDim.x) {
     const StripItem I = A.items[it];
     __syncthreads();
-    for (int q = tid; q < (int)(sizeof(TopoTileK) / 4); q += FX_NT)
+    for (int q = tid; q < (int)(sizeof(TopoTileK) / 4); q += HNT)
       reinterpret_cast<int*>(&Ts)[q] = reinterpret_cast<const int*>(A.tiles + I.tile)[q];
     __syncthreads();
     const ZView z = T.z;
@@ -1228,8 +1228,8 @@ __global__ void __launch_bounds__(FX_NT, 2) topousm_hybrid(const __grid_constant
           int sl = y - 1 - r - tbase;
           sl = sl < 0 ? 0 : sl % RING;
           OFF[i * HY_MAXNR + q] = make_int2(se * FX_EP, sl * FX_EP);
-        } else if (tid >= 64 && tid < 64 + T.ndec * G) {
-          const int d = (tid - 64) / G, i = (tid - 64) - ((tid - 64) / G) * G;
+        } else if (tid >= 32 && tid < 32 + T.ndec * G) {
+          const int d = (tid - 32) / G, i = (tid - 32) - ((tid - 32) / G) * G;
           const DecK& Dk = T.dec[d];
           const double cc = (double)(yg + i) * Dk.zy;
           const int sy2 = (int)floor(cc);
@@ -1685,6 +1685,7 @@ struct TopoJob {
   StripArgs A;
   void (*kern)(StripArgs) = nullptr;
   size_t smem = 0;
+  int threads = 0;  // block size (0: FX_NT for the fixed kernels, ST_NT otherwise)
   // bound device state
   char* base = nullptr;
   TopoScratch SS[AUX_STREAMS];
@@ -1745,7 +1746,7 @@ struct TopoJob {
     else window_nan_flags<<<dim3(256, ntiles), 256, 0, s>>>(tiles_dev, flags);
     FSG_LAUNCHED(1);
     if (fixed) timing_mark(s, true);
-    kern<<<grid, fixed ? FX_NT : ST_NT, smem, s>>>(A);
+    kern<<<grid, threads ? threads : (fixed ? FX_NT : ST_NT), smem, s>>>(A);
     if (fixed) timing_mark(s, false);
     FSG_LAUNCHED(1);
     return FSG_OK;
@@ -1871,20 +1872,33 @@ static int topousm_strip_prepare(const float* raster_dev, int64_t ld, const fsg_
   A.ring = fx_ring;
   if (J.fixed && nfull >= 2) {
     // hybrid: the ring holds the smaller radii only, the largest takes per-group row buffers
+    // 192 threads and 4-row groups (three CTAs per SM) when the strip has at most 192 output
+    // columns, else 256 threads and 8-row groups (two CTAs per SM)
     const int Rs = radii[nfull - 2];
-    const int hy_ring = 2 * Rs + FX_G + 1;
-    const size_t hsmem = HySmem::bytes(hy_ring);
-    if (2 * hsmem + 2 * 1024 <= (size_t)di.smem_per_sm) {
-      switch (nfull) {
-        case 2: J.kern = topousm_hybrid<2>; break;
-        case 3: J.kern = topousm_hybrid<3>; break;
-        default: J.kern = topousm_hybrid<4>; break;
+    const bool narrow = TW <= 192;
+    const int HG = narrow ? 4 : 8;
+    const int hy_ring = 2 * Rs + HG + 1;
+    const size_t hsmem = HySmem::bytes(hy_ring, HG);
+    if ((narrow ? 3 : 2) * (hsmem + 1024) <= (size_t)di.smem_per_sm && nfull <= HY_MAXNR) {
+      if (narrow) {
+        switch (nfull) {
+          case 2: J.kern = topousm_hybrid<2, 192, 4, 3>; break;
+          case 3: J.kern = topousm_hybrid<3, 192, 4, 3>; break;
+          default: J.kern = topousm_hybrid<4, 192, 4, 3>; break;
+        }
+      } else {
+        switch (nfull) {
+          case 2: J.kern = topousm_hybrid<2, 256, 8, 2>; break;
+          case 3: J.kern = topousm_hybrid<3, 256, 8, 2>; break;
+          default: J.kern = topousm_hybrid<4, 256, 8, 2>; break;
+        }
       }
+      J.threads = narrow ? 192 : 256;
       A.ring = hy_ring;
       J.smem = hsmem;
       FSG_CUDA(cudaFuncSetAttribute(J.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)J.smem));
       int per = 0;
-      FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, J.kern, FX_NT, J.smem));
+      FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, J.kern, J.threads, J.smem));
       J.grid = std::min((int)J.items.size(), di.sms * std::max(1, per));
       return FSG_OK;
     }
