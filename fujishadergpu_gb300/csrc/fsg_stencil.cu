@@ -761,7 +761,9 @@ __device__ __forceinline__ Q4 q4hdiff(Q4 f, float left, float right) {
   return {sub2(P2(f.lo.y, f.hi.x), P2(left, f.lo.x)), sub2(P2(f.hi.y, right), P2(f.lo.y, f.hi.x))};
 }
 
-template <bool CURV, unsigned OM, bool ALLF32>
+// ZONE: z factor 1 (hillshade's derivatives are p, q; rows above/below the
+// stencil's own window are then never read again, so they are not kept).
+template <bool CURV, unsigned OM, bool ALLF32, bool ZONE>
 __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kernel(const __grid_constant__ FastArgs A) {
   constexpr bool DIV = (OM & ((1u << FSG_OUT_DX) | (1u << FSG_OUT_DY))) != 0;
   constexpr int REACH = CURV ? 2 : 1;  // rows above / below an output row that feed it
@@ -922,14 +924,14 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
         q = dv4(q4sub(fp1, fm1), T.g1y);
       }
       Q4 pz = p, qz = q;
-      if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) {
+      if ((OM & (1u << FSG_OUT_HILLSHADE)) && !ZONE) {
         const f2 zf = S2(A.z);
         pz = dv4(hdiff(q4mul(f0, zf), mul2(e0, zf)), T.g1x);
         qz = dv4(q4sub(q4mul(fp1, zf), q4mul(fm1, zf)), T.g1y);
       }
       if (row_nan) {
         Q4 chk = q4add(p, q);
-        if ((OM & (1u << FSG_OUT_HILLSHADE)) && !A.z_is_one) chk = q4add(chk, q4add(pz, qz));
+        if ((OM & (1u << FSG_OUT_HILLSHADE)) && !ZONE) chk = q4add(chk, q4add(pz, qz));
         if (CURV) chk = q4add(q4add(chk, q4add(dxx, dxy)), q4add(dyy, dyx));
         bad |= (nout > 0 && f0.lo.x == f0.lo.x && chk.lo.x != chk.lo.x) ||
                (nout > 1 && f0.lo.y == f0.lo.y && chk.lo.y != chk.lo.y) ||
@@ -937,9 +939,9 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
                (nout > 3 && f0.hi.y == f0.hi.y && chk.hi.y != chk.hi.y);
       }
       f2 olo[FSG_STENCIL_NOUT], ohi[FSG_STENCIL_NOUT];
-      pixel_products2(L, T.slx, T.sly, A.z_is_one != 0, OM, p.lo, q.lo, pz.lo, qz.lo, dxx.lo, dxy.lo, dyy.lo,
+      pixel_products2(L, T.slx, T.sly, ZONE, OM, p.lo, q.lo, pz.lo, qz.lo, dxx.lo, dxy.lo, dyy.lo,
                       dyx.lo, olo);
-      pixel_products2(L, T.slx, T.sly, A.z_is_one != 0, OM, p.hi, q.hi, pz.hi, qz.hi, dxx.hi, dxy.hi, dyy.hi,
+      pixel_products2(L, T.slx, T.sly, ZONE, OM, p.hi, q.hi, pz.hi, qz.hi, dxx.hi, dxy.hi, dyy.hi,
                       dyx.hi, ohi);
       if (nan2(f0.lo) || nan2(f0.hi)) {
 #pragma unroll
@@ -1478,7 +1480,10 @@ static int stencil_prepare(const float* raster_dev, int64_t ld, int32_t raster_h
   switch (outmask) {
 #define FSG_CASE(M, C)                                                                         \
   case (M):                                                                                    \
-    fast = allf32 ? stencil_fast_kernel<C, (M), true> : stencil_fast_kernel<C, (M), false>;    \
+    if (((M) & HS) && A.z_is_one)                                                              \
+      fast = allf32 ? stencil_fast_kernel<C, (M), true, true> : stencil_fast_kernel<C, (M), false, true>; \
+    else                                                                                       \
+      fast = allf32 ? stencil_fast_kernel<C, (M), true, false> : stencil_fast_kernel<C, (M), false, false>; \
     fixup = allf32 ? stencil_fixup_kernel<(M), true> : stencil_fixup_kernel<(M), false>;       \
     break;
     FSG_CASE(HS | SL | CP | CR, true)
