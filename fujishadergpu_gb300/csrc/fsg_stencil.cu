@@ -19,6 +19,8 @@
 // lies in that region, computes dx/dy once into shared memory and emits all
 // requested planes with 4-pixel vector stores.
 #include <algorithm>
+#include <array>
+#include <mutex>
 #include <cstring>
 #include <vector>
 
@@ -1352,6 +1354,11 @@ struct StencilJob {
       A.tiles_dev = static_cast<const TileK*>(dev);
     }
   }
+  // the host image of the tables (tiles_bytes() bytes at dst)
+  void pack(char* dst) const {
+    if (fast) std::memcpy(dst, ft.data(), sizeof(FastTile) * ft.size());
+    else if (tk.size() > (size_t)INLINE_TILES) std::memcpy(dst, tk.data(), sizeof(TileK) * tk.size());
+  }
   int upload(void* dev, cudaStream_t s) const {
     if (fast) FSG_CUDA(cudaMemcpyAsync(dev, ft.data(), sizeof(FastTile) * ft.size(), cudaMemcpyHostToDevice, s));
     else if (tk.size() > (size_t)INLINE_TILES)
@@ -1612,4 +1619,247 @@ extern "C" int fsg_stencil_plan(const float* raster_dev, int64_t ld, int32_t ras
   }
   *plan = P;
   return FSG_OK;
+}
+
+// ------------------------------------------------------ host-buffer loop
+// Host-buffer tile loop of the fused stencil: the single-device equivalent of
+// process_dem_tiles' per-tile read -> H2D -> compute -> D2H cycle
+// (core/tile_processor.py:822-1024, :1629-1683), with the three stages of
+// consecutive batches overlapped.
+//
+// Consecutive tiles that form one row band of the grid (same core rows, cores
+// side by side, one output offset) are one batch: the union of their windows
+// goes down in one copy (one contiguous block when the band spans the
+// raster's full width), one prepared stencil job covers all of its tiles, and
+// each plane's band of cores comes back in one copy.  Other tiles are batches
+// of one.  All jobs are prepared, and their tile tables uploaded in one copy,
+// before the loop, which then issues only pinned copies and launches.
+// Batches are assigned round-robin to NSLOT slots; each slot owns a
+// device window buffer, one device buffer per requested plane and a stream,
+// so the H2D copy of one batch, the kernels of the previous one and the D2H
+// copies of the one before that run concurrently (separate copy engines for
+// the two directions).  The slots' streams are ordered after, and joined back
+// into, the caller's stream with events.
+namespace fsg {
+namespace {
+
+constexpr int NSLOT = 3;
+constexpr size_t kBandSlotBytes = (size_t)6 << 30;  // larger bands run tile by tile
+
+struct SlotStreams {
+  cudaStream_t s[NSLOT] = {};
+  cudaEvent_t done[NSLOT] = {};
+  cudaEvent_t start = nullptr;
+};
+std::mutex g_slot_mutex;
+SlotStreams g_slots[64];
+bool g_slots_ready[64] = {};
+
+int slot_streams(SlotStreams** out) {
+  int dev = 0;
+  FSG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(FSG_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_slot_mutex);
+  if (!g_slots_ready[dev]) {
+    SlotStreams& S = g_slots[dev];
+    for (int i = 0; i < NSLOT; ++i) {
+      FSG_CUDA(cudaStreamCreateWithFlags(&S.s[i], cudaStreamNonBlocking));
+      FSG_CUDA(cudaEventCreateWithFlags(&S.done[i], cudaEventDisableTiming));
+    }
+    FSG_CUDA(cudaEventCreateWithFlags(&S.start, cudaEventDisableTiming));
+    g_slots_ready[dev] = true;
+  }
+  *out = &g_slots[dev];
+  return FSG_OK;
+}
+
+size_t esize(int dtype) { return dtype == FSG_F32 ? 4 : (dtype == FSG_I16 ? 2 : 1); }
+
+// A batch: tiles [t0, t1) with the union of their windows and of their cores.
+struct Batch {
+  int t0, t1;
+  int wy0, wx0, wh, ww;  // window union (raster coords)
+  int cy0, cx0, ch, cw;  // core union (raster coords)
+  int oy0, ox0;          // output coords of (cy0, cx0)
+};
+
+std::vector<Batch> make_batches(const fsg_tile* tiles, int ntiles, int nplanes_f32_equiv) {
+  std::vector<Batch> out;
+  int t = 0;
+  while (t < ntiles) {
+    const fsg_tile& A = tiles[t];
+    Batch b{t, t + 1, A.win_y0, A.win_x0, A.win_h, A.win_w, A.core_y0, A.core_x0, A.core_h, A.core_w, A.out_y0,
+            A.out_x0};
+    int u = t + 1;
+    while (u < ntiles) {
+      const fsg_tile& B = tiles[u];
+      const fsg_tile& P = tiles[u - 1];
+      // same core rows, next core directly to the right, same output offset
+      if (B.core_y0 != A.core_y0 || B.core_h != A.core_h || B.core_x0 != P.core_x0 + P.core_w ||
+          B.out_y0 - B.core_y0 != A.out_y0 - A.core_y0 || B.out_x0 - B.core_x0 != A.out_x0 - A.core_x0 ||
+          B.core_w == 0)
+        break;
+      const int wy1 = std::max(b.wy0 + b.wh, B.win_y0 + B.win_h), wx1 = std::max(b.wx0 + b.ww, B.win_x0 + B.win_w);
+      const int wy0 = std::min(b.wy0, B.win_y0), wx0 = std::min(b.wx0, B.win_x0);
+      const size_t bytes = (size_t)(wy1 - wy0) * (wx1 - wx0) * 4 +
+                           (size_t)b.ch * (b.cw + B.core_w) * 4 * (size_t)nplanes_f32_equiv;
+      if (bytes > kBandSlotBytes) break;
+      b.wy0 = wy0;
+      b.wx0 = wx0;
+      b.wh = wy1 - wy0;
+      b.ww = wx1 - wx0;
+      b.cw += B.core_w;
+      b.t1 = ++u;
+    }
+    out.push_back(b);
+    t = u;
+  }
+  return out;
+}
+
+}  // namespace
+}  // namespace fsg
+
+
+extern "C" int fsg_stencil_host(const float* raster_host, int64_t ld, int32_t raster_h, int32_t raster_w,
+                                const fsg_tile* tiles, int32_t ntiles, const fsg_stencil_params* params,
+                                const fsg_plane* planes_host, void* stream) {
+  using namespace fsg;
+  if (!raster_host || !params || !planes_host || (ntiles > 0 && !tiles)) return fail(FSG_ERR_INVALID, "null argument");
+  if (ntiles < 0 || raster_h < 0 || raster_w < 0 || ld < raster_w) return fail(FSG_ERR_INVALID, "bad raster shape");
+  int st = validate_tiles(raster_h, raster_w, tiles, ntiles, 3);
+  if (st) return st;
+  std::vector<int> req;
+  for (int o = 0; o < FSG_STENCIL_NOUT; ++o)
+    if (planes_host[o].ptr) {
+      if (planes_host[o].dtype < FSG_F32 || planes_host[o].dtype > FSG_I16)
+        return fail(FSG_ERR_DTYPE, "plane %d: dtype %d", o, planes_host[o].dtype);
+      req.push_back(o);
+    }
+  if (req.empty()) return fail(FSG_ERR_INVALID, "no output plane requested");
+  if (ntiles == 0) return FSG_OK;
+  const std::vector<Batch> batches = make_batches(tiles, ntiles, (int)req.size());
+  int maxwh = 0, maxww = 0, maxch = 0, maxcw = 0;
+  for (const Batch& b : batches) {
+    maxwh = std::max(maxwh, b.wh);
+    maxww = std::max(maxww, b.ww);
+    maxch = std::max(maxch, b.ch);
+    maxcw = std::max(maxcw, b.cw);
+  }
+  if (maxch == 0 || maxcw == 0) return FSG_OK;
+  const int64_t wpitch = ((int64_t)maxww + 31) & ~(int64_t)31;  // elements, 128-byte rows
+  const int64_t cpitch = ((int64_t)maxcw + 127) & ~(int64_t)127;  // elements of each core plane row
+  size_t slot_bytes = (size_t)wpitch * maxwh * sizeof(float);
+  for (int o : req) slot_bytes += (size_t)cpitch * maxch * esize(planes_host[o].dtype) + 256;
+  slot_bytes = (slot_bytes + 255) & ~(size_t)255;
+  cudaStream_t caller = (cudaStream_t)stream;
+  SlotStreams* S = nullptr;
+  st = slot_streams(&S);
+  if (st) return st;
+  const int nslot = std::min<int>(NSLOT, (int)batches.size());
+  // every batch prepared first (its window and planes are its slot's buffers), the tile tables
+  // of all batches uploaded in one copy: inside the loop only pinned copies and launches remain
+  // (a pageable host-to-device copy synchronises its stream, which would stall the pipeline)
+  std::vector<StencilJob> jobs(batches.size());
+  std::vector<size_t> job_off(batches.size(), 0);
+  std::vector<int64_t> bpitch(batches.size(), 0);
+  std::vector<std::array<int64_t, FSG_STENCIL_NOUT>> opitch(batches.size());
+  std::vector<std::array<char*, FSG_STENCIL_NOUT>> optr(batches.size());
+  size_t tables = 0;
+  std::vector<fsg_tile> local;
+  const size_t slots_total = slot_bytes * nslot;
+  // pass 1: layout (device pointers are bound after the allocation)
+  for (size_t bi = 0; bi < batches.size(); ++bi) {
+    const Batch& B = batches[bi];
+    if (B.ch == 0 || B.cw == 0) continue;
+    bpitch[bi] = (B.wx0 == 0 && B.ww == raster_w && ld == raster_w) ? (int64_t)raster_w : wpitch;
+    for (int o : req) opitch[bi][o] = (B.cw == planes_host[o].ld) ? (int64_t)B.cw : cpitch;
+  }
+  StreamScratch scratch;
+  // the job tables' sizes depend on the tiles only: prepare against placeholder pointers, then rebind
+  for (size_t bi = 0; bi < batches.size(); ++bi) {
+    const Batch& B = batches[bi];
+    if (B.ch == 0 || B.cw == 0) continue;
+    const int k = (int)(bi % nslot);
+    fsg_plane dev_planes[FSG_STENCIL_NOUT];
+    std::memset(dev_planes, 0, sizeof(dev_planes));
+    size_t p = (size_t)wpitch * maxwh * sizeof(float);
+    for (int o : req) {
+      dev_planes[o] = planes_host[o];
+      dev_planes[o].ptr = reinterpret_cast<void*>((uintptr_t)(slot_bytes * k + p + 1));  // offset + 1 (non-null)
+      dev_planes[o].ld = opitch[bi][o];
+      p += ((size_t)cpitch * maxch * esize(planes_host[o].dtype) + 255) & ~(size_t)255;
+    }
+    local.assign(tiles + B.t0, tiles + B.t1);
+    for (fsg_tile& T : local) {
+      T.win_y0 -= B.wy0;
+      T.win_x0 -= B.wx0;
+      T.core_y0 -= B.wy0;
+      T.core_x0 -= B.wx0;
+      T.out_y0 = (T.core_y0 + B.wy0) - B.cy0;
+      T.out_x0 = (T.core_x0 + B.wx0) - B.cx0;
+    }
+    const float* win_off = reinterpret_cast<const float*>((uintptr_t)(slot_bytes * k + 1));
+    st = stencil_prepare(win_off, bpitch[bi], B.wh, B.ww, local.data(), (int)local.size(), params, dev_planes,
+                         jobs[bi]);
+    if (st) return st;
+    job_off[bi] = slots_total + tables;
+    tables += (jobs[bi].device_bytes() + 255) & ~(size_t)255;
+  }
+  st = scratch.alloc(slots_total + tables, caller);
+  if (st) return st;
+  char* base = static_cast<char*>(scratch.ptr);
+  std::vector<char> image(std::max<size_t>(tables, 1));
+  auto rebase = [&](const void* off) { return base + ((uintptr_t)off - 1); };
+  for (size_t bi = 0; bi < batches.size(); ++bi) {
+    const Batch& B = batches[bi];
+    if (B.ch == 0 || B.cw == 0) continue;
+    StencilJob& J = jobs[bi];
+    for (int o : req) {
+      optr[bi][o] = rebase(J.A.planes[o].ptr);
+      J.A.planes[o].ptr = optr[bi][o];
+      J.F.planes[o].ptr = optr[bi][o];
+    }
+    J.A.raster = reinterpret_cast<const float*>(rebase(J.A.raster));
+    J.F.raster = J.A.raster;
+    J.bind(base + job_off[bi]);
+    J.pack(image.data() + (job_off[bi] - slots_total));
+  }
+  if (tables) FSG_CUDA(cudaMemcpyAsync(base + slots_total, image.data(), tables, cudaMemcpyHostToDevice, caller));
+  FSG_CUDA(cudaEventRecord(S->start, caller));
+  for (int i = 0; i < nslot; ++i) FSG_CUDA(cudaStreamWaitEvent(S->s[i], S->start, 0));
+  int status = FSG_OK;
+  for (size_t bi = 0; bi < batches.size() && status == FSG_OK; ++bi) {
+    const Batch& B = batches[bi];
+    if (B.ch == 0 || B.cw == 0) continue;
+    const int k = (int)(bi % nslot);
+    cudaStream_t s = S->s[k];
+    float* win = reinterpret_cast<float*>(base + slot_bytes * k);
+    // H2D: the window union (one contiguous block for a full-width band)
+    cudaError_t e = cudaMemcpy2DAsync(win, bpitch[bi] * sizeof(float), raster_host + (int64_t)B.wy0 * ld + B.wx0,
+                                      ld * sizeof(float), (size_t)B.ww * sizeof(float), B.wh,
+                                      cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+      status = cuda_fail(e, "cudaMemcpy2DAsync(H2D window)");
+      break;
+    }
+    status = jobs[bi].enqueue(s);
+    if (status) break;
+    // D2H: the band of cores of every plane, into the caller's planes at (oy0, ox0)
+    for (int o : req) {
+      const size_t es = esize(planes_host[o].dtype);
+      char* dst = static_cast<char*>(planes_host[o].ptr) + ((int64_t)B.oy0 * planes_host[o].ld + B.ox0) * es;
+      e = cudaMemcpy2DAsync(dst, planes_host[o].ld * es, optr[bi][o], opitch[bi][o] * es, (size_t)B.cw * es, B.ch,
+                            cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) {
+        status = cuda_fail(e, "cudaMemcpy2DAsync(D2H plane)");
+        break;
+      }
+    }
+  }
+  for (int i = 0; i < nslot; ++i) {
+    cudaEventRecord(S->done[i], S->s[i]);
+    cudaStreamWaitEvent(caller, S->done[i], 0);
+  }
+  return status;
 }
