@@ -15,9 +15,10 @@
 //   (algorithms/tile/dask_bridge.py:173-187).
 //
 // atan is monotonic, so the per-direction extreme angle is atan of the
-// extreme slope ratio: each sample costs one load, one subtract, one
-// correctly rounded divide by the float32 distance (the reference's float32
-// division) and one max; atan runs once per direction.
+// extreme slope ratio: each sample costs one load, one subtract, one multiply
+// by the rounded reciprocal of its float32 distance (within 1.5 ulp of the
+// reference's float32 division; the mean angle's tolerance is 0.01 degree)
+// and one max; atan runs once per direction.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -71,13 +72,9 @@ __device__ __forceinline__ float load_z(const OpenArgs& A, int y, int x, const f
 
 typedef float2 f2;
 __device__ __forceinline__ f2 S2(float a) { return make_float2(a, a); }
-// (v - z) / d per component, correctly rounded (Markstein's correction, as
-// div_by); nz = -z, nd = -d (q * -d == -(q * d) exactly)
-__device__ __forceinline__ f2 slope2(f2 v, f2 nz, float nd, float r) {
-  const f2 num = __fadd2_rn(v, nz);
-  const f2 q = __fmul2_rn(num, S2(r));
-  const f2 e = __ffma2_rn(q, S2(nd), num);
-  return __ffma2_rn(e, S2(r), q);
+// (v - z) / d per component as (v - z) * RN(1/d); nz = -z
+__device__ __forceinline__ f2 slope2(f2 v, f2 nz, float r) {
+  return __fmul2_rn(__fadd2_rn(v, nz), S2(r));
 }
 __device__ __forceinline__ float nd_nan(float v, const OpenArgs& A) {
   return is_nodata(v, A.ndf, true) ? __int_as_float(0x7fc00000) : v;
@@ -88,8 +85,17 @@ __device__ __forceinline__ float nd_nan(float v, const OpenArgs& A) {
 // operand), atan of it once per direction, directional mean.  Blocks whose
 // rays stay inside the window (all but the window's outer ring) take the
 // interior path: one element offset per sample, no bounds checks.
-template <bool POS, bool HN>
-__global__ void __launch_bounds__(BX * BY) openness_kernel(const __grid_constant__ OpenArgs A) {
+// IDX32: the raster holds fewer than 2^32 elements, so the interior path
+// addresses samples with 32-bit element indices from the raster base.
+#ifndef FSG_OPEN_MINB
+#define FSG_OPEN_MINB 4  // resident blocks per SM the register budget must allow (occupancy hides the gathers)
+#endif
+#ifndef FSG_OPEN_UNROLL
+#define FSG_OPEN_UNROLL 1  // samples per iteration of the interior sample loop
+#endif
+constexpr int OPEN_UNROLL = FSG_OPEN_UNROLL;
+template <bool POS, bool HN, bool IDX32>
+__global__ void __launch_bounds__(BX * BY, FSG_OPEN_MINB) openness_kernel(const __grid_constant__ OpenArgs A) {
   extern __shared__ unsigned char osm[];
   int* soff = reinterpret_cast<int*>(osm);             // [ns] element offset oy * ld + ox
   float* sd = reinterpret_cast<float*>(soff + A.ns);   // [ns] distance
@@ -142,6 +148,9 @@ __global__ void __launch_bounds__(BX * BY) openness_kernel(const __grid_constant
       cnt[k] = S2(0.f);
     }
     const float* base = A.raster + (long long)yb * A.ld + x;
+    const unsigned idx0 = IDX32 ? (unsigned)((long long)yb * A.ld + x) : 0u;
+    // x is even and the raster base and row pitch keep even elements 8-byte aligned
+    const bool pair_ok = ((x & 1) == 0) && ((A.ld & 1) == 0) && ((reinterpret_cast<uintptr_t>(A.raster) & 7) == 0);
     f2 nz[RPT];
 #pragma unroll
     for (int k = 0; k < RPT; ++k) nz[k] = make_float2(-z[k].x, -z[k].y);
@@ -150,14 +159,22 @@ __global__ void __launch_bounds__(BX * BY) openness_kernel(const __grid_constant
 #pragma unroll
       for (int k = 0; k < RPT; ++k) ext[k] = S2(init);
       if (interior) {
+#pragma unroll OPEN_UNROLL
         for (int s = rb[d]; s < rb[d + 1]; ++s) {
-          const float* ps = base + soff[s];
-          const float nd = -sd[s], rr = sr[s];
+          const int so = soff[s];
+          const float rr = sr[s];
+          // the pixel pair's sample pair is 8-byte aligned when the offset is even (uniform per sample)
+          const bool pair = pair_ok && (so & 1) == 0;
 #pragma unroll
           for (int k = 0; k < RPT; ++k) {
-            f2 v = make_float2(__ldg(ps + (long long)k * A.ld), __ldg(ps + (long long)k * A.ld + 1));
+            const float* pk;
+            if (IDX32) pk = A.raster + (unsigned)(idx0 + (unsigned)k * (unsigned)A.ld + (unsigned)so);
+            else pk = base + (long long)k * A.ld + so;
+            f2 v;
+            if (pair) v = __ldg(reinterpret_cast<const float2*>(pk));
+            else v = make_float2(__ldg(pk), __ldg(pk + 1));
             if (HN) v = make_float2(nd_nan(v.x, A), nd_nan(v.y, A));
-            const f2 t = slope2(v, nz[k], nd, rr);
+            const f2 t = slope2(v, nz[k], rr);
             ext[k].x = POS ? fmaxf(ext[k].x, t.x) : fminf(ext[k].x, t.x);
             ext[k].y = POS ? fmaxf(ext[k].y, t.y) : fminf(ext[k].y, t.y);
           }
@@ -165,11 +182,11 @@ __global__ void __launch_bounds__(BX * BY) openness_kernel(const __grid_constant
       } else {
         for (int s = rb[d]; s < rb[d + 1]; ++s) {
           const int ox = sox[s], oy = soy[s];
-          const float nd = -sd[s], rr = sr[s];
+          const float rr = sr[s];
 #pragma unroll
           for (int k = 0; k < RPT; ++k) {
             const f2 v = make_float2(load_z(A, yb + k + oy, x + ox, T), load_z(A, yb + k + oy, x + 1 + ox, T));
-            const f2 t = slope2(v, nz[k], nd, rr);
+            const f2 t = slope2(v, nz[k], rr);
             ext[k].x = POS ? fmaxf(ext[k].x, t.x) : fminf(ext[k].x, t.x);
             ext[k].y = POS ? fmaxf(ext[k].y, t.y) : fminf(ext[k].y, t.y);
           }
@@ -424,8 +441,14 @@ static int openness_prepare(const float* raster_dev, int64_t ld, int32_t raster_
   if ((long long)p->max_distance * ld >= (1LL << 31))
     return fail(FSG_ERR_UNSUPPORTED, "max_distance %d x row pitch %lld exceeds 32-bit offsets", p->max_distance,
                 (long long)ld);
-  void (*kern)(OpenArgs) = A.positive ? (A.has_nodata ? openness_kernel<true, true> : openness_kernel<true, false>)
-                                      : (A.has_nodata ? openness_kernel<false, true> : openness_kernel<false, false>);
+  const bool idx32 = (unsigned long long)ld * (unsigned long long)raster_h < (1ull << 32);
+  void (*kern)(OpenArgs) = nullptr;
+  if (idx32)
+    kern = A.positive ? (A.has_nodata ? openness_kernel<true, true, true> : openness_kernel<true, false, true>)
+                      : (A.has_nodata ? openness_kernel<false, true, true> : openness_kernel<false, false, true>);
+  else
+    kern = A.positive ? (A.has_nodata ? openness_kernel<true, true, false> : openness_kernel<true, false, false>)
+                      : (A.has_nodata ? openness_kernel<false, true, false> : openness_kernel<false, false, false>);
   const size_t smem = (size_t)per_tile * (3 * sizeof(float) + 2 * sizeof(short)) + 16;
   if (smem > 48 * 1024) FSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
