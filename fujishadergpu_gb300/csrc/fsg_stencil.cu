@@ -1200,6 +1200,9 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
       for (int i = tid; i < XD_R * XD_C; i += XNT) {
         const int r = i / XD_C, c = i - (i / XD_C) * XD_C;
         const int gy = y0 - 2 + r, gx = x0 - 2 + c;
+        // an interior unit needs the derivatives within one cell of the pixels it recomputes
+        // (D row r, column c = E row r + 2, column c + 2)
+        if (!edge && !(((AF[r + 1] | AF[r + 2] | AF[r + 3]) >> (c + 1)) & 7ull)) continue;
         float dx = qnan, dy = qnan;
         if (gy >= T.wy0 && gy < T.wy1 && gx >= T.wx0 && gx < T.wx1) {
           dx = deriv_d<DIV>(T.g1x, gx, T.wx0, T.wx1, [&](int k) { return fe(gy, gx + k); });
