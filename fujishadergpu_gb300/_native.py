@@ -105,6 +105,7 @@ _SIGNATURES = {
     "fsg_launch_count": (C.c_int64, []),
     "fsg_timing_begin": (C.c_int, [C.c_int32]),
     "fsg_timing_end": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
+    "fsg_kernel_errors": (C.c_int, [C.POINTER(C.c_uint32)]),
     "fsg_nodata_mask": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                   C.c_void_p, C.c_int64, C.c_void_p]),
     "fsg_stencil": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
@@ -211,6 +212,13 @@ def check(status: int) -> None:
 
 def launch_count() -> int:
     return int(lib().fsg_launch_count())
+
+
+def kernel_errors() -> int:
+    """Device-side failure flags since the last call (cleared on read; 0 = none)."""
+    v = C.c_uint32(0)
+    check(lib().fsg_kernel_errors(C.byref(v)))
+    return int(v.value)
 
 
 class kernel_timer:

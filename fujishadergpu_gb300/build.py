@@ -71,7 +71,7 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     with cf.ThreadPoolExecutor(jobs) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), srcs))
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcuda"]
+    cmd = [nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

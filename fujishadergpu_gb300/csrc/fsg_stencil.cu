@@ -24,6 +24,9 @@
 #include <cstring>
 #include <vector>
 
+#include <cuda.h>
+#include <cstdlib>
+
 #include "fsg_common.cuh"
 
 namespace fsg {
@@ -544,7 +547,9 @@ __global__ void __launch_bounds__(NT, FSG_STENCIL_MINB) stencil_kernel(const __g
 // listed unit exactly (NaN fill, one-sided edge formulas), as two halves of
 // FW = 30 columns.
 constexpr int SW = 128, SH = 64, FW = 32, NQ = SW / FW;  // unit 128 x 64; fix-up in quarters of 32 columns
-constexpr int RW = SW + 4;  // ring row: the unit's 128 columns, then x0-2, x0-1, x0+128, x0+129
+// ring row: columns x0-4 .. x0+131 (the unit's 128 columns at offset 4, its halo x0-2, x0-1 at 2, 3
+// and x0+128, x0+129 at 132, 133), one tensor-copy box; rows 640 bytes apart (128-byte aligned)
+constexpr int RBOX = SW + 8, RW = 160;
 
 struct FastTile {
   int wy0, wx0, wy1, wx1, cy0, cx0, cy1, cx1, oy0, ox0;
@@ -567,7 +572,13 @@ struct FastArgs {
   unsigned* fix_count;  // number of entries in fix_list
   FF gw[5];                   // Gaussian fill weights (float-float)
   PlaneK planes[FSG_STENCIL_NOUT];
+  int use_tma;                // tmap describes the raster (16-byte aligned base and row pitch)
+  CUtensorMap tmap;           // 2-D float32 raster, box RBOX x 1
 };
+
+// Device-side failures the host reads with fsg_kernel_errors (bit 0: a streaming-pass
+// wait on a tensor copy ran out of polls).
+__device__ unsigned g_kernel_errors;
 
 constexpr unsigned FIX_EDGE = 0x80000000u, FIX_QSHIFT = 28, FIX_UNIT = (1u << FIX_QSHIFT) - 1u;
 // queue the quarters of unit u whose bit is set in qmask (entry = unit | quarter << 28 | edge flag)
@@ -750,6 +761,33 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile("{ .reg .b64 st; mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1; }" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+// bounded wait for phase `parity` of the barrier: false when it did not complete in time
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    unsigned done;
+    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                 : "=r"(done)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+// one box of the 2-D tensor map at element (x, y) into shared memory, completion on `bar`
+__device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap* map, int x, int y, unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
 // Four columns of a lane as two pairs, plus the lane's edge pair: lane 0 keeps
 // (f[x0-2], f[x0-1]) and lane 31 (f[x0+128], f[x0+129]) (unused elsewhere).
 struct Q4 {
@@ -769,12 +807,23 @@ template <bool CURV, unsigned OM, bool ALLF32, bool ZONE>
 __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kernel(const __grid_constant__ FastArgs A) {
   constexpr bool DIV = (OM & ((1u << FSG_OUT_DX) | (1u << FSG_OUT_DY))) != 0;
   constexpr int REACH = CURV ? 2 : 1;  // rows above / below an output row that feed it
-  __shared__ __align__(16) float ring_s[FSG_FAST_NT / 32][RING][RW];
+  extern __shared__ __align__(1024) float ring_dyn[];  // [warps][RING][RW] floats, then [warps][RING] barriers
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  float* ring = ring_s[threadIdx.x >> 5][0];
+  float* ring = ring_dyn + (size_t)(threadIdx.x >> 5) * RING * RW;
   const unsigned sbase = (unsigned)__cvta_generic_to_shared(ring);
+  const unsigned bbase = (unsigned)__cvta_generic_to_shared(ring_dyn + (size_t)(FSG_FAST_NT / 32) * RING * RW) +
+                         (unsigned)(threadIdx.x >> 5) * RING * 8u;  // this warp's RING barriers
+  if (A.use_tma) {
+    if (lane == 0) {
+      for (int i = 0; i < RING; ++i) mbar_init(bbase + 8u * i, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncwarp();
+  }
+  unsigned tma_issued = 0, tma_taken = 0;  // rows of this warp through the tensor path (slot, phase)
   const bool hn = A.has_nodata != 0;
   const Light L{A.lx, A.ly, A.lz, A.slope_unit};
   const float qnan = __int_as_float(0x7fc00000);
@@ -806,27 +855,44 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
     const int nout = min(4, max(0, xo - xl));
     // 16-byte copies need a 16-byte aligned start for every row (uniform per unit)
     const bool vload = ((A.ld & 3) == 0) && ((((uintptr_t)A.raster >> 2) + (uintptr_t)x0) & 3) == 0;
+    // the tensor path: one box per row from x0-4, whose x must be a multiple of 4 elements
+    const bool tma = A.use_tma && (x0 & 3) == 0;
     const bool lfull = xl + 3 < T.wx1;
     const int nrows = (y1 - y0) + 2 * REACH;      // rows y0-REACH .. y1+REACH-1
     const float* src0 = A.raster + (long long)(y0 - REACH) * A.ld;
-    // row k of the unit -> ring slot k % RING; RING-1 copy groups in flight
+    const unsigned tma0 = tma_issued;             // this unit's first tensor-path row
+    bool failed = false;
+    if (tma && lane == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // after any cp.async unit
+    __syncwarp();
+    // row k of the unit -> ring slot; RING-1 rows in flight
     auto issue = [&](int k) {
+      if (tma) {
+        if (k < nrows) {
+          const unsigned slot = (tma0 + (unsigned)k) % RING;
+          if (lane == 0) {
+            mbar_expect_tx(bbase + 8u * slot, RBOX * 4);
+            tma_load_2d(sbase + slot * (RW * 4), &A.tmap, x0 - 4, y0 - REACH + k, bbase + 8u * slot);
+          }
+          ++tma_issued;
+        }
+        return;
+      }
       if (k < nrows) {
         const float* gp = src0 + (long long)k * A.ld;
         const unsigned dst = sbase + (unsigned)((k % RING) * (RW * 4));
         if (vload && lfull) {
-          cp_async16(dst + 16 * lane, gp + xl);
+          cp_async16(dst + 16 + 16 * lane, gp + xl);
         } else {
 #pragma unroll
           for (int m = 0; m < 4; ++m)
-            if (xl + m < T.wx1) cp_async4(dst + 4 * (4 * lane + m), gp + xl + m);
+            if (xl + m < T.wx1) cp_async4(dst + 16 + 4 * (4 * lane + m), gp + xl + m);
         }
         if (lane == 0) {
-          cp_async4(dst + 4 * SW, gp + x0 - 2);
-          cp_async4(dst + 4 * SW + 4, gp + x0 - 1);
+          cp_async4(dst + 8, gp + x0 - 2);
+          cp_async4(dst + 12, gp + x0 - 1);
           if (x0 + SW + 1 < T.wx1) {
-            cp_async4(dst + 4 * SW + 8, gp + x0 + SW);
-            cp_async4(dst + 4 * SW + 12, gp + x0 + SW + 1);
+            cp_async4(dst + 4 * (SW + 4), gp + x0 + SW);
+            cp_async4(dst + 4 * (SW + 5), gp + x0 + SW + 1);
           }
         }
       }
@@ -835,13 +901,21 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
     int nan_left = 0;  // rows for which the NoData seen last still feeds an output
     // take row k: the lane's four columns and its edge pair
     auto take = [&](int k, Q4& f, f2& e) {
-      cp_async_wait<RING - 2>();
-      __syncwarp();
-      const float* rp = ring + (k % RING) * RW;
-      const float4 v = *reinterpret_cast<const float4*>(rp + 4 * lane);
-      const float4 h = *reinterpret_cast<const float4*>(rp + SW);
+      const float* rp;
+      if (tma) {
+        const unsigned slot = tma_taken % RING, parity = (tma_taken / RING) & 1u;
+        if (!mbar_wait(bbase + 8u * slot, parity)) failed = true;
+        ++tma_taken;
+        rp = ring + slot * RW;
+      } else {
+        cp_async_wait<RING - 2>();
+        __syncwarp();
+        rp = ring + (k % RING) * RW;
+      }
+      const float4 v = *reinterpret_cast<const float4*>(rp + 4 + 4 * lane);
+      const float2 h = *reinterpret_cast<const float2*>(rp + (e31lane ? SW + 4 : 2));
       f = {P2(v.x, v.y), P2(v.z, v.w)};
-      e = e31lane ? P2(h.z, h.w) : P2(h.x, h.y);
+      e = P2(h.x, h.y);
       __syncwarp();
       issue(k + RING - 1);
       if (hn) {
@@ -1002,6 +1076,16 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
           em1 = e0; e0 = ep1; ep1 = ne;
         }
       }
+    }
+    if (tma && __any_sync(0xffffffffu, failed)) {
+      // a tensor copy did not arrive in time: record it, give the copies still in flight a
+      // bounded wait, and stop this warp (the host reads the flag with fsg_kernel_errors)
+      if (lane == 0) {
+        atomicOr(&g_kernel_errors, 1u);
+        for (unsigned r = tma_taken; r < tma_issued; ++r) mbar_wait(bbase + 8u * (r % RING), (r / RING) & 1u);
+      }
+      __syncwarp();
+      return;
     }
     // quarters (eight lanes each) holding a pixel whose stencil reached NoData
     const unsigned bb = __ballot_sync(0xffffffffu, bad);
@@ -1330,6 +1414,25 @@ namespace fsg {
 // The eager entry point uploads the tables into stream-ordered scratch and
 // launches; a plan uploads them once into memory it owns, and each launch
 // then only issues a memset and kernels (capturable in a CUDA graph).
+constexpr size_t FAST_SMEM = sizeof(float) * (FSG_FAST_NT / 32) * RING * RW + 8 * (FSG_FAST_NT / 32) * RING;
+
+// cuTensorMapEncodeTiled is a driver entry point: it is looked up through the runtime once, so
+// the library loads (and its symbols resolve) where no driver is installed
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled_fn() {
+  static EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
 struct StencilJob {
   bool empty = true, fast = false;
   StencilArgs A;
@@ -1368,13 +1471,33 @@ struct StencilJob {
       FSG_CUDA(cudaMemcpyAsync(dev, tk.data(), sizeof(TileK) * tk.size(), cudaMemcpyHostToDevice, s));
     return FSG_OK;
   }
+  // the streaming pass's tensor map of the raster (once its device pointer is final): a 2-D
+  // float32 map with RBOX x 1 boxes; without a 16-byte aligned base and row pitch the pass
+  // fills its ring with cp.async instead
+  void encode_tmap() {
+    F.use_tma = 0;
+    if (!fast || !F.raster || A.rw < 1 || A.rh < 1) return;
+    if (((uintptr_t)F.raster & 15) != 0 || (F.ld & 3) != 0) return;
+    const char* off = getenv("FSG_NO_TMA");
+    if (off && off[0] == '1') return;
+    cuuint64_t dims[2] = {(cuuint64_t)A.rw, (cuuint64_t)A.rh};
+    cuuint64_t strides[1] = {(cuuint64_t)F.ld * sizeof(float)};
+    cuuint32_t box[2] = {(cuuint32_t)RBOX, 1};
+    cuuint32_t estr[2] = {1, 1};
+    const EncodeTiledFn enc = encode_tiled_fn();
+    if (!enc) return;
+    const CUresult r = enc(&F.tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(F.raster), dims, strides, box,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    F.use_tma = r == CUDA_SUCCESS ? 1 : 0;
+  }
   // launches only (no host memory involved)
   int enqueue(cudaStream_t s) const {
     if (empty) return FSG_OK;
     if (fast) {
       FSG_CUDA(cudaMemsetAsync(F.fix_count, 0, sizeof(unsigned), s));
       timing_mark(s, true);
-      fastk<<<fgrid, FSG_FAST_NT, 0, s>>>(F);
+      fastk<<<fgrid, FSG_FAST_NT, FAST_SMEM, s>>>(F);
       timing_mark(s, false);
       FSG_LAUNCHED(1);
       fixk<<<xgrid, XNT, FIX_SMEM, s>>>(F);
@@ -1545,7 +1668,8 @@ static int stencil_prepare(const float* raster_dev, int64_t ld, int32_t raster_h
     J.fastk = fast;
     J.fixk = fixup;
     int fper = 0;
-    FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fper, fast, FSG_FAST_NT, 0));
+    FSG_CUDA(cudaFuncSetAttribute(fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FAST_SMEM));
+    FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fper, fast, FSG_FAST_NT, FAST_SMEM));
     J.fgrid = std::min((units + FSG_FAST_NT / 32 - 1) / (FSG_FAST_NT / 32), di.sms * std::max(1, fper));  // one unit per warp
     FSG_CUDA(cudaFuncSetAttribute(fixup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FIX_SMEM));
     int xper = 0;
@@ -1580,6 +1704,7 @@ extern "C" int fsg_stencil(const float* raster_dev, int64_t ld, int32_t raster_h
   StencilJob J;
   int st = stencil_prepare(raster_dev, ld, raster_h, raster_w, tiles, ntiles, params, planes, J);
   if (st || J.empty) return st;
+  J.encode_tmap();
   cudaStream_t s = (cudaStream_t)stream;
   StreamScratch scratch;
   const size_t bytes = J.device_bytes();
@@ -1601,6 +1726,7 @@ extern "C" int fsg_stencil_plan(const float* raster_dev, int64_t ld, int32_t ras
   *plan = nullptr;
   StencilPlan* P = new StencilPlan();
   int st = stencil_prepare(raster_dev, ld, raster_h, raster_w, tiles, ntiles, params, planes, P->J);
+  if (!st) P->J.encode_tmap();
   const size_t bytes = st ? 0 : P->J.device_bytes();
   if (!st && bytes) {
     cudaError_t e = cudaMalloc(&P->dev, bytes);
@@ -1825,6 +1951,7 @@ extern "C" int fsg_stencil_host(const float* raster_host, int64_t ld, int32_t ra
     }
     J.A.raster = reinterpret_cast<const float*>(rebase(J.A.raster));
     J.F.raster = J.A.raster;
+    J.encode_tmap();
     J.bind(base + job_off[bi]);
     J.pack(image.data() + (job_off[bi] - slots_total));
   }
@@ -1865,4 +1992,15 @@ extern "C" int fsg_stencil_host(const float* raster_host, int64_t ld, int32_t ra
     cudaStreamWaitEvent(caller, S->done[i], 0);
   }
   return status;
+}
+
+extern "C" int fsg_kernel_errors(uint32_t* flags) {
+  using namespace fsg;
+  if (!flags) return fail(FSG_ERR_INVALID, "null argument");
+  unsigned v = 0;
+  FSG_CUDA(cudaMemcpyFromSymbol(&v, g_kernel_errors, sizeof(v)));
+  const unsigned zero = 0;
+  FSG_CUDA(cudaMemcpyToSymbol(g_kernel_errors, &zero, sizeof(zero)));
+  *flags = v;
+  return FSG_OK;
 }

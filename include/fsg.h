@@ -98,6 +98,10 @@ int64_t fsg_launch_count(void);
  * (measurement support for the roofline figures). */
 int fsg_timing_begin(int32_t max_launches);
 int fsg_timing_end(double* total_ms, int32_t* launches);
+/* Device-side failures since the last call, cleared on read (synchronises): bit 0 = the
+ * fused stencil's streaming pass gave up waiting for a tensor-memory copy (its outputs
+ * are then incomplete).  No reference counterpart. */
+int fsg_kernel_errors(uint32_t* flags);
 
 /* NoData mask (core/tile_processor.py:185-196): mask_dev[i] = 1 where
  * isnan(v) or (has_nodata and (|v - nodata| <= 1e-6 in float32, or v == nodata)). */

@@ -228,3 +228,38 @@ def test_host_buffer_tile_loop_equals_device_path(fsg, dtype):
     for n in names:
         a, b = to_np(dev[n]), host[n].numpy()
         assert np.array_equal(a, b, equal_nan=True), n
+
+
+@pytest.mark.parametrize("offset", [0, 1])
+def test_tensor_copy_ring_equals_cp_async_ring(fsg, offset):
+    """The streaming pass fills its row ring with one tensor-memory copy per row when the raster
+    and the unit columns are 16-byte aligned, else with cp.async; both give identical planes,
+    and no wait on a tensor copy runs out (fsg_kernel_errors)."""
+    from fujishadergpu_gb300 import _native as N
+    from fujishadergpu_gb300.algorithms import _stencil as S
+    from fujishadergpu_gb300.core import tile_loop as loop
+    H, W = 900, 1100
+    base = torch.from_numpy(_fbm_nan(H, W + 4, 77, 10)).cuda()
+    d = base[:, offset:offset + W]  # offset 1: unaligned columns, the cp.async ring everywhere
+    v = __import__("fujishadergpu_gb300._arrays", fromlist=["x"]).as_device_f32_2d(d)
+    tiles = loop.make_tiles(loop.tile_grid(H, W, 512, 8), pixel_scale_x=5.0, pixel_scale_y=-5.0)
+    names = ["hillshade", "slope", "curvature_profile", "curvature_planform"]
+    sp = S.make_params(pixel_size=5.0)
+    outs = {}
+    for mode in ("tma", "cp_async"):
+        if mode == "cp_async":
+            os.environ["FSG_NO_TMA"] = "1"
+        try:
+            o = {n: torch.full((H, W), 3.0, device="cuda") for n in names}
+            S.launch(v, tiles, sp, {S.OUTPUT_INDEX[n]: S.make_plane(o[n]) for n in names})
+            torch.cuda.synchronize()
+            outs[mode] = o
+        finally:
+            os.environ.pop("FSG_NO_TMA", None)
+    assert N.kernel_errors() == 0
+    for n in names:
+        a, b = outs["tma"][n], outs["cp_async"][n]
+        assert torch.equal(a.nan_to_num(-9.0), b.nan_to_num(-9.0)), n
+    kw = dict(pixel_size=5.0, psx=5.0, psy=-5.0)
+    dem = to_np(d)
+    assert_close_range(outs["tma"]["hillshade"][8:-8, 8:-8], R.hillshade(dem, **kw)[8:-8, 8:-8], 1.0, "hs")
