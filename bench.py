@@ -18,10 +18,18 @@ disks) cut into 4096^2 tiles with an 8 px halo, all tiles in one launch.
 the reference itself is CuPy-only and cannot run on the host) with all host
 cores on the same workload definition.
 
-The line also carries ``extra``: the topousm_fast tile loop (32768^2, radii
-2..2048) and openness (16384^2, 16 directions, R = 256; reference 10-sample
-rays and the dense every-step march on a 4096^2 crop), each device-timed
-(``--no-extra`` skips them).
+The line also carries ``extra``, each section device-timed (``--no-extra``
+skips them; ``--workload <section>`` prints one section alone):
+  topousm_fast       the tile loop at 32768^2, radii 2..2048
+  openness           16384^2, 16 directions, R = 256: the reference's 10-sample
+                     rays, and the dense every-step march on a 4096^2 crop
+  ambient_occlusion  16384^2, 16 samples x 4 rings, radius 10 and 30
+  openness_surrogate the CNN surrogate against the exact kernels
+  spatial            spatial (multi-radius) mode of the stencil products and
+                     openness at 8192^2
+  batched            uneven tiles over a 3-level overview pyramid (hillshade,
+                     topousm_fast, openness) as prepared plans replayed in one
+                     CUDA graph
 """
 from __future__ import annotations
 
@@ -429,6 +437,38 @@ def openness_section(args):
     return {"workload": f"openness positive, 16 dirs, R=256, 5 m, {n}x{n} (reference sampling)", **res}
 
 
+def ambient_occlusion_section(args):
+    """Ambient occlusion (16 samples x 4 rings, radius 10 and 30, 5 m) on a 16384^2 fBm+ridged DEM
+    in 4096^2 tiles with the tile loop's 64 px halo: one step = the field kernel (the samples)
+    and the finish kernel (Gaussian, gamma, stretch, store) over all tiles."""
+    import torch
+    from fujishadergpu_gb300 import _arrays, _native, synth
+    from fujishadergpu_gb300.algorithms import _impl_ambient_occlusion as AO
+    from fujishadergpu_gb300.algorithms._stencil import make_plane
+    from fujishadergpu_gb300.core import tile_loop
+    n = args.openness_size
+    dem = synth.fbm_ridged_device(n, n, hurst=0.7, seed_fbm=5, seed_ridged=6, lo=0.0, hi=3000.0)
+    v = _arrays.as_device_f32_2d(dem)
+    tiles = tile_loop.make_tiles(tile_loop.tile_grid(n, n, 4096, 64), pixel_scale_x=5.0, pixel_scale_y=-5.0)
+    out = torch.empty((n, n), device="cuda")
+    plane = make_plane(out)
+    stream = torch.cuda.current_stream()
+    res = {}
+    for radius in (10.0, 30.0):
+        params = AO.make_params(radius=radius, pixel_size=5.0, stretch=(0.5, 0.45))
+        steps = max(1, args.extra_steps // 2)
+        fn = lambda: AO.run_ambient_occlusion(v, tiles, params, plane, stream=int(stream.cuda_stream))  # noqa: E731
+        with _native.kernel_timer(max_launches=steps + 1) as kt:
+            ms = _time_ms(fn, steps, 1, stream)
+        field_ms = kt.ms / max(1, kt.launches)
+        res[f"radius_{int(radius)}"] = {"value": round(n * n / (ms * 1e-3) / 1e6, 1), "unit": "Mpix/s",
+                                        "ms_per_step": round(ms, 3), "field_kernel_ms": round(field_ms, 3),
+                                        "samples_per_px": 64,
+                                        "gsamples_per_s": round(n * n * 64 / (field_ms * 1e-3) / 1e9, 1)}
+    del dem, out
+    return {"workload": f"ambient occlusion, 16 samples x 4 rings, 5 m, {n}x{n}, 4096^2 tiles", **res}
+
+
 def spatial_section(args):
     """Spatial (multi-radius) mode on an 8192^2 fBm+ridged DEM (5 m, 4096^2 tiles): hillshade,
     slope and curvature with radii 2, 8, 32, 128 and openness with distances 4, 16, 64, 256
@@ -553,7 +593,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["stencil", "topousm", "openness", "surrogate", "spatial", "batched"],
+    ap.add_argument("--workload", choices=["stencil", "topousm", "openness", "ambient_occlusion", "surrogate",
+                                           "spatial", "batched"],
                     default="stencil",
                     help="stencil: the headline line; topousm / openness: that section alone (profiling)")
     ap.add_argument("--size", type=int, default=32768)
@@ -574,7 +615,8 @@ def main():
 
     rank, world, _ = dist_setup(args.gpus)
     if args.workload != "stencil":
-        sec = {"topousm": topousm_section, "openness": openness_section, "surrogate": surrogate_section,
+        sec = {"topousm": topousm_section, "openness": openness_section,
+               "ambient_occlusion": ambient_occlusion_section, "surrogate": surrogate_section,
                "spatial": spatial_section, "batched": batched_section}[args.workload](args)
         if rank == 0:
             print(json.dumps({"section": args.workload, **sec}))
@@ -586,6 +628,8 @@ def main():
         line["extra"] = {"topousm_fast": topousm_section(args)}
         torch.cuda.empty_cache()
         line["extra"]["openness"] = openness_section(args)
+        torch.cuda.empty_cache()
+        line["extra"]["ambient_occlusion"] = ambient_occlusion_section(args)
         torch.cuda.empty_cache()
         line["extra"]["openness_surrogate"] = surrogate_section(args)
         torch.cuda.empty_cache()

@@ -90,6 +90,12 @@ class StoreFinish(C.Structure):
 COMBINE_WSUM, COMBINE_MAX, COMBINE_MIN = 0, 1, 2
 
 
+class AoParams(C.Structure):
+    _fields_ = [("num_samples", C.c_int32), ("has_nodata", C.c_int32), ("radius", C.c_double),
+                ("intensity", C.c_double), ("pixel_size", C.c_double), ("nodata", C.c_double),
+                ("stretch_lo", C.c_double), ("stretch_scale", C.c_double)]
+
+
 class OpennessParams(C.Structure):
     _fields_ = [("openness_type", C.c_int32), ("num_directions", C.c_int32), ("max_distance", C.c_int32),
                 ("mode", C.c_int32), ("pixel_size", C.c_double), ("nodata", C.c_double),
@@ -138,6 +144,11 @@ _SIGNATURES = {
     "fsg_openness_plan": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
                                     C.POINTER(OpennessParams), C.POINTER(Plane), C.c_void_p, C.c_int64,
                                     C.POINTER(C.c_void_p)]),
+    "fsg_ambient_occlusion": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,
+                                        C.POINTER(AoParams), C.POINTER(Plane), C.c_void_p]),
+    "fsg_ambient_occlusion_plan": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile),
+                                             C.c_int32, C.POINTER(AoParams), C.POINTER(Plane),
+                                             C.POINTER(C.c_void_p)]),
     "fsg_openness_offsets": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                        C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32]),
     "fsg_affine": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32,

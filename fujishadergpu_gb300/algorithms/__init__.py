@@ -6,6 +6,8 @@ array; the classes keep the ``process(dem_gpu, **params)`` /
 ``get_default_params()`` interface of algorithms/tile_shared.py:19-44.
 """
 from ._base import Constants, TileAlgorithm
+from ._impl_ambient_occlusion import (AmbientOcclusionAlgorithm, compute_ambient_occlusion_block,
+                                      compute_ambient_occlusion_spatial_block)
 from ._impl_curvature import CurvatureAlgorithm, compute_curvature_block
 from ._impl_hillshade import HillshadeAlgorithm, compute_hillshade_block
 from ._impl_openness import OpennessAlgorithm, compute_openness_raw_degrees, compute_openness_vectorized
@@ -24,6 +26,7 @@ __all__ = [
     "compute_curvature_block", "CurvatureAlgorithm",
     "compute_openness_vectorized", "compute_openness_raw_degrees", "OpennessAlgorithm",
     "compute_openness_spatial_block",
+    "compute_ambient_occlusion_block", "compute_ambient_occlusion_spatial_block", "AmbientOcclusionAlgorithm",
     "compute_topousm_fast_efficient_block", "compute_topousm_fast_large_coarse_field",
     "split_radii_by_threshold", "topousm_fast_default_large_radius_threshold", "TopoUSMFastAlgorithm",
     "topousm_fast_stat_func", "robust_unsigned_stretch_stat_func",

@@ -1,6 +1,7 @@
-"""Spatial (multi-radius) mode of the stencil products and of openness.
+"""Spatial (multi-radius) mode of the stencil products, openness and ambient occlusion.
 
-Reference behaviour, per product (hillshade, slope, curvature, openness):
+Reference behaviour, per product (hillshade, slope, curvature, openness,
+ambient occlusion):
 
 * ``_smooth_for_radius`` (algorithms/_nan_utils.py:527-552) -> ``fsg_smooth``;
   ``compute_hillshade_spatial_block`` (_impl_hillshade.py:57-67),
@@ -10,6 +11,8 @@ Reference behaviour, per product (hillshade, slope, curvature, openness):
   of the NaN-aware f x f decimation (``fsg_downsample_nan_aware``) with the
   distance divided and the pixel scales multiplied by f, zoomed back to the
   block (``fsg_upsample_to_shape``, evaluated only over the window's core).
+* ``compute_ambient_occlusion_spatial_block`` (_impl_ambient_occlusion.py:124-157):
+  the same, with the radius divided by f (at least 1, not rounded).
 * The local multi-radius branch of ``_direct_hillshade``
   (algorithms/tile/dask_bridge.py:72-108, ``_combine_direct`` :28-69): the
   spatial block per radius on the whole window, float32-normalised weights.
@@ -38,7 +41,9 @@ from .. import _arrays
 from .. import _native as N
 from . import _stencil as S
 
-ALGO_FACTOR = {"hillshade": 1.0, "slope": 1.0, "curvature": 1.1, "openness": 1.4}   # _nan_utils.py:571-581
+ALGO_FACTOR = {"hillshade": 1.0, "slope": 1.0, "curvature": 1.1, "openness": 1.4,   # _nan_utils.py:571-581
+               "ambient_occlusion": 1.5}
+RAY_PRODUCTS = ("openness", "ambient_occlusion")
 PRODUCTS = tuple(ALGO_FACTOR)
 STENCIL_PRODUCTS = ("hillshade", "slope", "curvature")
 
@@ -157,15 +162,60 @@ def _openness_spatial_into(src_ptr, src_ld, src_h, src_w, core, max_distance, kw
                                       C.c_void_p(out.data_ptr()), int(out.stride(0)), stream))
 
 
+def _ao_spatial_into(src_ptr, src_ld, src_h, src_w, core, radius, kw, pixel_size, psx, psy, out, buf=None):
+    """compute_ambient_occlusion_spatial_block (_impl_ambient_occlusion.py:124-157) of the
+    array ``src``, evaluated over ``core`` (y0, x0, h, w) of it into ``out`` (h x w, float32).
+
+    Factor 1: the AO kernel with the window = all of src.  Factor f > 1: the f x f NaN-aware
+    decimation, AO there with the radius max(1, r / f) and the pixel scales x f, then the
+    NaN-aware zoom back to src's shape over the core only.
+    """
+    from ._impl_ambient_occlusion import make_params, run_ambient_occlusion, whole_tile
+    from ._stencil import make_plane
+    torch = _arrays._torch()
+    lib = N.lib()
+    stream = C.c_void_p(_arrays.current_stream_handle())
+    f = downsample_factor(float(radius), pixel_size, "ambient_occlusion")
+    sx, sy = abs(float(psx)), abs(float(psy))
+    if buf is None:
+        def buf(name, n):
+            return torch.empty(int(n), device=out.device, dtype=torch.float32)
+    ns, it = int(kw.get("num_samples", 16)), float(kw.get("intensity", 1.0))
+    if f <= 1:
+        view = _arrays.DevView(None, int(src_ptr), int(src_h), int(src_w), int(src_ld), "torch")
+        p = make_params(num_samples=ns, radius=float(radius), intensity=it, pixel_size=pixel_size)
+        run_ambient_occlusion(view, [whole_tile(src_h, src_w, sx, sy, core)], p, make_plane(out))
+        return
+    hs, ws = (src_h + f - 1) // f, (src_w + f - 1) // f
+    small = buf("os_small", hs * ws)[: hs * ws].view(hs, ws)
+    N.check(lib.fsg_downsample_nan_aware(C.c_void_p(src_ptr), int(src_ld), int(src_h), int(src_w), int(f),
+                                         C.c_void_p(small.data_ptr()), ws, stream))
+    rsmall = buf("os_resp", hs * ws)[: hs * ws].view(hs, ws)
+    sview = _arrays.DevView(small, small.data_ptr(), hs, ws, ws, "torch")
+    p = make_params(num_samples=ns, radius=max(1.0, float(radius) / float(f)), intensity=it,
+                    pixel_size=float(pixel_size) * f)
+    run_ambient_occlusion(sview, [whole_tile(hs, ws, sx * f, sy * f)], p, make_plane(rsmall))
+    N.check(lib.fsg_upsample_to_shape(C.c_void_p(rsmall.data_ptr()), ws, hs, ws, int(src_h), int(src_w),
+                                      int(core[0]), int(core[1]), int(core[2]), int(core[3]),
+                                      C.c_void_p(out.data_ptr()), int(out.stride(0)), stream))
+
+
+def _ray_spatial_into(product, *args, **kwargs):
+    fn = _openness_spatial_into if product == "openness" else _ao_spatial_into
+    return fn(*args, **kwargs)
+
+
 def spatial_block(block, product: str, radius, *, pixel_size=1.0, pixel_scale_x=None, pixel_scale_y=None, **kw):
     """The spatial block function of ``product`` (smoothing, then the product; openness:
-    compute_openness_spatial_block with ``radius`` as the maximum distance)."""
+    compute_openness_spatial_block with ``radius`` as the maximum distance; ambient
+    occlusion: compute_ambient_occlusion_spatial_block)."""
     v = _arrays.as_device_f32_2d(block)
-    if product == "openness":
+    if product in RAY_PRODUCTS:
         out = _arrays.empty(v.h, v.w, device=v.tensor.device)
         psx, psy = S.resolve_scales(pixel_size, pixel_scale_x, pixel_scale_y)
         if v.h * v.w:
-            _openness_spatial_into(v.ptr, v.ld, v.h, v.w, (0, 0, v.h, v.w), radius, kw, pixel_size, psx, psy, out)
+            _ray_spatial_into(product, v.ptr, v.ld, v.h, v.w, (0, 0, v.h, v.w), radius, kw, pixel_size, psx, psy,
+                              out)
         return _arrays.wrap_result(out, v.origin)
     sm = _arrays.empty(v.h, v.w, device=v.tensor.device)
     _smooth_into(v.ptr, v.ld, v.h, v.w, radius, pixel_size, product, sm)
@@ -285,7 +335,7 @@ def spatial_depth(product: str, radius) -> int:
     """depth_for_scale (_impl_hillshade.py:98, _impl_slope.py:62, _impl_curvature.py:85,
     _impl_openness.py:196)."""
     r = float(radius)
-    if product == "openness":
+    if product in RAY_PRODUCTS:   # _impl_ambient_occlusion.py:182
         return int(r) + 1
     return max(3, int(r * 2 + 2)) if product == "curvature" else max(2, int(r * 2 + 1))
 
@@ -295,13 +345,15 @@ def spatial_scales(product: str, radii) -> List[float]:
     ``float(int(max(2, round(r))))`` as its maximum distance (_impl_openness.py:193)."""
     if product == "openness":
         return [float(int(max(2, round(float(r))))) for r in radii]
+    if product == "ambient_occlusion":   # _impl_ambient_occlusion.py:180
+        return [float(max(1, int(round(float(r))))) for r in radii]
     return [float(r) for r in radii]
 
 
 def spatial_is_large(product: str, scale, threshold: int) -> bool:
     """is_large: ``int(round(r)) > thr`` (_impl_hillshade.py:103), ``int(md) > thr`` for
     openness (_impl_openness.py:197)."""
-    if product == "openness":
+    if product in RAY_PRODUCTS:   # _impl_ambient_occlusion.py:183
         return int(scale) > threshold
     return int(round(float(scale))) > threshold
 
@@ -391,9 +443,9 @@ def spatial_tile(raster: _arrays.DevView, win: Tuple[int, int, int, int], core: 
             N.check(lib.fsg_pad_reflect(C.c_void_p(raster.ptr), raster.ld, raster.h, raster.w, wy, wx, wh, ww, d,
                                         ndv, has_nd, C.c_void_p(padded.data_ptr()), pw, stream))
             pcore = (d + cy - wy, d + cx - wx, ch, cw)
-            if product == "openness":
-                _openness_spatial_into(padded.data_ptr(), pw, ph, pw, pcore, r, kw, pixel_size, psx, psy, resp,
-                                       buf=buf)
+            if product in RAY_PRODUCTS:
+                _ray_spatial_into(product, padded.data_ptr(), pw, ph, pw, pcore, r, kw, pixel_size, psx, psy, resp,
+                                  buf=buf)
             else:
                 smooth = buf("smooth", ph * pw)[: ph * pw].view(ph, pw)
                 _smooth_into(padded.data_ptr(), pw, ph, pw, r, pixel_size, product, smooth)
@@ -405,7 +457,7 @@ def spatial_tile(raster: _arrays.DevView, win: Tuple[int, int, int, int], core: 
     fin.divisor = plan.divisor
     fin.stretch_lo, fin.stretch_scale = 0.0, 0.0
     fin.keep_nodata_values = 0 if mask_nodata else 1
-    if product == "openness" and isinstance(stretch, (tuple, list)) and len(stretch) >= 2 \
+    if product in RAY_PRODUCTS and isinstance(stretch, (tuple, list)) and len(stretch) >= 2 \
             and float(stretch[1]) > 1e-12:
         fin.stretch_lo, fin.stretch_scale = float(stretch[0]), float(stretch[1])
     N.check(lib.fsg_masked_store(C.c_void_p(acc.data_ptr()), cw, C.c_void_p(raster.ptr), raster.ld, raster.h,
@@ -470,7 +522,7 @@ def spatial_stencil(name: str, dem_gpu, params: dict):
         overview = _GivenOverview(cdem, float(p["_overview_decimation"]), p.get("_tile_full_shape") or (v.h, v.w))
     origin = p.get("_tile_origin") or (0, 0)
     origin = (int(origin[0]), int(origin[1]))
-    stretch = p.get("global_stats") if name == "openness" else None
+    stretch = p.get("global_stats") if name in RAY_PRODUCTS else None
     if str(agg or "mean").lower() == "stack":
         return _arrays.wrap_result(_stack_tile(v, name, radii, weights, kw, px, psx, psy, overview, origin, stretch),
                                    v.origin)
@@ -494,6 +546,8 @@ def _product_kwargs(name: str, p: dict) -> dict:
     if name == "openness":
         return {"openness_type": str(p.get("openness_type", "positive")),
                 "num_directions": int(p.get("num_directions", 16))}
+    if name == "ambient_occlusion":
+        return {"num_samples": int(p.get("num_samples", 16)), "intensity": float(p.get("intensity", 1.0))}
     return {"curvature_type": str(p.get("curvature_type", "mean"))}
 
 

@@ -23,6 +23,7 @@ import numpy as np
 
 from .. import _arrays
 from .. import _native as N
+from ..algorithms import _impl_ambient_occlusion as AO
 from ..algorithms import _impl_openness as OP
 from ..algorithms import _impl_topousm_fast as TU
 from ..algorithms import _stencil as S
@@ -34,7 +35,9 @@ from ..io.raster_info import tile_pixel_scales
 
 logger = logging.getLogger(__name__)
 
-HOT_PATH_ALGORITHMS = ("hillshade", "slope", "curvature", "topousm_fast", "openness")
+HOT_PATH_ALGORITHMS = ("hillshade", "slope", "curvature", "topousm_fast", "openness", "ambient_occlusion")
+SPATIAL_ALGORITHMS = ("hillshade", "slope", "curvature", "openness", "ambient_occlusion")
+RAY_ALGORITHMS = ("openness", "ambient_occlusion")
 MAX_DEPTH = 150  # algorithms/_base.py:16
 
 
@@ -80,7 +83,7 @@ def required_padding(algorithm: str, params: dict, sigma: float, tile_size: int)
         radii, _ = normalize_topousm_radii(params.get("radii"), params.get("weights"))
         if radii:
             required = max(required, int(max(radii) + 16))
-    if mode == "spatial" and algorithm in ("hillshade", "slope", "curvature", "openness"):
+    if mode == "spatial" and algorithm in SPATIAL_ALGORITHMS:
         radii = params.get("radii") or auto_spatial_radii(None)
         radii_f = [float(r) for r in radii if float(r) > 0]
         overview_active = bool(params.get("radii")) and algorithm != "topousm_fast"
@@ -90,7 +93,7 @@ def required_padding(algorithm: str, params: dict, sigma: float, tile_size: int)
             max_radius = int(round(max(small)))
         else:
             max_radius = max(int(round(r)) for r in radii_f)
-        if algorithm == "openness":
+        if algorithm in RAY_ALGORITHMS:
             required = max(required, int(max_radius + 16))
         else:
             required = max(required, int(max_radius * 2 + 2))
@@ -161,8 +164,8 @@ def global_stats_prepass(dem_dev, algorithm: str, params: dict, *, nodata=None, 
 
     Runs the algorithm's raw block function on up to grid^2 windows (one GPU
     call over all windows), trims each by its margin, pools the valid values
-    and returns the algorithm's stats: topousm_fast -> (p99|x|,), openness ->
-    (p1, p99 - p1).  Returns None when no window qualifies.
+    and returns the algorithm's stats: topousm_fast -> (p99|x|,), openness and
+    ambient occlusion -> (p1, p99 - p1).  Returns None when no window qualifies.
     """
     torch = _arrays._torch()
     H, W = dem_dev.shape
@@ -170,7 +173,19 @@ def global_stats_prepass(dem_dev, algorithm: str, params: dict, *, nodata=None, 
         radii = params.get("_topousm_fast_full_radii") or params.get("radii")
         max_scale = max(float(r) for r in radii)
     else:
-        max_scale = float(params.get("max_distance", 50))
+        # _norm_stat_max_scale (_norm_stats.py:103-121): the largest of the radii, the
+        # radius and the maximum distance the parameters carry
+        vals = []
+        if isinstance(params.get("radii"), (list, tuple)) and params.get("radii"):
+            vals.append(max(float(r) for r in params["radii"]))
+        for key in ("radius", "max_distance"):
+            if params.get(key):
+                vals.append(float(params[key]))
+        if algorithm == "openness" and not params.get("max_distance"):
+            vals.append(50.0)   # the block function's default distance
+        if algorithm == "ambient_occlusion" and not params.get("radius"):
+            vals.append(10.0)   # the block function's default radius
+        max_scale = max(vals) if vals else 16.0
     margin = max(1, int(max_scale + 16))
     tile = max(min(2048, max_tile), 4 * margin)
     bbox = _valid_bbox(dem_dev, nodata)
@@ -189,6 +204,13 @@ def global_stats_prepass(dem_dev, algorithm: str, params: dict, *, nodata=None, 
             w = params.get("_topousm_fast_full_weights") or params.get("weights")
             raw = TU.compute_topousm_fast_efficient_block(a, radii=radii, weights=w,
                                                           pixel_size=float(params.get("pixel_size", 1.0)))
+        elif algorithm == "ambient_occlusion":
+            raw, _ = AO.ambient_occlusion_plane(a, num_samples=params.get("num_samples", 16),
+                                                radius=params.get("radius", 10.0),
+                                                intensity=params.get("intensity", 1.0),
+                                                pixel_size=params.get("pixel_size", 1.0),
+                                                pixel_scale_x=params.get("pixel_scale_x"),
+                                                pixel_scale_y=params.get("pixel_scale_y"))
         else:
             raw, _, _ = OP.openness_planes(a, openness_type=params.get("openness_type", "positive"),
                                            num_directions=params.get("num_directions", 16),
@@ -265,7 +287,7 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
         params["radii"] = r
         if not params.get("weights"):
             params["weights"] = auto_spatial_weights(len(r))
-    spatial = mode == "spatial" and algorithm in ("hillshade", "slope", "curvature", "openness")
+    spatial = mode == "spatial" and algorithm in SPATIAL_ALGORITHMS
     if spatial:
         dr, dw = sanitize_spatial_radii_weights(algorithm, params.get("radii"), params.get("weights"))
         if dr is not None:
@@ -304,9 +326,9 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
 
     if spatial:
         stretch = None
-        if algorithm == "openness":
-            # the openness stats describe the local display openness at max_distance in every
-            # mode (_norm_stats.py:45-46, :195-283)
+        if algorithm in RAY_ALGORITHMS:
+            # the openness / AO stats describe the local display value (max_distance / radius)
+            # in every mode (_norm_stats.py:42-46, :195-283)
             stretch = params.get("global_stats")
             if stretch is None:
                 stretch = global_stats_prepass(v.tensor, algorithm, dict(params, pixel_scale_x=psx,
@@ -330,6 +352,15 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
                                   coarse=params.get("_topousm_fast_coarse_field"),
                                   w_large=params.get("_topousm_fast_w_large", 0.0), full_shape=(H, W), scale=scale)
         TU.run_topousm(v, tiles, tp, S.make_plane(out, output_dtype, qp))
+    elif algorithm == "ambient_occlusion":
+        stats = params.get("global_stats")
+        if stats is None:
+            stats = global_stats_prepass(v.tensor, algorithm, dict(params, pixel_scale_x=psx, pixel_scale_y=psy),
+                                         nodata=nodata)
+        res.stats = stats
+        ap = AO.make_params(num_samples=params.get("num_samples", 16), radius=params.get("radius", 10.0),
+                            intensity=params.get("intensity", 1.0), pixel_size=px, nodata=nodata, stretch=stats)
+        AO.run_ambient_occlusion(v, tiles, ap, S.make_plane(out, output_dtype, qp))
     else:  # openness
         stats = params.get("global_stats")
         if stats is None:
@@ -348,13 +379,14 @@ def sanitize_spatial_radii_weights(algorithm: str, radii, weights):
     """_sanitize_spatial_radii_weights_for_tile (core/tile_processor.py:102-172).
 
     Stencil products: integer radii >= 1, duplicates merged with their weights.
-    openness: integer radii >= 2 (non-positive ones dropped with their weights),
+    openness and ambient occlusion: integer radii >= 2 (non-positive ones dropped with
+    their weights),
     weights kept only when every kept radius has one, then de-duplicated.
     Returns (radii, weights) or (None, weights) when no radius survives.
     """
     if not isinstance(radii, (list, tuple)) or len(radii) == 0:
         return None, weights
-    if algorithm != "openness":
+    if algorithm not in RAY_ALGORITHMS:
         ints = []
         for r in radii:
             try:

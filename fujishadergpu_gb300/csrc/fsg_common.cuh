@@ -8,6 +8,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <vector>
 
 #include "fsg.h"
 
@@ -124,6 +125,26 @@ __device__ __forceinline__ float quantize(float v, float qa, float qb, int qmin,
 struct FF {
   float hi, lo;
 };
+// scipy.ndimage._gaussian_kernel1d(sigma, 0, int(4 sigma + 0.5)) normalised in
+// float64, as float-float pairs [0..R] (0 = centre).
+inline std::vector<FF> ff_gaussian(double sigma, int* radius) {
+  const int R = (int)(4.0 * sigma + 0.5);
+  std::vector<double> phi(2 * R + 1);
+  const double c = -0.5 / (sigma * sigma);
+  double s = 0.0;
+  for (int k = -R; k <= R; ++k) {
+    phi[k + R] = std::exp(c * (double)((long long)k * k));
+    s += phi[k + R];
+  }
+  std::vector<FF> g(R + 1);
+  for (int k = 0; k <= R; ++k) {
+    const double v = phi[k + R] / s;
+    g[k].hi = (float)v;
+    g[k].lo = (float)(v - (double)g[k].hi);
+  }
+  *radius = R;
+  return g;
+}
 __device__ __forceinline__ FF two_sum(float a, float b) {
   float s = __fadd_rn(a, b);
   float bb = __fsub_rn(s, a);
@@ -193,6 +214,20 @@ __device__ __forceinline__ float atan_poly(float x) {
   float r = a * p;
   if (inv) r = 1.57079632679489661923f - r;
   return copysignf(r, x);
+}
+// atan_poly's polynomial for a pair of arguments in [0, 1] (paired FP32 FMAs).
+__device__ __forceinline__ float2 atan01_pair(float2 a) {
+  auto c = [](float v) { return make_float2(v, v); };
+  const float2 a2 = __fmul2_rn(a, a);
+  float2 p = c(-0x1.09b3ep-8f);
+  p = __ffma2_rn(a2, p, c(0x1.662f9cp-6f));
+  p = __ffma2_rn(a2, p, c(-0x1.ca055ep-5f));
+  p = __ffma2_rn(a2, p, c(0x1.8af07cp-4f));
+  p = __ffma2_rn(a2, p, c(-0x1.1cd902p-3f));
+  p = __ffma2_rn(a2, p, c(0x1.988166p-3f));
+  p = __ffma2_rn(a2, p, c(-0x1.554c3ap-2f));
+  p = __ffma2_rn(a2, p, c(0x1.ffffeap-1f));
+  return __fmul2_rn(a, p);
 }
 
 }  // namespace fsg

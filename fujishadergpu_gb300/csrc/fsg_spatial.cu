@@ -352,27 +352,6 @@ __global__ void masked_store(const __grid_constant__ StoreArgs A) {
 // ------------------------------------------------------------ host
 dim3 blocks2d(int h, int w) { return dim3((w + 31) / 32, (h + 7) / 8); }
 
-// scipy.ndimage._gaussian_kernel1d(sigma, 0, int(4 sigma + 0.5)) normalised in
-// float64, as float-float pairs [0..R] (0 = centre).
-std::vector<FF> ff_gaussian(double sigma, int* radius) {
-  const int R = (int)(4.0 * sigma + 0.5);
-  std::vector<double> phi(2 * R + 1);
-  const double c = -0.5 / (sigma * sigma);
-  double s = 0.0;
-  for (int k = -R; k <= R; ++k) {
-    phi[k + R] = std::exp(c * (double)((long long)k * k));
-    s += phi[k + R];
-  }
-  std::vector<FF> g(R + 1);
-  for (int k = 0; k <= R; ++k) {
-    const double v = phi[k + R] / s;
-    g[k].hi = (float)v;
-    g[k].lo = (float)(v - (double)g[k].hi);
-  }
-  *radius = R;
-  return g;
-}
-
 constexpr size_t kMaxTable = 1 << 16;  // Gaussian weight table bytes (radius <= 8191)
 
 struct Arena {

@@ -302,6 +302,33 @@ int fsg_openness_plan(const float* raster_dev, int64_t ld, int32_t raster_h, int
                       const fsg_tile* tiles, int32_t ntiles, const fsg_openness_params* params,
                       const fsg_plane* display, float* raw_deg_dev, int64_t raw_ld, fsg_plan** plan);
 
+/* ------------------------------------------------------- ambient occlusion */
+typedef struct fsg_ao_params {
+  int32_t num_samples;      /* directions per ring, default 16 */
+  int32_t has_nodata;
+  double radius;            /* pixels, default 10 */
+  double intensity;         /* default 1 */
+  double pixel_size;        /* fallback when |pixel_scale| < 1e-9 */
+  double nodata;
+  double stretch_lo, stretch_scale;  /* display stretch (p1, p99 - p1); scale <= 1e-12: none */
+} fsg_ao_params;
+
+/* Ambient occlusion over a list of tiles: per window, 4 rings x num_samples
+ * edge-padded samples, clamped elevation angle weighted by the ring's distance
+ * factor, AO = clip(1 - mean * intensity, 0, 1), Gaussian sigma 1 ('nearest'
+ * at the window edge), ^(1/2.2), NaN at NoData, optional stretch, written as
+ * float32 or int16/uint8 codes to `out` at the cores.  Replaces
+ * compute_ambient_occlusion_block (algorithms/_impl_ambient_occlusion.py:32-121)
+ * called per tile by _direct_ambient_occlusion
+ * (algorithms/tile/dask_bridge.py:190-203). */
+int fsg_ambient_occlusion(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                          const fsg_tile* tiles, int32_t ntiles, const fsg_ao_params* params,
+                          const fsg_plane* out, void* stream);
+/* fsg_ambient_occlusion prepared as a plan (same arguments, no stream). */
+int fsg_ambient_occlusion_plan(const float* raster_dev, int64_t ld, int32_t raster_h, int32_t raster_w,
+                               const fsg_tile* tiles, int32_t ntiles, const fsg_ao_params* params,
+                               const fsg_plane* out, fsg_plan** plan);
+
 /* Host-only: the ray offsets the kernel uses (dx, dy per sample, directions in
  * order; ray_len[d] samples for direction d).  Returns FSG_ERR_WORKSPACE with
  * ray_len filled if `capacity` is too small. */

@@ -313,6 +313,8 @@ def spatial_block(block, product, radius, *, pixel_size=1.0, **kw):
     openness: compute_openness_spatial_block with ``radius`` as the maximum distance."""
     if product == "openness":
         return openness_spatial_block(block, max_distance=radius, pixel_size=pixel_size, **kw)
+    if product == "ambient_occlusion":
+        return ambient_occlusion_spatial_block(block, radius=radius, pixel_size=pixel_size, **kw)
     sm = smooth_for_radius(block, radius, pixel_size=pixel_size, algorithm=product)
     return stencil_product(sm, product, pixel_size=pixel_size, **kw)
 
@@ -321,7 +323,7 @@ def spatial_depth(product, radius):
     """depth_for_scale of the spatial branches (_impl_hillshade.py:98, _impl_slope.py:62,
     _impl_curvature.py:85, _impl_openness.py:196)."""
     r = float(radius)
-    if product == "openness":
+    if product in ("openness", "ambient_occlusion"):   # _impl_ambient_occlusion.py:182
         return int(r) + 1
     if product == "curvature":
         return max(3, int(r * 2 + 2))
@@ -333,13 +335,15 @@ def spatial_scales(product, radii):
     ``float(int(max(2, round(r))))`` (_impl_openness.py:193)."""
     if product == "openness":
         return [float(int(max(2, round(float(r))))) for r in radii]
+    if product == "ambient_occlusion":   # _impl_ambient_occlusion.py:180
+        return [float(max(1, int(round(float(r))))) for r in radii]
     return [float(r) for r in radii]
 
 
 def spatial_is_large(product, scale, threshold):
     """is_large of the spatial branches: ``int(round(r)) > thr`` (_impl_hillshade.py:103,
     _impl_slope.py:63, _impl_curvature.py:86), ``int(md) > thr`` for openness (:197)."""
-    if product == "openness":
+    if product in ("openness", "ambient_occlusion"):   # _impl_ambient_occlusion.py:183
         return int(scale) > threshold
     return int(round(float(scale))) > threshold
 
@@ -468,8 +472,9 @@ def spatial_window(window, product, radii, weights, *, origin=(0, 0), full_shape
                                                        **kw))
             out.append(map_overlap_reflect(fn, window, spatial_depth(product, r)).astype(np.float32))
     comb = combine_responses(out, weights, product, agg)
-    if product == "openness":
-        # apply_display_stretch_dask after the combination (_impl_openness.py:216)
+    if product in ("openness", "ambient_occlusion"):
+        # apply_display_stretch_dask after the combination (_impl_openness.py:216,
+        # _impl_ambient_occlusion.py:203)
         comb = apply_stretch(comb, stretch)
     return (comb, out) if return_responses else comb
 
@@ -689,6 +694,83 @@ def dense_offsets(num_directions, max_distance):
     return out
 
 
+def ao_offsets(num_samples, radius):
+    """_impl_ambient_occlusion.py:54-88: per ring r = radius * (0.25, 0.5, 0.75, 1.0), the
+    offsets (np.round(r cos), np.round(r sin)) of each sample direction (half-even), with the
+    ring's distance factor 1 - 0.3 * ring; (0, 0) offsets are skipped."""
+    ang = np.linspace(0, 2 * np.pi, num_samples, endpoint=False)
+    dirs = np.stack([np.cos(ang), np.sin(ang)], axis=1)
+    out = []
+    for rf in (0.25, 0.5, 0.75, 1.0):
+        r = radius * rf
+        dxs = np.round(r * dirs[:, 0]).astype(int)
+        dys = np.round(r * dirs[:, 1]).astype(int)
+        for i in range(num_samples):
+            dx, dy = int(dxs[i]), int(dys[i])
+            if dx == 0 and dy == 0:
+                continue
+            out.append((dx, dy, 1.0 - rf * 0.3))
+    return out
+
+
+def ambient_occlusion(block, *, num_samples=16, radius=10.0, intensity=1.0, pixel_size=1.0,
+                      psx=None, psy=None):
+    """_impl_ambient_occlusion.py:32-121 (compute_ambient_occlusion_block).
+
+    Edge-padded samples (the block's border values stand in beyond it), elevation angle
+    atan(dz / d) clamped to [0, pi/4] and normalised, weighted by the ring's distance
+    factor and averaged over the valid samples; AO = clip(1 - mean * intensity, 0, 1),
+    NaN cells set to 1, Gaussian sigma 1 ('nearest'), gamma 1/2.2, NaN restored.
+    """
+    h, w = block.shape
+    dt = block.dtype.type
+    nan = np.isnan(block)
+    sx = abs(float(psx)) if psx is not None else float(pixel_size)
+    sy = abs(float(psy)) if psy is not None else float(pixel_size)
+    if sx < 1e-9:
+        sx = float(pixel_size) if pixel_size else 1.0
+    if sy < 1e-9:
+        sy = float(pixel_size) if pixel_size else 1.0
+    D = max(1, int(round(float(radius))))
+    pad = np.pad(block, D, mode="edge")
+    total = np.zeros((h, w), dtype=block.dtype)
+    count = np.zeros((h, w), dtype=block.dtype)
+    for dx, dy, df in ao_offsets(num_samples, radius):
+        shifted = pad[D + dy:D + dy + h, D + dx:D + dx + w]
+        dist = max(float(np.hypot(float(dx) * sx, float(dy) * sy)), 1e-9)
+        ang = np.arctan((shifted - block) / dist)
+        occ = np.minimum(np.maximum(0, ang) / (np.pi / 4), 1.0)
+        valid = ~(np.isnan(shifted) | nan)
+        total += np.where(valid, occ * df, 0)
+        count += np.where(valid, 1.0, 0)
+    count = np.maximum(count, 1.0)
+    mean = total / count
+    ao = np.clip(1.0 - mean * intensity, 0, 1)
+    if nan.any():
+        ao = ndi.gaussian_filter(np.where(nan, 1.0, ao), sigma=1.0, mode="nearest")
+    else:
+        ao = ndi.gaussian_filter(ao, sigma=1.0, mode="nearest")
+    out = np.power(ao, GAMMA)
+    return _restore_nan(out, nan).astype(block.dtype)
+
+
+def ambient_occlusion_spatial_block(block, *, num_samples=16, radius=10.0, intensity=1.0, pixel_size=1.0,
+                                    psx=None, psy=None):
+    """_impl_ambient_occlusion.py:124-157 (compute_ambient_occlusion_spatial_block): AO of the
+    NaN-aware f x f decimated block (f from the radius, algorithm factor 1.5) with the radius
+    divided (at least 1) and the pixel scales multiplied by f, zoomed back to the block."""
+    f = downsample_factor(float(radius), pixel_size=pixel_size, algorithm="ambient_occlusion")
+    if f <= 1:
+        return ambient_occlusion(block, num_samples=num_samples, radius=radius, intensity=intensity,
+                                 pixel_size=pixel_size, psx=psx, psy=psy)
+    small = downsample_nan_aware(block, f)
+    res = ambient_occlusion(small, num_samples=num_samples, radius=max(1.0, float(radius) / float(f)),
+                            intensity=intensity, pixel_size=float(pixel_size) * float(f),
+                            psx=None if psx is None else float(abs(float(psx)) * f),
+                            psy=None if psy is None else float(abs(float(psy)) * f))
+    return upsample_to_shape(res, block.shape)
+
+
 def stretch_stats(values):
     """_global_stats.py:181-203 (robust_unsigned_stretch_stat_func): (p1, p99-p1)."""
     if values is None:
@@ -723,6 +805,7 @@ OUTPUT_VALUE_RANGES = {  # io/output_encoding.py:40-73 (hot-path subset)
     "hillshade": (0.0, 1.0),
     "curvature": (0.0, 1.0),
     "openness": (0.0, 1.0),
+    "ambient_occlusion": (0.0, 1.0),
     "slope": (0.0, 90.0),
 }
 _INT_MAXPOS = {"int16": 32767, "uint8": 255}

@@ -316,5 +316,59 @@ def main():
     print("golden fixtures written to", HERE)
 
 
+AO_SPATIAL_RADII = (8.0, 40.0, 100.0)   # decimation factors 1, 2, 4 at 5 m (algorithm factor 1.5)
+
+
+def main_ambient_occlusion():
+    """ambient_occlusion.npz / .json: compute_ambient_occlusion_block and its spatial block."""
+    ref = reference_shim.load()
+    _stub_rasterio()
+    import importlib
+    ao_mod = ref._impl_ambient_occlusion
+    db = importlib.import_module("FujiShaderGPU.algorithms.tile.dask_bridge")
+    arrays = {}
+    meta = {}
+    a1 = _with_disks(synth.fbm(72, 90, hurst=0.7, seed=41, lo=0.0, hi=900.0), 4, 42, 2.0, 7.0)
+    yy, xx = np.mgrid[0:61, 0:61]
+    peak = (300.0 - 12.0 * np.sqrt((xx - 30.0) ** 2 + (yy - 30.0) ** 2)).astype(np.float32)
+    a5 = synth.fbm(40, 50, hurst=0.8, seed=43, lo=0.0, hi=400.0)
+    a5[10:13, 20:24] = np.nan
+    cases = [
+        # name, dem, num_samples, radius, intensity, pixel_size, psx, psy
+        ("a1_fbm_nan", a1, 16, 10.0, 1.0, 5.0, 5.0, -5.0),
+        ("a2_aniso", a1[:50, :64].copy(), 8, 5.5, 0.7, 4.0, 3.0, -5.0),
+        ("a3_r1", a1[:30, :41].copy(), 12, 1.0, 1.0, 2.0, None, None),
+        ("a4_peak_pit", np.concatenate([peak, -peak], axis=1), 16, 6.0, 2.0, 1.0, None, None),
+        ("a5_wide_radius", a5, 16, 30.0, 1.0, 2.0, 2.0, -2.0),
+        ("a6_flat", np.full((20, 24), 7.0, np.float32), 16, 4.0, 1.0, 1.0, None, None),
+    ]
+    for n, d, ns, r, it, px, psx, psy in cases:
+        arrays[f"{n}/dem"] = d
+        arrays[f"{n}/ao"] = ao_mod.compute_ambient_occlusion_block(
+            d.copy(), num_samples=ns, radius=r, intensity=it, pixel_size=px,
+            pixel_scale_x=psx, pixel_scale_y=psy)
+        meta[n] = {"num_samples": ns, "radius": r, "intensity": it, "pixel_size": px, "psx": psx, "psy": psy}
+    # the tile path's direct call with the display stretch (algorithms/tile/dask_bridge.py:190-203)
+    arrays["a1_fbm_nan/direct_stretch"] = db._direct_ambient_occlusion(
+        a1.copy(), dict(num_samples=16, radius=10.0, intensity=1.0, pixel_size=5.0, pixel_scale_x=5.0,
+                        pixel_scale_y=-5.0, global_stats=(0.55, 0.4)))
+    sp = synth.fbm(120, 136, hurst=0.8, seed=44, lo=0.0, hi=2500.0)
+    sp_nan = _with_disks(sp, 4, 45, 6.0, 14.0)
+    for dn, d in (("clean", sp), ("nan", sp_nan)):
+        arrays[f"spatial_{dn}/dem"] = d
+        for r in AO_SPATIAL_RADII:
+            arrays[f"spatial_{dn}/ao_{int(r)}"] = ao_mod.compute_ambient_occlusion_spatial_block(
+                d.copy(), num_samples=16, radius=r, intensity=1.0, pixel_size=5.0,
+                pixel_scale_x=5.0, pixel_scale_y=-5.0)
+    np.savez_compressed(os.path.join(HERE, "ambient_occlusion.npz"), **arrays)
+    with open(os.path.join(HERE, "ambient_occlusion.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+
+
 if __name__ == "__main__":
-    main()
+    # "--section ambient_occlusion" regenerates that fixture alone
+    if "--section" in sys.argv and sys.argv[sys.argv.index("--section") + 1] == "ambient_occlusion":
+        main_ambient_occlusion()
+    else:
+        main()
+        main_ambient_occlusion()

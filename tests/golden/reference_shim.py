@@ -79,6 +79,7 @@ def load():
         "FujiShaderGPU.algorithms._impl_curvature",
         "FujiShaderGPU.algorithms._impl_topousm_fast",
         "FujiShaderGPU.algorithms._impl_openness",
+        "FujiShaderGPU.algorithms._impl_ambient_occlusion",
         "FujiShaderGPU.algorithms._normalization",
         "FujiShaderGPU.algorithms._global_stats",
         "FujiShaderGPU.algorithms.common.spatial_mode",

@@ -164,6 +164,36 @@ def test_openness_bit_exact(golden_dir, case):
         _eq(out, g[f"{case}/{ot}"])
 
 
+AO_CASES = ["a1_fbm_nan", "a2_aniso", "a3_r1", "a4_peak_pit", "a5_wide_radius", "a6_flat"]
+
+
+@pytest.mark.parametrize("case", AO_CASES)
+def test_ambient_occlusion_bit_exact(golden_dir, case):
+    """compute_ambient_occlusion_block (_impl_ambient_occlusion.py:32-121): non-integer and
+    unit radii, anisotropic scales, clamped (steep) and zero (flat) occlusion, NaN cells."""
+    g = _load(golden_dir, "ambient_occlusion")
+    m = _meta(golden_dir, "ambient_occlusion")[case]
+    out = R.ambient_occlusion(g[f"{case}/dem"].copy(), num_samples=m["num_samples"], radius=m["radius"],
+                              intensity=m["intensity"], pixel_size=m["pixel_size"], psx=m["psx"], psy=m["psy"])
+    _eq(out, g[f"{case}/ao"])
+
+
+def test_ambient_occlusion_stretch_and_spatial_bit_exact(golden_dir):
+    """_direct_ambient_occlusion's display stretch (tile/dask_bridge.py:190-203) and
+    compute_ambient_occlusion_spatial_block (_impl_ambient_occlusion.py:124-157) at
+    decimation factors 1, 2 and 4, with and without NoData."""
+    g = _load(golden_dir, "ambient_occlusion")
+    a = R.ambient_occlusion(g["a1_fbm_nan/dem"].copy(), num_samples=16, radius=10.0, pixel_size=5.0, psx=5.0,
+                            psy=-5.0)
+    _eq(R.apply_stretch(a, (0.55, 0.4)), g["a1_fbm_nan/direct_stretch"])
+    for dn in ("clean", "nan"):
+        dem = g[f"spatial_{dn}/dem"]
+        for r in (8, 40, 100):
+            _eq(R.ambient_occlusion_spatial_block(dem.copy(), num_samples=16, radius=float(r), pixel_size=5.0,
+                                                  psx=5.0, psy=-5.0), g[f"spatial_{dn}/ao_{r}"])
+    assert [R.downsample_factor(r, pixel_size=5.0, algorithm="ambient_occlusion") for r in (8, 40, 100)] == [1, 2, 4]
+
+
 @pytest.mark.parametrize("variant", ["clean", "nan"])
 def test_openness_spatial_pieces_bit_exact(golden_dir, variant):
     """_downsample_nan_aware (block mean, enclosed voids filled, exterior kept NaN),
