@@ -1020,3 +1020,236 @@ def resolve_spatial_radii_weights(radii, weights, pixel_size, short_side_px=None
 
 
 __all__ = [n for n in dir() if not n.startswith("_")]
+
+
+# =============================================================================
+# prepare: NoData detection and void fill (io/dem_preprocess.py,
+# algorithms/_pyramid_fill.py, utils/nodata_handler.py)
+# =============================================================================
+FILL_MODES = ("none", "enclosed", "all")   # io/dem_preprocess.py:57
+
+NODATA_SENTINELS = (   # io/dem_preprocess.py:228-238
+    0.0, -9999.0, -99999.0, 9999.0,
+    -32768.0, 32767.0, -32767.0, 65535.0,
+    -2147483648.0, 2147483647.0, -2147483647.0,
+    -128.0, 127.0, 255.0,
+)
+
+
+def pushpull_fill(coarse, valid):
+    """_pyramid_fill.py:24-84 (pushpull_fill) with NumPy and scipy's zoom: push (x2
+    valid-weighted coarsening by zoom order 1 'nearest' until every cell has support or
+    the grid is 1x1), pull (zoom back up level by level, filling unsupported cells),
+    known cells kept exactly."""
+    f32 = np.float32
+    out = coarse.astype(f32, copy=True)
+    if bool(valid.all()):
+        return out
+    if not bool(valid.any()):
+        return np.zeros_like(out, dtype=f32)
+    eps = f32(1e-6)
+    w = valid.astype(f32)
+    vw = np.where(valid, out, f32(0.0)).astype(f32)
+    vws, ws = [vw], [w]
+    while max(vws[-1].shape[:2]) > 1 and float(ws[-1].min()) <= 1e-6:
+        ch, cw = vws[-1].shape[:2]
+        nh, nw = max(1, ch // 2), max(1, cw // 2)
+        zy, zx = nh / float(ch), nw / float(cw)
+        num = ndi.zoom(vws[-1], zoom=(zy, zx), order=1, mode="nearest")
+        den = ndi.zoom(ws[-1], zoom=(zy, zx), order=1, mode="nearest")
+        wv = np.minimum(den, f32(1.0))
+        mean = np.where(den > eps, num / np.maximum(den, eps), f32(0.0))
+        vws.append((mean * wv).astype(f32))
+        ws.append(wv.astype(f32))
+    filled = np.where(ws[-1] > eps, vws[-1] / np.maximum(ws[-1], eps), f32(0.0)).astype(f32)
+    for lvl in range(len(vws) - 2, -1, -1):
+        th, tw = vws[lvl].shape[:2]
+        fh, fw = filled.shape[:2]
+        up = ndi.zoom(filled, zoom=(th / float(fh), tw / float(fw)), order=1, mode="nearest")
+        ph, pw = max(0, th - up.shape[0]), max(0, tw - up.shape[1])
+        if ph or pw:
+            up = np.pad(up, ((0, ph), (0, pw)), mode="edge")
+        up = up[:th, :tw]
+        wl = ws[lvl]
+        vl = np.where(wl > eps, vws[lvl] / np.maximum(wl, eps), f32(0.0))
+        filled = np.where(wl > eps, vl, up).astype(f32)
+    return np.where(valid, out, filled).astype(f32)
+
+
+def coarse_shape(width, height, coarse_max):
+    """io/dem_preprocess.py:278-282 (_coarse_shape) -> (ch, cw)."""
+    scale = max(width / coarse_max, height / coarse_max, 1.0)
+    return max(1, int(round(height / scale))), max(1, int(round(width / scale)))
+
+
+def coarse_oversample(ch, cw, k=4, max_intermediate=4096):
+    """io/dem_preprocess.py:537-539 and :156-158: the oversampling of the nearest read."""
+    k = max(2, int(k))
+    while k > 2 and max(ch * k, cw * k) > int(max_intermediate):
+        k -= 1
+    return k
+
+
+def nan_aware_coarse_average(sample, masked, ch, cw, src_nodata, extra_nodata):
+    """io/dem_preprocess.py:135-188 (_nan_aware_coarse_average) on an oversampled nearest
+    sample (``masked``: the read's own NoData mask) -> (coarse, void mask)."""
+    ih, iw = sample.shape
+    k = ih // ch
+    a = sample.astype(np.float32, copy=False)
+    m = masked | ~np.isfinite(a)
+    if src_nodata is not None and np.isfinite(src_nodata):
+        m = m | (a == np.float32(src_nodata))
+    for v in extra_nodata:
+        if np.isfinite(v):
+            m = m | (a == np.float32(v))
+    a = np.where(m, np.nan, a).reshape(ch, k, cw, k)
+    finite = np.isfinite(a)
+    cnt = finite.sum(axis=(1, 3))
+    s = np.nansum(a, axis=(1, 3))
+    cmask = cnt == 0
+    coarse = np.where(cmask, np.float32(0.0), s / np.maximum(cnt, 1)).astype(np.float32)
+    return coarse, cmask
+
+
+def detect_border_nodata(sample, valid, *, min_border_fraction=0.5, min_total_fraction=0.02):
+    """io/dem_preprocess.py:191-225 (_detect_border_nodata)."""
+    h, w = sample.shape
+    if h < 8 or w < 8:
+        return None
+    ring = np.concatenate([sample[0, :], sample[-1, :], sample[1:-1, 0], sample[1:-1, -1]])
+    ring_valid = np.concatenate([valid[0, :], valid[-1, :], valid[1:-1, 0], valid[1:-1, -1]])
+    ring = ring[ring_valid & np.isfinite(ring)]
+    if ring.size == 0:
+        return None
+    vals, counts = np.unique(ring, return_counts=True)
+    i = int(np.argmax(counts))
+    cand = float(vals[i])
+    if counts[i] / ring.size < float(min_border_fraction):
+        return None
+    if float(np.mean(sample == np.float32(cand))) < float(min_total_fraction):
+        return None
+    return cand
+
+
+def detect_sentinel_nodata(sample, valid, *, min_fraction=0.05):
+    """io/dem_preprocess.py:241-275 (_detect_sentinel_nodata)."""
+    finite = sample[valid & np.isfinite(sample)]
+    if finite.size < 64:
+        return None
+    vals, counts = np.unique(finite, return_counts=True)
+    i = int(np.argmax(counts))
+    cand = float(vals[i])
+    if counts[i] / float(finite.size) < float(min_fraction):
+        return None
+    known = any(abs(cand - s) <= 1e-6 * max(1.0, abs(s)) for s in NODATA_SENTINELS)
+    if known or abs(cand) >= 1e30 or cand == float(vals[0]) or cand == float(vals[-1]):
+        return cand
+    return None
+
+
+def edge_connected_mask(mask):
+    """utils/nodata_handler.py:13-25 (_edge_connected_mask): masked cells 4-connected to the
+    array's border."""
+    if not np.any(mask):
+        return np.zeros_like(mask, dtype=bool)
+    seeds = np.zeros_like(mask, dtype=bool)
+    seeds[0, :] = mask[0, :]
+    seeds[-1, :] = mask[-1, :]
+    seeds[:, 0] = mask[:, 0]
+    seeds[:, -1] = mask[:, -1]
+    if not np.any(seeds):
+        return np.zeros_like(mask, dtype=bool)
+    return ndi.binary_propagation(seeds, mask=mask).astype(bool, copy=False)
+
+
+def sample_coarse_band(surface, exterior, row_off, band_h, width, height, ch, cw):
+    """io/dem_preprocess.py:729-767 (_sample_coarse): bilinear samples of the coarse surface
+    (and of the exterior mask, > 0.5) at the band's pixel centres, float32 coordinates."""
+    rr = (row_off + np.arange(band_h, dtype=np.float32) + np.float32(0.5)) * np.float32(ch / height) \
+        - np.float32(0.5)
+    cc = (np.arange(width, dtype=np.float32) + np.float32(0.5)) * np.float32(cw / width) - np.float32(0.5)
+    coords = np.empty((2, band_h, width), dtype=np.float32)
+    coords[0] = rr[:, None]
+    coords[1] = cc[None, :]
+    fill_vals = ndi.map_coordinates(surface, coords, order=1, mode="nearest", output=np.float32)
+    if exterior is None:
+        ext = np.zeros((band_h, width), dtype=bool)
+    else:
+        ext = ndi.map_coordinates(exterior.astype(np.float32), coords, order=1, mode="nearest") > 0.5
+    return fill_vals, ext
+
+
+def apply_band_fill(band, masked, *, row_off, width, height, ch, cw, do_fill, surface, exterior, extra_nodata,
+                    fill_mode, out_nodata):
+    """io/dem_preprocess.py:770-826 (_apply_band_fill) on one full-width row band
+    (``masked``: the read's own NoData mask)."""
+    arr = np.array(band, dtype=np.float32, copy=True)
+    wmask = masked | ~np.isfinite(arr)
+    for v in extra_nodata:
+        wmask = wmask | (arr == np.float32(v))
+    if wmask.any():
+        arr[wmask] = np.float32(np.nan)
+    if do_fill and wmask.any():
+        fill_vals, ext = sample_coarse_band(surface, exterior, row_off, arr.shape[0], width, height, ch, cw)
+        fill_here = wmask & ~ext if fill_mode == "enclosed" else wmask
+        arr[fill_here] = fill_vals[fill_here]
+    if out_nodata is None:
+        if not np.isfinite(arr).all():
+            raise RuntimeError(f"fill_mode='all' left {int(np.count_nonzero(~np.isfinite(arr)))} non-finite pixels")
+    else:
+        arr[~np.isfinite(arr)] = np.float32(np.nan)
+    return arr
+
+
+def nearest_sample(dem, oh, ow):
+    """A nearest-neighbour read of ``dem`` at oh x ow: source index floor((i + 0.5) * n / o).
+    Stands in for GDAL's NEAREST overview read (absent here; parity of this step unpinned)."""
+    h, w = dem.shape
+    ys = np.minimum(((np.arange(oh) + 0.5) * (h / oh)).astype(np.int64), h - 1)
+    xs = np.minimum(((np.arange(ow) + 0.5) * (w / ow)).astype(np.int64), w - 1)
+    return dem[ys][:, xs]
+
+
+def prepare_dem(dem, *, nodata=None, fill_mode="enclosed", coarse_max=2048, nodata_override=None,
+                detect_nodata=True, nodata_border_fraction=0.5, nodata_sentinel_fraction=0.05):
+    """preprocess_dem_to_cog (io/dem_preprocess.py:462-726) on an in-memory raster, minus the
+    GDAL/COG I/O: NoData detection on the nearest coarse sample, the NaN-aware coarse
+    average, push-pull fill, the exterior mask ('enclosed'), then the full-resolution
+    normalise-and-fill of every row (one band: the fill samples global coordinates, so
+    bands give the same pixels).  Returns (array, info)."""
+    height, width = dem.shape
+    ch, cw = coarse_shape(width, height, coarse_max)
+    extra = []
+    if nodata_override is not None and np.isfinite(nodata_override):
+        extra.append(float(nodata_override))
+    k = coarse_oversample(ch, cw)
+    nn = nearest_sample(dem, ch * k, cw * k).astype(np.float32)
+    declared = np.zeros(nn.shape, bool)
+    if nodata is not None:
+        declared = np.isnan(nn) if np.isnan(nodata) else (nn == np.float32(nodata))
+    if detect_nodata:
+        nn_valid = (~declared) & np.isfinite(nn)
+        for det in (detect_sentinel_nodata(nn, nn_valid, min_fraction=nodata_sentinel_fraction),
+                    detect_border_nodata(nn, nn_valid, min_border_fraction=nodata_border_fraction)):
+            if det is None:
+                continue
+            already = any(np.isclose(det, v) for v in extra)
+            decl = nodata is not None and np.isclose(det, float(nodata))
+            if not already and not decl:
+                extra.append(float(det))
+    coarse, cmask = nan_aware_coarse_average(nn, declared, ch, cw, nodata, extra)
+    cvalid = (~cmask) & np.isfinite(coarse)
+    do_fill = fill_mode != "none" and bool((~cvalid).any())
+    surface = exterior = None
+    if do_fill:
+        surface = pushpull_fill(coarse, cvalid)
+        if fill_mode == "enclosed":
+            exterior = edge_connected_mask(~cvalid)
+    out_nodata = None if fill_mode == "all" else float("nan")
+    masked = np.zeros(dem.shape, bool)
+    if nodata is not None and not np.isnan(nodata):
+        masked = dem == np.float32(nodata)
+    out = apply_band_fill(dem, masked, row_off=0, width=width, height=height, ch=ch, cw=cw, do_fill=do_fill,
+                          surface=surface, exterior=exterior, extra_nodata=extra, fill_mode=fill_mode,
+                          out_nodata=out_nodata)
+    return out, {"extra_nodata": extra, "coarse_shape": (ch, cw), "oversample": k, "do_fill": do_fill}

@@ -365,10 +365,120 @@ def main_ambient_occlusion():
         json.dump(meta, f, indent=1, sort_keys=True)
 
 
+def _stub_gdal_modules():
+    """dem_preprocess imports rasterio and osgeo.gdal at module level; the functions the
+    fixtures call use neither, so empty stand-ins let the module import."""
+    import types
+    for name in ("rasterio", "rasterio.enums", "rasterio.windows", "osgeo", "osgeo.gdal"):
+        if name not in sys.modules:
+            sys.modules[name] = types.ModuleType(name)
+    sys.modules["rasterio.enums"].Resampling = type("Resampling", (), {"nearest": 0, "average": 5})
+    sys.modules["rasterio.windows"].Window = object
+    sys.modules["rasterio.windows"].transform = lambda *a, **k: None
+    sys.modules["osgeo"].gdal = sys.modules["osgeo.gdal"]
+
+
+def main_prepare():
+    """prepare.npz / .json: push-pull fill, the NaN-aware coarse average, the NoData detection
+    rules, the edge-connected mask and the per-band normalise-and-fill
+    (io/dem_preprocess.py, algorithms/_pyramid_fill.py, utils/nodata_handler.py)."""
+    reference_shim.load()
+    _stub_gdal_modules()
+    import importlib
+    from scipy.ndimage import zoom as sp_zoom
+    pf = importlib.import_module("FujiShaderGPU.algorithms._pyramid_fill")
+    nh = importlib.import_module("FujiShaderGPU.utils.nodata_handler")
+    dp = importlib.import_module("FujiShaderGPU.io.dem_preprocess")
+    arrays, meta = {}, {}
+    rng = np.random.default_rng(61)
+    # push-pull fill
+    c1 = synth.fbm(40, 56, hurst=0.8, seed=62, lo=0.0, hi=1200.0)
+    v1 = ~synth.nodata_disks(40, 56, count=4, seed=63, rmin=2.0, rmax=7.0)
+    v1[:, :5] = False
+    c2 = synth.fbm(3, 70, hurst=0.8, seed=64, lo=0.0, hi=500.0)
+    v2 = np.ones((3, 70), bool)
+    v2[:, 20:62] = False
+    c3 = synth.fbm(17, 9, hurst=0.8, seed=65, lo=0.0, hi=50.0)
+    v3 = rng.random((17, 9)) > 0.7
+    for n, c, v in (("pp1", c1, v1), ("pp2_wide", c2, v2), ("pp3_sparse", c3, v3),
+                    ("pp4_all_valid", c3, np.ones_like(v3)), ("pp5_none_valid", c3, np.zeros_like(v3))):
+        arrays[f"{n}/coarse"], arrays[f"{n}/valid"] = c, v
+        arrays[f"{n}/filled"] = pf.pushpull_fill(c.copy(), v.copy(), xp=np, zoom=sp_zoom)
+    # NaN-aware coarse average of a k x k oversampled nearest sample
+    sm = synth.fbm(48, 64, hurst=0.7, seed=66, lo=-20.0, hi=800.0)
+    sm[:, :10] = -9999.0
+    sm[30:34, 40:44] = 0.0
+    sm[5:9, 50:60] = np.nan
+    decl = np.zeros(sm.shape, bool)
+    decl[20:24, 20:28] = True
+    arrays["avg/sample"], arrays["avg/declared"] = sm, decl
+    co, cm = dp._nan_aware_coarse_average(None, 12, 16, None, [-9999.0, 0.0], oversample=4,
+                                          sample_ma=np.ma.masked_array(sm, mask=decl))
+    arrays["avg/coarse"], arrays["avg/void"] = co, cm
+    # NoData detection rules
+    det = {}
+    frame = synth.fbm(64, 64, hurst=0.7, seed=67, lo=10.0, hi=900.0)
+    frame[:6, :] = 0.0
+    frame[-6:, :] = 0.0
+    frame[:, :6] = 0.0
+    frame[:, -6:] = 0.0
+    spread = synth.fbm(64, 64, hurst=0.7, seed=68, lo=10.0, hi=900.0)
+    spread[rng.random((64, 64)) < 0.1] = -9999.0
+    extreme = synth.fbm(64, 64, hurst=0.7, seed=69, lo=10.0, hi=900.0)
+    extreme[rng.random((64, 64)) < 0.08] = 10.0
+    midval = synth.fbm(64, 64, hurst=0.7, seed=70, lo=10.0, hi=900.0)
+    midval[rng.random((64, 64)) < 0.08] = 500.0
+    for n, a in (("frame", frame), ("spread", spread), ("extreme", extreme), ("midval", midval),
+                 ("clean", synth.fbm(64, 64, hurst=0.7, seed=71, lo=10.0, hi=900.0))):
+        valid = np.isfinite(a)
+        arrays[f"det_{n}/sample"] = a
+        det[n] = [dp._detect_sentinel_nodata(a, valid, min_fraction=0.05),
+                  dp._detect_border_nodata(a, valid, min_border_fraction=0.5)]
+    meta["detect"] = det
+    meta["coarse_shape"] = [[w, h, m, list(dp._coarse_shape(w, h, m))]
+                            for w, h, m in ((65536, 32768, 2048), (1000, 3000, 2048), (100, 50, 2048),
+                                            (5000, 5000, 2048), (4097, 2049, 1024))]
+    # edge-connected mask
+    em = rng.random((50, 60)) < 0.45
+    arrays["edge/mask"] = em
+    arrays["edge/connected"] = nh._edge_connected_mask(em)
+    # per-band normalise-and-fill (enclosed and all), band at a row offset
+    H, W = 96, 120
+    full = synth.fbm(H, W, hurst=0.8, seed=72, lo=0.0, hi=1500.0)
+    holes = synth.nodata_disks(H, W, count=4, seed=73, rmin=3.0, rmax=9.0)
+    full[holes] = -9999.0
+    full[:, :8] = np.nan
+    ch, cw = 24, 30   # the full band itself as the 4x oversampled sample
+    cavg, cvoid = dp._nan_aware_coarse_average(None, ch, cw, None, [-9999.0], oversample=4,
+                                               sample_ma=np.ma.masked_array(full, mask=np.zeros((H, W), bool)))
+    cvalid = (~cvoid) & np.isfinite(cavg)
+    surface = pf.pushpull_fill(cavg, cvalid, xp=np, zoom=sp_zoom)
+    ext = nh._edge_connected_mask(~cvalid)
+    arrays["band/full"], arrays["band/surface"], arrays["band/exterior"] = full, surface, ext
+    arrays["band/coarse"], arrays["band/cvalid"] = cavg, cvalid
+    row_off, bh = 40, 33
+    band = np.ma.masked_array(full[row_off:row_off + bh], mask=np.zeros((bh, W), bool))
+    for mode, out_nd in (("enclosed", float("nan")), ("all", None)):
+        arrays[f"band/{mode}"] = dp._apply_band_fill(
+            band, row_off=row_off, bh=bh, width=W, height=H, ch=ch, cw=cw, do_fill=True, surface=surface,
+            exterior_coarse=ext if mode == "enclosed" else None, extra_nodata=[-9999.0], fill_mode=mode,
+            out_nodata=out_nd)
+    fv, ex = dp._sample_coarse(surface, ext, row_off, bh, W, H, ch, cw)
+    arrays["band/sample_vals"], arrays["band/sample_ext"] = fv, ex
+    meta["band"] = {"row_off": row_off, "bh": bh, "ch": ch, "cw": cw}
+    np.savez_compressed(os.path.join(HERE, "prepare.npz"), **arrays)
+    with open(os.path.join(HERE, "prepare.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+
+
+SECTIONS = {"ambient_occlusion": lambda: main_ambient_occlusion(), "prepare": lambda: main_prepare()}
+
+
 if __name__ == "__main__":
-    # "--section ambient_occlusion" regenerates that fixture alone
-    if "--section" in sys.argv and sys.argv[sys.argv.index("--section") + 1] == "ambient_occlusion":
-        main_ambient_occlusion()
+    # "--section <name>" regenerates that fixture alone
+    if "--section" in sys.argv:
+        SECTIONS[sys.argv[sys.argv.index("--section") + 1]]()
     else:
         main()
-        main_ambient_occlusion()
+        for fn in SECTIONS.values():
+            fn()

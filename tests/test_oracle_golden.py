@@ -315,3 +315,48 @@ def test_nodata_mask_merges_nan_and_sentinel():
     assert m.tolist() == [[True, True, False, True], [False, False, False, False]]
     assert R.nodata_mask(d, float("nan")).tolist() == np.isnan(d).tolist()
     assert R.nodata_mask(d, None) is None
+
+
+PP_CASES = ["pp1", "pp2_wide", "pp3_sparse", "pp4_all_valid", "pp5_none_valid"]
+
+
+@pytest.mark.parametrize("case", PP_CASES)
+def test_pushpull_fill_bit_exact(golden_dir, case):
+    """pushpull_fill (_pyramid_fill.py:24-84): voids with an exterior strip, a wide void in a
+    3-row grid (the apex collapses the long axis), sparse support, all / no valid cells."""
+    g = _load(golden_dir, "prepare")
+    _eq(R.pushpull_fill(g[f"{case}/coarse"], g[f"{case}/valid"]), g[f"{case}/filled"])
+
+
+def test_prepare_pieces_bit_exact(golden_dir):
+    """_nan_aware_coarse_average (declared mask + sentinels), _detect_sentinel_nodata /
+    _detect_border_nodata (frame, spread sentinel, range extreme, mid-range spike, clean),
+    _coarse_shape, _edge_connected_mask, _sample_coarse and _apply_band_fill
+    (io/dem_preprocess.py:135-275, 729-826; utils/nodata_handler.py:13-25)."""
+    g = _load(golden_dir, "prepare")
+    m = _meta(golden_dir, "prepare")
+    co, cm = R.nan_aware_coarse_average(g["avg/sample"], g["avg/declared"], 12, 16, None, [-9999.0, 0.0])
+    _eq(co, g["avg/coarse"])
+    assert np.array_equal(cm, g["avg/void"])
+    for n, (sent, border) in m["detect"].items():
+        a = g[f"det_{n}/sample"]
+        v = np.isfinite(a)
+        assert R.detect_sentinel_nodata(a, v) == sent, n
+        assert R.detect_border_nodata(a, v) == border, n
+    for w, h, cmax, ref in m["coarse_shape"]:
+        assert list(R.coarse_shape(w, h, cmax)) == ref
+    assert np.array_equal(R.edge_connected_mask(g["edge/mask"]), g["edge/connected"])
+    b = m["band"]
+    full = g["band/full"]
+    H, W = full.shape
+    band = full[b["row_off"]:b["row_off"] + b["bh"]]
+    for mode, out_nd in (("enclosed", float("nan")), ("all", None)):
+        out = R.apply_band_fill(band, np.zeros(band.shape, bool), row_off=b["row_off"], width=W, height=H,
+                                ch=b["ch"], cw=b["cw"], do_fill=True, surface=g["band/surface"],
+                                exterior=g["band/exterior"] if mode == "enclosed" else None,
+                                extra_nodata=[-9999.0], fill_mode=mode, out_nodata=out_nd)
+        _eq(out, g[f"band/{mode}"])
+    fv, ex = R.sample_coarse_band(g["band/surface"], g["band/exterior"], b["row_off"], b["bh"], W, H, b["ch"],
+                                  b["cw"])
+    _eq(fv, g["band/sample_vals"])
+    assert np.array_equal(ex, g["band/sample_ext"])
