@@ -149,6 +149,19 @@ _SIGNATURES = {
     "fsg_ambient_occlusion_plan": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile),
                                              C.c_int32, C.POINTER(AoParams), C.POINTER(Plane),
                                              C.POINTER(C.c_void_p)]),
+    "fsg_nearest_sample": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double,
+                                     C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]),
+    "fsg_coarse_average": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                     C.POINTER(C.c_double), C.c_int32, C.c_void_p, C.c_int64, C.c_void_p,
+                                     C.c_int64, C.POINTER(C.c_int32), C.c_void_p]),
+    "fsg_pushpull_fill": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p,
+                                    C.c_int64, C.c_void_p]),
+    "fsg_edge_connected": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
+                                     C.c_void_p]),
+    "fsg_fill_apply": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double,
+                                 C.c_int32, C.POINTER(C.c_double), C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
+                                 C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
+                                 C.POINTER(C.c_int32), C.c_void_p]),
     "fsg_openness_offsets": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                        C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32]),
     "fsg_affine": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_int32,

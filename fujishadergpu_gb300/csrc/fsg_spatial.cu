@@ -118,27 +118,6 @@ __global__ void any_nan(const float* __restrict__ a, long long ld, int h, int w,
 }
 
 // --------------------------------------------------------- decimation
-// NumPy's pairwise float32 sum of n (<= 16) values x(0..n-1).
-template <class Fn>
-__device__ __forceinline__ float np_pairwise(int n, Fn x) {
-  if (n < 8) {
-    float r = 0.f;
-    for (int i = 0; i < n; ++i) r = __fadd_rn(r, x(i));
-    return r;
-  }
-  float r[8];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) r[j] = x(j);
-  int i = 8;
-  for (; i < n - (n % 8); i += 8)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) r[j] = __fadd_rn(r[j], x(i + j));
-  float res = __fadd_rn(__fadd_rn(__fadd_rn(r[0], r[1]), __fadd_rn(r[2], r[3])),
-                        __fadd_rn(__fadd_rn(r[4], r[5]), __fadd_rn(r[6], r[7])));
-  for (; i < n; ++i) res = __fadd_rn(res, x(i));
-  return res;
-}
-
 // _downsample_nan_aware's cell mean (_nan_utils.py:629-641): cells padded
 // with NaN at the ragged edge, tot / max(cnt, 1) where cnt > 0 else NaN.
 __global__ void block_mean_np(const float* __restrict__ src, long long ld, int h, int w, int f, float* out,
@@ -198,32 +177,7 @@ __global__ void zoom_linear(const float* __restrict__ a, long long ld, int h, in
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= ow || y >= oh) return;
   const int zy = min(y0 + y, zh - 1), zx = min(x0 + x, zw - 1);
-  const double cy = __dmul_rn((double)zy, fy), cx = __dmul_rn((double)zx, fx);
-  const double sy = floor(cy), sx = floor(cx);
-  const double ty = __dsub_rn(cy, sy), tx = __dsub_rn(cx, sx);
-  const int iy0 = clamp_idx((int)sy, h), iy1 = clamp_idx((int)sy + 1, h);
-  const int ix0 = clamp_idx((int)sx, w), ix1 = clamp_idx((int)sx + 1, w);
-  const double wy0 = __dsub_rn(1.0, ty), wx0 = __dsub_rn(1.0, tx);
-  const float v00 = __ldg(a + (long long)iy0 * ld + ix0), v01 = __ldg(a + (long long)iy0 * ld + ix1);
-  const float v10 = __ldg(a + (long long)iy1 * ld + ix0), v11 = __ldg(a + (long long)iy1 * ld + ix1);
-  auto lerp4 = [&](double a00, double a01, double a10, double a11) {
-    double t = __dmul_rn(__dmul_rn(a00, wy0), wx0);
-    t = __dadd_rn(t, __dmul_rn(__dmul_rn(a01, wy0), tx));
-    t = __dadd_rn(t, __dmul_rn(__dmul_rn(a10, ty), wx0));
-    t = __dadd_rn(t, __dmul_rn(__dmul_rn(a11, ty), tx));
-    return __double2float_rn(t);
-  };
-  float r;
-  if (nan_flag == nullptr || *nan_flag == 0) {
-    r = lerp4(v00, v01, v10, v11);
-  } else {
-    auto fv = [](float v) { return v == v ? (double)v : 0.0; };
-    auto fw = [](float v) { return v == v ? 1.0 : 0.0; };
-    const float num = lerp4(fv(v00), fv(v01), fv(v10), fv(v11));
-    const float den = lerp4(fw(v00), fw(v01), fw(v10), fw(v11));
-    r = den > 1e-3f ? __fdiv_rn(num, fmaxf(den, 1e-6f)) : kQNaN;
-  }
-  out[(long long)y * old + x] = r;
+  out[(long long)y * old + x] = zoom1_at(a, ld, h, w, zy, zx, fy, fx, nan_flag != nullptr && *nan_flag != 0);
 }
 
 // ------------------------------------------------------ tile pieces

@@ -335,6 +335,55 @@ int fsg_ambient_occlusion_plan(const float* raster_dev, int64_t ld, int32_t rast
 int fsg_openness_offsets(int32_t num_directions, int32_t max_distance, int32_t mode, int32_t* ox, int32_t* oy,
                          int32_t* ray_len, int32_t capacity);
 
+/* --------------------------------------------------------------- prepare */
+/* The NoData detection and void fill of preprocess_dem_to_cog
+ * (io/dem_preprocess.py:462-726) on in-memory device rasters; the GDAL / COG
+ * file I/O around it is not part of this library. */
+enum fsg_fill_mode { FSG_FILL_NONE = 0, FSG_FILL_ENCLOSED = 1, FSG_FILL_ALL = 2 };
+
+/* Nearest-neighbour read of the raster at oh x ow (source index
+ * trunc((i + 0.5) * n / o) per axis; stands in for GDAL's NEAREST read,
+ * io/dem_preprocess.py:540-546) and, when declared_dev is not NULL, its
+ * declared-NoData mask (value == nodata, or NaN for a NaN nodata). */
+int fsg_nearest_sample(const float* raster_dev, int64_t ld, int32_t h, int32_t w, int32_t oh, int32_t ow,
+                       double nodata, int32_t has_nodata, float* sample_dev, int64_t sample_ld,
+                       uint8_t* declared_dev, int64_t declared_ld, void* stream);
+
+/* _nan_aware_coarse_average (io/dem_preprocess.py:135-188) of a (ch k) x (cw k)
+ * sample: a sample is NoData when declared, non-finite or equal (as float32) to
+ * one of nodata_values (at most 16); coarse = float32(sum / count) of the valid
+ * samples (0 for a void), valid = count > 0; *any_void (nullable, synchronises)
+ * tells whether some cell is a void. */
+int fsg_coarse_average(const float* sample_dev, int64_t ld, const uint8_t* declared_dev, int64_t declared_ld,
+                       int32_t ch, int32_t cw, int32_t k, const double* nodata_values, int32_t n_values,
+                       float* coarse_dev, int64_t coarse_ld, uint8_t* valid_dev, int64_t valid_ld,
+                       int32_t* any_void, void* stream);
+
+/* pushpull_fill (algorithms/_pyramid_fill.py:24-84): a fully finite surface,
+ * valid cells kept exactly (synchronises once per push level). */
+int fsg_pushpull_fill(const float* coarse_dev, int64_t coarse_ld, const uint8_t* valid_dev, int64_t valid_ld,
+                      int32_t h, int32_t w, float* out_dev, int64_t out_ld, void* stream);
+
+/* _edge_connected_mask (utils/nodata_handler.py:13-25): the mask cells
+ * 4-connected to a border cell of the mask (the mask: cells != 0, or == 0 with
+ * invert set); synchronises per pass. */
+int fsg_edge_connected(const uint8_t* mask_dev, int64_t mask_ld, int32_t h, int32_t w, int32_t invert,
+                       uint8_t* out_dev, int64_t out_ld, void* stream);
+
+/* _apply_band_fill + _sample_coarse (io/dem_preprocess.py:729-826) over rows
+ * [row0, row0 + rows) of the raster: NoData (declared, non-finite, one of
+ * extra_nodata) -> NaN; with a fill mode and a surface, NoData cells take the
+ * bilinear ('nearest') sample of the ch x cw surface at ((y + 0.5) ch/h - 0.5,
+ * (x + 0.5) cw/w - 0.5) in float32, except, for FSG_FILL_ENCLOSED, where the
+ * bilinear exterior mask exceeds 0.5.  Row r goes to out + (r - row0) * out_ld
+ * (out may be the raster itself).  *nonfinite (nullable, synchronises): with
+ * FSG_FILL_ALL, some cell stayed non-finite. */
+int fsg_fill_apply(const float* raster_dev, int64_t ld, int32_t h, int32_t w, int32_t row0, int32_t rows,
+                   double nodata, int32_t has_nodata, const double* extra_nodata, int32_t n_extra,
+                   int32_t fill_mode, const float* surface_dev, int64_t surface_ld, const uint8_t* exterior_dev,
+                   int64_t exterior_ld, int32_t ch, int32_t cw, float* out_dev, int64_t out_ld, int32_t* nonfinite,
+                   void* stream);
+
 /* ------------------------------------------------------------- spatial mode */
 /* _smooth_for_radius(block, radius, pixel_size, algorithm)
  * (algorithms/_nan_utils.py:527-552): identity for radius <= 1, else the

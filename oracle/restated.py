@@ -1207,7 +1207,9 @@ def nearest_sample(dem, oh, ow):
     h, w = dem.shape
     ys = np.minimum(((np.arange(oh) + 0.5) * (h / oh)).astype(np.int64), h - 1)
     xs = np.minimum(((np.arange(ow) + 0.5) * (w / ow)).astype(np.int64), w - 1)
-    return dem[ys][:, xs]
+    # C order, as a raster read returns it: NumPy's float32 reduction order over the
+    # coarse cells (and so the rounding of their sums) follows the memory layout
+    return np.ascontiguousarray(dem[ys][:, xs])
 
 
 def prepare_dem(dem, *, nodata=None, fill_mode="enclosed", coarse_max=2048, nodata_override=None,
