@@ -24,6 +24,7 @@ skips them; ``--workload <section>`` prints one section alone):
   openness           16384^2, 16 directions, R = 256: the reference's 10-sample
                      rays, and the dense every-step march on a 4096^2 crop
   ambient_occlusion  16384^2, 16 samples x 4 rings, radius 10 and 30
+  prepare            NoData detection and void fill of a 32768^2 DEM
   openness_surrogate the CNN surrogate against the exact kernels
   spatial            spatial (multi-radius) mode of the stencil products and
                      openness at 8192^2
@@ -469,6 +470,37 @@ def ambient_occlusion_section(args):
     return {"workload": f"ambient occlusion, 16 samples x 4 rings, 5 m, {n}x{n}, 4096^2 tiles", **res}
 
 
+def prepare_section(args):
+    """The prepare step (NoData detection and void fill) on a 32768^2 fBm DEM with ~2 % NaN
+    disks, an undeclared 0-valued exterior frame and a declared -32768 patch: the whole
+    prepare_dem call (coarse sample, host detection rules, coarse average, push-pull,
+    exterior mask, full-resolution fill), and its full-resolution kernel alone against
+    the HBM roofline (4 B read + 4 B written per pixel)."""
+    import torch
+    from fujishadergpu_gb300 import _native, synth
+    from fujishadergpu_gb300.io import dem_preprocess as P
+    n = args.size
+    dem = synth.fbm_device(n, n, hurst=0.8, seed=9, lo=50.0, hi=3000.0)
+    synth.nodata_disks_device(dem, count=max(1, int(200 * (n / 16384) ** 2)), seed=10, rmin=10.0, rmax=200.0)
+    dem[: n // 50, :] = 0.0
+    dem[:, -n // 40:] = 0.0
+    out = torch.empty_like(dem)
+    stream = torch.cuda.current_stream()
+    steps = max(1, args.extra_steps // 2)
+    fn = lambda: P.prepare_dem(dem, nodata=-32768.0, fill_mode="enclosed", out=out)  # noqa: E731
+    with _native.kernel_timer(max_launches=steps + 1) as kt:
+        ms = _time_ms(fn, steps, 1, stream)
+    kms = kt.ms / max(1, kt.launches)
+    hbm, _, src = peaks()
+    gbs = n * n * 8 / (kms * 1e-3) / 1e9
+    res = {"raster": [n, n], "value": round(n * n / (ms * 1e-3) / 1e6, 1), "unit": "Mpix/s",
+           "ms_per_step": round(ms, 3), "fill_kernel_ms": round(kms, 3),
+           "fill_kernel_roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm, "peak_source": src,
+                                    "unit": "GB/s", "frac": round(gbs / hbm, 4)}}
+    del dem, out
+    return {"workload": f"prepare (fill_mode enclosed, coarse_max 2048), {n}x{n}", **res}
+
+
 def spatial_section(args):
     """Spatial (multi-radius) mode on an 8192^2 fBm+ridged DEM (5 m, 4096^2 tiles): hillshade,
     slope and curvature with radii 2, 8, 32, 128 and openness with distances 4, 16, 64, 256
@@ -594,7 +626,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["stencil", "topousm", "openness", "ambient_occlusion", "surrogate",
-                                           "spatial", "batched"],
+                                           "spatial", "batched", "prepare"],
                     default="stencil",
                     help="stencil: the headline line; topousm / openness: that section alone (profiling)")
     ap.add_argument("--size", type=int, default=32768)
@@ -617,6 +649,7 @@ def main():
     if args.workload != "stencil":
         sec = {"topousm": topousm_section, "openness": openness_section,
                "ambient_occlusion": ambient_occlusion_section, "surrogate": surrogate_section,
+               "prepare": prepare_section,
                "spatial": spatial_section, "batched": batched_section}[args.workload](args)
         if rank == 0:
             print(json.dumps({"section": args.workload, **sec}))
@@ -630,6 +663,8 @@ def main():
         line["extra"]["openness"] = openness_section(args)
         torch.cuda.empty_cache()
         line["extra"]["ambient_occlusion"] = ambient_occlusion_section(args)
+        torch.cuda.empty_cache()
+        line["extra"]["prepare"] = prepare_section(args)
         torch.cuda.empty_cache()
         line["extra"]["openness_surrogate"] = surrogate_section(args)
         torch.cuda.empty_cache()

@@ -154,6 +154,11 @@ _SIGNATURES = {
     "fsg_coarse_average": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                      C.POINTER(C.c_double), C.c_int32, C.c_void_p, C.c_int64, C.c_void_p,
                                      C.c_int64, C.POINTER(C.c_int32), C.c_void_p]),
+    "fsg_value_mode": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p, C.c_int64, C.c_double,
+                                 C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_void_p]),
+    "fsg_count_equal": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.POINTER(C.c_int64),
+                                  C.c_void_p]),
     "fsg_pushpull_fill": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p,
                                     C.c_int64, C.c_void_p]),
     "fsg_edge_connected": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,

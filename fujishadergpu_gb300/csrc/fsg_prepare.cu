@@ -213,32 +213,38 @@ struct FillArgs {
   int* nonfinite;              // set when 'all' leaves a non-finite cell
 };
 
-__global__ void fill_apply_k(const __grid_constant__ FillArgs A) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= A.rows || j >= A.w) return;
-  const int y = A.row0 + i;
-  float v = __ldg(A.raster + (long long)y * A.ld + j);
+// One pixel of the fill (raster row y, column x, value v).
+__device__ __forceinline__ float fill_pixel(const FillArgs& A, int y, int x, float v) {
   const bool declared = A.decl_mode == 1 ? (v != v) : (A.decl_mode == 2 ? v == A.ndf : false);
   const bool wm = declared || !isfinite(v) || in_set(A.extra, v);
-  if (wm) v = __int_as_float(0x7fc00000);
-  if (A.do_fill && wm) {
+  if (!wm) return v;
+  v = __int_as_float(0x7fc00000);
+  if (A.do_fill) {
     // (row + 0.5) * f32(ch / height) - 0.5 in float32, as _sample_coarse builds it
     const float rr = __fsub_rn(__fmul_rn(__fadd_rn((float)y, 0.5f), A.ry), 0.5f);
-    const float cc = __fsub_rn(__fmul_rn(__fadd_rn((float)j, 0.5f), A.rx), 0.5f);
+    const float cc = __fsub_rn(__fmul_rn(__fadd_rn((float)x, 0.5f), A.rx), 0.5f);
     bool ext = false;
     if (!A.fill_all && A.exterior) {
-      // map_coordinates of the 0/1 mask (float32) > 0.5
+      // map_coordinates of the 0/1 mask (float32) > 0.5; four equal corners give
+      // exactly 0, or 1 within float64 rounding, so only mixed corners are evaluated
       const double cy = (double)rr, cx = (double)cc;
       const double sy = floor(cy), sx = floor(cx);
-      const double ty = cy - sy, tx = cx - sx;
       const int iy0 = clamp_idx((int)sy, A.ch), iy1 = clamp_idx((int)sy + 1, A.ch);
       const int ix0 = clamp_idx((int)sx, A.cw), ix1 = clamp_idx((int)sx + 1, A.cw);
-      auto e = [&](int yy, int xx) { return A.exterior[(long long)yy * A.eld + xx] ? 1.0 : 0.0; };
-      double t = __dmul_rn(__dmul_rn(e(iy0, ix0), __dsub_rn(1.0, ty)), __dsub_rn(1.0, tx));
-      t = __dadd_rn(t, __dmul_rn(__dmul_rn(e(iy0, ix1), __dsub_rn(1.0, ty)), tx));
-      t = __dadd_rn(t, __dmul_rn(__dmul_rn(e(iy1, ix0), ty), __dsub_rn(1.0, tx)));
-      t = __dadd_rn(t, __dmul_rn(__dmul_rn(e(iy1, ix1), ty), tx));
-      ext = __double2float_rn(t) > 0.5f;
+      const uint8_t* E = A.exterior;
+      const int n1 = (E[(long long)iy0 * A.eld + ix0] != 0) + (E[(long long)iy0 * A.eld + ix1] != 0) +
+                     (E[(long long)iy1 * A.eld + ix0] != 0) + (E[(long long)iy1 * A.eld + ix1] != 0);
+      if (n1 == 4) {
+        ext = true;
+      } else if (n1 > 0) {
+        const double ty = cy - sy, tx = cx - sx;
+        auto e = [&](int yy, int xx) { return E[(long long)yy * A.eld + xx] ? 1.0 : 0.0; };
+        double t = __dmul_rn(__dmul_rn(e(iy0, ix0), __dsub_rn(1.0, ty)), __dsub_rn(1.0, tx));
+        t = __dadd_rn(t, __dmul_rn(__dmul_rn(e(iy0, ix1), __dsub_rn(1.0, ty)), tx));
+        t = __dadd_rn(t, __dmul_rn(__dmul_rn(e(iy1, ix0), ty), __dsub_rn(1.0, tx)));
+        t = __dadd_rn(t, __dmul_rn(__dmul_rn(e(iy1, ix1), ty), tx));
+        ext = __double2float_rn(t) > 0.5f;
+      }
     }
     if (!ext) v = lerp1_at(A.surface, A.sld, A.ch, A.cw, (double)rr, (double)cc, false);
   }
@@ -246,7 +252,18 @@ __global__ void fill_apply_k(const __grid_constant__ FillArgs A) {
     if (A.fill_all) atomicOr(A.nonfinite, 1);
     v = __int_as_float(0x7fc00000);
   }
-  A.out[(long long)i * A.old + j] = v;
+  return v;
+}
+
+// One thread per pixel: the NoData pixels' float64 interpolation is a long
+// dependent chain on GB300's low-rate FP64 pipe, and as many resident warps as
+// possible hide it (a grid-stride variant with four pixels per thread and one
+// wave of blocks measured 1.5-1.8x slower).
+__global__ void __launch_bounds__(256) fill_apply_k(const __grid_constant__ FillArgs A) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= A.rows || x >= A.w) return;
+  const int y = A.row0 + i;
+  A.out[(long long)i * A.old + x] = fill_pixel(A, y, x, __ldg(A.raster + (long long)y * A.ld + x));
 }
 
 // flags[0] |= some cell invalid, flags[1] |= some cell valid
@@ -265,6 +282,96 @@ __global__ void mask_any_k(const uint8_t* __restrict__ m, long long mld, int h, 
 void zoom_axis(int n, int t, int* out, double* step) {
   *out = (int)std::nearbyint((double)n * ((double)t / (double)n));
   *step = *out > 1 ? (double)(n - 1) / (double)(*out - 1) : 1.0;
+}
+
+// ------------------------------------------------------- value statistics
+// Exact value counts for the NoData detection rules (_detect_sentinel_nodata,
+// io/dem_preprocess.py:241-275): keys are the float bit patterns with -0 folded
+// into +0 (np.unique merges them).  Pass 1 counts the finite, undeclared samples
+// per high 16 bits of the order-preserving key and tracks the smallest and
+// largest key; pass 2 counts every value of up to MAX_HEAVY heavy high-16 bins.
+// Equal keys of a warp are merged before their atomic (match.any), so a
+// dominant value costs one atomic per warp.
+constexpr int MAX_HEAVY = 64;
+
+__device__ __forceinline__ unsigned order_key(float v) {
+  unsigned u = __float_as_uint(v == 0.0f ? 0.0f : v);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void value_hist_k(const float* __restrict__ a, long long ld, int h, int w, const uint8_t* __restrict__ decl,
+                             long long dld, unsigned* __restrict__ hist, unsigned* kmin, unsigned* kmax) {
+  const long long n = (long long)h * w;
+  const unsigned lane = threadIdx.x & 31;
+  unsigned lo = 0xffffffffu, hi = 0u;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += (long long)gridDim.x * blockDim.x) {
+    const long long i = base + threadIdx.x;
+    bool ok = false;
+    unsigned k = 0;
+    if (i < n) {
+      const int y = (int)(i / w), x = (int)(i - (long long)y * w);
+      const float v = __ldg(a + (long long)y * ld + x);
+      ok = isfinite(v) && !(decl && decl[(long long)y * dld + x]);
+      k = order_key(v);
+    }
+    const unsigned act = __ballot_sync(0xffffffffu, ok);
+    if (ok) {
+      lo = min(lo, k);
+      hi = max(hi, k);
+      const unsigned bin = k >> 16;
+      const unsigned peers = __match_any_sync(act, bin);
+      if ((unsigned)(__ffs(peers) - 1) == lane) atomicAdd(hist + bin, (unsigned)__popc(peers));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if (lane == 0) {
+    atomicMin(kmin, lo);
+    atomicMax(kmax, hi);
+  }
+}
+
+// slot_of[bin]: the heavy slot of a high-16 bin, or -1
+__global__ void value_count_k(const float* __restrict__ a, long long ld, int h, int w,
+                             const uint8_t* __restrict__ decl, long long dld, const short* __restrict__ slot_of,
+                             unsigned* __restrict__ counts) {
+  const long long n = (long long)h * w;
+  const unsigned lane = threadIdx.x & 31;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += (long long)gridDim.x * blockDim.x) {
+    const long long i = base + threadIdx.x;
+    int slot = -1;
+    unsigned k = 0;
+    if (i < n) {
+      const int y = (int)(i / w), x = (int)(i - (long long)y * w);
+      const float v = __ldg(a + (long long)y * ld + x);
+      if (isfinite(v) && !(decl && decl[(long long)y * dld + x])) {
+        k = order_key(v);
+        slot = slot_of[k >> 16];
+      }
+    }
+    const bool ok = slot >= 0;
+    const unsigned act = __ballot_sync(0xffffffffu, ok);
+    if (ok) {
+      const unsigned peers = __match_any_sync(act, k);
+      if ((unsigned)(__ffs(peers) - 1) == lane)
+        atomicAdd(counts + (size_t)slot * 65536u + (k & 0xffffu), (unsigned)__popc(peers));
+    }
+  }
+}
+
+// number of samples equal (as float32) to v
+__global__ void count_equal_k(const float* __restrict__ a, long long ld, int h, int w, float v,
+                              unsigned long long* count) {
+  const long long n = (long long)h * w;
+  unsigned c = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(i / w), x = (int)(i - (long long)y * w);
+    c += __ldg(a + (long long)y * ld + x) == v ? 1u : 0u;
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, (unsigned long long)c);
 }
 
 int nodata_set(const double* vals, int n, NodataSet* s) {
@@ -488,6 +595,7 @@ extern "C" int fsg_fill_apply(const float* raster_dev, int64_t ld, int32_t h, in
   if (st) return st;
   A.nonfinite = static_cast<int*>(flag.ptr);
   FSG_CUDA(cudaMemsetAsync(A.nonfinite, 0, sizeof(int), s));
+  if ((rows + 7) / 8 > 65535) return fail(FSG_ERR_UNSUPPORTED, "more than 524280 rows in one call");
   timing_mark(s, true);
   fill_apply_k<<<grid2d(rows, w), dim3(32, 8), 0, s>>>(A);
   timing_mark(s, false);
@@ -498,5 +606,108 @@ extern "C" int fsg_fill_apply(const float* raster_dev, int64_t ld, int32_t h, in
     if (st) return st;
     *nonfinite = v;
   }
+  return FSG_OK;
+}
+
+extern "C" int fsg_value_mode(const float* sample_dev, int64_t ld, int32_t h, int32_t w, const uint8_t* declared_dev,
+                              int64_t declared_ld, double min_fraction, int64_t* n_finite, double* vmin,
+                              double* vmax, double* mode_value, int64_t* mode_count, void* stream) {
+  if (!sample_dev || !n_finite || !vmin || !vmax || !mode_value || !mode_count)
+    return fail(FSG_ERR_INVALID, "null argument");
+  if (h <= 0 || w <= 0 || ld < w || (declared_dev && declared_ld < w)) return fail(FSG_ERR_SHAPE, "bad sample shape");
+  cudaStream_t s = (cudaStream_t)stream;
+  DeviceInfo di;
+  int st = device_info(&di);
+  if (st) return st;
+  StreamScratch scr;
+  const size_t hist_b = 65536 * sizeof(unsigned), counts_b = (size_t)MAX_HEAVY * 65536 * sizeof(unsigned);
+  st = scr.alloc(hist_b + counts_b + 65536 * sizeof(short) + 64, s);
+  if (st) return st;
+  unsigned* hist = static_cast<unsigned*>(scr.ptr);
+  unsigned* counts = hist + 65536;
+  short* slot_of = reinterpret_cast<short*>(counts + (size_t)MAX_HEAVY * 65536);
+  unsigned* kminmax = reinterpret_cast<unsigned*>(slot_of + 65536);
+  const unsigned init[2] = {0xffffffffu, 0u};
+  FSG_CUDA(cudaMemsetAsync(hist, 0, hist_b, s));
+  FSG_CUDA(cudaMemcpyAsync(kminmax, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  const long long n = (long long)h * w;
+  const int grid = (int)std::min<long long>((n + 255) / 256, (long long)di.sms * 8);
+  value_hist_k<<<grid, 256, 0, s>>>(sample_dev, ld, h, w, declared_dev, declared_ld, hist, kminmax, kminmax + 1);
+  FSG_LAUNCHED(1);
+  std::vector<unsigned> hh(65536);
+  unsigned mm[2];
+  FSG_CUDA(cudaMemcpyAsync(hh.data(), hist, hist_b, cudaMemcpyDeviceToHost, s));
+  FSG_CUDA(cudaMemcpyAsync(mm, kminmax, sizeof(mm), cudaMemcpyDeviceToHost, s));
+  FSG_CUDA(cudaStreamSynchronize(s));
+  long long nf = 0;
+  for (unsigned c : hh) nf += c;
+  *n_finite = nf;
+  *mode_count = 0;
+  *mode_value = std::nan("");
+  *vmin = *vmax = std::nan("");
+  if (nf == 0) return FSG_OK;
+  auto val = [](unsigned k) {
+    const unsigned u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    float f;
+    std::memcpy(&f, &u, sizeof(f));
+    return (double)f;
+  };
+  *vmin = val(mm[0]);
+  *vmax = val(mm[1]);
+  // a value holding at least min_fraction of the samples lies in a bin that does
+  std::vector<short> so(65536, -1);
+  std::vector<int> heavy;
+  for (int b = 0; b < 65536; ++b)
+    if (hh[b] > 0 && (double)hh[b] / (double)nf >= min_fraction) {
+      if ((int)heavy.size() == MAX_HEAVY) return fail(FSG_ERR_UNSUPPORTED, "min_fraction too small");
+      so[b] = (short)heavy.size();
+      heavy.push_back(b);
+    }
+  if (heavy.empty()) return FSG_OK;  // no value reaches min_fraction: the mode does not matter
+  FSG_CUDA(cudaMemcpyAsync(slot_of, so.data(), 65536 * sizeof(short), cudaMemcpyHostToDevice, s));
+  FSG_CUDA(cudaMemsetAsync(counts, 0, heavy.size() * 65536 * sizeof(unsigned), s));
+  value_count_k<<<grid, 256, 0, s>>>(sample_dev, ld, h, w, declared_dev, declared_ld, slot_of, counts);
+  FSG_LAUNCHED(1);
+  std::vector<unsigned> cc(heavy.size() * 65536);
+  FSG_CUDA(cudaMemcpyAsync(cc.data(), counts, cc.size() * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  FSG_CUDA(cudaStreamSynchronize(s));
+  // the most frequent value, the smallest on ties (np.unique + argmax); heavy bins and
+  // their low halves ascend with the key, i.e. with the value
+  long long best = 0;
+  unsigned bestk = 0;
+  for (size_t h2 = 0; h2 < heavy.size(); ++h2)
+    for (unsigned lo = 0; lo < 65536; ++lo) {
+      const unsigned c = cc[h2 * 65536 + lo];
+      if ((long long)c > best) {
+        best = c;
+        bestk = ((unsigned)heavy[h2] << 16) | lo;
+      }
+    }
+  *mode_count = best;
+  *mode_value = val(bestk);
+  return FSG_OK;
+}
+
+extern "C" int fsg_count_equal(const float* sample_dev, int64_t ld, int32_t h, int32_t w, double value,
+                               int64_t* count, void* stream) {
+  if (!sample_dev || !count) return fail(FSG_ERR_INVALID, "null argument");
+  if (h <= 0 || w <= 0 || ld < w) return fail(FSG_ERR_SHAPE, "bad sample shape");
+  cudaStream_t s = (cudaStream_t)stream;
+  StreamScratch scr;
+  int st = scr.alloc(sizeof(unsigned long long), s);
+  if (st) return st;
+  FSG_CUDA(cudaMemsetAsync(scr.ptr, 0, sizeof(unsigned long long), s));
+  DeviceInfo di;
+  st = device_info(&di);
+  if (st) return st;
+  const long long n = (long long)h * w;
+  const int grid = (int)std::min<long long>((n + 255) / 256, (long long)di.sms * 8);
+  count_equal_k<<<grid, 256, 0, s>>>(sample_dev, ld, h, w, (float)value,
+                                     static_cast<unsigned long long*>(scr.ptr));
+  FSG_LAUNCHED(1);
+  unsigned long long c = 0;
+  FSG_CUDA(cudaMemcpyAsync(&c, scr.ptr, sizeof(c), cudaMemcpyDeviceToHost, s));
+  FSG_CUDA(cudaStreamSynchronize(s));
+  *count = (int64_t)c;
   return FSG_OK;
 }

@@ -10,9 +10,11 @@ for ``fill_mode='enclosed'``, marks the border-connected voids as exterior, and
 allowed voids from the bilinear coarse surface.  Here the raster is a device
 array and the file I/O is left out; (1), (3), (4) and (5) are CUDA kernels
 (``fsg_nearest_sample``, ``fsg_coarse_average``, ``fsg_pushpull_fill``,
-``fsg_edge_connected``, ``fsg_fill_apply``).  (2) is the reference's host
-heuristic (``np.unique`` counts over the coarse sample), kept on the host as
-in the reference.
+``fsg_edge_connected``, ``fsg_fill_apply``); for (2) the exact value counts
+come from the device (``fsg_value_mode``, ``fsg_count_equal``) and only the
+decisions and the few thousand ring values are handled on the host.
+``detect_sentinel_nodata`` / ``detect_border_nodata`` keep the reference's
+host signatures for NumPy samples.
 """
 from __future__ import annotations
 
@@ -92,6 +94,50 @@ def detect_sentinel_nodata(sample: np.ndarray, valid: np.ndarray, *, min_fractio
     return None
 
 
+def _known_or_extreme(cand: float, vmin: float, vmax: float) -> bool:
+    known = any(abs(cand - s) <= 1e-6 * max(1.0, abs(s)) for s in NODATA_SENTINELS)
+    return known or abs(cand) >= 1e30 or cand == vmin or cand == vmax
+
+
+def _sentinel_rule(sample, declared, min_fraction: float, stream) -> Optional[float]:
+    """detect_sentinel_nodata on the device sample: the value statistics come from
+    fsg_value_mode (exact counts), the decision is the reference's."""
+    h, w = sample.shape
+    nf, lo, hi, mv, mc = C.c_int64(), C.c_double(), C.c_double(), C.c_double(), C.c_int64()
+    N.check(N.lib().fsg_value_mode(C.c_void_p(sample.data_ptr()), w, h, w, C.c_void_p(declared.data_ptr()), w,
+                                   float(min_fraction), C.byref(nf), C.byref(lo), C.byref(hi), C.byref(mv),
+                                   C.byref(mc), stream))
+    if nf.value < 64 or mc.value == 0 or mc.value / float(nf.value) < float(min_fraction):
+        return None
+    cand = float(mv.value)
+    return cand if _known_or_extreme(cand, float(lo.value), float(hi.value)) else None
+
+
+def _border_rule(sample, declared, min_border_fraction: float, stream, min_total_fraction: float = 0.02):
+    """detect_border_nodata with the outer ring on the host and the whole-sample count of
+    the candidate from fsg_count_equal."""
+    h, w = sample.shape
+    if h < 8 or w < 8:
+        return None
+    parts = [(sample[0, :], declared[0, :]), (sample[-1, :], declared[-1, :]),
+             (sample[1:-1, 0], declared[1:-1, 0]), (sample[1:-1, -1], declared[1:-1, -1])]
+    ring = np.concatenate([p.cpu().numpy() for p, _ in parts])
+    ok = np.concatenate([(d.cpu().numpy() == 0) for _, d in parts])
+    ring = ring[ok & np.isfinite(ring)]
+    if ring.size == 0:
+        return None
+    vals, counts = np.unique(ring, return_counts=True)
+    i = int(np.argmax(counts))
+    cand = float(vals[i])
+    if counts[i] / ring.size < float(min_border_fraction):
+        return None
+    cnt = C.c_int64()
+    N.check(N.lib().fsg_count_equal(C.c_void_p(sample.data_ptr()), w, h, w, cand, C.byref(cnt), stream))
+    if cnt.value / float(h * w) < float(min_total_fraction):
+        return None
+    return cand
+
+
 @dataclass
 class PrepareResult:
     array: object                        # the normalised / filled raster (device, float32)
@@ -141,10 +187,8 @@ def prepare_dem(dem, *, nodata: Optional[float] = None, fill_mode: str = "enclos
                                    C.c_void_p(sample.data_ptr()), cw * k, C.c_void_p(declared.data_ptr()), cw * k,
                                    stream))
     if detect_nodata:
-        nn = sample.cpu().numpy()
-        nn_valid = (declared.cpu().numpy() == 0) & np.isfinite(nn)
-        for det in (detect_sentinel_nodata(nn, nn_valid, min_fraction=nodata_sentinel_fraction),
-                    detect_border_nodata(nn, nn_valid, min_border_fraction=nodata_border_fraction)):
+        for det in (_sentinel_rule(sample, declared, nodata_sentinel_fraction, stream),
+                    _border_rule(sample, declared, nodata_border_fraction, stream)):
             if det is None:
                 continue
             already = any(np.isclose(det, x) for x in extra)

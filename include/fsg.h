@@ -359,6 +359,19 @@ int fsg_coarse_average(const float* sample_dev, int64_t ld, const uint8_t* decla
                        float* coarse_dev, int64_t coarse_ld, uint8_t* valid_dev, int64_t valid_ld,
                        int32_t* any_void, void* stream);
 
+/* The value statistics of _detect_sentinel_nodata (io/dem_preprocess.py:241-275)
+ * over the finite, undeclared samples: their number, smallest and largest value,
+ * and, when some value holds at least min_fraction of them, the most frequent
+ * value (the smallest on ties) and its count (*mode_count = 0 otherwise).
+ * -0 and +0 count as one value.  Synchronises. */
+int fsg_value_mode(const float* sample_dev, int64_t ld, int32_t h, int32_t w, const uint8_t* declared_dev,
+                   int64_t declared_ld, double min_fraction, int64_t* n_finite, double* vmin, double* vmax,
+                   double* mode_value, int64_t* mode_count, void* stream);
+
+/* Number of samples equal (as float32) to value.  Synchronises. */
+int fsg_count_equal(const float* sample_dev, int64_t ld, int32_t h, int32_t w, double value, int64_t* count,
+                    void* stream);
+
 /* pushpull_fill (algorithms/_pyramid_fill.py:24-84): a fully finite surface,
  * valid cells kept exactly (synchronises once per push level). */
 int fsg_pushpull_fill(const float* coarse_dev, int64_t coarse_ld, const uint8_t* valid_dev, int64_t valid_ld,

@@ -159,3 +159,39 @@ def test_prepare_without_nodata_is_identity_and_override(lib):
     _eq(res.array, ref, "override")
     with pytest.raises(ValueError):
         P.prepare_dem(torch.from_numpy(dem).cuda(), fill_mode="bogus")
+
+
+def test_value_statistics_match_numpy_unique(lib, golden_dir):
+    """fsg_value_mode against np.unique + argmax (the detection rule's statistics): the
+    golden detection samples, ties (the smaller value wins), -0 and +0 as one value, and
+    declared cells left out."""
+    g, _ = _golden(golden_dir)
+    rng = np.random.default_rng(5)
+    tie = rng.integers(-3, 4, size=(300, 257)).astype(np.float32)
+    tie[tie == 0] = np.float32(-0.0)
+    tie[::7, ::3] = 0.0
+    tie[5:9, :] = np.nan
+    decl = np.zeros(tie.shape, bool)
+    decl[100:140, 17:90] = True
+    samples = [(g[f"det_{n}/sample"], None) for n in ("frame", "spread", "extreme", "midval", "clean")]
+    samples += [(tie, decl), (tie, None)]
+    for a, d in samples:
+        t = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        h, w = a.shape
+        dm = torch.from_numpy((d if d is not None else np.zeros(a.shape, bool)).astype(np.uint8)).cuda()
+        nf, lo, hi, mv, mc = C.c_int64(), C.c_double(), C.c_double(), C.c_double(), C.c_int64()
+        lib.check(lib.lib().fsg_value_mode(_p(t), w, h, w, _p(dm), w, 0.05, C.byref(nf), C.byref(lo), C.byref(hi),
+                                           C.byref(mv), C.byref(mc), _s()))
+        valid = np.isfinite(a) & ~(d if d is not None else np.zeros(a.shape, bool))
+        fin = a[valid]
+        vals, counts = np.unique(fin, return_counts=True)
+        assert nf.value == fin.size
+        assert lo.value == float(vals[0]) and hi.value == float(vals[-1])
+        i = int(np.argmax(counts))
+        if counts[i] / float(fin.size) >= 0.05:
+            assert mc.value == int(counts[i]) and mv.value == float(vals[i])
+        else:
+            assert mc.value == 0 or mc.value / float(fin.size) < 0.05
+        c = C.c_int64()
+        lib.check(lib.lib().fsg_count_equal(_p(t), w, h, w, float(vals[i]), C.byref(c), _s()))
+        assert c.value == int(np.sum(a == np.float32(vals[i])))
