@@ -9,8 +9,9 @@ Tolerances (stated once, used everywhere):
     of tanh there; NumPy's and CUDA's float32 tanh differ in that bit), the
     pre-gamma value (tanh+1)/2 agrees to 4 ulps of tanh (2^-23).
   * exact openness: mean angle within 0.01 degree.
-  * ambient occlusion (output in [0, 1]): 1e-5 (a polynomial arctan within
-    1.5e-7 rad and a reciprocal multiply stand in for float32 atan and division).
+  * ambient occlusion (output in [0, 1]): 1e-5 (a polynomial for the normalised
+    occlusion atan(t) / (pi/4), within 6.3e-7, and a reciprocal multiply stand in
+    for float32 atan and division).
   * a weighted combination of curvature displays (spatial mode): 1e-5 plus
     the sum over responses of weight x that response's own allowance (1e-5,
     or in its tail the display change of 2^-23 in the pre-gamma value).
