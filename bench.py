@@ -180,6 +180,10 @@ def _cpu_tile_job(args):
     elif kind == "openness":
         R.openness(dem, openness_type="positive", num_directions=16, max_distance=params["md"],
                    pixel_size=5.0, psx=5.0, psy=-5.0)
+    elif kind == "ambient_occlusion":
+        R.ambient_occlusion(dem, num_samples=16, radius=params["radius"], pixel_size=5.0, psx=5.0, psy=-5.0)
+    elif kind == "prepare":
+        R.prepare_dem(dem, fill_mode="enclosed", coarse_max=params["coarse_max"])
     return core * core, time.perf_counter() - t0
 
 
@@ -467,6 +471,13 @@ def ambient_occlusion_section(args):
                                         "samples_per_px": 64,
                                         "gsamples_per_s": round(n * n * 64 / (field_ms * 1e-3) / 1e9, 1)}
     del dem, out
+    if not args.no_cpu_baseline:
+        procs = max(1, os.cpu_count() or 1)
+        rate = cpu_oracle_rate("ambient_occlusion", procs=procs, tiles=procs, core=1024, pad=16,
+                               params={"radius": 10.0})
+        res["cpu_baseline"] = {"value": round(rate, 2), "unit": "Mpix/s", "cores": procs, "kind": "port",
+                               "sample": f"{procs} tiles of 1056^2, oracle compute_ambient_occlusion_block "
+                                         "(radius 10), one tile per process"}
     return {"workload": f"ambient occlusion, 16 samples x 4 rings, 5 m, {n}x{n}, 4096^2 tiles", **res}
 
 
@@ -498,6 +509,13 @@ def prepare_section(args):
            "fill_kernel_roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm, "peak_source": src,
                                     "unit": "GB/s", "frac": round(gbs / hbm, 4)}}
     del dem, out
+    if not args.no_cpu_baseline:
+        procs = max(1, os.cpu_count() or 1)
+        rate = cpu_oracle_rate("prepare", procs=procs, tiles=procs, core=2048, pad=0,
+                               params={"coarse_max": 128})
+        res["cpu_baseline"] = {"value": round(rate, 2), "unit": "Mpix/s", "cores": procs, "kind": "port",
+                               "sample": f"{procs} rasters of 2048^2 (2 NaN disks each), oracle prepare "
+                                         "(coarse_max 128, the same 16x ratio), one raster per process"}
     return {"workload": f"prepare (fill_mode enclosed, coarse_max 2048), {n}x{n}", **res}
 
 
