@@ -14,7 +14,7 @@ implicit-GEMM tensor-core kernels of csrc/fsg_conv.cu (BF16 operands, FP32
 accumulation), forward and backward; PyTorch holds the tensors and runs the
 optimiser (AdamW) and the elementwise glue.
 
-The exact kernel stays the judge: ``check_and_fallback`` recomputes a sampled
+The exact kernel stays the arbiter: ``check_and_fallback`` recomputes a sampled
 block of each tile exactly and redoes the whole tile exactly when the
 surrogate's mean absolute error there exceeds the threshold (2 degrees).
 """
@@ -287,7 +287,7 @@ def load_default(device: str = "cuda") -> Optional[OpennessSurrogate]:
 def surrogate_tile_loop(dem, infos, model: OpennessSurrogate, *, pixel_size: float = 5.0, max_distance: int = 256,
                         num_directions: int = 16, threshold_deg: float = 2.0, check: int = 128,
                         out=None) -> Dict[str, object]:
-    """Mean openness angle (degrees) of every tile core from the surrogate, judged by the exact
+    """Mean openness angle (degrees) of every tile core from the surrogate, checked against the exact
     kernel: an exact check block of ``check`` x ``check`` pixels at each core's centre; a tile
     whose block MAE exceeds ``threshold_deg`` is recomputed exactly.  ``infos``: TileInfo list
     (windows with a halo >= max_distance).  Returns the plane and the per-tile report."""
