@@ -461,6 +461,9 @@ static int ao_prepare(const float* raster_dev, int64_t ld, int32_t raster_h, int
   st = device_info(&di);
   if (st) return st;
   const size_t tables = (size_t)ns * sizeof(AoSample) + (size_t)((ns + 3) & ~3) * sizeof(int);
+  if (tables > di.smem_optin)
+    return fail(FSG_ERR_UNSUPPORTED, "%d samples need %zu B of shared-memory tables (at most %zu)", ns, tables,
+                di.smem_optin);
   const int spitch = APW + 2 * reach;
   const size_t staged = tables + sizeof(float) * (size_t)spitch * (APH + 2 * reach);
   if (staged <= di.smem_optin) {
