@@ -289,10 +289,11 @@ void zoom_axis(int n, int t, int* out, double* step) {
 // io/dem_preprocess.py:241-275): keys are the float bit patterns with -0 folded
 // into +0 (np.unique merges them).  Pass 1 counts the finite, undeclared samples
 // per high 16 bits of the order-preserving key and tracks the smallest and
-// largest key; pass 2 counts every value of up to MAX_HEAVY heavy high-16 bins.
+// largest key; pass 2 counts every value of the heavy high-16 bins (those holding at
+// least the rule's fraction: at most 1 / fraction of them, MAX_HEAVY in all).
 // Equal keys of a warp are merged before their atomic (match.any), so a
 // dominant value costs one atomic per warp.
-constexpr int MAX_HEAVY = 64;
+constexpr int MAX_HEAVY = 4096;
 
 __device__ __forceinline__ unsigned order_key(float v) {
   unsigned u = __float_as_uint(v == 0.0f ? 0.0f : v);
@@ -335,7 +336,7 @@ __global__ void value_hist_k(const float* __restrict__ a, long long ld, int h, i
 
 // slot_of[bin]: the heavy slot of a high-16 bin, or -1
 __global__ void value_count_k(const float* __restrict__ a, long long ld, int h, int w,
-                             const uint8_t* __restrict__ decl, long long dld, const short* __restrict__ slot_of,
+                             const uint8_t* __restrict__ decl, long long dld, const int* __restrict__ slot_of,
                              unsigned* __restrict__ counts) {
   const long long n = (long long)h * w;
   const unsigned lane = threadIdx.x & 31;
@@ -620,12 +621,11 @@ extern "C" int fsg_value_mode(const float* sample_dev, int64_t ld, int32_t h, in
   int st = device_info(&di);
   if (st) return st;
   StreamScratch scr;
-  const size_t hist_b = 65536 * sizeof(unsigned), counts_b = (size_t)MAX_HEAVY * 65536 * sizeof(unsigned);
-  st = scr.alloc(hist_b + counts_b + 65536 * sizeof(short) + 64, s);
+  const size_t hist_b = 65536 * sizeof(unsigned);
+  st = scr.alloc(hist_b + 65536 * sizeof(int) + 64, s);
   if (st) return st;
   unsigned* hist = static_cast<unsigned*>(scr.ptr);
-  unsigned* counts = hist + 65536;
-  short* slot_of = reinterpret_cast<short*>(counts + (size_t)MAX_HEAVY * 65536);
+  int* slot_of = reinterpret_cast<int*>(hist + 65536);
   unsigned* kminmax = reinterpret_cast<unsigned*>(slot_of + 65536);
   const unsigned init[2] = {0xffffffffu, 0u};
   FSG_CUDA(cudaMemsetAsync(hist, 0, hist_b, s));
@@ -655,16 +655,20 @@ extern "C" int fsg_value_mode(const float* sample_dev, int64_t ld, int32_t h, in
   *vmin = val(mm[0]);
   *vmax = val(mm[1]);
   // a value holding at least min_fraction of the samples lies in a bin that does
-  std::vector<short> so(65536, -1);
+  std::vector<int> so(65536, -1);
   std::vector<int> heavy;
   for (int b = 0; b < 65536; ++b)
     if (hh[b] > 0 && (double)hh[b] / (double)nf >= min_fraction) {
-      if ((int)heavy.size() == MAX_HEAVY) return fail(FSG_ERR_UNSUPPORTED, "min_fraction too small");
-      so[b] = (short)heavy.size();
+      if ((int)heavy.size() == MAX_HEAVY) return fail(FSG_ERR_UNSUPPORTED, "min_fraction %g too small", min_fraction);
+      so[b] = (int)heavy.size();
       heavy.push_back(b);
     }
   if (heavy.empty()) return FSG_OK;  // no value reaches min_fraction: the mode does not matter
-  FSG_CUDA(cudaMemcpyAsync(slot_of, so.data(), 65536 * sizeof(short), cudaMemcpyHostToDevice, s));
+  StreamScratch cscr;  // exact counts of the heavy bins' values
+  st = cscr.alloc(heavy.size() * 65536 * sizeof(unsigned), s);
+  if (st) return st;
+  unsigned* counts = static_cast<unsigned*>(cscr.ptr);
+  FSG_CUDA(cudaMemcpyAsync(slot_of, so.data(), 65536 * sizeof(int), cudaMemcpyHostToDevice, s));
   FSG_CUDA(cudaMemsetAsync(counts, 0, heavy.size() * 65536 * sizeof(unsigned), s));
   value_count_k<<<grid, 256, 0, s>>>(sample_dev, ld, h, w, declared_dev, declared_ld, slot_of, counts);
   FSG_LAUNCHED(1);

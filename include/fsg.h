@@ -363,7 +363,9 @@ int fsg_coarse_average(const float* sample_dev, int64_t ld, const uint8_t* decla
  * over the finite, undeclared samples: their number, smallest and largest value,
  * and, when some value holds at least min_fraction of them, the most frequent
  * value (the smallest on ties) and its count (*mode_count = 0 otherwise).
- * -0 and +0 count as one value.  Synchronises. */
+ * -0 and +0 count as one value.  FSG_ERR_UNSUPPORTED when more than 4096
+ * 16-bit key bins reach min_fraction (min_fraction far below 1 / 4096).
+ * Synchronises. */
 int fsg_value_mode(const float* sample_dev, int64_t ld, int32_t h, int32_t w, const uint8_t* declared_dev,
                    int64_t declared_ld, double min_fraction, int64_t* n_finite, double* vmin, double* vmax,
                    double* mode_value, int64_t* mode_count, void* stream);
