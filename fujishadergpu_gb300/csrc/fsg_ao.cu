@@ -26,8 +26,9 @@
 //                    a thread evaluates two columns (x, x + 32) of four rows with
 //                    paired FP32 arithmetic.  Blocks without NoData skip the
 //                    validity bookkeeping (count = number of samples).
-//   ao_finish_kernel the separable Gaussian in float-float from a shared-memory
-//                    tile of the field, gamma, NaN, stretch and the store.
+//   ao_finish_kernel the separable Gaussian (compensated float32 dot products)
+//                    from a shared-memory tile of the field, gamma, NaN,
+//                    stretch and the store.
 // Reaches too large for shared memory read the raster directly (clamped loads).
 #include <algorithm>
 #include <cmath>
@@ -226,13 +227,30 @@ __global__ void __launch_bounds__(AX * AY) ao_field_kernel(const __grid_constant
   }
 }
 
-// scipy's symmetric 9-tap correlate1d in float-float, rounded to float32:
-// x[4] w0 + (x[0] + x[8]) w4 + ... + (x[3] + x[5]) w1.
+// scipy's symmetric 9-tap correlate1d (float64 weights and accumulator),
+// x[4] w0 + (x[0] + x[8]) w4 + ... + (x[3] + x[5]) w1, rounded to float32.
+// Compensated dot product (Ogita, Rump and Oishi's Dot2): each pair sum and
+// each product with the weight's high part is split exactly (TwoSum,
+// TwoProduct by FMA), the running sum is kept exact by TwoSum, and all
+// low-order terms (the splits' errors and the weights' low parts) collect in
+// one float32 correction; the result is as accurate as a twice-as-wide
+// accumulation rounded once.
 __device__ __forceinline__ float gsum9(const FF* w, const float* x) {
-  FF acc = ff_mul({x[4], 0.f}, w[0]);
+  float s = __fmul_rn(x[4], w[0].hi);
+  float c = __fmaf_rn(x[4], w[0].hi, -s);
+  c = __fmaf_rn(x[4], w[0].lo, c);
 #pragma unroll
-  for (int k = 4; k >= 1; --k) acc = ff_add(acc, ff_mul(two_sum(x[4 - k], x[4 + k]), w[k]));
-  return __fadd_rn(acc.hi, acc.lo);
+  for (int k = 4; k >= 1; --k) {
+    const FF p = two_sum(x[4 - k], x[4 + k]);
+    const float q = __fmul_rn(p.hi, w[k].hi);
+    float e = __fmaf_rn(p.hi, w[k].hi, -q);
+    e = __fmaf_rn(p.hi, w[k].lo, e);
+    e = __fmaf_rn(p.lo, w[k].hi, e);
+    const FF t = two_sum(s, q);
+    s = t.hi;
+    c = __fadd_rn(c, __fadd_rn(t.lo, e));
+  }
+  return __fadd_rn(s, c);
 }
 
 __global__ void __launch_bounds__(AX * AY) ao_finish_kernel(const __grid_constant__ AoArgs A) {
