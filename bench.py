@@ -159,6 +159,11 @@ def max_over_ranks(x: float, world: int) -> float:
 
 
 # ------------------------------------------------------- CPU oracle baseline
+# The CPU legs use the GPU workload's NoData law: disks of radius U(10, 200) px
+# at 122 disks per 16384^2 (~2 % of the pixels), i.e. 2 disks per 2048^2 tile.
+CPU_TILE = 2048
+CPU_NODATA = {"disks": (2, 10.0, 200.0)}
+CPU_NODATA_NOTE = "NoData: 2 disks of radius U(10,200) px per tile (the GPU workload's 122 per 16384^2)"
 def _cpu_tile_job(args):
     """One tile of the reference's CPU algorithm (oracle port), returns core pixels."""
     kind, seed, core, pad, params = args
@@ -167,7 +172,8 @@ def _cpu_tile_job(args):
     from oracle import restated as R
     n = core + 2 * pad
     dem = synth.fbm(n, n, hurst=0.7, seed=seed, lo=0.0, hi=4000.0)
-    dem[synth.nodata_disks(n, n, count=2, seed=seed + 1, rmin=10.0, rmax=60.0)] = np.nan
+    disks = params.get("disks", (2, 10.0, 60.0))  # (count, rmin, rmax) of the NoData disks
+    dem[synth.nodata_disks(n, n, count=disks[0], seed=seed + 1, rmin=disks[1], rmax=disks[2])] = np.nan
     t0 = time.perf_counter()
     if kind == "stencil":
         kw = dict(pixel_size=5.0, psx=5.0, psy=-5.0)
@@ -210,7 +216,7 @@ def stencil_workload(args, rank, world):
 
     from fujishadergpu_gb300 import _arrays, _native, synth
     from fujishadergpu_gb300.algorithms import _stencil as S
-    from oracle.restated import tile_grid
+    from fujishadergpu_gb300.core import tile_loop
 
     H = W = args.size
     tile, halo = args.tile, args.halo
@@ -224,14 +230,7 @@ def stencil_workload(args, rank, world):
     view = _arrays.as_device_f32_2d(dem)
     params = S.make_params(azimuth=315.0, altitude=45.0, pixel_size=5.0)
     planes = {S.OUTPUT_INDEX[n]: S.make_plane(outs[n]) for n in names}
-    tiles = []
-    for (ty, tx, cx, cy, cw, ch, wx, wy, ww, wh) in tile_grid(H, W, tile, halo):
-        t = _native.Tile()
-        t.win_y0, t.win_x0, t.win_h, t.win_w = wy, wx, wh, ww
-        t.core_y0, t.core_x0, t.core_h, t.core_w = cy, cx, ch, cw
-        t.out_y0, t.out_x0 = cy, cx
-        t.pixel_scale_x, t.pixel_scale_y = 5.0, -5.0
-        tiles.append(t)
+    tiles = tile_loop.make_tiles(tile_loop.tile_grid(H, W, tile, halo), pixel_scale_x=5.0, pixel_scale_y=-5.0)
     stream = torch.cuda.current_stream()
     sh = int(stream.cuda_stream)
 
@@ -692,10 +691,10 @@ def main():
     if rank == 0:
         if not args.no_cpu_baseline and world == 1:
             procs = max(1, os.cpu_count() or 1)
-            rate = cpu_oracle_rate("stencil", procs=procs, tiles=procs, core=1024, pad=8)
+            rate = cpu_oracle_rate("stencil", procs=procs, tiles=procs, core=CPU_TILE, pad=8, params=CPU_NODATA)
             line["cpu_baseline"] = {"value": round(rate, 2), "unit": "Mpix/s", "cores": procs, "kind": "port",
-                                    "sample": f"{procs} tiles of 1024^2 (+8 px halo), oracle hillshade+slope+"
-                                              "profile+planform, one tile per process"}
+                                    "sample": f"{procs} tiles of {CPU_TILE}^2 (+8 px halo), oracle hillshade+slope+"
+                                              "profile+planform, one tile per process; " + CPU_NODATA_NOTE}
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
@@ -710,11 +709,12 @@ def reference_arm(args):
     procs = max(1, os.cpu_count() or 1)
     rates = []
     for i in range(args.warmup + args.steps):
-        r = cpu_oracle_rate("stencil", procs=procs, tiles=procs, core=1024, pad=8, seed=200 + 31 * i)
+        r = cpu_oracle_rate("stencil", procs=procs, tiles=procs, core=CPU_TILE, pad=8, seed=200 + 31 * i,
+                            params=CPU_NODATA)
         if i >= args.warmup:
             rates.append(r)
     v = statistics.median(rates)
-    px_step = procs * 1024 * 1024
+    px_step = procs * CPU_TILE * CPU_TILE
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -731,9 +731,9 @@ def reference_arm(args):
         "data": "synthetic (seeded spectral fBm, Hurst 0.7, 0-4000 m, NoData disks)",
         "config": {"workload": "fused hillshade+slope(deg)+profile+planform curvature, float32 planes",
                    "raster": [args.size, args.size], "tile": args.tile, "halo": args.halo,
-                   "sample_per_step": f"{procs} tiles of 1024^2"},
+                   "sample_per_step": f"{procs} tiles of {CPU_TILE}^2"},
         "cpu_baseline": {"value": round(v, 2), "unit": "Mpix/s", "cores": procs, "kind": "port",
-                         "sample": f"{procs} tiles of 1024^2 per step, one per process"},
+                         "sample": f"{procs} tiles of {CPU_TILE}^2 per step, one per process; " + CPU_NODATA_NOTE},
         "e2e": {"value": round(v, 2), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference is CuPy-only; its CPU algorithm is timed through the NumPy/SciPy oracle port",
     }

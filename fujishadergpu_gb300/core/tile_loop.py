@@ -116,6 +116,13 @@ def make_tiles(infos: Sequence[TileInfo], *, pixel_scale_x: float, pixel_scale_y
     return tiles
 
 
+def _load_algorithm(name: str):
+    """core/tile_processor.py:807-820: a new instance of
+    ``algorithms/tile/<name>.py``'s class, ``ValueError`` for an unknown name."""
+    from ..algorithms.registry import load_algorithm
+    return load_algorithm(name)
+
+
 # --------------------------------------------------------------- global stats
 def stratified_windows(width, height, by0, by1, bx0, bx1, *, grid=3, tile=4096):
     """algorithms/_norm_stats.py:64-100: unique grid x grid windows over the valid bbox."""

@@ -347,7 +347,9 @@ std::mutex g_noalloc_mutex;
 void* g_noalloc_ptr[64] = {};
 
 // Device address of g_noalloc_scratch on the current device, looked up once per
-// device (host code only has a stand-in for the symbol, not its address).
+// device (host code only has a stand-in for the symbol, not its address).  The
+// address belongs to the device's primary context: it is not looked up again
+// after a cudaDeviceReset, which the header tells callers not to do.
 int noalloc_scratch(NoAllocScratch** out) {
   int dev = 0;
   FSG_CUDA(cudaGetDevice(&dev));

@@ -13,8 +13,6 @@ array and the file I/O is left out; (1), (3), (4) and (5) are CUDA kernels
 ``fsg_edge_connected``, ``fsg_fill_apply``); for (2) the exact value counts
 come from the device (``fsg_value_mode``, ``fsg_count_equal``) and only the
 decisions and the few thousand ring values are handled on the host.
-``detect_sentinel_nodata`` / ``detect_border_nodata`` keep the reference's
-host signatures for NumPy samples.
 """
 from __future__ import annotations
 
@@ -54,54 +52,15 @@ def coarse_oversample(ch: int, cw: int, k: int = 4, max_intermediate: int = 4096
     return k
 
 
-def detect_border_nodata(sample: np.ndarray, valid: np.ndarray, *, min_border_fraction: float = 0.5,
-                         min_total_fraction: float = 0.02) -> Optional[float]:
-    """_detect_border_nodata (:191-225): a single finite value holding at least
-    ``min_border_fraction`` of the grid's outer ring and ``min_total_fraction`` of the grid."""
-    h, w = sample.shape
-    if h < 8 or w < 8:
-        return None
-    ring = np.concatenate([sample[0, :], sample[-1, :], sample[1:-1, 0], sample[1:-1, -1]])
-    ok = np.concatenate([valid[0, :], valid[-1, :], valid[1:-1, 0], valid[1:-1, -1]])
-    ring = ring[ok & np.isfinite(ring)]
-    if ring.size == 0:
-        return None
-    vals, counts = np.unique(ring, return_counts=True)
-    i = int(np.argmax(counts))
-    cand = float(vals[i])
-    if counts[i] / ring.size < float(min_border_fraction):
-        return None
-    if float(np.mean(sample == np.float32(cand))) < float(min_total_fraction):
-        return None
-    return cand
-
-
-def detect_sentinel_nodata(sample: np.ndarray, valid: np.ndarray, *, min_fraction: float = 0.05) -> Optional[float]:
-    """_detect_sentinel_nodata (:241-275): the most frequent finite value when it holds at
-    least ``min_fraction`` of the grid and is a known fill sentinel, |v| >= 1e30 or the
-    minimum / maximum of the data."""
-    finite = sample[valid & np.isfinite(sample)]
-    if finite.size < 64:
-        return None
-    vals, counts = np.unique(finite, return_counts=True)
-    i = int(np.argmax(counts))
-    cand = float(vals[i])
-    if counts[i] / float(finite.size) < float(min_fraction):
-        return None
-    known = any(abs(cand - s) <= 1e-6 * max(1.0, abs(s)) for s in NODATA_SENTINELS)
-    if known or abs(cand) >= 1e30 or cand == float(vals[0]) or cand == float(vals[-1]):
-        return cand
-    return None
-
-
 def _known_or_extreme(cand: float, vmin: float, vmax: float) -> bool:
     known = any(abs(cand - s) <= 1e-6 * max(1.0, abs(s)) for s in NODATA_SENTINELS)
     return known or abs(cand) >= 1e30 or cand == vmin or cand == vmax
 
 
 def _sentinel_rule(sample, declared, min_fraction: float, stream) -> Optional[float]:
-    """detect_sentinel_nodata on the device sample: the value statistics come from
-    fsg_value_mode (exact counts), the decision is the reference's."""
+    """The sentinel rule of _detect_sentinel_nodata (io/dem_preprocess.py:241-275) on the
+    device sample: the value statistics come from fsg_value_mode (exact counts), the
+    decision is the reference's."""
     h, w = sample.shape
     nf, lo, hi, mv, mc = C.c_int64(), C.c_double(), C.c_double(), C.c_double(), C.c_int64()
     N.check(N.lib().fsg_value_mode(C.c_void_p(sample.data_ptr()), w, h, w, C.c_void_p(declared.data_ptr()), w,
@@ -114,8 +73,8 @@ def _sentinel_rule(sample, declared, min_fraction: float, stream) -> Optional[fl
 
 
 def _border_rule(sample, declared, min_border_fraction: float, stream, min_total_fraction: float = 0.02):
-    """detect_border_nodata with the outer ring on the host and the whole-sample count of
-    the candidate from fsg_count_equal."""
+    """The border rule of _detect_border_nodata (io/dem_preprocess.py:191-225) with the
+    outer ring on the host and the whole-sample count of the candidate from fsg_count_equal."""
     h, w = sample.shape
     if h < 8 or w < 8:
         return None
@@ -237,5 +196,4 @@ def prepare_dem(dem, *, nodata: Optional[float] = None, fill_mode: str = "enclos
                          {"coarse": coarse, "valid": valid})
 
 
-__all__ = ["prepare_dem", "PrepareResult", "FILL_MODES", "coarse_shape", "coarse_oversample",
-           "detect_border_nodata", "detect_sentinel_nodata"]
+__all__ = ["prepare_dem", "PrepareResult", "FILL_MODES", "coarse_shape", "coarse_oversample"]

@@ -253,7 +253,8 @@ int fsg_std(const float* values_dev, int64_t n, double* out, void* stream);
  * Limits: at most 16 percentiles per call (nq > 16 -> FSG_ERR_WORKSPACE); any n.
  * The first call on a device looks up the array's device address (once per
  * device, with that device current); make that first call before any stream
- * capture.  All calls share the one array: calls that overlap on the GPU (other
+ * capture.  The address stays valid for the life of the device's primary
+ * context: do not call it again after cudaDeviceReset on that device.  All calls share the one array: calls that overlap on the GPU (other
  * streams, other host threads) race and must be serialised by the caller.
  * Synchronises `stream`. */
 int fsg_percentile_noalloc(const float* values_dev, int64_t n, int32_t abs_values, const double* q, int32_t nq,

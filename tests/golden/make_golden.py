@@ -1,9 +1,9 @@
 """Generate the golden fixtures in this folder from the reference's own code.
 
-Run in a container that holds the reference sources (default
-``/root/reference``; override with ``FSG_REFERENCE_ROOT``)::
+Run in a container that holds the reference sources, naming the folder that
+contains its ``FujiShaderGPU`` package (or set ``FSG_REFERENCE_ROOT``)::
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference <reference checkout>
 
 It imports the reference's unmodified block functions through
 ``reference_shim`` (CuPy -> NumPy, cupyx.scipy.ndimage -> scipy.ndimage) and
@@ -475,6 +475,8 @@ SECTIONS = {"ambient_occlusion": lambda: main_ambient_occlusion(), "prepare": la
 
 
 if __name__ == "__main__":
+    if "--reference" in sys.argv:
+        os.environ["FSG_REFERENCE_ROOT"] = sys.argv[sys.argv.index("--reference") + 1]
     # "--section <name>" regenerates that fixture alone
     if "--section" in sys.argv:
         SECTIONS[sys.argv[sys.argv.index("--section") + 1]]()

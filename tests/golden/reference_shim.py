@@ -16,7 +16,19 @@ import types
 import numpy as np
 import scipy.ndimage as _ndi
 
-REFERENCE_ROOT = os.environ.get("FSG_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_root() -> str:
+    """The folder that holds the reference's ``FujiShaderGPU`` package, from the
+    ``FSG_REFERENCE_ROOT`` environment variable (required; ``make_golden.py``
+    sets it from its ``--reference`` argument)."""
+    root = os.environ.get("FSG_REFERENCE_ROOT")
+    if not root:
+        raise RuntimeError("set FSG_REFERENCE_ROOT (or pass --reference to make_golden.py) to the folder "
+                           "holding the reference's FujiShaderGPU package")
+    if not os.path.isdir(os.path.join(root, "FujiShaderGPU")):
+        raise RuntimeError(f"no FujiShaderGPU package under {root!r}")
+    return root
 
 
 def _install_shim() -> None:
@@ -62,8 +74,9 @@ def _install_shim() -> None:
     sys.modules["dask"] = dask
     sys.modules["dask.array"] = dask_array
 
-    if REFERENCE_ROOT not in sys.path:
-        sys.path.insert(0, REFERENCE_ROOT)
+    root = reference_root()
+    if root not in sys.path:
+        sys.path.insert(0, root)
 
 
 def load():
