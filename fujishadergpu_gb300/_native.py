@@ -79,7 +79,10 @@ class TopoUSMParams(C.Structure):
                 ("has_nodata", C.c_int32), ("pixel_size", C.c_double), ("nodata", C.c_double),
                 ("coarse_dev", C.c_void_p), ("coarse_ld", C.c_int64), ("coarse_h", C.c_int32),
                 ("coarse_w", C.c_int32), ("full_h", C.c_int64), ("full_w", C.c_int64), ("w_large", C.c_double),
-                ("scale", C.c_double)]
+                ("scale", C.c_double), ("path", C.c_int32)]
+
+
+TOPOUSM_PATHS = {"exact": 0, "tensor": 1}
 
 
 class StoreFinish(C.Structure):

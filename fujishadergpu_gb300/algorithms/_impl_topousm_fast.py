@@ -24,7 +24,12 @@ def downsample_factor(radius: float, pixel_size: float) -> int:
 
 
 def make_params(radii: Sequence[int], weights: Sequence[float], pixel_size: float, *, nodata=None,
-                coarse=None, w_large: float = 0.0, full_shape=None, scale: float = 0.0):
+                coarse=None, w_large: float = 0.0, full_shape=None, scale: float = 0.0, path: str = "exact"):
+    """``path``: arithmetic of the full-resolution box means, ``"exact"`` (64-bit
+    fixed-point sums on the CUDA cores) or ``"tensor"`` (split-BF16 banded products on
+    the tensor cores; tiles holding NoData fall back to the exact kernel)."""
+    if path not in N.TOPOUSM_PATHS:
+        raise ValueError(f"unknown topousm path {path!r}; choose from {sorted(N.TOPOUSM_PATHS)}")
     n = len(radii)
     rr = (C.c_int32 * max(1, n))(*[int(r) for r in radii])
     ww = (C.c_double * max(1, n))(*[float(w) for w in weights])
@@ -45,6 +50,7 @@ def make_params(radii: Sequence[int], weights: Sequence[float], pixel_size: floa
         p.full_h, p.full_w = int(full_shape[0]), int(full_shape[1])
         p.w_large = float(w_large)
     p.scale = float(scale)
+    p.path = N.TOPOUSM_PATHS[path]
     return p, keep
 
 
@@ -73,14 +79,14 @@ def _resolve_weights(radii, weights):
 
 
 def _raw_topousm(block, radii, weights, pixel_size, *, coarse=None, w_large=0.0, offset=(0, 0),
-                 full_shape=None, scale=0.0, out_dtype="float32", qp=None):
+                 full_shape=None, scale=0.0, out_dtype="float32", qp=None, path="exact"):
     from ._stencil import make_plane
     v = _arrays.as_device_f32_2d(block)
     out = _arrays.empty(v.h, v.w, out_dtype, device=v.tensor.device)
     if v.h * v.w == 0:
         return out, v
     params, keep = make_params(radii, weights, pixel_size, coarse=coarse, w_large=w_large,
-                               full_shape=full_shape, scale=scale)
+                               full_shape=full_shape, scale=scale, path=path)
     t = _window_tile(v.h, v.w)
     if coarse is not None:
         # Global origin of the window: fsg_topousm takes it from win_y0/win_x0,
@@ -111,14 +117,16 @@ def _raw_with_offset(v, params, keep, offset, full_shape, out, out_dtype, qp):
 
 
 def compute_topousm_fast_efficient_block(block, *, radii: Optional[List[int]] = None,
-                                         weights: Optional[List[float]] = None, pixel_size: float = 1.0):
+                                         weights: Optional[List[float]] = None, pixel_size: float = 1.0,
+                                         path: str = "exact"):
     """Raw multiscale unsharp mask sum_i w_i (z - mean_{r_i}(z)) of one window
-    (_impl_topousm_fast.py:49-100)."""
+    (_impl_topousm_fast.py:49-100).  ``path`` (not in the reference): ``"exact"`` or
+    ``"tensor"``, the arithmetic of the full-resolution box means (see make_params)."""
     if radii is None:
         radii = [4, 16, 64]
     radii = [int(r) for r in radii]
     weights = _resolve_weights(radii, weights)
-    out, v = _raw_topousm(block, radii, weights, pixel_size)
+    out, v = _raw_topousm(block, radii, weights, pixel_size, path=path)
     return _arrays.wrap_result(out, v.origin)
 
 

@@ -357,7 +357,8 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
         scale = float(stats[0]) if stats else 0.0
         tp, keep = TU.make_params(params["radii"], params["weights"] or [], px, nodata=nodata,
                                   coarse=params.get("_topousm_fast_coarse_field"),
-                                  w_large=params.get("_topousm_fast_w_large", 0.0), full_shape=(H, W), scale=scale)
+                                  w_large=params.get("_topousm_fast_w_large", 0.0), full_shape=(H, W), scale=scale,
+                                  path=params.get("topousm_path", "exact"))
         TU.run_topousm(v, tiles, tp, S.make_plane(out, output_dtype, qp))
     elif algorithm == "ambient_occlusion":
         stats = params.get("global_stats")

@@ -54,6 +54,9 @@ struct DeviceInfo {
 // Properties of the current device (cached per device).
 int device_info(DeviceInfo* out);
 
+// Reads and clears the tensor-core topousm kernel's error word (fsg_topousm_tc.cu).
+int tc_take_errors(unsigned* flags);
+
 // Checks a tile list against a raster (windows inside, cores inside windows,
 // windows at least `min_window` px on each axis).
 int validate_tiles(int32_t raster_h, int32_t raster_w, const fsg_tile* tiles, int32_t ntiles,

@@ -934,6 +934,11 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
     auto dv = [](f2 num, Step a) { return DIV ? div_by2(num, a.d2, a.rcp) : mul2(num, S2(a.rcp)); };
     auto dv4 = [&](Q4 num, Step a) { return Q4{dv(num.lo, a), dv(num.hi, a)}; };
     auto dv1 = [](float num, Step a) { return DIV ? div_by(num, a.d2, a.rcp) : __fmul_rn(num, a.rcp); };
+    // First derivatives that feed the second ones are always correctly rounded: the
+    // second differences of np.gradient's float32 first derivatives amplify a one-ulp
+    // difference in them (by ~|dx| / |dxx step|, up to ~1e3 on smooth terrain).
+    auto dv4e = [](Q4 num, Step a) { return Q4{div_by2(num.lo, a.d2, a.rcp), div_by2(num.hi, a.d2, a.rcp)}; };
+    auto dv1e = [](float num, Step a) { return div_by(num, a.d2, a.rcp); };
     // horizontal central difference of a row: neighbours from the adjacent lanes or the edge pair
     auto hdiff = [&](Q4 f, f2 e) {
       float left = __shfl_up_sync(0xffffffffu, f.hi.y, 1), right = __shfl_down_sync(0xffffffffu, f.lo.x, 1);
@@ -970,12 +975,12 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
     Q4 dxm1{}, dym1{}, dx0{}, dy0{};
     float xd0 = 0.f, yd0 = 0.f;  // edge-lane dx / dy of row 0 (outside column)
     if (CURV) {
-      dxm1 = dv4(hdiff(fm1, em1), T.g1x);
-      dym1 = dv4(q4sub(f0, fm2), T.g1y);
-      dx0 = dv4(hdiff(f0, e0), T.g1x);
-      dy0 = dv4(q4sub(fp1, fm1), T.g1y);
-      xd0 = dv1(edge_dx(f0, e0), T.g1x);
-      yd0 = dv1(__fsub_rn(e31lane ? ep1.x : ep1.y, e31lane ? em1.x : em1.y), T.g1y);
+      dxm1 = dv4e(hdiff(fm1, em1), T.g1x);
+      dym1 = dv4e(q4sub(f0, fm2), T.g1y);
+      dx0 = dv4e(hdiff(f0, e0), T.g1x);
+      dy0 = dv4e(q4sub(fp1, fm1), T.g1y);
+      xd0 = dv1e(edge_dx(f0, e0), T.g1x);
+      yd0 = dv1e(__fsub_rn(e31lane ? ep1.x : ep1.y, e31lane ? em1.x : em1.y), T.g1y);
     }
     bool bad = false;
 #pragma unroll ROW_UNROLL
@@ -985,10 +990,10 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
       Q4 p, q, dxx{}, dxy{}, dyy{}, dyx{}, dxp1{}, dyp1{};
       float xp1 = 0.f, yp1 = 0.f;
       if (CURV) {
-        dxp1 = dv4(hdiff(fp1, ep1), T.g1x);
-        dyp1 = dv4(q4sub(fp2, f0), T.g1y);
-        xp1 = dv1(edge_dx(fp1, ep1), T.g1x);
-        yp1 = dv1(__fsub_rn(e31lane ? ep2.x : ep2.y, e31lane ? e0.x : e0.y), T.g1y);
+        dxp1 = dv4e(hdiff(fp1, ep1), T.g1x);
+        dyp1 = dv4e(q4sub(fp2, f0), T.g1y);
+        xp1 = dv1e(edge_dx(fp1, ep1), T.g1x);
+        yp1 = dv1e(__fsub_rn(e31lane ? ep2.x : ep2.y, e31lane ? e0.x : e0.y), T.g1y);
         p = dx0;
         q = dy0;
         dxx = dv4(hdiff(dx0, P2(xd0, xd0)), T.c2x);
@@ -1289,8 +1294,9 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
         if (!edge && !(((AF[r + 1] | AF[r + 2] | AF[r + 3]) >> (c + 1)) & 7ull)) continue;
         float dx = qnan, dy = qnan;
         if (gy >= T.wy0 && gy < T.wy1 && gx >= T.wx0 && gx < T.wx1) {
-          dx = deriv_d<DIV>(T.g1x, gx, T.wx0, T.wx1, [&](int k) { return fe(gy, gx + k); });
-          dy = deriv_d<DIV>(T.g1y, gy, T.wy0, T.wy1, [&](int k) { return fe(gy + k, gx); });
+          // correctly rounded: the second differences amplify their last bit (as in the fast pass)
+          dx = deriv_d<true>(T.g1x, gx, T.wx0, T.wx1, [&](int k) { return fe(gy, gx + k); });
+          dy = deriv_d<true>(T.g1y, gy, T.wy0, T.wy1, [&](int k) { return fe(gy + k, gx); });
         }
         DX[i] = dx;
         DY[i] = dy;
@@ -2001,6 +2007,9 @@ extern "C" int fsg_kernel_errors(uint32_t* flags) {
   FSG_CUDA(cudaMemcpyFromSymbol(&v, g_kernel_errors, sizeof(v)));
   const unsigned zero = 0;
   FSG_CUDA(cudaMemcpyToSymbol(g_kernel_errors, &zero, sizeof(zero)));
-  *flags = v;
+  unsigned t = 0;
+  const int st = tc_take_errors(&t);
+  if (st) return st;
+  *flags = v | t;
   return FSG_OK;
 }

@@ -24,7 +24,7 @@
 #include <mutex>
 #include <vector>
 
-#include "fsg_filters.cuh"
+#include "fsg_topousm.cuh"
 
 namespace fsg {
 namespace {
@@ -399,54 +399,10 @@ __global__ void overview_kernel(ZView z, AView out) {
 // reflected columns).  The epilogue adds the decimated radii (bilinear zoom of
 // their coarse means, as accum_upsample), the large-radius field, the scale and
 // the encoding, and stores each output pixel once.
-constexpr int ST_NT = 256, ST_G = 8, ST_SEG = 8, ST_MAXR = 64, ST_MAXN = 6, ST_MAXD = 4;
 // shared-memory row of ST_NT buffer columns; column c lives at c + c / 8 so
 // that threads walking 8-column segments hit distinct banks
 constexpr int ST_ROW = ST_NT + ST_NT / 8;
 __device__ __forceinline__ int sidx(int c) { return c + (c >> 3); }
-
-struct DecK {       // one decimated radius of a tile
-  const float* ms;  // its coarse mean (ROW_MEAN output), row pitch w
-  int h, w;
-  double zy, zx;    // corner-aligned zoom factors (in - 1) / (out - 1)
-  float weight;
-};
-
-struct TopoTileK {
-  ZView z;                 // the window
-  int cy0, cx0, ch, cw;    // core, window coordinates
-  int gy0, gx0;            // global coordinates of the window origin
-  char* out;               // output plane at the core origin
-  const int* nan_flag;     // NoData anywhere in the window
-  DecK dec[ST_MAXD];
-  int ndec;
-};
-
-struct StripItem {
-  int tile, x0, y0, y1;    // output columns [x0, x0 + TW) (window), rows [y0, y1)
-};
-
-struct StripArgs {
-  const TopoTileK* tiles;
-  const StripItem* items;
-  int nitems;
-  int nr, R, TW;
-  int radii[ST_MAXN];
-  float weights[ST_MAXN];
-  float fn[ST_MAXN], rn[ST_MAXN];  // box size 2r+1 and RN(1/(2r+1))
-  const float* field;      // large-radius field (nullable)
-  long long fld;
-  int fh, fw;
-  float sy, sx, w_large, scale;
-  float rscale;            // RN(1 / scale)
-  long long old;
-  int dtype;
-  float qa, qb;
-  int qmin, qmax;
-  int have_small;
-  int ring;                // topousm_fixed: rows of the prefix ring (2R + 2G + 1)
-  const unsigned* zmax;    // topousm_fixed: max |z| over the windows (float bits)
-};
 
 __device__ __forceinline__ float field_at(const StripArgs& A, int gy, int gx) {
   // _nan_utils.py:276-281: coords in float32, map_coordinates order 1, 'nearest' (as field_sample).
@@ -802,7 +758,8 @@ __global__ void __launch_bounds__(FX_NT, 1) topousm_fixed(const __grid_constant_
     rn2[q] = 1.0f / n2f[q];
     wq[q] = A.weights[q];
   }
-  for (int it = blockIdx.x; it < A.nitems; it += gridDim.x) {
+  const int nitems = A.nitems_dev ? *A.nitems_dev : A.nitems;  // device-built list: tensor-path fix-up
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const StripItem I = A.items[it];
     __syncthreads();
     for (int q = tid; q < (int)(sizeof(TopoTileK) / 4); q += FX_NT)
@@ -1093,7 +1050,8 @@ __global__ void __launch_bounds__(HNT, MINB) topousm_hybrid(const __grid_constan
     wq[q] = A.weights[q];
   }
   const int Rs = A.radii[NS - 1];
-  for (int it = blockIdx.x; it < A.nitems; it += gridDim.x) {
+  const int nitems = A.nitems_dev ? *A.nitems_dev : A.nitems;  // device-built list: tensor-path fix-up
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const StripItem I = A.items[it];
     __syncthreads();
     for (int q = tid; q < (int)(sizeof(TopoTileK) / 4); q += HNT)
@@ -1669,7 +1627,19 @@ static int decimated_mean_dev(const ZView& z, int r, int f, TopoScratch& S, cons
 // enqueue() issues only launches, memsets and event fork/join of the
 // per-window decimation pipelines on the auxiliary streams (capturable).
 struct TopoJob {
+  TopoJob() = default;
+  TopoJob(const TopoJob&) = delete;
+  TopoJob& operator=(const TopoJob&) = delete;
+  ~TopoJob() {
+    if (TA) tc_release(TA);
+  }
   bool empty = true, fixed = false;
+  // tensor-core path (fsg_topousm_tc.cu): its CTA tiles, the device-built list of
+  // tiles with NoData that the exact kernel (kern) then computes, and its count
+  bool tc = false;
+  TcArgs* TA = nullptr;
+  size_t tc_smem = 0, tci_off = 0, fix_off = 0, fixc_off = 0;
+  std::vector<int4> tc_it;
   int ntiles = 0, nfull = 0, NS = 0, maxh = 1, maxw = 1, grid = 0;
   std::vector<TopoTileK> tk;
   std::vector<StripItem> items;
@@ -1710,12 +1680,21 @@ struct TopoJob {
     A.tiles = reinterpret_cast<const TopoTileK*>(base + tiles_off);
     A.items = reinterpret_cast<const StripItem*>(base + items_off);
     A.zmax = reinterpret_cast<const unsigned*>(flags + ntiles);
+    if (tc) {
+      StripItem* fix = reinterpret_cast<StripItem*>(base + fix_off);
+      int* fixc = reinterpret_cast<int*>(base + fixc_off);
+      A.items = fix;
+      A.nitems_dev = fixc;
+      tc_bind(TA, A.tiles, reinterpret_cast<const int4*>(base + tci_off), (int)tc_it.size(), fix, fixc,
+              reinterpret_cast<unsigned*>(flags + ntiles));
+    }
   }
   int upload(cudaStream_t s) const {
     if (!g1.empty()) FSG_CUDA(cudaMemcpyAsync(base + g1_off, g1.data(), g1.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     if (!gv.empty()) FSG_CUDA(cudaMemcpyAsync(base + gv_off, gv.data(), gv.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     FSG_CUDA(cudaMemcpyAsync(base + tiles_off, tk.data(), sizeof(TopoTileK) * ntiles, cudaMemcpyHostToDevice, s));
     FSG_CUDA(cudaMemcpyAsync(base + items_off, items.data(), sizeof(StripItem) * items.size(), cudaMemcpyHostToDevice, s));
+    if (tc) FSG_CUDA(cudaMemcpyAsync(base + tci_off, tc_it.data(), sizeof(int4) * tc_it.size(), cudaMemcpyHostToDevice, s));
     return FSG_OK;
   }
 
@@ -1742,6 +1721,24 @@ struct TopoJob {
     int* flags = reinterpret_cast<int*>(base + flags_off);
     const TopoTileK* tiles_dev = reinterpret_cast<const TopoTileK*>(base + tiles_off);
     FSG_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (ntiles + 1), s));
+    if (tc) {
+      FSG_CUDA(cudaMemsetAsync(base + fixc_off, 0, sizeof(int), s));
+      // The tensor kernel records max |z| of every input region it stages; with a
+      // largest radius of 32 those regions are exactly what the exact kernel's strips
+      // of the listed tiles read, otherwise the strips reach further and the windows
+      // are scanned first.
+      if (A.R != 32) {
+        window_absmax<<<dim3(128, ntiles), 256, 0, s>>>(tiles_dev, reinterpret_cast<unsigned*>(flags + ntiles));
+        FSG_LAUNCHED(1);
+      }
+      timing_mark(s, true);
+      int st2 = tc_launch(TA, tc_smem, s);
+      timing_mark(s, false);
+      if (st2) return st2;
+      kern<<<grid, threads ? threads : FX_NT, smem, s>>>(A);  // the listed tiles, exact NaN-aware means
+      FSG_LAUNCHED(1);
+      return FSG_OK;
+    }
     if (fixed) window_absmax<<<dim3(128, ntiles), 256, 0, s>>>(tiles_dev, reinterpret_cast<unsigned*>(flags + ntiles));
     else window_nan_flags<<<dim3(256, ntiles), 256, 0, s>>>(tiles_dev, flags);
     FSG_LAUNCHED(1);
@@ -1753,8 +1750,8 @@ struct TopoJob {
   }
 };
 
-static int topousm_strip_prepare(const float* raster_dev, int64_t ld, const fsg_tile* tiles, int32_t ntiles,
-                                 const fsg_topousm_params* p, const fsg_plane* out, int nfull, TopoJob& J) {
+static int topousm_strip_prepare_exact(const float* raster_dev, int64_t ld, const fsg_tile* tiles, int32_t ntiles,
+                                       const fsg_topousm_params* p, const fsg_plane* out, int nfull, TopoJob& J) {
   const std::vector<int> radii(p->radii, p->radii + p->nradii);
   J.ntiles = ntiles;
   J.nfull = nfull;
@@ -1931,6 +1928,32 @@ static int topousm_strip_prepare(const float* raster_dev, int64_t ld, const fsg_
   int per_sm = 0;
   FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, J.kern, ST_NT, J.smem));
   J.grid = std::min((int)J.items.size(), di.sms * std::max(1, per_sm));
+  return FSG_OK;
+}
+
+// The tensor-core path over the same job: its CTA tiles and the fix-up list
+// after the exact job's device tables; the exact kernel (already chosen: the
+// fixed-point hybrid or single-ring kernel) takes the listed tiles.
+static int topousm_tc_setup(TopoJob& J, int nfull) {
+  tc_items(J.tk.data(), J.ntiles, &J.tc_it);
+  if (J.tc_it.empty()) return FSG_OK;
+  const size_t n = J.tc_it.size();
+  auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  J.tci_off = al(J.total);
+  J.fix_off = J.tci_off + al(sizeof(int4) * n);
+  J.fixc_off = J.fix_off + al(sizeof(StripItem) * n);
+  J.total = J.fixc_off + 256;
+  int st = tc_prepare(&J.TA, J.A, nfull, &J.tc_smem);
+  if (st) return st;
+  J.tc = true;
+  return FSG_OK;
+}
+
+static int topousm_strip_prepare(const float* raster_dev, int64_t ld, const fsg_tile* tiles, int32_t ntiles,
+                                 const fsg_topousm_params* p, const fsg_plane* out, int nfull, TopoJob& J) {
+  int st = topousm_strip_prepare_exact(raster_dev, ld, tiles, ntiles, p, out, nfull, J);
+  if (st || J.empty) return st;
+  if (p->path == FSG_TOPOUSM_TENSOR && J.fixed && tc_supported(J.A.radii, nfull)) return topousm_tc_setup(J, nfull);
   return FSG_OK;
 }
 

@@ -100,7 +100,9 @@ int fsg_timing_begin(int32_t max_launches);
 int fsg_timing_end(double* total_ms, int32_t* launches);
 /* Device-side failures since the last call, cleared on read (synchronises): bit 0 = the
  * fused stencil's streaming pass gave up waiting for a tensor-memory copy (its outputs
- * are then incomplete).  No reference counterpart. */
+ * are then incomplete); bit 1 = the tensor-core topousm_fast kernel gave up waiting on
+ * one of its pipeline barriers (its tiles are then incomplete).  No reference
+ * counterpart. */
 int fsg_kernel_errors(uint32_t* flags);
 
 /* NoData mask (core/tile_processor.py:185-196): mask_dev[i] = 1 where
@@ -184,7 +186,16 @@ typedef struct fsg_topousm_params {
   double w_large;
   /* p99(|raw|) divisor (_normalization.py:35-41); 0 = write the raw sum. */
   double scale;
+  /* Arithmetic of the full-resolution box means (no reference counterpart):
+   * FSG_TOPOUSM_EXACT = 64-bit fixed-point running sums on the CUDA cores;
+   * FSG_TOPOUSM_TENSOR = banded Toeplitz products on the tcgen05 tensor cores in
+   * split BF16 (three terms per FP32 operand, FP32 accumulation) for windows
+   * without NoData, the exact kernel for tiles that hold NoData.  The tensor path
+   * applies to at most 4 full-resolution radii, each 2..32 (else: exact). */
+  int32_t path;
 } fsg_topousm_params;
+
+enum fsg_topousm_path { FSG_TOPOUSM_EXACT = 0, FSG_TOPOUSM_TENSOR = 1 };
 
 /* topousm_fast over a list of tiles; writes each core into `out` (float32 or
  * int16/uint8 codes).  Replaces, per tile, dask_bridge._direct_topousm_fast

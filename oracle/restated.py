@@ -625,15 +625,20 @@ def openness_offsets(num_directions, max_distance):
 
 
 def openness(block, *, openness_type="positive", num_directions=16, max_distance=50,
-             pixel_size=1.0, psx=None, psy=None, raw_degrees=False, offsets=None):
+             pixel_size=1.0, psx=None, psy=None, raw_degrees=False, offsets=None, rows=None):
     """_impl_openness.py:31-132 (compute_openness_vectorized).
 
     ``raw_degrees=True`` returns the directional mean angle in degrees before the
     /(pi/2), clip and gamma display mapping (the quantity the 0.01 degree
     parity gate is stated on).  ``offsets`` (per direction, a list of (dx, dy))
     replaces the reference's 10 sampled distances, e.g. with every step of the
-    ray for the dense ray-march.
+    ray for the dense ray-march.  ``rows=(y0, y1)`` returns only those output
+    rows (the samples still come from the whole block), the same values as
+    rows y0..y1 of the full result.
     """
+    full = block
+    y0, y1 = (0, block.shape[0]) if rows is None else (int(rows[0]), int(rows[1]))
+    block = full[y0:y1]
     h, w = block.shape
     nan = np.isnan(block)
     positive = openness_type == "positive"
@@ -649,16 +654,17 @@ def openness(block, *, openness_type="positive", num_directions=16, max_distance
     D = max([max(abs(ox), abs(oy)) for ray in offsets for ox, oy in ray] or [0])
     zero = block.dtype.type(0)
     if D > 0:
-        pad = np.pad(np.where(nan, 0.0, block), D, mode="edge")
-        pad_valid = np.pad(~nan, D, mode="constant", constant_values=False)
+        fnan = np.isnan(full)
+        pad = np.pad(np.where(fnan, 0.0, full), D, mode="edge")
+        pad_valid = np.pad(~fnan, D, mode="constant", constant_values=False)
     angle_sum = np.zeros((h, w), dtype=block.dtype)
     count = np.zeros((h, w), dtype=block.dtype)
     for ray in offsets:
         ext = np.full((h, w), init, dtype=block.dtype)
         any_valid = np.zeros((h, w), dtype=bool)
         for ox, oy in ray:
-            shifted = pad[D + oy:D + oy + h, D + ox:D + ox + w]
-            sv = pad_valid[D + oy:D + oy + h, D + ox:D + ox + w]
+            shifted = pad[D + y0 + oy:D + y0 + oy + h, D + ox:D + ox + w]
+            sv = pad_valid[D + y0 + oy:D + y0 + oy + h, D + ox:D + ox + w]
             dist = max(float(np.hypot(float(ox) * sx, float(oy) * sy)), 1e-9)
             ang = np.arctan((shifted - block) / dist)
             valid = sv & ~nan

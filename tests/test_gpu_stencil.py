@@ -134,16 +134,12 @@ def test_nodata_sentinel_is_masked(fsg):
 
 
 def _tile_descs(H, W, tile, pad, psx, psy):
-    from fujishadergpu_gb300._native import Tile
-    out = []
-    for (ty, tx, cx, cy, cw, ch, wx, wy, ww, wh) in R.tile_grid(H, W, tile, pad):
-        t = Tile()
-        t.win_y0, t.win_x0, t.win_h, t.win_w = wy, wx, wh, ww
-        t.core_y0, t.core_x0, t.core_h, t.core_w = cy, cx, ch, cw
-        t.out_y0, t.out_x0 = cy, cx
-        t.pixel_scale_x, t.pixel_scale_y = psx, psy
-        out.append(t)
-    return out
+    """The product's tile descriptors (core.tile_loop), checked against the oracle's grid."""
+    from fujishadergpu_gb300.core import tile_loop
+    infos = tile_loop.tile_grid(H, W, tile, pad)
+    assert [(i.ty, i.tx, i.core_x, i.core_y, i.core_w, i.core_h, i.win_x, i.win_y, i.win_w, i.win_h)
+            for i in infos] == [tuple(t) for t in R.tile_grid(H, W, tile, pad)]
+    return tile_loop.make_tiles(infos, pixel_scale_x=psx, pixel_scale_y=psy)
 
 
 @pytest.mark.parametrize("tile,pad", [(128, 8), (100, 2), (256, 64)])
