@@ -363,12 +363,33 @@ def _time_ms(fn, steps, warmup, stream):
     return e0.elapsed_time(e1) / steps
 
 
+def tc_issued_flops(radii_full, n_tiles):
+    """Tensor FLOPs the tcgen05 topousm kernel issues: per 128 x 192 CTA tile and
+    full-resolution radius r, pass 1 = two column halves x the K steps (16 input rows)
+    the band reaches x 3 digit MMAs of 128 x 128 x 16; pass 2 = the K steps (16 input
+    columns) x 3 split MMAs of 128 x 192 x 16 (the K-step ranges of fsg_topousm_tc.cu)."""
+    def ceil_div(a, b):
+        return -((-a) // b)
+    per = 0
+    for r in radii_full:
+        j1lo, j1hi = max(0, ceil_div(17 - r, 16)), min(11, (159 + r) // 16)
+        j2lo, j2hi = max(0, ceil_div(17 - r, 16)), min(15, (223 + r) // 16)
+        per += 2 * (j1hi - j1lo + 1) * 3 * 2 * 128 * 128 * 16
+        per += (j2hi - j2lo + 1) * 3 * 2 * 128 * 192 * 16
+    return per * n_tiles
+
+
 def topousm_section(args):
     """topousm_fast on a 32768^2 fBm+ridged DEM (Hurst 0.8, 0-3500 m, 10 m), radii 2..2048 with
     2^n weights, 4096^2 tiles.  One step = the whole tile loop with the global scale known: NaN-aware
-    overview + large-radius coarse field + every tile's small-radius pass and normalisation."""
+    overview + large-radius coarse field + every tile's small-radius pass and normalisation.
+    Both arithmetic paths of the full-resolution box means are timed: "exact" (64-bit fixed-point
+    running sums on the CUDA cores) and "tensor" (split-BF16 banded products on tcgen05), each
+    with its error against the float64 oracle on one 4096^2 tile window."""
+    import numpy as np
     import torch
-    from fujishadergpu_gb300 import synth
+    from fujishadergpu_gb300 import _native, synth
+    from fujishadergpu_gb300.algorithms import _impl_topousm_fast as TU
     from fujishadergpu_gb300.core import tile_loop
     n = args.topousm_size
     dem = synth.fbm_ridged_device(n, n, hurst=0.8, seed_fbm=3, seed_ridged=4, lo=0.0, hi=3500.0)
@@ -381,27 +402,71 @@ def topousm_section(args):
     res = tile_loop.process_dem_array(dem, "topousm_fast", **kw)
     torch.cuda.synchronize()
     first_s = time.perf_counter() - t0
-    stats = res.stats
+    stats, pad = res.stats, res.padding
     del res
     stream = torch.cuda.current_stream()
-    from fujishadergpu_gb300 import _native
-    with _native.kernel_timer(max_launches=args.extra_steps + 2) as kt:
-        ms = _time_ms(lambda: tile_loop.process_dem_array(dem, "topousm_fast", global_stats=stats, **kw),
-                      args.extra_steps, 2, stream)
     px = n * n
     hbm, _, _ = peaks()
-    kms = kt.ms / max(1, kt.launches)
-    gbs = 8.0 * px / (ms * 1e-3) / 1e9
-    kgbs = 8.0 * px / (kms * 1e-3) / 1e9
+    pk = {}
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+    except OSError:
+        pass
+    bf16 = float(pk.get("bf16_tflops", 1900.0))
+    # CTA tiles of the tensor kernel: 128 x 192 over every 4096^2 core
+    ntile_rows = -(-min(4096, n) // 128)
+    ntile_cols = -(-min(4096, n) // 192)
+    n_cta = (-(-n // 4096)) ** 2 * ntile_rows * ntile_cols
+    small = [r for r in radii if r <= max(256, 4096 // 16)]
+    full_res = [r for r in small if TU.downsample_factor(r, 10.0) == 1]
+    out = {"workload": f"topousm_fast {n}x{n} fBm+ridged, radii {radii}, 2^n weights, 10 m, 4096^2 tiles",
+           "first_call_s_incl_stats_prepass": round(first_s, 3),
+           "p99_scale": float(stats[0]) if stats else None, "dtype": "f32"}
+    for path in ("exact", "tensor"):
+        with _native.kernel_timer(max_launches=args.extra_steps + 2) as kt:
+            ms = _time_ms(lambda: tile_loop.process_dem_array(dem, "topousm_fast", global_stats=stats,
+                                                              topousm_path=path, **kw),
+                          args.extra_steps, 2, stream)
+        kms = kt.ms / max(1, kt.launches)
+        gbs = 8.0 * px / (ms * 1e-3) / 1e9
+        kgbs = 8.0 * px / (kms * 1e-3) / 1e9
+        sec = {"value": round(px / (ms * 1e-3) / 1e6, 1), "unit": "Mpix/s", "ms_per_step": round(ms, 3),
+               "roofline": {"bound": "hbm", "achieved": round(kgbs, 1), "peak": hbm, "unit": "GB/s",
+                            "frac": round(kgbs / hbm, 4), "algorithmic_bytes_per_px": 8,
+                            "kernel": ("topousm_hybrid (exact fixed-point full-resolution radii + epilogue)"
+                                       if path == "exact" else
+                                       "topousm_tc (tcgen05 split-BF16 banded box means + epilogue)"),
+                            "kernel_ms": round(kms, 3), "step_achieved": round(gbs, 1),
+                            "step_frac": round(gbs / hbm, 4)}}
+        if path == "tensor":
+            fl = tc_issued_flops(full_res, n_cta)
+            tf = fl / (kms * 1e-3) / 1e12
+            sec["tensor_roofline"] = {"bound": "tensor", "issued_tflop_per_launch": round(fl / 1e12, 3),
+                                      "achieved": round(tf, 1), "peak": bf16, "unit": "TFLOP/s",
+                                      "frac": round(tf / bf16, 4), "peak_kind": "measured bf16 (burst)",
+                                      "cta_tiles": n_cta}
+        out[path] = sec
+    out["tensor_speedup_kernel"] = round(out["exact"]["roofline"]["kernel_ms"] /
+                                         max(1e-9, out["tensor"]["roofline"]["kernel_ms"]), 3)
+    out["tensor_speedup_step"] = round(out["exact"]["ms_per_step"] / max(1e-9, out["tensor"]["ms_per_step"]), 3)
+    # error against float64: the per-tile radii of one interior tile window, both paths
+    if not getattr(args, "no_fp64_check", False):
+        from oracle import restated as R
+        t = tile_loop.tile_grid(n, n, 4096, pad)[min(len(tile_loop.tile_grid(n, n, 4096, pad)) - 1, 9)]
+        win = dem[t.win_y:t.win_y + t.win_h, t.win_x:t.win_x + t.win_w].contiguous()
+        sw = [w[radii.index(r)] for r in small]
+        ref64 = R.topousm_block(win.cpu().numpy().astype(np.float64), radii=small, weights=sw, pixel_size=10.0)
+        sc = R.topousm_scale(ref64)[0]
+        for path in ("exact", "tensor"):
+            g = TU.compute_topousm_fast_efficient_block(win, radii=small, weights=sw, pixel_size=10.0,
+                                                        path=path).cpu().numpy().astype(np.float64)
+            e = float(np.nanmax(np.abs(g - ref64)))
+            out[path]["fp64_error"] = {"max_abs_m": e, "rel_to_p99": e / sc,
+                                       "window": [t.win_y, t.win_x, t.win_h, t.win_w],
+                                       "radii": small, "p99_m": sc}
     del dem
-    return {"workload": f"topousm_fast {n}x{n} fBm+ridged, radii {radii}, 2^n weights, 10 m, 4096^2 tiles",
-            "value": round(px / (ms * 1e-3) / 1e6, 1), "unit": "Mpix/s", "ms_per_step": round(ms, 3),
-            "roofline": {"bound": "hbm", "achieved": round(kgbs, 1), "peak": hbm, "unit": "GB/s",
-                         "frac": round(kgbs / hbm, 4), "algorithmic_bytes_per_px": 8,
-                         "kernel": "topousm_fixed (full-resolution radii + epilogue)", "kernel_ms": round(kms, 3),
-                         "step_achieved": round(gbs, 1), "step_frac": round(gbs / hbm, 4)},
-            "first_call_s_incl_stats_prepass": round(first_s, 3),
-            "p99_scale": float(stats[0]) if stats else None, "dtype": "f32"}
+    return out
 
 
 def openness_section(args):
@@ -651,6 +716,8 @@ def main():
     ap.add_argument("--halo", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the topousm / openness sections")
+    ap.add_argument("--no-fp64-check", action="store_true",
+                    help="skip the float64 error statement of the topousm section (host oracle on one tile)")
     ap.add_argument("--topousm-size", type=int, default=32768)
     ap.add_argument("--openness-size", type=int, default=16384)
     ap.add_argument("--spatial-size", type=int, default=8192)

@@ -230,22 +230,23 @@ __device__ __forceinline__ void pixel_products(const Light& L, float sign_x, flo
   }
   if (om & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) | (1u << FSG_OUT_CURV_PLANFORM) |
             (1u << FSG_OUT_CURV_PROFILE))) {
-    float p2 = p * p, q2 = q * q, pq = p * q;
-    float g2 = p2 + q2, one_g2 = 1.0f + g2;
+    float p2 = fmul(p, p), q2 = fmul(q, q), tpq = fmul(fmul(2.0f, p), q);
+    float g2 = fadd(p2, q2), one_g2 = fadd(1.0f, g2);
     float s15 = one_g2 * sqrt_approx(one_g2);  // (1 + p^2 + q^2)^1.5
+    // numerators in NumPy's float32 order, every operation rounded (their terms cancel)
     if (om & (1u << FSG_OUT_CURV_MEAN)) {
-      float s = (dxy + dyx) * 0.5f;
-      float num = (1.0f + q2) * dxx - 2.0f * pq * s + (1.0f + p2) * dyy;
+      float s = fmul(fadd(dxy, dyx), 0.5f);
+      float num = fadd(fsub(fmul(fadd(1.0f, q2), dxx), fmul(tpq, s)), fmul(fadd(1.0f, p2), dyy));
       o[FSG_OUT_CURV_MEAN] = gamma_display(-num * rcp_approx(2.0f * s15 + 1e-10f));
     }
     if (om & (1u << FSG_OUT_CURV_GAUSSIAN))
-      o[FSG_OUT_CURV_GAUSSIAN] = gamma_display((dxx * dyy - dxy * dxy) * rcp_approx(one_g2 * one_g2));
+      o[FSG_OUT_CURV_GAUSSIAN] = gamma_display(fsub(fmul(dxx, dyy), fmul(dxy, dxy)) * rcp_approx(one_g2 * one_g2));
     if (om & (1u << FSG_OUT_CURV_PLANFORM)) {
-      float num = q2 * dxx - 2.0f * pq * dxy + p2 * dyy;
+      float num = fadd(fsub(fmul(q2, dxx), fmul(tpq, dxy)), fmul(p2, dyy));
       o[FSG_OUT_CURV_PLANFORM] = gamma_display(-num * rcp_approx(g2 * sqrt_approx(g2) + 1e-10f));
     }
     if (om & (1u << FSG_OUT_CURV_PROFILE)) {
-      float num = p2 * dxx + 2.0f * pq * dxy + q2 * dyy;
+      float num = fadd(fadd(fmul(p2, dxx), fmul(tpq, dxy)), fmul(q2, dyy));
       o[FSG_OUT_CURV_PROFILE] = gamma_display(-num * rcp_approx(g2 * s15 + 1e-10f));
     }
   }
@@ -701,9 +702,11 @@ __device__ __forceinline__ void pixel_products2(const Light& L, float slx, float
       const f2 m = mul2(S2(-0.45454545454545453f), P2(lg2_approx(l.x), lg2_approx(l.y)));
       return P2(ex2_approx(m.x), ex2_approx(m.y));
     };
+    // Numerators in NumPy's float32 order, every operation rounded (no FMA): their
+    // terms cancel on smooth terrain, so another rounding order moves k visibly.
     if (om & (1u << FSG_OUT_CURV_MEAN)) {
       const f2 sm = mul2(add2(dxy, dyx), S2(0.5f));
-      const f2 num = fma2(add2(S2(1.0f), p2), dyy, sub2(mul2(add2(S2(1.0f), q2), dxx), mul2(pq2, sm)));
+      const f2 num = add2(sub2(mul2(add2(S2(1.0f), q2), dxx), mul2(pq2, sm)), mul2(add2(S2(1.0f), p2), dyy));
       o[FSG_OUT_CURV_MEAN] = display(num, fma2(S2(2.0f * C), s15, S2(1e-10f * C)));
     }
     if (om & (1u << FSG_OUT_CURV_GAUSSIAN)) {
@@ -712,11 +715,11 @@ __device__ __forceinline__ void pixel_products2(const Light& L, float slx, float
       o[FSG_OUT_CURV_GAUSSIAN] = display(P2(-num.x, -num.y), mul2(den, S2(C)));
     }
     if (om & (1u << FSG_OUT_CURV_PLANFORM)) {
-      const f2 num = fma2(p2, dyy, sub2(mul2(q2, dxx), mul2(pq2, dxy)));
+      const f2 num = add2(sub2(mul2(q2, dxx), mul2(pq2, dxy)), mul2(p2, dyy));
       o[FSG_OUT_CURV_PLANFORM] = display(num, fma2(g2c, P2(sqrt_approx(g2.x), sqrt_approx(g2.y)), S2(1e-10f * C)));
     }
     if (om & (1u << FSG_OUT_CURV_PROFILE)) {
-      const f2 num = fma2(q2, dyy, fma2(pq2, dxy, mul2(p2, dxx)));
+      const f2 num = add2(add2(mul2(p2, dxx), mul2(pq2, dxy)), mul2(q2, dyy));
       o[FSG_OUT_CURV_PROFILE] = display(num, fma2(g2c, s15, S2(1e-10f * C)));
     }
   }
@@ -934,9 +937,9 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
     auto dv = [](f2 num, Step a) { return DIV ? div_by2(num, a.d2, a.rcp) : mul2(num, S2(a.rcp)); };
     auto dv4 = [&](Q4 num, Step a) { return Q4{dv(num.lo, a), dv(num.hi, a)}; };
     auto dv1 = [](float num, Step a) { return DIV ? div_by(num, a.d2, a.rcp) : __fmul_rn(num, a.rcp); };
-    // First derivatives that feed the second ones are always correctly rounded: the
-    // second differences of np.gradient's float32 first derivatives amplify a one-ulp
-    // difference in them (by ~|dx| / |dxx step|, up to ~1e3 on smooth terrain).
+    // The curvature's derivatives are always correctly rounded: the second differences of
+    // np.gradient's float32 first derivatives amplify a one-ulp difference in them (by
+    // ~|dx| / |dxx step|, up to ~1e3 on smooth terrain), and the numerators cancel.
     auto dv4e = [](Q4 num, Step a) { return Q4{div_by2(num.lo, a.d2, a.rcp), div_by2(num.hi, a.d2, a.rcp)}; };
     auto dv1e = [](float num, Step a) { return div_by(num, a.d2, a.rcp); };
     // horizontal central difference of a row: neighbours from the adjacent lanes or the edge pair
@@ -996,10 +999,10 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
         yp1 = dv1e(__fsub_rn(e31lane ? ep2.x : ep2.y, e31lane ? e0.x : e0.y), T.g1y);
         p = dx0;
         q = dy0;
-        dxx = dv4(hdiff(dx0, P2(xd0, xd0)), T.c2x);
-        dxy = dv4(q4sub(dxp1, dxm1), T.c2y);
-        dyy = dv4(q4sub(dyp1, dym1), T.c2y);
-        if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = dv4(hdiff(dy0, P2(yd0, yd0)), T.c2x);
+        dxx = dv4e(hdiff(dx0, P2(xd0, xd0)), T.c2x);
+        dxy = dv4e(q4sub(dxp1, dxm1), T.c2y);
+        dyy = dv4e(q4sub(dyp1, dym1), T.c2y);
+        if (OM & (1u << FSG_OUT_CURV_MEAN)) dyx = dv4e(hdiff(dy0, P2(yd0, yd0)), T.c2x);
       } else {
         p = dv4(hdiff(f0, e0), T.g1x);
         q = dv4(q4sub(fp1, fm1), T.g1y);
@@ -1320,11 +1323,11 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
           auto dya = [&](int yy, int xx) { return DY[(yy - (y0 - 2)) * XD_C + (xx - (x0 - 2))]; };
           p = dxa(gy, gx);
           q = dya(gy, gx);
-          dxx = deriv_d<DIV>(T.c2x, gx, T.wx0, T.wx1, [&](int k) { return dxa(gy, gx + k); });
-          dxy = deriv_d<DIV>(T.c2y, gy, T.wy0, T.wy1, [&](int k) { return dxa(gy + k, gx); });
-          dyy = deriv_d<DIV>(T.c2y, gy, T.wy0, T.wy1, [&](int k) { return dya(gy + k, gx); });
+          dxx = deriv_d<true>(T.c2x, gx, T.wx0, T.wx1, [&](int k) { return dxa(gy, gx + k); });
+          dxy = deriv_d<true>(T.c2y, gy, T.wy0, T.wy1, [&](int k) { return dxa(gy + k, gx); });
+          dyy = deriv_d<true>(T.c2y, gy, T.wy0, T.wy1, [&](int k) { return dya(gy + k, gx); });
           if (OM & (1u << FSG_OUT_CURV_MEAN))
-            dyx = deriv_d<DIV>(T.c2x, gx, T.wx0, T.wx1, [&](int k) { return dya(gy, gx + k); });
+            dyx = deriv_d<true>(T.c2x, gx, T.wx0, T.wx1, [&](int k) { return dya(gy, gx + k); });
         } else {
           p = deriv_d<DIV>(T.g1x, gx, T.wx0, T.wx1, [&](int k) { return fe(gy, gx + k); });
           q = deriv_d<DIV>(T.g1y, gy, T.wy0, T.wy1, [&](int k) { return fe(gy + k, gx); });
