@@ -18,6 +18,12 @@ A histogram source gives a rank's histograms: the GPU
 (``DeviceHistograms``, the ``fsg_key_histogram`` kernel) or NumPy
 (``NumpyHistograms``, for host-side arrays).  ``allreduce`` sums an int64
 NumPy array over the ranks (``torch_allreduce`` wraps torch.distributed).
+
+``core.tile_loop.process_dem_array`` runs sharded when a ``Shard`` is given or
+a torch.distributed process group of more than one rank is initialised: each
+rank computes its band of tile rows, its round-robin share of the
+statistics windows, and the statistics through this merge (the reference
+broadcasts them to its Dask workers, core/dask_processor.py:1011-1016).
 """
 from __future__ import annotations
 
@@ -91,7 +97,7 @@ class DeviceHistograms:
         t = values if hasattr(values, "data_ptr") else _arrays.as_device_f32_2d(values).tensor
         self.t = t.reshape(-1).contiguous().float()
         self.absolute = 1 if absolute else 0
-        self._count = None
+        self._count = None if self.t.numel() > 0 else 0
 
     def count(self) -> int:
         if self._count is None:
@@ -101,6 +107,8 @@ class DeviceHistograms:
 
     def histogram(self, prefix: int, mask: int, shift: int, bits: int) -> np.ndarray:
         from .. import _arrays
+        if self.t.numel() == 0:
+            return np.zeros(1 << bits, dtype=np.int64)
         out = (C.c_uint64 * (1 << bits))()
         self._N.check(self._N.lib().fsg_key_histogram(
             C.c_void_p(self.t.data_ptr()), int(self.t.numel()), self.absolute, C.c_uint32(prefix),
@@ -180,3 +188,87 @@ def distributed_topousm_scale(src, allreduce) -> Tuple[float]:
     """topousm_fast_stat_func's scale p99(|x|) over all shards (src built with absolute=True)."""
     (p99,), n = distributed_percentile(src, [99.0], allreduce)
     return (p99,)
+
+
+# ------------------------------------------------------- the shard of a run
+class Shard:
+    """This process's part of a sharded run: ``world`` ranks, this one ``rank``,
+    ``allreduce`` the sum over the ranks of an int64 / float64 NumPy array."""
+
+    def __init__(self, world: int, rank: int, allreduce: Callable[[np.ndarray], np.ndarray]):
+        if world < 1 or not 0 <= rank < world:
+            raise ValueError(f"rank {rank} outside a world of {world}")
+        self.world, self.rank, self.allreduce = int(world), int(rank), allreduce
+
+    def mine(self, items: Sequence) -> List:
+        """Round-robin share of a list every rank builds identically."""
+        return [x for i, x in enumerate(items) if i % self.world == self.rank]
+
+
+def torch_allreduce_any(group=None) -> Callable[[np.ndarray], np.ndarray]:
+    """As torch_allreduce, for int64 or float64 arrays."""
+    import torch
+    import torch.distributed as dist
+
+    def reduce(a: np.ndarray) -> np.ndarray:
+        a = np.ascontiguousarray(a)
+        backend = dist.get_backend(group)
+        dev = "cuda" if backend == "nccl" else "cpu"
+        t = torch.from_numpy(a.copy()).to(dev)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+        return t.cpu().numpy()
+    return reduce
+
+
+def shard_from_environment(group=None) -> Optional["Shard"]:
+    """A Shard over the initialised torch.distributed process group when it has more
+    than one rank; None otherwise (single-device run)."""
+    try:
+        import torch.distributed as dist
+    except ImportError:  # pragma: no cover
+        return None
+    if not (dist.is_available() and dist.is_initialized()):
+        return None
+    world = dist.get_world_size(group)
+    if world <= 1:
+        return None
+    return Shard(world, dist.get_rank(group), torch_allreduce_any(group))
+
+
+def _union_std(values: np.ndarray, allreduce) -> float:
+    """Population standard deviation of the union of the ranks' valid values (float64 sums)."""
+    v = np.asarray(values, dtype=np.float64)
+    v = v[~np.isnan(v)]
+    tot = allreduce(np.array([v.size, v.sum()], dtype=np.float64))
+    n, s = int(tot[0]), float(tot[1])
+    if n == 0:
+        return 0.0
+    mean = s / n
+    ss = float(allreduce(np.array([np.square(v - mean).sum()], dtype=np.float64))[0])
+    return math.sqrt(ss / n)
+
+
+def sharded_topousm_stat(src_abs, values_host_fn, allreduce) -> Tuple[float]:
+    """topousm_fast_stat_func over the union of the shards: p99(|x|) from the exact
+    histogram merge, falling back to the standard deviation, then 1.0
+    (_normalization.py:21-32).  ``values_host_fn()`` gives this rank's values on the
+    host (only called for the fallback)."""
+    (p,), n = distributed_percentile(src_abs, [99.0], allreduce)
+    if n > 0:
+        if p > 1e-9:
+            return (p,)
+        sd = _union_std(values_host_fn(), allreduce)
+        return (sd if sd > 1e-9 else 1.0,)
+    return (1.0,)
+
+
+def sharded_stretch_stat(src, allreduce) -> Tuple[float, float]:
+    """robust_unsigned_stretch_stat_func over the union: (p1, p99 - p1)
+    (_global_stats.py:181-203)."""
+    (lo, hi), n = distributed_percentile(src, [1.0, 99.0], allreduce)
+    if n == 0:
+        return (0.0, 0.0)
+    sc = hi - lo
+    if not (sc > 1e-12):
+        return (lo, 0.0)
+    return (lo, sc)

@@ -143,16 +143,28 @@ def stratified_windows(width, height, by0, by1, bx0, bx1, *, grid=3, tile=4096):
     return out
 
 
-def _valid_bbox(dem_dev, nodata) -> Optional[Tuple[int, int, int, int]]:
-    """Valid-data bounding box from a nearest-resampled overview (_norm_stats.py:253-264)."""
-    torch = _arrays._torch()
-    H, W = dem_dev.shape
+def bbox_sample_indices(H: int, W: int):
+    """Rows and columns of the nearest-resampled overview the valid-data box is
+    taken from (_norm_stats.py:253-264): index floor((i + 0.5) * n / o), o = n // cov."""
     cov = max(1, max(W, H) // 512)
     oh, ow = max(1, H // cov), max(1, W // cov)
-    # nearest resampling to (oh, ow): source index floor((i + 0.5) * H / oh)
-    ys = ((torch.arange(oh, device=dem_dev.device, dtype=torch.float64) + 0.5) * (H / oh)).long().clamp_(max=H - 1)
-    xs = ((torch.arange(ow, device=dem_dev.device, dtype=torch.float64) + 0.5) * (W / ow)).long().clamp_(max=W - 1)
-    ov = dem_dev.index_select(0, ys).index_select(1, xs)
+    ys = np.minimum(((np.arange(oh, dtype=np.float64) + 0.5) * (H / oh)).astype(np.int64), H - 1)
+    xs = np.minimum(((np.arange(ow, dtype=np.float64) + 0.5) * (W / ow)).astype(np.int64), W - 1)
+    return ys, xs, cov
+
+
+def _valid_bbox(dem_dev, nodata, sample=None) -> Optional[Tuple[int, int, int, int]]:
+    """Valid-data bounding box from a nearest-resampled overview (_norm_stats.py:253-264);
+    ``sample`` = ((H, W), that overview as a device array) when the raster is not on the device."""
+    torch = _arrays._torch()
+    if sample is not None:
+        (H, W), ov = sample
+        cov = bbox_sample_indices(H, W)[2]
+    else:
+        H, W = dem_dev.shape
+        ys, xs, cov = bbox_sample_indices(H, W)
+        ov = dem_dev.index_select(0, torch.from_numpy(ys).to(dem_dev.device)).index_select(
+            1, torch.from_numpy(xs).to(dem_dev.device))
     valid = torch.isfinite(ov)
     if nodata is not None and not math.isnan(float(nodata)):
         valid &= ~((ov - float(nodata)).abs() <= 1e-6)
@@ -166,16 +178,26 @@ def _valid_bbox(dem_dev, nodata) -> Optional[Tuple[int, int, int, int]]:
 
 
 def global_stats_prepass(dem_dev, algorithm: str, params: dict, *, nodata=None, grid: int = 3,
-                         max_tile: int = 4096, min_valid_frac: float = 0.02):
+                         max_tile: int = 4096, min_valid_frac: float = 0.02, shard=None, source=None):
     """Full-resolution stratified-window statistics (_norm_stats.py:176-298).
 
     Runs the algorithm's raw block function on up to grid^2 windows (one GPU
     call over all windows), trims each by its margin, pools the valid values
     and returns the algorithm's stats: topousm_fast -> (p99|x|,), openness and
     ambient occlusion -> (p1, p99 - p1).  Returns None when no window qualifies.
+    With a ``shard`` (core.sharding.Shard) each rank evaluates its round-robin
+    share of the windows and the statistics of the union come from the exact
+    histogram merge: every rank returns the numbers one device would.
+    ``source`` (a ``(shape, window_fn, bbox)`` triple) replaces ``dem_dev`` when
+    the raster is not on the device: ``window_fn(y0, x0, h, w)`` returns a window
+    as a device array, ``bbox`` the valid-data box (or None).
     """
     torch = _arrays._torch()
-    H, W = dem_dev.shape
+    if source is not None:
+        (H, W), window_fn, bbox_src = source
+    else:
+        H, W = dem_dev.shape
+        window_fn = lambda y0, x0, h, w: dem_dev[y0:y0 + h, x0:x0 + w]  # noqa: E731
     if algorithm == "topousm_fast":
         radii = params.get("_topousm_fast_full_radii") or params.get("radii")
         max_scale = max(float(r) for r in radii)
@@ -195,14 +217,16 @@ def global_stats_prepass(dem_dev, algorithm: str, params: dict, *, nodata=None, 
         max_scale = max(vals) if vals else 16.0
     margin = max(1, int(max_scale + 16))
     tile = max(min(2048, max_tile), 4 * margin)
-    bbox = _valid_bbox(dem_dev, nodata)
+    bbox = bbox_src if source is not None else _valid_bbox(dem_dev, nodata)
     if bbox is None:
         return None
     wins = stratified_windows(W, H, *bbox, grid=grid, tile=min(tile, max(W, H)))
+    if shard is not None:
+        wins = shard.mine(wins)
     pooled = []
     nanmask_needed = nodata is not None and not (isinstance(nodata, float) and math.isnan(nodata))
     for wy0, wx0, tw, th in wins:
-        a = dem_dev[wy0:wy0 + th, wx0:wx0 + tw]
+        a = window_fn(wy0, wx0, th, tw)
         if nanmask_needed:
             a = torch.where((a - float(nodata)).abs() <= 1e-6, torch.full_like(a, float("nan")), a)
         if float(torch.isfinite(a).float().mean()) < min_valid_frac:
@@ -229,13 +253,25 @@ def global_stats_prepass(dem_dev, algorithm: str, params: dict, *, nodata=None, 
         if m > 0:
             raw = raw[m:-m, m:-m]
         pooled.append(raw.reshape(-1))
-    if not pooled:
-        return None
-    vals = torch.cat(pooled)
-    if algorithm == "topousm_fast":
-        st = topousm_fast_stat_func(vals)
+    if shard is not None:
+        from . import sharding as SH
+        vals = torch.cat(pooled) if pooled else torch.empty(0, device="cuda")
+        if int(shard.allreduce(np.array([len(pooled)], dtype=np.int64))[0]) == 0:
+            return None
+        if algorithm == "topousm_fast":
+            st = SH.sharded_topousm_stat(SH.DeviceHistograms(vals, absolute=True),
+                                         lambda: vals.cpu().numpy(), shard.allreduce)
+        else:
+            finite = torch.where(torch.isfinite(vals), vals, torch.full_like(vals, float("nan")))
+            st = SH.sharded_stretch_stat(SH.DeviceHistograms(finite), shard.allreduce)
     else:
-        st = robust_unsigned_stretch_stat_func(vals)
+        if not pooled:
+            return None
+        vals = torch.cat(pooled)
+        if algorithm == "topousm_fast":
+            st = topousm_fast_stat_func(vals)
+        else:
+            st = robust_unsigned_stretch_stat_func(vals)
     if not st or not math.isfinite(float(st[-1])) or float(st[-1]) <= 1e-9:
         return None
     return st
@@ -251,27 +287,14 @@ class LoopResult:
     padding: int
     stats: Optional[tuple] = None
     extras: Dict[str, object] = field(default_factory=dict)
+    rows: Tuple[int, int] = (0, 0)  # raster rows this process wrote (its band when sharded)
 
 
-def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Optional[int] = None,
-                      sigma: float = 10.0, pixel_size: Optional[float] = None, pixel_scale_x: Optional[float] = None,
-                      pixel_scale_y: Optional[float] = None, transform=None, geographic: bool = False,
-                      nodata: Optional[float] = None, output_dtype: str = "float32", output_range=None,
-                      multiscale_mode: bool = True, **algo_params) -> LoopResult:
-    """Run one hot-path algorithm over an in-memory raster with the reference's tile semantics.
-
-    ``dem``: 2-D float32 host (NumPy) or device array.  ``transform``: the
-    (a, b, c, d, e, f) affine of a geographic raster (per-tile metric scales).
-    Returns full-raster planes on the device.
-    """
-    if algorithm not in HOT_PATH_ALGORITHMS:
-        raise ValueError(f"{algorithm!r} is not on the GB300 hot path ({', '.join(HOT_PATH_ALGORITHMS)})")
-    torch = _arrays._torch()
-    v = _arrays.as_device_f32_2d(dem, name="dem")
-    H, W = v.h, v.w
-    output_dtype = str(output_dtype or "float32").lower()
-    if output_dtype not in SUPPORTED_OUTPUT_DTYPES:
-        raise ValueError(f"Unsupported output_dtype={output_dtype!r}. Choose from {SUPPORTED_OUTPUT_DTYPES}.")
+def resolve_run(algorithm: str, H: int, W: int, algo_params: dict, *, output_dtype: str, output_range,
+                pixel_size, pixel_scale_x, pixel_scale_y, multiscale_mode: bool):
+    """The parameter logic the reference runs before its tile loop: output encoding,
+    pixel scales, local / spatial radii and weights (core/tile_processor.py:1027-1281).
+    Returns (params, quantise params, output dtype, px, psx, psy, spatial)."""
     params = dict(algo_params)
     qp = None
     if output_dtype in ("int16", "uint8"):
@@ -304,32 +327,79 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
             elif params.get("weights") is not None:
                 params["weights"] = None
 
-    # topousm_fast large-radius overview split (tile_processor.py:1236-1281)
-    if algorithm == "topousm_fast":
-        full_r, full_w = normalize_topousm_radii(params.get("radii"), params.get("weights"))
-        if full_w is None and full_r:
-            full_w = [1.0 / len(full_r)] * len(full_r)
-        params["radii"], params["weights"] = full_r, full_w
-        thr = TU.topousm_fast_default_large_radius_threshold(int(tile_size))
-        sr, sw, lr, lw = TU.split_radii_by_threshold(full_r, full_w, thr)
-        if lr:
-            scale = max(W / 2048.0, H / 2048.0, 1.0)
-            ow, oh = max(1, int(round(W / scale))), max(1, int(round(H / scale)))
-            coarse_dem = TU.overview(v.tensor, (oh, ow), nodata=nodata)
-            field = TU.compute_topousm_fast_large_coarse_field(coarse_dem, large_radii=lr, large_weights=lw,
-                                                               decimation=float(scale))
-            params.update({"_topousm_fast_full_radii": list(full_r), "_topousm_fast_full_weights": list(full_w),
-                           "radii": sr, "weights": sw, "_topousm_fast_coarse_field": field,
-                           "_topousm_fast_small_radii": sr, "_topousm_fast_small_weights": sw,
-                           "_topousm_fast_w_large": float(sum(lw)), "_topousm_fast_full_shape": (H, W)})
+    return params, qp, output_dtype, px, psx, psy, spatial
 
+
+def topousm_split(params: dict, H: int, W: int, tile_size: int, overview_fn) -> None:
+    """topousm_fast's large-radius overview split (core/tile_processor.py:1236-1281):
+    radii above max(256, tile/16) leave the per-tile list and become one coarse
+    field on the <= 2048 px overview that ``overview_fn(oh, ow)`` returns."""
+    full_r, full_w = normalize_topousm_radii(params.get("radii"), params.get("weights"))
+    if full_w is None and full_r:
+        full_w = [1.0 / len(full_r)] * len(full_r)
+    params["radii"], params["weights"] = full_r, full_w
+    thr = TU.topousm_fast_default_large_radius_threshold(int(tile_size))
+    sr, sw, lr, lw = TU.split_radii_by_threshold(full_r, full_w, thr)
+    if lr:
+        scale = max(W / 2048.0, H / 2048.0, 1.0)
+        ow, oh = max(1, int(round(W / scale))), max(1, int(round(H / scale)))
+        coarse_dem = overview_fn(oh, ow)
+        field = TU.compute_topousm_fast_large_coarse_field(coarse_dem, large_radii=lr, large_weights=lw,
+                                                           decimation=float(scale))
+        params.update({"_topousm_fast_full_radii": list(full_r), "_topousm_fast_full_weights": list(full_w),
+                       "radii": sr, "weights": sw, "_topousm_fast_coarse_field": field,
+                       "_topousm_fast_small_radii": sr, "_topousm_fast_small_weights": sw,
+                       "_topousm_fast_w_large": float(sum(lw)), "_topousm_fast_full_shape": (H, W)})
+
+
+def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Optional[int] = None,
+                      sigma: float = 10.0, pixel_size: Optional[float] = None, pixel_scale_x: Optional[float] = None,
+                      pixel_scale_y: Optional[float] = None, transform=None, geographic: bool = False,
+                      nodata: Optional[float] = None, output_dtype: str = "float32", output_range=None,
+                      multiscale_mode: bool = True, shard="auto", **algo_params) -> LoopResult:
+    """Run one hot-path algorithm over an in-memory raster with the reference's tile semantics.
+
+    ``dem``: 2-D float32 host (NumPy) or device array.  ``transform``: the
+    (a, b, c, d, e, f) affine of a geographic raster (per-tile metric scales).
+    Returns full-raster planes on the device.
+
+    ``shard``: ``"auto"`` (default) runs sharded when a torch.distributed process
+    group of more than one rank is initialised, a ``core.sharding.Shard`` runs as
+    that rank, ``None`` / ``False`` runs the whole raster.  A sharded rank writes
+    the cores of its band of tile rows (``LoopResult.rows``; the other rows keep
+    the NoData value) and takes the global statistics from the exact cross-rank
+    merge, so the union of the bands equals the single-device result.
+    """
+    if algorithm not in HOT_PATH_ALGORITHMS:
+        raise ValueError(f"{algorithm!r} is not on the GB300 hot path ({', '.join(HOT_PATH_ALGORITHMS)})")
+    torch = _arrays._torch()
+    v = _arrays.as_device_f32_2d(dem, name="dem")
+    H, W = v.h, v.w
+    output_dtype = str(output_dtype or "float32").lower()
+    if output_dtype not in SUPPORTED_OUTPUT_DTYPES:
+        raise ValueError(f"Unsupported output_dtype={output_dtype!r}. Choose from {SUPPORTED_OUTPUT_DTYPES}.")
+    params, qp, output_dtype, px, psx, psy, spatial = resolve_run(
+        algorithm, H, W, algo_params, output_dtype=output_dtype, output_range=output_range, pixel_size=pixel_size,
+        pixel_scale_x=pixel_scale_x, pixel_scale_y=pixel_scale_y, multiscale_mode=multiscale_mode)
+    if algorithm == "topousm_fast":
+        topousm_split(params, H, W, tile_size, lambda oh, ow: TU.overview(v.tensor, (oh, ow), nodata=nodata))
+
+    if shard == "auto":
+        from .sharding import shard_from_environment
+        shard = shard_from_environment()
+    elif shard is False:
+        shard = None
     pad = required_padding(algorithm, params, sigma, tile_size) if padding is None else int(padding)
     infos = tile_grid(H, W, int(tile_size), pad)
+    if shard is not None:
+        from .sharding import shard_tiles
+        infos = shard_tiles(infos, shard.world, shard.rank)
     tiles = make_tiles(infos, pixel_scale_x=psx, pixel_scale_y=psy, transform=transform, geographic=geographic)
     out = _arrays.empty(H, W, output_dtype, device=v.tensor.device)
     fill = 0 if output_dtype != "float32" else float("nan")
     out.fill_(fill)  # tiles skipped for NoData keep the NoData value
-    res = LoopResult(out, output_dtype, qp, len(tiles), pad)
+    rows = (min((t.core_y for t in infos), default=0), max((t.core_y + t.core_h for t in infos), default=0))
+    res = LoopResult(out, output_dtype, qp, len(tiles), pad, rows=rows)
 
     if spatial:
         stretch = None
@@ -339,10 +409,27 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
             stretch = params.get("global_stats")
             if stretch is None:
                 stretch = global_stats_prepass(v.tensor, algorithm, dict(params, pixel_scale_x=psx,
-                                                                         pixel_scale_y=psy), nodata=nodata)
+                                                                         pixel_scale_y=psy), nodata=nodata,
+                                               shard=shard)
             res.stats = stretch
         _spatial_loop(v, infos, tiles, algorithm, params, px, nodata, out, output_dtype, qp, stretch)
-    elif algorithm in ("hillshade", "slope", "curvature"):
+    else:
+        stats = params.get("global_stats")
+        if (stats is None or (algorithm == "topousm_fast" and not stats)) and \
+                algorithm in ("topousm_fast", "ambient_occlusion", "openness"):
+            stats = global_stats_prepass(v.tensor, algorithm, dict(params, pixel_scale_x=psx, pixel_scale_y=psy),
+                                         nodata=nodata, shard=shard)
+        if algorithm in ("topousm_fast", "ambient_occlusion", "openness"):
+            res.stats = stats
+        launch_local(algorithm, v, tiles, params, px, nodata, S.make_plane(out, output_dtype, qp), stats, (H, W))
+    return res
+
+
+def launch_local(algorithm: str, v, tiles, params: dict, px: float, nodata, plane, stats, full_shape) -> None:
+    """The kernel call of a local-mode product (and of topousm_fast) over a tile list:
+    ``v`` the raster view the tiles address, ``plane`` the output plane in raster
+    coordinates, ``stats`` the global statistics (None: raw / unstretched)."""
+    if algorithm in ("hillshade", "slope", "curvature"):
         name = {"hillshade": "hillshade", "slope": "slope"}.get(algorithm)
         if algorithm == "curvature":
             ct = params.get("curvature_type", "mean")
@@ -350,37 +437,24 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
         sp = S.make_params(azimuth=params.get("azimuth", 315.0), altitude=params.get("altitude", 45.0),
                            z_factor=params.get("z_factor", 1.0), pixel_size=px, nodata=nodata,
                            unit=params.get("unit", "degree"))
-        S.launch(v, tiles, sp, {S.OUTPUT_INDEX[name]: S.make_plane(out, output_dtype, qp)})
+        S.launch(v, tiles, sp, {S.OUTPUT_INDEX[name]: plane})
     elif algorithm == "topousm_fast":
-        stats = params.get("global_stats") or global_stats_prepass(v.tensor, algorithm, params, nodata=nodata)
-        res.stats = stats
         scale = float(stats[0]) if stats else 0.0
         tp, keep = TU.make_params(params["radii"], params["weights"] or [], px, nodata=nodata,
                                   coarse=params.get("_topousm_fast_coarse_field"),
-                                  w_large=params.get("_topousm_fast_w_large", 0.0), full_shape=(H, W), scale=scale,
-                                  path=params.get("topousm_path", "exact"))
-        TU.run_topousm(v, tiles, tp, S.make_plane(out, output_dtype, qp))
+                                  w_large=params.get("_topousm_fast_w_large", 0.0), full_shape=full_shape,
+                                  scale=scale, path=params.get("topousm_path", "exact"))
+        TU.run_topousm(v, tiles, tp, plane)
     elif algorithm == "ambient_occlusion":
-        stats = params.get("global_stats")
-        if stats is None:
-            stats = global_stats_prepass(v.tensor, algorithm, dict(params, pixel_scale_x=psx, pixel_scale_y=psy),
-                                         nodata=nodata)
-        res.stats = stats
         ap = AO.make_params(num_samples=params.get("num_samples", 16), radius=params.get("radius", 10.0),
                             intensity=params.get("intensity", 1.0), pixel_size=px, nodata=nodata, stretch=stats)
-        AO.run_ambient_occlusion(v, tiles, ap, S.make_plane(out, output_dtype, qp))
+        AO.run_ambient_occlusion(v, tiles, ap, plane)
     else:  # openness
-        stats = params.get("global_stats")
-        if stats is None:
-            stats = global_stats_prepass(v.tensor, algorithm, dict(params, pixel_scale_x=psx, pixel_scale_y=psy),
-                                         nodata=nodata)
-        res.stats = stats
         op = OP.make_params(openness_type=params.get("openness_type", "positive"),
                             num_directions=params.get("num_directions", 16),
                             max_distance=params.get("max_distance", 50), pixel_size=px,
                             sampling=params.get("sampling", "reference"), nodata=nodata, stretch=stats)
-        OP.run_openness(v, tiles, op, S.make_plane(out, output_dtype, qp))
-    return res
+        OP.run_openness(v, tiles, op, plane)
 
 
 def sanitize_spatial_radii_weights(algorithm: str, radii, weights):

@@ -92,3 +92,51 @@ def test_two_gloo_ranks_agree_with_the_union(tmp_path):
     ref = list(np.percentile(v, QS)) + [float(v.size)]
     for r in range(2):
         assert list(np.load(out % r)) == ref
+
+
+def _stat_rank(rank, world, port, shards, out_path):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        shard = SH.shard_from_environment()
+        assert shard is not None and shard.world == world and shard.rank == rank
+        v = shards[rank]
+        top = SH.sharded_topousm_stat(SH.NumpyHistograms(v, absolute=True), lambda: v, shard.allreduce)
+        flat = SH.sharded_topousm_stat(SH.NumpyHistograms(np.zeros_like(v), absolute=True),
+                                       lambda: np.zeros_like(v), shard.allreduce)
+        st = SH.sharded_stretch_stat(SH.NumpyHistograms(v), shard.allreduce)
+        np.save(out_path % rank, np.array(list(top) + list(flat) + list(st), dtype=np.float64))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_statistics_equal_the_reference_stat_funcs(tmp_path):
+    """topousm_fast_stat_func and robust_unsigned_stretch_stat_func of the union, on every rank
+    (including the all-zero fallback to the standard deviation, then 1.0)."""
+    from oracle import restated as R
+    mp = pytest.importorskip("torch.multiprocessing")
+    x = _data(60_001, 21)
+    shards = [x[:17_000], x[17_000:]]
+    out = str(tmp_path / "stat%d.npy")
+    mp.start_processes(_stat_rank, args=(2, _free_port(), shards, out), nprocs=2, join=True, start_method="spawn")
+    # exact float32 order statistics with FP64 interpolation = np.percentile of the float64 values
+    # (the reference's float32 interpolation is within one float32 ulp of it)
+    x64 = x[~np.isnan(x)].astype(np.float64)
+    p1, p99 = np.percentile(x64, [1.0, 99.0])
+    ref = [float(np.percentile(np.abs(x64), 99.0)), 1.0, float(p1), float(p99 - p1)]
+    r32 = list(R.topousm_scale(x)) + [1.0] + list(R.stretch_stats(x))
+    for r in range(2):
+        got = list(np.load(out % r))
+        assert got == ref
+        assert got == pytest.approx(r32, rel=2e-7)
+
+
+def test_shard_round_robin_and_validation():
+    sh = [SH.Shard(3, r, lambda a: a) for r in range(3)]
+    items = list(range(10))
+    assert sorted(sum((s.mine(items) for s in sh), [])) == items
+    with pytest.raises(ValueError):
+        SH.Shard(2, 2, lambda a: a)
+    assert SH.shard_from_environment() is None
