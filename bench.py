@@ -703,6 +703,7 @@ def batched_section(args):
     eager_ms = _time_ms(b.step, max(1, args.extra_steps // 2), 1, stream)
     b.capture()
     graph_ms = _time_ms(b.replay, args.extra_steps, 2, stream)
+    per_product = b.product_graph_ms(args.extra_steps)
     px = b.pyr.pixels
     res = {"workload": f"batched uneven tiles: {H}x{W} geographic fBm (1 arcsec columns, lat 45-30), 3 overview "
                        "levels, hillshade + topousm_fast (radii 2..512) + openness (R=256, 16 dirs) per tile",
@@ -711,6 +712,8 @@ def batched_section(args):
            "plans": len(b.plans),
            "value": round(px / (graph_ms * 1e-3) / 1e6, 1), "unit": "Mpix/s (all levels, 3 products)",
            "ms_per_step_graph": round(graph_ms, 2), "ms_per_step_eager": round(eager_ms, 2),
+           "ms_per_product_graph": {k: round(v, 2) for k, v in per_product.items()},
+           "scheduling": "each product's units popped from a device-side atomic queue by persistent CTAs / warps",
            "setup_s_incl_autotune_and_stats": round(setup_s, 2),
            "autotune_costs_ns_per_px": {k: {c: round(v * 1e6, 4) for c, v in cv.items()}
                                         for k, cv in b.tuner.measured.items()}}

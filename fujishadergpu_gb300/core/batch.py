@@ -144,6 +144,7 @@ class BatchedTiles:
         self.tile_counts: Dict[str, int] = {}
         self.stats: Dict[str, list] = {}
         self.plans: List[PL.Plan] = []
+        self.plan_products: List[str] = []   # product of each plan
         self._graph: Optional[PL.GraphStep] = None
         shape = tuple(self.pyr.atlas.shape)
         for prod in cfg.products:
@@ -234,6 +235,7 @@ class BatchedTiles:
         out = self.outputs[prod]
         view = self.pyr.view
         n = 0
+        n0 = len(self.plans)
         if prod == "topousm_fast":
             for L, ts in zip(self.pyr.levels, sizes):
                 _, tiles = level_tiles(L, ts, self._padding(prod, ts))
@@ -246,6 +248,7 @@ class BatchedTiles:
             n = len(tiles)
             # one plan over the tiles of every level (per-tile pixel scales carry the level)
             self.plans += self._level_plans(prod, self.pyr.levels[0], tiles, out, view)
+        self.plan_products += [prod] * (len(self.plans) - n0)
         self.tile_counts[prod] = n
 
     # ------------------------------------------------------------ autotune
@@ -303,6 +306,26 @@ class BatchedTiles:
         if self._graph is None:
             self.capture()
         self._graph.replay()
+
+    def product_graph_ms(self, steps: int = 4) -> Dict[str, float]:
+        """Device time of each product's share of the step: that product's plans captured
+        into their own CUDA graph and replayed ``steps`` times (CUDA events around the
+        replays on the current stream)."""
+        torch = _arrays._torch()
+        out = {}
+        for prod in dict.fromkeys(self.plan_products):
+            ps = [p for p, q in zip(self.plans, self.plan_products) if q == prod]
+            g = PL.GraphStep(lambda ps=ps: [p.launch() for p in ps])
+            g.replay()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(max(1, steps)):
+                g.replay()
+            e1.record()
+            torch.cuda.synchronize()
+            out[prod] = e0.elapsed_time(e1) / max(1, steps)
+        return out
 
     def result(self) -> BatchResult:
         return BatchResult(self.outputs, dict(self.tile_sizes), dict(self.tile_counts), dict(self.stats))

@@ -61,6 +61,7 @@ struct OpenArgs {
   int qmin, qmax;
   float* raw;                  // mean angle in degrees (nullable)
   long long rld;
+  unsigned* queue;             // work queue: next block of the flattened tile list (zeroed per launch)
 };
 
 __device__ __forceinline__ float load_z(const OpenArgs& A, int y, int x, const fsg_tile& T) {
@@ -106,7 +107,17 @@ __global__ void __launch_bounds__(BX * BY, FSG_OPEN_MINB) openness_kernel(const 
   int loaded = -1;
   const float init = POS ? -INFINITY : INFINITY;
   const float half_pi = 1.57079637050628662109375f;  // f32(pi/2)
-  for (int blk = blockIdx.x; blk < A.total_blocks; blk += gridDim.x) {
+  // Blocks of all tiles (of any size and overview level) are popped from one device
+  // queue, so CTAs that draw cheap blocks take more of them.  The pop is uniform
+  // over the CTA (thread 0 draws, a barrier publishes it).
+  __shared__ int s_blk;
+  auto pop = [&]() -> int {
+    __syncthreads();
+    if (tid == 0) s_blk = (int)atomicAdd(A.queue, 1u);
+    __syncthreads();
+    return s_blk;
+  };
+  for (int blk = pop(); blk < A.total_blocks; blk = pop()) {
     int lo = 0, hi = A.ntiles - 1;
     while (lo < hi) {
       int mid = (lo + hi + 1) >> 1;
@@ -306,7 +317,7 @@ namespace fsg {
 struct OpenJob {
   bool empty = true;
   std::vector<char> host;
-  size_t o_s = 0, o_rb = 0, o_ts = 0, o_b0 = 0, o_t = 0, o_re = 0;
+  size_t o_s = 0, o_rb = 0, o_ts = 0, o_b0 = 0, o_t = 0, o_re = 0, o_q = 0;
   OpenArgs A;
   void (*kern)(OpenArgs) = nullptr;
   int grid = 0;
@@ -319,6 +330,7 @@ struct OpenJob {
     A.tile_sample0 = reinterpret_cast<const int*>(base + o_ts);
     A.block0 = reinterpret_cast<const int*>(base + o_b0);
     A.tiles = reinterpret_cast<const fsg_tile*>(base + o_t);
+    A.queue = reinterpret_cast<unsigned*>(base + o_q);
   }
   int upload(void* dev, cudaStream_t s) const {
     FSG_CUDA(cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, s));
@@ -326,6 +338,7 @@ struct OpenJob {
   }
   int enqueue(cudaStream_t s) const {
     if (empty) return FSG_OK;
+    FSG_CUDA(cudaMemsetAsync(A.queue, 0, sizeof(unsigned), s));
     timing_mark(s, true);
     kern<<<grid, dim3(BX, BY), smem, s>>>(A);
     timing_mark(s, false);
@@ -393,7 +406,7 @@ static int openness_prepare(const float* raster_dev, int64_t ld, int32_t raster_
   size_t b_re = reach.size() * sizeof(int);
   size_t b_tiles = (size_t)ntiles * sizeof(fsg_tile);
   auto al = [](size_t n) { return (n + 255) & ~(size_t)255; };
-  size_t bytes = al(b_samples) + al(b_rb) + al(b_ts) + al(b_b0) + al(b_tiles) + al(b_re);
+  size_t bytes = al(b_samples) + al(b_rb) + al(b_ts) + al(b_b0) + al(b_tiles) + al(b_re) + al(sizeof(unsigned));
   std::vector<char>& host = J.host;
   host.assign(bytes, 0);
   size_t off = 0;
@@ -409,6 +422,8 @@ static int openness_prepare(const float* raster_dev, int64_t ld, int32_t raster_
   J.o_b0 = put(block0.data(), b_b0);
   J.o_t = put(tiles, b_tiles);
   J.o_re = put(reach.data(), b_re);
+  const unsigned qzero = 0u;
+  J.o_q = put(&qzero, sizeof(unsigned));  // the work queue's head
   OpenArgs& A = J.A;
   std::memset(&A, 0, sizeof(A));
   A.raster = raster_dev;

@@ -571,6 +571,7 @@ struct FastArgs {
   int ntiles, total_units;
   unsigned* fix_list;   // unit quarters for the fix-up pass: unit | quarter << 28 | FIX_EDGE (touches a window edge)
   unsigned* fix_count;  // number of entries in fix_list
+  unsigned* queue;      // work queue: next unit of the flattened tile list (zeroed per launch)
   FF gw[5];                   // Gaussian fill weights (float-float)
   PlaneK planes[FSG_STENCIL_NOUT];
   int use_tma;                // tmap describes the raster (16-byte aligned base and row pitch)
@@ -831,7 +832,16 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
   const Light L{A.lx, A.ly, A.lz, A.slope_unit};
   const float qnan = __int_as_float(0x7fc00000);
   const bool e0lane = lane == 0, e31lane = lane == 31;
-  for (int u = warp; u < A.total_units; u += nwarps) {
+  // Units of all tiles (of any size and overview level) are popped from one device
+  // queue, one per warp at a time, so warps that draw cheap units take more of them.
+  auto pop = [&]() -> int {
+    unsigned v = 0;
+    if (lane == 0) v = atomicAdd(A.queue, 1u);
+    return (int)__shfl_sync(0xffffffffu, v, 0);
+  };
+  (void)warp;
+  (void)nwarps;
+  for (int u = pop(); u < A.total_units; u = pop()) {
     const UnitGeom g = unit_geom(A, u);
     const FastTile& TG = A.tiles[g.t];
     const int x0 = g.x0, y0 = g.y0, y1 = g.y1, xo = g.xo;
@@ -1457,14 +1467,15 @@ struct StencilJob {
     return fast ? (sizeof(FastTile) * ft.size() + 255) & ~(size_t)255
                 : (tk.size() > (size_t)INLINE_TILES ? (sizeof(TileK) * tk.size() + 255) & ~(size_t)255 : 0);
   }
-  size_t device_bytes() const { return tiles_bytes() + (fast ? sizeof(unsigned) * ((size_t)NQ * units + 1) : 0); }
+  size_t device_bytes() const { return tiles_bytes() + (fast ? sizeof(unsigned) * ((size_t)NQ * units + 2) : 0); }
   // point the kernel arguments at the tables / fix-up list in `dev`
   void bind(void* dev) {
     if (fast) {
       unsigned* fix = reinterpret_cast<unsigned*>(static_cast<unsigned char*>(dev) + tiles_bytes());
       F.tiles = static_cast<const FastTile*>(dev);
       F.fix_count = fix;
-      F.fix_list = fix + 1;
+      F.queue = fix + 1;
+      F.fix_list = fix + 2;
     } else if (tk.size() > (size_t)INLINE_TILES) {
       A.tiles_dev = static_cast<const TileK*>(dev);
     }
@@ -1504,7 +1515,7 @@ struct StencilJob {
   int enqueue(cudaStream_t s) const {
     if (empty) return FSG_OK;
     if (fast) {
-      FSG_CUDA(cudaMemsetAsync(F.fix_count, 0, sizeof(unsigned), s));
+      FSG_CUDA(cudaMemsetAsync(F.fix_count, 0, 2 * sizeof(unsigned), s));  // fix-up count and queue head
       timing_mark(s, true);
       fastk<<<fgrid, FSG_FAST_NT, FAST_SMEM, s>>>(F);
       timing_mark(s, false);
