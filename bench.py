@@ -48,7 +48,6 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-ALG_BYTES_STENCIL_F32 = 4 + 4 * 4   # DEM read + 4 float32 planes written, per pixel
 METRIC = "Mpix/s on 32k² DEM; exact vs surrogate openness at ≤2° MAE; % of HBM roofline"
 
 
@@ -210,7 +209,7 @@ def cpu_oracle_rate(kind: str, *, procs: int, tiles: int, core: int, pad: int, p
 
 
 # ----------------------------------------------------------- stencil workload
-def stencil_workload(args, rank, world):
+def stencil_workload(args, rank, world, out_dtype="float32"):
     import numpy as np
     import torch
 
@@ -227,10 +226,16 @@ def stencil_workload(args, rank, world):
     synth.nodata_disks_device(dem, count=ndisks, seed=3)
     nodata_frac = float(torch.isnan(dem).float().mean().item())
     names = ["hillshade", "slope", "curvature_profile", "curvature_planform"]
-    outs = {n: torch.empty((H, W), device="cuda", dtype=torch.float32) for n in names}
+    from fujishadergpu_gb300.io.output_encoding import quantize_params
+    tdt = torch.float32 if out_dtype == "float32" else torch.uint8
+    esz = 4 if out_dtype == "float32" else 1
+    qps = {n: (None if out_dtype == "float32" else
+               quantize_params(0.0, 90.0 if n == "slope" else 1.0, out_dtype)) for n in names}
+    alg_bytes = 4 + 4 * esz   # DEM read + the four planes written, per pixel
+    outs = {n: torch.empty((H, W), device="cuda", dtype=tdt) for n in names}
     view = _arrays.as_device_f32_2d(dem)
     params = S.make_params(azimuth=315.0, altitude=45.0, pixel_size=5.0)
-    planes = {S.OUTPUT_INDEX[n]: S.make_plane(outs[n]) for n in names}
+    planes = {S.OUTPUT_INDEX[n]: S.make_plane(outs[n], out_dtype, qps[n]) for n in names}
     from fujishadergpu_gb300.core.sharding import shard_tiles
     infos = shard_tiles(tile_loop.tile_grid(H, W, tile, halo), world, rank)
     tiles = tile_loop.make_tiles(infos, pixel_scale_x=5.0, pixel_scale_y=-5.0)
@@ -266,8 +271,8 @@ def stencil_workload(args, rank, world):
     value = px / (ms * 1e-3) / 1e6
     hbm, _, peak_kind = peaks()
     # dominant kernel: the streaming pass of this rank over its band (px_rank pixels)
-    achieved = ALG_BYTES_STENCIL_F32 * px_rank / (fast_ms * 1e-3) / 1e9
-    step_gbs = ALG_BYTES_STENCIL_F32 * px_rank / (e0.elapsed_time(e1) / args.steps * 1e-3) / 1e9  # whole step
+    achieved = alg_bytes * px_rank / (fast_ms * 1e-3) / 1e9
+    step_gbs = alg_bytes * px_rank / (e0.elapsed_time(e1) / args.steps * 1e-3) / 1e9  # whole step
 
     # ---- e2e: host (pinned) buffers through the C ABI (fsg_stencil_host): this rank's band
     # of the DEM and of the four planes in host memory; per row band of tiles one H2D
@@ -278,8 +283,8 @@ def stencil_workload(args, rank, world):
     cy1 = max(int(t.core_y0) + int(t.core_h) for t in tiles)
     host_dem = torch.empty((wy1 - wy0, W), dtype=torch.float32, pin_memory=True)
     host_dem.copy_(dem[wy0:wy1])
-    host_out = {n: torch.empty((cy1 - cy0, W), dtype=torch.float32, pin_memory=True) for n in names}
-    hplanes = {S.OUTPUT_INDEX[n]: S.host_plane(host_out[n]) for n in names}
+    host_out = {n: torch.empty((cy1 - cy0, W), dtype=tdt, pin_memory=True) for n in names}
+    hplanes = {S.OUTPUT_INDEX[n]: S.host_plane(host_out[n], out_dtype, qps[n]) for n in names}
     htiles = []
     for t in tiles:  # the same tiles in the coordinates of the host buffers
         u = _native.Tile()
@@ -295,7 +300,7 @@ def stencil_workload(args, rank, world):
         x0, x1 = bands.get(k, (1 << 30, -1))
         bands[k] = (min(x0, int(t.win_x0)), max(x1, int(t.win_x0) + int(t.win_w)))
     h2d_bytes = sum(k[2] * (x1 - x0) * 4 for k, (x0, x1) in bands.items())
-    d2h_bytes = px_rank * 4 * len(names)
+    d2h_bytes = px_rank * esz * len(names)
 
     def e2e_step():
         S.launch_host(host_dem, htiles, params, hplanes, stream=sh)
@@ -312,8 +317,8 @@ def stencil_workload(args, rank, world):
     torch.cuda.synchronize()
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e2e_steps, world)
     # correctness spot check of the host path against the device planes
-    ok = all(torch.equal(host_out[n][::4097, ::4097].cuda().nan_to_num(-7.0),
-                         outs[n][cy0:cy1][::4097, ::4097].nan_to_num(-7.0)) for n in names)
+    ok = all(torch.equal(host_out[n][::4097, ::4097].cuda().float().nan_to_num(-7.0),
+                         outs[n][cy0:cy1][::4097, ::4097].float().nan_to_num(-7.0)) for n in names)
     del host_dem, host_out
 
     line = {
@@ -329,7 +334,7 @@ def stencil_workload(args, rank, world):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded spectral fBm, Hurst 0.7, 0-4000 m, NoData disks)",
-        "config": {"workload": "fused hillshade+slope(deg)+profile+planform curvature, float32 planes",
+        "config": {"workload": f"fused hillshade+slope(deg)+profile+planform curvature, {out_dtype} planes",
                    "raster": [H, W], "pixel_m": 5.0, "tile": tile, "halo": halo, "tiles": len(tiles),
                    "nodata_frac": round(nodata_frac, 4), "outputs": names,
                    "l2": "inputs larger than L2 (DEM %.1f GiB, no flush)" % (px * 4 / 2 ** 30),
@@ -338,9 +343,10 @@ def stencil_workload(args, rank, world):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "peak_kind": peak_kind + " (burst copy)",
                      "kernel": "stencil_fast_kernel (fused streaming pass)", "kernel_ms": round(fast_ms, 4),
-                     "algorithmic_bytes_per_px": ALG_BYTES_STENCIL_F32,
-                     "algorithmic_bytes_per_launch": ALG_BYTES_STENCIL_F32 * px_rank,
-                     "traffic": profiled_traffic("stencil_fast_kernel_fused4_f32", px_rank),
+                     "algorithmic_bytes_per_px": alg_bytes,
+                     "algorithmic_bytes_per_launch": alg_bytes * px_rank,
+                     "traffic": (profiled_traffic("stencil_fast_kernel_fused4_f32", px_rank)
+                                 if out_dtype == "float32" else None),
                      "step_achieved": round(step_gbs, 1), "step_frac": round(step_gbs / hbm, 4)},
         "e2e": {"value": round(px / (e2e_ms * 1e-3) / 1e6, 1), "unit": "Mpix/s",
                 "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
@@ -763,7 +769,11 @@ def main():
     if not args.no_extra:
         import torch
         torch.cuda.empty_cache()
-        line["extra"] = {"topousm_fast": topousm_section(args)}
+        u8 = stencil_workload(args, rank, world, out_dtype="uint8")
+        line["extra"] = {"stencil_uint8": {k: u8[k] for k in ("value", "unit", "ms_per_step", "config", "roofline",
+                                                               "e2e", "gpu_launches")}}
+        torch.cuda.empty_cache()
+        line["extra"]["topousm_fast"] = topousm_section(args)
         torch.cuda.empty_cache()
         line["extra"]["openness"] = openness_section(args)
         torch.cuda.empty_cache()
