@@ -7,7 +7,10 @@ Tolerances (stated once, used everywhere):
   * curvature display ((tanh(100k)+1)/2)^(1/2.2): 1e-5, or, where tanh(100k)
     is within a few float32 ulps of -1 (the gamma step amplifies the last bit
     of tanh there; NumPy's and CUDA's float32 tanh differ in that bit), the
-    pre-gamma value (tanh+1)/2 agrees to 4 ulps of tanh (2^-23).
+    pre-gamma value (tanh+1)/2 agrees to 4 ulps of tanh (2^-23); and, at cells
+    where the reference's own float32 curvature is ill-conditioned (its
+    numerator's terms cancel), 1e-5 plus twice the distance between the
+    reference's float32 and float64 results there.
   * exact openness: mean angle within 0.01 degree.
   * ambient occlusion (output in [0, 1]): 1e-5 (a polynomial for the normalised
     occlusion atan(t) / (pi/4), within 6.3e-7, and a reciprocal multiply stand in
@@ -61,8 +64,13 @@ def assert_close_rel(got, ref, what="", rel=1e-5, atol=0.0):
     assert not bad.any(), f"{what}: {int(bad.sum())} cells over rel {rel}; worst {float((d - lim).max()):.3e}"
 
 
-def assert_curvature_close(got, ref, what=""):
-    """Display-domain 1e-5, or the pre-gamma tail rule described in the module docstring."""
+def assert_curvature_close(got, ref, what="", ref64_at=None):
+    """Display-domain 1e-5, or the pre-gamma tail rule described in the module docstring.
+
+    ``ref64_at(ys, xs)`` (optional) gives the same algorithm in float64 at those cells:
+    where the reference's own float32 result is ill-conditioned (its numerator's terms
+    cancel), a cell also passes when |got - ref| <= 1e-5 + 2 |ref - ref64|, i.e. within
+    twice the reference's own float32 error there."""
     got = to_np(got).astype(np.float64)
     ref = to_np(ref).astype(np.float64)
     assert_same_nan(got, ref, what)
@@ -73,6 +81,14 @@ def assert_curvature_close(got, ref, what=""):
     ug, ur = g ** 2.2, r ** 2.2
     tail = (~ok) & (np.minimum(ug, ur) < 1e-4) & (np.abs(ug - ur) <= CURV_TAIL_TOL)
     bad = ~(ok | tail)
+    if bad.any() and ref64_at is not None:
+        ys, xs = np.nonzero(m)
+        ys, xs = ys[bad], xs[bad]
+        r64 = np.asarray(ref64_at(ys, xs), dtype=np.float64)
+        own = np.abs(r[bad] - r64)
+        cond = d[bad] <= 1e-5 + 2.0 * own
+        idx = np.flatnonzero(bad)
+        bad[idx[cond]] = False
     assert not bad.any(), (f"{what}: {int(bad.sum())} cells off; worst display diff "
                            f"{float(d[bad].max()):.3e}")
     return int(tail.sum())
