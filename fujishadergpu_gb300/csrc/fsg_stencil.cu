@@ -972,9 +972,10 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
       const long long col = (long long)(T.ox0 + xl - T.cx0);
       optr[k] = static_cast<char*>(P.ptr) + ((long long)(T.oy0 + y0 - T.cy0) * P.ld + col) * esz;
       ostep[k] = P.ld * esz;
-      vstore[k] = esz == 4 && ((P.ld & 3) == 0) &&
-                  ((((uintptr_t)P.ptr >> 2) + (uintptr_t)(T.ox0 + x0 - T.cx0)) & 3) == 0 &&
-                  (((uintptr_t)P.ptr & 3) == 0);
+      // four pixels of a lane in one store: 16 bytes (float32), 8 (int16) or 4 (uint8) at an
+      // address aligned to that size (the row pitch and the unit's first column keep it)
+      const uintptr_t a0 = (uintptr_t)P.ptr + (uintptr_t)((long long)(T.ox0 + x0 - T.cx0) * esz);
+      vstore[k] = ((P.ld & 3) == 0) && (a0 % (uintptr_t)(4 * esz)) == 0;
     }
     int kr = 0;  // next unit row to take
     Q4 fm2{}, fm1, f0, fp1, fp2{};
@@ -1067,13 +1068,24 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
                               quantize(ohi[kk].x, P.qa, P.qb, P.qmin, P.qmax),
                               quantize(ohi[kk].y, P.qa, P.qb, P.qmin, P.qmax)};
           if (P.dtype == FSG_U8) {
+            if (vstore[kk] && nout == 4) {  // one 4-byte store: a warp writes 128 contiguous bytes
+              *reinterpret_cast<uint32_t*>(dst) = (uint32_t)(int)c[0] | ((uint32_t)(int)c[1] << 8) |
+                                                  ((uint32_t)(int)c[2] << 16) | ((uint32_t)(int)c[3] << 24);
+            } else {
 #pragma unroll
-            for (int m = 0; m < 4; ++m)
-              if (m < nout) reinterpret_cast<uint8_t*>(dst)[m] = (uint8_t)(int)c[m];
+              for (int m = 0; m < 4; ++m)
+                if (m < nout) reinterpret_cast<uint8_t*>(dst)[m] = (uint8_t)(int)c[m];
+            }
           } else {
+            if (vstore[kk] && nout == 4) {  // one 8-byte store
+              *reinterpret_cast<uint2*>(dst) =
+                  make_uint2(((uint32_t)(int)c[0] & 0xFFFFu) | ((uint32_t)(int)c[1] << 16),
+                             ((uint32_t)(int)c[2] & 0xFFFFu) | ((uint32_t)(int)c[3] << 16));
+            } else {
 #pragma unroll
-            for (int m = 0; m < 4; ++m)
-              if (m < nout) reinterpret_cast<int16_t*>(dst)[m] = (int16_t)(int)c[m];
+              for (int m = 0; m < 4; ++m)
+                if (m < nout) reinterpret_cast<int16_t*>(dst)[m] = (int16_t)(int)c[m];
+            }
           }
         }
         optr[kk] += ostep[kk];

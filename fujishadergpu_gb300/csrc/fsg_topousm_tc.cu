@@ -83,7 +83,7 @@ constexpr int TC_MMA_WARP = 12;
 constexpr int TC_NT = 13 * 32;
 constexpr int TC_EPI_PITCH = 100;           // floats per staged row of 96 outputs
 constexpr int TC_D1H_COL = 0, TC_D1L_COL = 128, TC_D2_COL = 256, TC_TMEM_COLS = 512;
-constexpr int TC_RT_BYTES = 64;             // per output row: decimated-grid and field row coordinates, Py
+constexpr int TC_RT_BYTES = 80;             // per output row: decimated-grid and field row coordinates, Py (hi, lo)
 constexpr int TC_PAR_BYTES = 16 + 4 * TC_IW; // per tile: c, 2^-k, k, flags; o(col)
 
 struct TcLayout {
@@ -92,7 +92,8 @@ struct TcLayout {
   __host__ __device__ int aring() const { return zring() + TC_NZ * TC_ZSTAGE; }
   __host__ __device__ int rows() const { return aring() + TC_NA * TC_ASTAGE; }
   __host__ __device__ int params() const { return rows() + TC_TH * TC_RT_BYTES; }
-  __host__ __device__ int bars() const { return params() + 2 * TC_PAR_BYTES; }
+  __host__ __device__ int rowoff() const { return params() + 2 * TC_PAR_BYTES; }  // [192] input-row offsets
+  __host__ __device__ int bars() const { return rowoff() + TC_IH * 8; }
   __host__ __device__ int total() const { return bars() + 512; }
 };
 // barrier block (byte offsets)
@@ -335,6 +336,7 @@ __global__ void __launch_bounds__(TC_NT, 1) topousm_tc(const __grid_constant__ T
       if (is_nodata(c, z.ndf, nd)) c = 0.f;
       float mloc = 0.f;
       bool seen = false;
+#pragma unroll 4
       for (int item = tid; item < TC_IH * (TC_IW / 8); item += TC_PROD) {
         const int i = item / (TC_IW / 8), g = item - (item / (TC_IW / 8)) * (TC_IW / 8);
         float v[8];
@@ -366,6 +368,8 @@ __global__ void __launch_bounds__(TC_NT, 1) topousm_tc(const __grid_constant__ T
       const int k = max(-60, min(60, TC_QBITS - e2));
       const float sk = ldexpf(1.0f, k);
       int* P = params(titer);
+      long long* roff = reinterpret_cast<long long*>(sm + L.rowoff());
+      if (tid < TC_IH) roff[tid] = (long long)reflect_idx(y0 - TC_HALO + tid, z.h) * z.ld;  // 'reflect' rows
       {
         // o(col) = Q(centre row, col)
         const float* crow = z.p + (long long)reflect_idx(y0 - TC_HALO + TC_CROW, z.h) * z.ld;
@@ -379,39 +383,73 @@ __global__ void __launch_bounds__(TC_NT, 1) topousm_tc(const __grid_constant__ T
         }
       }
       if (!prod_sync()) break;  // o(col) visible to every producer; red[] free again
-      // -- phase B: per radius and column half, the K steps of the band
-      for (int rr = 0; rr < A.nr; ++rr) {
-        for (int hh = 1; hh >= 0; --hh) {
-          for (int j = A.j1lo[rr]; j <= A.j1hi[rr]; ++j, ++n) {
-            const int s = (int)(n % TC_NZ);
-            const unsigned u = n / TC_NZ;
-            if (!bar_wait(B + BZE + 8 * s, (u & 1u) ^ 1u, abort_flag)) goto prod_done;
-            const unsigned zs = sbase + (unsigned)(L.zring() + s * TC_ZSTAGE);
-            const int kk = tid & 15, g = tid >> 4;       // row of the K step, 8-column group of the half
-            const int i = TC_IH - 1 - 16 * j - kk;       // reversed K: k = 16 j + kk <-> input row i
-            const int col0 = TC_HW * hh + 8 * g;         // input column
-            float v[8];
-            load8(reflect_idx(y0 - TC_HALO + i, z.h), xb + col0, v);
-            uint32_t hw[4], mw[4], lw[4];
+      // -- phase B: per radius and column half, the K steps of the band; the next step's
+      //    eight values are loaded while this step's are converted and stored
+      {
+        const int kk = tid & 15, g = tid >> 4;  // row of the K step, 8-column group of the half
+        auto fetch = [&](int j, int hh, float (&v)[8]) {
+          const int i = TC_IH - 1 - 16 * j - kk;  // reversed K: k = 16 j + kk <-> input row i
+          const float* row = z.p + roff[i];
+          const int wx0 = xb + TC_HW * hh + 8 * g;
+          if (vec && wx0 >= 0 && wx0 + 8 <= z.w) {
+            const float4 a4 = __ldg(reinterpret_cast<const float4*>(row + wx0));
+            const float4 b4 = __ldg(reinterpret_cast<const float4*>(row + wx0) + 1);
+            v[0] = a4.x; v[1] = a4.y; v[2] = a4.z; v[3] = a4.w;
+            v[4] = b4.x; v[5] = b4.y; v[6] = b4.z; v[7] = b4.w;
+          } else {
 #pragma unroll
-            for (int e = 0; e < 8; e += 2) {
-              const int qa = is_nodata(v[e], z.ndf, nd) ? 0
-                             : __float2int_rn(__fmul_rn(__fsub_rn(v[e], c), sk)) - P[4 + col0 + e];
-              const int qb = is_nodata(v[e + 1], z.ndf, nd) ? 0
-                             : __float2int_rn(__fmul_rn(__fsub_rn(v[e + 1], c), sk)) - P[4 + col0 + e + 1];
-              const Split3 d = digits3(qa, qb);
-              hw[e >> 1] = d.h;
-              mw[e >> 1] = d.m;
-              lw[e >> 1] = d.l;
-            }
-            // MN-major B operand: element (column n, k) at (n/8)*256 + (k/8)*128 + (k%8)*16 + (n%8)*2
-            const unsigned off = (unsigned)(g * 256 + (kk >> 3) * 128 + (kk & 7) * 16);
-            st_shared_v4(zs + off, hw[0], hw[1], hw[2], hw[3]);
-            st_shared_v4(zs + TC_ZSPLIT + off, mw[0], mw[1], mw[2], mw[3]);
-            st_shared_v4(zs + 2 * TC_ZSPLIT + off, lw[0], lw[1], lw[2], lw[3]);
-            fence_async_smem();
-            bar_arrive(B + BZF + 8 * s);
+            for (int e = 0; e < 8; ++e) v[e] = __ldg(row + reflect_idx(wx0 + e, z.w));
           }
+        };
+        int rr = 0, hh = 1, j = A.j1lo[0];
+        float v[8];
+        fetch(j, hh, v);
+        bool more = true;
+        while (more) {
+          int nr = rr, nh = hh, nj = j + 1;  // the step after this one
+          if (nj > A.j1hi[nr]) {
+            if (nh == 1) {
+              nh = 0;
+              nj = A.j1lo[nr];
+            } else {
+              ++nr;
+              nh = 1;
+              nj = nr < A.nr ? A.j1lo[nr] : 0;
+            }
+          }
+          more = nr < A.nr;
+          float vn[8];
+          if (more) fetch(nj, nh, vn);
+          const int s = (int)(n % TC_NZ);
+          const unsigned u = n / TC_NZ;
+          if (!bar_wait(B + BZE + 8 * s, (u & 1u) ^ 1u, abort_flag)) goto prod_done;
+          const unsigned zs = sbase + (unsigned)(L.zring() + s * TC_ZSTAGE);
+          const int col0 = TC_HW * hh + 8 * g;  // input column
+          uint32_t hw[4], mw[4], lw[4];
+#pragma unroll
+          for (int e = 0; e < 8; e += 2) {
+            const int qa = is_nodata(v[e], z.ndf, nd) ? 0
+                           : __float2int_rn(__fmul_rn(__fsub_rn(v[e], c), sk)) - P[4 + col0 + e];
+            const int qb = is_nodata(v[e + 1], z.ndf, nd) ? 0
+                           : __float2int_rn(__fmul_rn(__fsub_rn(v[e + 1], c), sk)) - P[4 + col0 + e + 1];
+            const Split3 d = digits3(qa, qb);
+            hw[e >> 1] = d.h;
+            mw[e >> 1] = d.m;
+            lw[e >> 1] = d.l;
+          }
+          // MN-major B operand: element (column n, k) at (n/8)*256 + (k/8)*128 + (k%8)*16 + (n%8)*2
+          const unsigned off = (unsigned)(g * 256 + (kk >> 3) * 128 + (kk & 7) * 16);
+          st_shared_v4(zs + off, hw[0], hw[1], hw[2], hw[3]);
+          st_shared_v4(zs + TC_ZSPLIT + off, mw[0], mw[1], mw[2], mw[3]);
+          st_shared_v4(zs + 2 * TC_ZSPLIT + off, lw[0], lw[1], lw[2], lw[3]);
+          fence_async_smem();
+          bar_arrive(B + BZF + 8 * s);
+          ++n;
+          rr = nr;
+          hh = nh;
+          j = nj;
+#pragma unroll
+          for (int e = 0; e < 8; ++e) v[e] = vn[e];
         }
       }
       bar_arrive(B + BTF + 8 * (titer & 3));
@@ -605,6 +643,7 @@ __global__ void __launch_bounds__(TC_NT, 1) topousm_tc(const __grid_constant__ T
           rf[14] = cy - f0;
         }
         rf[15] = (float)py;
+        rf[16] = (float)(py - (double)rf[15]);  // Py = hi + lo (float-float)
       }
       for (int half = 0; half < 2; ++half) {
 #pragma unroll 1
@@ -633,7 +672,7 @@ __global__ void __launch_bounds__(TC_NT, 1) topousm_tc(const __grid_constant__ T
             for (int col = xo + TC_HALO - r; col <= xo + TC_HALO + r; ++col) so += P[4 + col];
             ox += A.crw[rr] * (double)so;
           }
-          const float oxf = (float)ox;
+          const float oxh = (float)ox, oxl = (float)(ox - (double)oxh);  // Ox = hi + lo
           int dxa[ST_MAXD], dxb[ST_MAXD], dya[ST_MAXD];
           float dfx[ST_MAXD], dm[ST_MAXD][4];
 #pragma unroll
@@ -670,8 +709,12 @@ __global__ void __launch_bounds__(TC_NT, 1) topousm_tc(const __grid_constant__ T
             const int* ri = reinterpret_cast<const int*>(rtab + mm * TC_RT_BYTES);
             const float* rf = reinterpret_cast<const float*>(rtab + mm * TC_RT_BYTES);
             // sum_r w_r (z - mean_r) = W (z - c) - 2^-k (D2 + Py + Ox)
-            const float u = __fadd_rn(stage[mm * TC_EPI_PITCH + te], __fadd_rn(rf[15], oxf));
-            float a = __fsub_rn(__fmul_rn(wsum, __fsub_rn(zv, c)), __fmul_rn(u, isk));
+            // u = D2 + Py + Ox in float-float (Py and Ox are large, D2 second differences only)
+            const FF t = two_sum(rf[15], oxh);
+            const FF t2 = two_sum(t.hi, stage[mm * TC_EPI_PITCH + te]);
+            const float ulo = __fadd_rn(__fadd_rn(t.lo, t2.lo), __fadd_rn(rf[16], oxl));
+            // W (z - c) - 2^-k u: the power-of-two scaling is exact and the large terms cancel
+            float a = __fsub_rn(__fsub_rn(__fmul_rn(wsum, __fsub_rn(zv, c)), __fmul_rn(t2.hi, isk)), __fmul_rn(ulo, isk));
 #pragma unroll
             for (int d = 0; d < ST_MAXD; ++d) {
               if (d >= T.ndec) break;
