@@ -396,8 +396,10 @@ def process_dem_array(dem, algorithm: str, *, tile_size: int = 4096, padding: Op
         infos = shard_tiles(infos, shard.world, shard.rank)
     tiles = make_tiles(infos, pixel_scale_x=psx, pixel_scale_y=psy, transform=transform, geographic=geographic)
     out = _arrays.empty(H, W, output_dtype, device=v.tensor.device)
-    fill = 0 if output_dtype != "float32" else float("nan")
-    out.fill_(fill)  # tiles skipped for NoData keep the NoData value
+    if shard is not None or spatial:
+        # rows of other ranks, and spatial-mode tiles skipped for NoData, keep the NoData
+        # value; otherwise the local kernels write every core pixel of the covering grid
+        out.fill_(0 if output_dtype != "float32" else float("nan"))
     rows = (min((t.core_y for t in infos), default=0), max((t.core_y + t.core_h for t in infos), default=0))
     res = LoopResult(out, output_dtype, qp, len(tiles), pad, rows=rows)
 

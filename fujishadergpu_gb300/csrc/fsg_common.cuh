@@ -118,6 +118,19 @@ __device__ __forceinline__ float quantize(float v, float qa, float qb, int qmin,
   return fminf(fmaxf(dn, (float)qmin), (float)qmax);
 }
 
+// The same code without the conversion pipe (rintf and the float -> int cast
+// are quarter-rate instructions): the value is clamped first (clamping to
+// integer bounds commutes with rint) and then added to 1.5 * 2^23, where the
+// spacing of float32 is 1, so the sum's round-to-nearest-even is
+// 1.5 * 2^23 + rint(value) and its bit pattern is 0x4B400000 + rint(value) for
+// |value| < 2^22.  Returns that bit pattern: its low 8 bits are the uint8 code,
+// its low 16 bits the int16 code (two's complement); non-finite -> code 0.
+__device__ __forceinline__ uint32_t quantize_bits(float v, float qa, float qb, float fmin, float fmax) {
+  float x = fminf(fmaxf(__fadd_rn(__fmul_rn(qa, v), qb), fmin), fmax);
+  x = isfinite(v) ? x : 0.0f;
+  return __float_as_uint(__fadd_rn(x, 12582912.0f));
+}
+
 // ---------------------------------------------------- fast transcendentals
 // Float-float ("double-single") arithmetic on the FP32 pipes: a value is
 // hi + lo with |lo| <= ulp(hi)/2, about 48 significant bits.  Used for the

@@ -634,6 +634,14 @@ __device__ __forceinline__ f2 S2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ f2 add2(f2 a, f2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ f2 sub2(f2 a, f2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 __device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
+// quantize_bits on a pair (the multiply, add and rounding add paired)
+__device__ __forceinline__ uint2 quantize_bits2(f2 v, float qa, float qb, float fmin, float fmax) {
+  f2 x = add2(mul2(v, S2(qa)), S2(qb));
+  x.x = isfinite(v.x) ? fminf(fmaxf(x.x, fmin), fmax) : 0.0f;
+  x.y = isfinite(v.y) ? fminf(fmaxf(x.y, fmin), fmax) : 0.0f;
+  const f2 t = add2(x, S2(12582912.0f));
+  return make_uint2(__float_as_uint(t.x), __float_as_uint(t.y));
+}
 __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ bool nan2(f2 a) { return (a.x != a.x) | (a.y != a.y); }
 // div_by on both components (Markstein's correction, as div_by)
@@ -1062,29 +1070,28 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
             if (nout > 3) d[3] = ohi[kk].y;
           }
         } else {
+          // code bit patterns (quantize_bits: the code in the low 8 / 16 bits)
           const PlaneK& P = A.planes[kk];
-          const float c[4] = {quantize(olo[kk].x, P.qa, P.qb, P.qmin, P.qmax),
-                              quantize(olo[kk].y, P.qa, P.qb, P.qmin, P.qmax),
-                              quantize(ohi[kk].x, P.qa, P.qb, P.qmin, P.qmax),
-                              quantize(ohi[kk].y, P.qa, P.qb, P.qmin, P.qmax)};
+          const float fmin = (float)P.qmin, fmax = (float)P.qmax;
+          const uint2 cl = quantize_bits2(olo[kk], P.qa, P.qb, fmin, fmax);
+          const uint2 ch = quantize_bits2(ohi[kk], P.qa, P.qb, fmin, fmax);
+          const uint32_t c[4] = {cl.x, cl.y, ch.x, ch.y};
           if (P.dtype == FSG_U8) {
             if (vstore[kk] && nout == 4) {  // one 4-byte store: a warp writes 128 contiguous bytes
-              *reinterpret_cast<uint32_t*>(dst) = (uint32_t)(int)c[0] | ((uint32_t)(int)c[1] << 8) |
-                                                  ((uint32_t)(int)c[2] << 16) | ((uint32_t)(int)c[3] << 24);
+              *reinterpret_cast<uint32_t*>(dst) =
+                  __byte_perm(__byte_perm(c[0], c[1], 0x0040), __byte_perm(c[2], c[3], 0x0040), 0x5410);
             } else {
 #pragma unroll
               for (int m = 0; m < 4; ++m)
-                if (m < nout) reinterpret_cast<uint8_t*>(dst)[m] = (uint8_t)(int)c[m];
+                if (m < nout) reinterpret_cast<uint8_t*>(dst)[m] = (uint8_t)c[m];
             }
           } else {
             if (vstore[kk] && nout == 4) {  // one 8-byte store
-              *reinterpret_cast<uint2*>(dst) =
-                  make_uint2(((uint32_t)(int)c[0] & 0xFFFFu) | ((uint32_t)(int)c[1] << 16),
-                             ((uint32_t)(int)c[2] & 0xFFFFu) | ((uint32_t)(int)c[3] << 16));
+              *reinterpret_cast<uint2*>(dst) = make_uint2(__byte_perm(c[0], c[1], 0x5410), __byte_perm(c[2], c[3], 0x5410));
             } else {
 #pragma unroll
               for (int m = 0; m < 4; ++m)
-                if (m < nout) reinterpret_cast<int16_t*>(dst)[m] = (int16_t)(int)c[m];
+                if (m < nout) reinterpret_cast<uint16_t*>(dst)[m] = (uint16_t)c[m];
             }
           }
         }
@@ -1555,6 +1562,12 @@ static int stencil_prepare(const float* raster_dev, int64_t ld, int32_t raster_h
     if (!planes[o].ptr) continue;
     if (planes[o].dtype < FSG_F32 || planes[o].dtype > FSG_I16)
       return fail(FSG_ERR_DTYPE, "plane %d: dtype %d", o, planes[o].dtype);
+    if (planes[o].dtype != FSG_F32) {  // codes are clamped to [q_min, q_max]: they must fit the type
+      const int lo = planes[o].dtype == FSG_U8 ? 0 : -32768, hi = planes[o].dtype == FSG_U8 ? 255 : 32767;
+      if (planes[o].q_min < lo || planes[o].q_max > hi)
+        return fail(FSG_ERR_INVALID, "plane %d: code range [%d, %d] outside [%d, %d]", o, planes[o].q_min,
+                    planes[o].q_max, lo, hi);
+    }
     outmask |= 1u << o;
   }
   if (!outmask) return fail(FSG_ERR_INVALID, "no output plane requested");

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "fsg_topousm.cuh"
@@ -35,7 +36,8 @@ constexpr float kQNaN = __builtin_nanf("");
 // ----------------------------------------------------------- column passes
 // Box: vm = mean over rows [y-r, y+r] of v (NaN -> 0), wm = mean of valid.
 template <class Src>
-__global__ void __launch_bounds__(NT) box_cols(Src src, int r, int chunk, int nan_aware, AView vm, AView wm) {
+__device__ __forceinline__ void box_cols_body(const Src& src, int r, int chunk, int nan_aware, const AView& vm,
+                                              const AView& wm) {
   const int x = blockIdx.x * NT + threadIdx.x;
   if (x >= src.w) return;
   const int y0 = blockIdx.y * chunk;
@@ -65,11 +67,15 @@ __global__ void __launch_bounds__(NT) box_cols(Src src, int r, int chunk, int na
   }
 }
 
+template <class Src>
+__global__ void __launch_bounds__(NT) box_cols(Src src, int r, int chunk, int nan_aware, AView vm, AView wm) {
+  box_cols_body(src, r, chunk, nan_aware, vm, wm);
+}
+
 // Gaussian column pass (mode 'nearest'): weights g[0..R] (g[0] centre).
 template <class Src>
-__global__ void __launch_bounds__(NT) gauss_cols(Src src, const float* __restrict__ g, int R, int nan_aware,
-                                                 AView vm, AView wm, const int* run_if) {
-  if (run_if && *run_if == 0) return;  // nothing to do (e.g. a void fill without voids)
+__device__ __forceinline__ void gauss_cols_body(const Src& src, const float* __restrict__ g, int R, int nan_aware,
+                                                const AView& vm, const AView& wm) {
   const int x = blockIdx.x * NT + threadIdx.x;
   if (x >= src.w) return;
   for (int y = blockIdx.y; y < src.h; y += gridDim.y) {
@@ -87,6 +93,13 @@ __global__ void __launch_bounds__(NT) gauss_cols(Src src, const float* __restric
   vm.ref(y, x) = sv;
   if (nan_aware) wm.ref(y, x) = sw;
   }
+}
+
+template <class Src>
+__global__ void __launch_bounds__(NT) gauss_cols(Src src, const float* __restrict__ g, int R, int nan_aware,
+                                                 AView vm, AView wm, const int* run_if) {
+  if (run_if && *run_if == 0) return;  // nothing to do (e.g. a void fill without voids)
+  gauss_cols_body(src, g, R, nan_aware, vm, wm);
 }
 
 // ------------------------------------------------------------- row passes
@@ -111,14 +124,18 @@ struct RowArgs {
 
 constexpr int SEG = 8;
 
-__global__ void __launch_bounds__(NT) row_pass(const __grid_constant__ RowArgs A) {
-  if (A.run_if && *A.run_if == 0) return;
+// shared-memory row of the row pass: column c at c + c / SEG, so the lanes of a
+// warp (one SEG-column segment each, SEG = 8 apart) read distinct banks
+__device__ __forceinline__ int rp_idx(int c) { return c + c / SEG; }
+__host__ __device__ inline int rp_pitch(int span) { return span + span / SEG + 1; }
+
+__device__ __forceinline__ void row_pass_body(const RowArgs& A) {
   extern __shared__ float sm[];
   const int w = A.vm.w, h = A.vm.h;
   const int r = A.r;
-  const int span = A.tw + 2 * r;
+  const int span = A.tw + 2 * r, pitch = rp_pitch(span);
   float* sv = sm;
-  float* sw = sm + A.th * span;
+  float* sw = sm + A.th * pitch;
   const int ty0 = blockIdx.y * A.th, tx0 = blockIdx.x * A.tw;
   for (int i = threadIdx.x; i < A.th * span; i += NT) {
     int rr = i / span, c = i - rr * span;
@@ -126,8 +143,8 @@ __global__ void __launch_bounds__(NT) row_pass(const __grid_constant__ RowArgs A
     if (y >= h) continue;
     int xs = tx0 - r + c;
     int x = A.gauss ? clamp_idx(xs, w) : reflect_idx(xs, w);
-    sv[i] = A.vm.at(y, x);
-    if (A.nan_aware) sw[i] = A.wm.at(y, x);
+    sv[rr * pitch + rp_idx(c)] = A.vm.at(y, x);
+    if (A.nan_aware) sw[rr * pitch + rp_idx(c)] = A.wm.at(y, x);
   }
   __syncthreads();
   const int segs_per_row = A.tw / SEG;
@@ -135,16 +152,18 @@ __global__ void __launch_bounds__(NT) row_pass(const __grid_constant__ RowArgs A
   const int x_begin = tx0 + (threadIdx.x - rr * segs_per_row) * SEG;
   const int y = ty0 + rr;
   if (rr >= A.th || y >= h || x_begin >= w) return;
-  const float* rv = sv + rr * span;
-  const float* rw = sw + rr * span;
+  const float* rv = sv + rr * pitch;
+  const float* rw = sw + rr * pitch;
+  auto V = [&](int c) { return rv[rp_idx(c)]; };
+  auto Wt = [&](int c) { return rw[rp_idx(c)]; };
   const int n = 2 * r + 1;
   const float fn = (float)n;
   CSum hv, hw;
   const int c0 = x_begin - tx0;  // smem column of x_begin - r
   if (!A.gauss) {
     for (int k = 0; k < n; ++k) {
-      hv.add(rv[c0 + k]);
-      if (A.nan_aware) hw.add(rw[c0 + k]);
+      hv.add(V(c0 + k));
+      if (A.nan_aware) hw.add(Wt(c0 + k));
     }
   }
   for (int j = 0; j < SEG; ++j) {
@@ -152,13 +171,12 @@ __global__ void __launch_bounds__(NT) row_pass(const __grid_constant__ RowArgs A
     if (x >= w) break;
     float num, den;
     if (A.gauss) {
-      const float* pv = rv + c0 + j + r;
-      const float* pw = rw + c0 + j + r;
-      float a = A.g[0] * pv[0];
-      float b = A.nan_aware ? A.g[0] * pw[0] : 0.f;
+      const int cc = c0 + j + r;
+      float a = A.g[0] * V(cc);
+      float b = A.nan_aware ? A.g[0] * Wt(cc) : 0.f;
       for (int k = 1; k <= r; ++k) {
-        a = fmaf(A.g[k], __fadd_rn(pv[-k], pv[k]), a);
-        if (A.nan_aware) b = fmaf(A.g[k], __fadd_rn(pw[-k], pw[k]), b);
+        a = fmaf(A.g[k], __fadd_rn(V(cc - k), V(cc + k)), a);
+        if (A.nan_aware) b = fmaf(A.g[k], __fadd_rn(Wt(cc - k), Wt(cc + k)), b);
       }
       num = a;
       den = b;
@@ -166,11 +184,11 @@ __global__ void __launch_bounds__(NT) row_pass(const __grid_constant__ RowArgs A
       num = __fdiv_rn(hv.value(), fn);
       den = A.nan_aware ? __fdiv_rn(hw.value(), fn) : 1.f;
       if (j + 1 < SEG) {
-        hv.add(rv[c0 + j + n]);
-        hv.add(-rv[c0 + j]);
+        hv.add(V(c0 + j + n));
+        hv.add(-V(c0 + j));
         if (A.nan_aware) {
-          hw.add(rw[c0 + j + n]);
-          hw.add(-rw[c0 + j]);
+          hw.add(Wt(c0 + j + n));
+          hw.add(-Wt(c0 + j));
         }
       }
     }
@@ -189,6 +207,11 @@ __global__ void __launch_bounds__(NT) row_pass(const __grid_constant__ RowArgs A
       acc = A.first ? d : __fadd_rn(acc, d);
     }
   }
+}
+
+__global__ void __launch_bounds__(NT) row_pass(const __grid_constant__ RowArgs A) {
+  if (A.run_if && *A.run_if == 0) return;
+  row_pass_body(A);
 }
 
 // ------------------------------------------------------------ decimation
@@ -226,6 +249,157 @@ __global__ void voidfill_combine(AView coarse, AView sv, AView sw, const int* fl
   float c = coarse.at(i, j);
   float w = sw.at(i, j);
   if (c != c && w > 0.5f) coarse.ref(i, j) = __fdiv_rn(sv.at(i, j), fmaxf(w, 1e-6f));
+}
+
+// ---------------------------------------------- batched window decimation
+// The decimated radii of all windows of a strip job go through each stage in
+// one launch (blockIdx.z = work item: one window and one decimated radius), so
+// a stage of a 64-tile raster is one grid of 64x the blocks of one window's
+// (the per-window grids are a few dozen blocks and latency-bound).  Per item:
+//   small = NaN-aware f x f block mean of the window         (dec_downsample)
+//   if small has NaN cells: void fill with the Gaussian gv   (dec_fill_cols, dec_rows 0, dec_fill)
+//   ms = box(2 rs + 1, reflect) of small, NaN-aware, or      (dec_mean_cols, dec_rows 1)
+//        Gaussian(sigma 1, nearest) when rs <= 1
+// The arithmetic is that of the per-window kernels above (decimated_mean).
+struct DecItem {
+  ZView z;                      // window
+  int f, hs, ws;                // decimation factor, decimated grid
+  int rs;                       // radius at the decimated resolution
+  int R;                        // void-fill Gaussian radius
+  const float* gv;              // void-fill weights g[0..R]
+  const float* g1;              // sigma-1 weights g[0..4]
+  float *small, *vm, *wm, *sw;  // hs x ws scratch (ld = ws)
+  float* ms;                    // coarse mean (hs x ws); first the void fill's numerator
+  int* flag;                    // any NaN cell in small
+  unsigned* zmax;               // nullable: max |z| over the window's valid cells (float bits)
+};
+
+__device__ __forceinline__ AView dec_view(float* p, const DecItem& D) { return AView{p, D.ws, D.hs, D.ws}; }
+
+// NaN-aware f x f block means (downsample_kernel) and, for the item that
+// carries zmax, the window's max |z| over finite cells (window_absmax's
+// quantity, folded into this read of the window).
+__global__ void dec_downsample(const DecItem* items) {
+  const DecItem& D = items[blockIdx.z];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  float amax = 0.f;
+  if (i < D.hs && j < D.ws) {
+    float tot = 0.f, cnt = 0.f;
+    const int y0 = i * D.f, x0 = j * D.f;
+    auto take = [&](float v) {  // NoData is NaN here (ZView)
+      if (isfinite(v)) {
+        tot = __fadd_rn(tot, v);
+        cnt = __fadd_rn(cnt, 1.f);
+        amax = fmaxf(amax, fabsf(v));
+      }
+    };
+    const float* p0 = D.z.p + (long long)y0 * D.z.ld + x0;
+    // whole cells with 16-byte aligned rows: four columns per load, in the same order
+    if ((D.f & 3) == 0 && y0 + D.f <= D.z.h && x0 + D.f <= D.z.w && (D.z.ld & 3) == 0 &&
+        (reinterpret_cast<uintptr_t>(p0) & 15) == 0) {
+      for (int a = 0; a < D.f; ++a) {
+        const float4* r4 = reinterpret_cast<const float4*>(p0 + (long long)a * D.z.ld);
+        for (int b = 0; b < D.f / 4; ++b) {
+          const float4 v = __ldg(r4 + b);
+          const bool h = D.z.has_nodata != 0;
+          take(is_nodata(v.x, D.z.ndf, h) ? kQNaN : v.x);
+          take(is_nodata(v.y, D.z.ndf, h) ? kQNaN : v.y);
+          take(is_nodata(v.z, D.z.ndf, h) ? kQNaN : v.z);
+          take(is_nodata(v.w, D.z.ndf, h) ? kQNaN : v.w);
+        }
+      }
+    } else {
+      for (int a = 0; a < D.f; ++a) {
+        const int y = y0 + a;
+        if (y >= D.z.h) break;
+        for (int b = 0; b < D.f; ++b) {
+          const int x = x0 + b;
+          if (x >= D.z.w) break;
+          take(D.z.at(y, x));
+        }
+      }
+    }
+    const float m = cnt > 0.f ? __fdiv_rn(tot, fmaxf(cnt, 1.f)) : kQNaN;
+    D.small[(long long)i * D.ws + j] = m;
+    if (m != m) atomicOr(D.flag, 1);
+  }
+  if (D.zmax) {  // block-uniform: block maximum, one atomic only where it raises the running value
+    __shared__ float wmax[8];
+    for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    if ((t & 31) == 0) wmax[t >> 5] = amax;
+    __syncthreads();
+    if (t == 0) {
+      float m = wmax[0];
+      for (int w = 1; w < (int)((blockDim.x * blockDim.y) >> 5); ++w) m = fmaxf(m, wmax[w]);
+      // the running value only grows, so a stale read can only let a redundant atomic through
+      if (m > 0.f && m > __uint_as_float(*reinterpret_cast<volatile unsigned*>(D.zmax)))
+        atomicMax(D.zmax, __float_as_uint(m));
+    }
+  }
+}
+
+// Void fill, column pass: Gaussian(gv, nearest) of small -> vm, wm.
+__global__ void __launch_bounds__(NT) dec_fill_cols(const DecItem* items) {
+  const DecItem& D = items[blockIdx.z];
+  if (*D.flag == 0 || blockIdx.x * NT >= D.ws) return;
+  gauss_cols_body(dec_view(D.small, D), D.gv, D.R, 1, dec_view(D.vm, D), dec_view(D.wm, D));
+}
+
+// Row passes. stage 0: void fill, Gaussian(gv) rows of vm, wm -> numerator (ms),
+// denominator (sw); stage 1: the mean of the radius, rows of vm, wm -> ms.
+__global__ void __launch_bounds__(NT) dec_rows(const DecItem* items, int stage, int th, int tw) {
+  const DecItem& D = items[blockIdx.z];
+  if ((stage == 0 && *D.flag == 0) || blockIdx.x * tw >= D.ws || blockIdx.y * th >= D.hs) return;
+  RowArgs A;
+  A.vm = dec_view(D.vm, D);
+  A.wm = dec_view(D.wm, D);
+  A.nan_aware = 1;
+  A.th = th;
+  A.tw = tw;
+  A.run_if = nullptr;
+  A.weight = 0.f;
+  A.first = 0;
+  A.z = D.z;
+  A.out2 = dec_view(D.sw, D);
+  A.out = dec_view(D.ms, D);
+  if (stage == 0) {
+    A.mode = ROW_PAIR;
+    A.gauss = 1;
+    A.r = D.R;
+    A.g = D.gv;
+  } else {
+    A.mode = ROW_MEAN;
+    A.gauss = D.rs <= 1;
+    A.r = D.rs <= 1 ? 4 : D.rs;
+    A.g = D.g1;
+  }
+  row_pass_body(A);
+}
+
+// _nan_utils.py:655-667 (voidfill_combine): small = where(nan & sw > 0.5, sv / max(sw, 1e-6), small)
+__global__ void dec_fill(const DecItem* items) {
+  const DecItem& D = items[blockIdx.z];
+  if (*D.flag == 0) return;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= D.hs || j >= D.ws) return;
+  const long long o = (long long)i * D.ws + j;
+  const float c = D.small[o], w = D.sw[o];
+  if (c != c && w > 0.5f) D.small[o] = __fdiv_rn(D.ms[o], fmaxf(w, 1e-6f));
+}
+
+// Column pass of the radius's mean: box(2 rs + 1, reflect) or Gaussian(sigma 1, nearest).
+__global__ void __launch_bounds__(NT) dec_mean_cols(const DecItem* items, int chunk) {
+  const DecItem& D = items[blockIdx.z];
+  if (blockIdx.x * NT >= D.ws) return;
+  if (D.rs <= 1) {
+    gauss_cols_body(dec_view(D.small, D), D.g1, 4, 1, dec_view(D.vm, D), dec_view(D.wm, D));
+  } else {
+    if (blockIdx.y * chunk >= D.hs) return;
+    box_cols_body(dec_view(D.small, D), D.rs, chunk, 1, dec_view(D.vm, D), dec_view(D.wm, D));
+  }
 }
 
 // ------------------------------------------------------------- upsample
@@ -358,19 +532,31 @@ __global__ void overview_kernel(ZView z, AView out) {
   const int xa = (int)(((long long)j * z.w) / out.w), xb = (int)(((long long)(j + 1) * z.w) / out.w);
   FF acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   int cnt = 0;
+  auto add4 = [&](const float (&v)[4]) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      if (!is_nodata(v[m], z.ndf, z.has_nodata != 0)) {
+        const FF t = two_sum(acc[m].hi, v[m]);
+        acc[m] = {t.hi, __fadd_rn(acc[m].lo, t.lo)};
+        ++cnt;
+      }
+    }
+  };
+  // 16-byte loads when the cell's rows start aligned (same chains, same order)
+  const bool vec = (z.ld & 3) == 0 && (reinterpret_cast<uintptr_t>(z.p + xa) & 15) == 0;
   for (int y = ya; y < yb; ++y) {
     const float* row = z.p + (long long)y * z.ld;
     int x = xa;
-    for (; x + 3 < xb; x += 4) {
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const float v = __ldg(row + x + m);
-        if (!is_nodata(v, z.ndf, z.has_nodata != 0)) {
-          const FF t = two_sum(acc[m].hi, v);
-          acc[m] = {t.hi, __fadd_rn(acc[m].lo, t.lo)};
-          ++cnt;
-        }
+    if (vec) {
+      for (; x + 3 < xb; x += 4) {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(row + x));
+        const float v[4] = {q.x, q.y, q.z, q.w};
+        add4(v);
       }
+    }
+    for (; x + 3 < xb; x += 4) {
+      const float v[4] = {__ldg(row + x), __ldg(row + x + 1), __ldg(row + x + 2), __ldg(row + x + 3)};
+      add4(v);
     }
     for (; x < xb; ++x) {
       const float v = __ldg(row + x);
@@ -1342,7 +1528,7 @@ static void row_geometry(int r, int nan_aware, int w, int* th, int* tw, size_t* 
   static const int THS[] = {8, 4, 2, 1};
   for (int t : THS) {
     int ttw = NT * SEG / t;
-    size_t bytes = (size_t)t * (ttw + 2 * r) * sizeof(float) * (nan_aware ? 2 : 1);
+    size_t bytes = (size_t)t * rp_pitch(ttw + 2 * r) * sizeof(float) * (nan_aware ? 2 : 1);
     if (bytes <= 96 * 1024 || t == 1) {
       *th = t;
       *tw = ttw;
@@ -1566,60 +1752,6 @@ static bool strip_path_ok(const std::vector<int>& radii, double pixel_size, int*
   return true;
 }
 
-// Streams on which the per-window decimation pipelines of one call run side
-// by side (each window's pipeline is a chain of small launches); created once
-// per device, joined back into the caller's stream with events.
-constexpr int AUX_STREAMS = 8;
-struct AuxStreams {
-  int device = -1;
-  cudaStream_t st[AUX_STREAMS];
-  cudaEvent_t fork, join[AUX_STREAMS];
-};
-static int aux_streams(AuxStreams** out) {
-  static std::mutex mu;
-  static AuxStreams pool[64];
-  int dev = 0;
-  FSG_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return fail(FSG_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
-  std::lock_guard<std::mutex> lk(mu);
-  AuxStreams& a = pool[dev];
-  if (a.device != dev) {
-    for (int i = 0; i < AUX_STREAMS; ++i) {
-      FSG_CUDA(cudaStreamCreateWithFlags(&a.st[i], cudaStreamNonBlocking));
-      FSG_CUDA(cudaEventCreateWithFlags(&a.join[i], cudaEventDisableTiming));
-    }
-    FSG_CUDA(cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming));
-    a.device = dev;
-  }
-  *out = &a;
-  return FSG_OK;
-}
-
-// Coarse mean of one decimated radius of a window with its void-fill weights
-// already on the device (gv, radius R): the launches of decimated_mean only.
-static int decimated_mean_dev(const ZView& z, int r, int f, TopoScratch& S, const float* gv, int R, float* ms,
-                              cudaStream_t s) {
-  const int hs = std::max(1, (z.h + f - 1) / f), ws = std::max(1, (z.w + f - 1) / f);
-  AView small = resize(S.small, hs, ws);
-  FSG_CUDA(cudaMemsetAsync(S.flag, 0, sizeof(int), s));
-  Grid2 gd = grid2d(hs, ws);
-  downsample_kernel<<<gd.g, gd.b, 0, s>>>(z, f, small, S.flag);
-  FSG_LAUNCHED(1);
-  RowArgs ra;
-  std::memset(&ra, 0, sizeof(ra));
-  ra.mode = ROW_PAIR;
-  ra.out = resize(S.ssv, hs, ws);
-  ra.out2 = resize(S.ssw, hs, ws);
-  ra.run_if = S.flag;
-  int st = launch_gauss(small, gv, R, 1, resize(S.svm, hs, ws), resize(S.swm, hs, ws), ra, s);
-  if (st) return st;
-  voidfill_combine<<<gd.g, gd.b, 0, s>>>(small, resize(S.ssv, hs, ws), resize(S.ssw, hs, ws), S.flag);
-  FSG_LAUNCHED(1);
-  const int rs = std::max(1, (int)std::nearbyint((double)r / f));
-  AView out{ms, ws, hs, ws};
-  return mean_for_radius(small, rs, S, out, s);
-}
-
 // One topousm_fast strip-path job: host images of every device table (tile
 // descriptors, strip items, Gaussian weight tables), the layout of its device
 // buffer and the launch parameters.  The eager entry point uploads the images
@@ -1640,34 +1772,39 @@ struct TopoJob {
   TcArgs* TA = nullptr;
   size_t tc_smem = 0, tci_off = 0, fix_off = 0, fixc_off = 0;
   std::vector<int4> tc_it;
-  int ntiles = 0, nfull = 0, NS = 0, maxh = 1, maxw = 1, grid = 0;
+  int ntiles = 0, nfull = 0, maxh = 1, maxw = 1, grid = 0;
   std::vector<TopoTileK> tk;
   std::vector<StripItem> items;
-  struct DecWork {
-    int t, r, f, R;
-    size_t ms_off, gv_off;  // bytes from the dec area / floats into the weight table
+  // batched decimation: one DecItem per (window, decimated radius); consecutive
+  // items with the same (f, rs, R) form launch chunks of at most nslots items,
+  // item k of a chunk using scratch slot k
+  struct DecRef {
+    int t, slot;
+    size_t gv, ms;  // floats into the weight table / bytes from the dec area
+    bool zmax;      // this item's downsample also takes the window's max |z|
   };
-  std::vector<DecWork> work;
+  struct DecChunk {
+    int first, count, maxhs, maxws, rs, R;
+  };
+  std::vector<DecItem> ditems;
+  std::vector<DecRef> dref;
+  std::vector<DecChunk> dchunks;
+  bool absmax_fused = false;  // every window's max |z| comes from its downsample
+  size_t slot_bytes = 0, slot_plane = 0;
+  int nslots = 0;
   std::vector<float> gv, g1;
   std::vector<size_t> dec_ms;  // per (tile, dec), tile-major: byte offset of its coarse mean in the dec area
-  size_t one_small = 0, topo_bytes = 0, dec_bytes = 0, g1_off = 0, gv_off = 0, tiles_off = 0, items_off = 0,
-         flags_off = 0, total = 0;
+  size_t topo_bytes = 0, dec_bytes = 0, g1_off = 0, gv_off = 0, tiles_off = 0, items_off = 0, ditems_off = 0,
+         dflags_off = 0, flags_off = 0, total = 0;
   StripArgs A;
   void (*kern)(StripArgs) = nullptr;
   size_t smem = 0;
   int threads = 0;  // block size (0: FX_NT for the fixed kernels, ST_NT otherwise)
   // bound device state
   char* base = nullptr;
-  TopoScratch SS[AUX_STREAMS];
-  AuxStreams* aux = nullptr;
 
   void bind(void* dev) {
     base = static_cast<char*>(dev);
-    float* g1d = reinterpret_cast<float*>(base + g1_off);
-    for (int i = 0; i < NS; ++i) {
-      SS[i].carve_small(base + (size_t)i * one_small, maxh, maxw);
-      SS[i].g1 = g1d;
-    }
     int* flags = reinterpret_cast<int*>(base + flags_off);
     for (int t = 0; t < ntiles; ++t) {
       tk[t].nan_flag = flags + t;
@@ -1677,6 +1814,24 @@ struct TopoJob {
     size_t k = 0;
     for (int t = 0; t < ntiles; ++t)
       for (int d = 0; d < tk[t].ndec; ++d) tk[t].dec[d].ms = reinterpret_cast<float*>(base + topo_bytes + dec_ms[k++]);
+    const float* g1d = reinterpret_cast<const float*>(base + g1_off);
+    const float* gvd = reinterpret_cast<const float*>(base + gv_off);
+    int* dflags = reinterpret_cast<int*>(base + dflags_off);
+    for (size_t i = 0; i < ditems.size(); ++i) {
+      DecItem& D = ditems[i];
+      const DecRef& r = dref[i];
+      char* sl = base + (size_t)r.slot * slot_bytes;
+      D.z = tk[r.t].z;
+      D.small = reinterpret_cast<float*>(sl);
+      D.vm = reinterpret_cast<float*>(sl + slot_plane);
+      D.wm = reinterpret_cast<float*>(sl + 2 * slot_plane);
+      D.sw = reinterpret_cast<float*>(sl + 3 * slot_plane);
+      D.ms = reinterpret_cast<float*>(base + topo_bytes + r.ms);
+      D.gv = gvd + r.gv;
+      D.g1 = g1d;
+      D.flag = dflags + i;
+      D.zmax = r.zmax ? reinterpret_cast<unsigned*>(flags + ntiles) : nullptr;
+    }
     A.tiles = reinterpret_cast<const TopoTileK*>(base + tiles_off);
     A.items = reinterpret_cast<const StripItem*>(base + items_off);
     A.zmax = reinterpret_cast<const unsigned*>(flags + ntiles);
@@ -1694,40 +1849,59 @@ struct TopoJob {
     if (!gv.empty()) FSG_CUDA(cudaMemcpyAsync(base + gv_off, gv.data(), gv.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     FSG_CUDA(cudaMemcpyAsync(base + tiles_off, tk.data(), sizeof(TopoTileK) * ntiles, cudaMemcpyHostToDevice, s));
     FSG_CUDA(cudaMemcpyAsync(base + items_off, items.data(), sizeof(StripItem) * items.size(), cudaMemcpyHostToDevice, s));
+    if (!ditems.empty())
+      FSG_CUDA(cudaMemcpyAsync(base + ditems_off, ditems.data(), sizeof(DecItem) * ditems.size(), cudaMemcpyHostToDevice, s));
     if (tc) FSG_CUDA(cudaMemcpyAsync(base + tci_off, tc_it.data(), sizeof(int4) * tc_it.size(), cudaMemcpyHostToDevice, s));
+    return FSG_OK;
+  }
+
+  // the decimated radii of every window: per chunk one launch per stage
+  int enqueue_decimation(cudaStream_t s) const {
+    const DecItem* dev = reinterpret_cast<const DecItem*>(base + ditems_off);
+    for (const DecChunk& c : dchunks) {
+      const DecItem* it = dev + c.first;
+      const dim3 b2(32, 8);
+      const dim3 g2((c.maxws + 31) / 32, (c.maxhs + 7) / 8, c.count);
+      dec_downsample<<<g2, b2, 0, s>>>(it);
+      // void fill (skipped on the device for grids without NaN cells)
+      dec_fill_cols<<<dim3((c.maxws + NT - 1) / NT, std::min(c.maxhs, 65535), c.count), NT, 0, s>>>(it);
+      int th, tw;
+      size_t smem;
+      row_geometry(c.R, 1, c.maxws, &th, &tw, &smem);
+      if (smem > 48 * 1024) FSG_CUDA(cudaFuncSetAttribute(dec_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      dec_rows<<<dim3((c.maxws + tw - 1) / tw, (c.maxhs + th - 1) / th, c.count), NT, smem, s>>>(it, 0, th, tw);
+      dec_fill<<<g2, b2, 0, s>>>(it);
+      // the radius's mean
+      const int chunk = 128;  // rows per block of the box column pass (as launch_box)
+      if (c.rs <= 1)
+        dec_mean_cols<<<dim3((c.maxws + NT - 1) / NT, std::min(c.maxhs, 65535), c.count), NT, 0, s>>>(it, chunk);
+      else
+        dec_mean_cols<<<dim3((c.maxws + NT - 1) / NT, (c.maxhs + chunk - 1) / chunk, c.count), NT, 0, s>>>(it, chunk);
+      row_geometry(c.rs <= 1 ? 4 : c.rs, 1, c.maxws, &th, &tw, &smem);
+      if (smem > 48 * 1024) FSG_CUDA(cudaFuncSetAttribute(dec_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      dec_rows<<<dim3((c.maxws + tw - 1) / tw, (c.maxhs + th - 1) / th, c.count), NT, smem, s>>>(it, 1, th, tw);
+      FSG_LAUNCHED(6);
+    }
     return FSG_OK;
   }
 
   int enqueue(cudaStream_t s) const {
     if (empty) return FSG_OK;
-    int st = FSG_OK;
-    if (NS > 0) {
-      FSG_CUDA(cudaEventRecord(aux->fork, s));
-      for (int i = 0; i < NS; ++i) FSG_CUDA(cudaStreamWaitEvent(aux->st[i], aux->fork, 0));
-      const float* gvd = reinterpret_cast<const float*>(base + gv_off);
-      for (size_t i = 0; i < work.size() && !st; ++i) {
-        const DecWork& w = work[i];
-        const int si = (int)(i % (size_t)NS);
-        TopoScratch S = SS[si];
-        st = decimated_mean_dev(tk[w.t].z, w.r, w.f, S, gvd + w.gv_off, w.R,
-                                reinterpret_cast<float*>(base + topo_bytes + w.ms_off), aux->st[si]);
-      }
-      for (int i = 0; i < NS; ++i) {  // join (also on error: the scratch is released on s)
-        FSG_CUDA(cudaEventRecord(aux->join[i], aux->st[i]));
-        FSG_CUDA(cudaStreamWaitEvent(s, aux->join[i], 0));
-      }
-      if (st) return st;
-    }
     int* flags = reinterpret_cast<int*>(base + flags_off);
     const TopoTileK* tiles_dev = reinterpret_cast<const TopoTileK*>(base + tiles_off);
     FSG_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (ntiles + 1), s));
+    if (!ditems.empty()) {
+      FSG_CUDA(cudaMemsetAsync(base + dflags_off, 0, sizeof(int) * ditems.size(), s));
+      int st = enqueue_decimation(s);
+      if (st) return st;
+    }
     if (tc) {
       FSG_CUDA(cudaMemsetAsync(base + fixc_off, 0, sizeof(int), s));
       // The tensor kernel records max |z| of every input region it stages; with a
       // largest radius of 32 those regions are exactly what the exact kernel's strips
       // of the listed tiles read, otherwise the strips reach further and the windows
-      // are scanned first.
-      if (A.R != 32) {
+      // are scanned first (by the decimation's downsample when every window has one).
+      if (A.R != 32 && !absmax_fused) {
         window_absmax<<<dim3(128, ntiles), 256, 0, s>>>(tiles_dev, reinterpret_cast<unsigned*>(flags + ntiles));
         FSG_LAUNCHED(1);
       }
@@ -1739,9 +1913,15 @@ struct TopoJob {
       FSG_LAUNCHED(1);
       return FSG_OK;
     }
-    if (fixed) window_absmax<<<dim3(128, ntiles), 256, 0, s>>>(tiles_dev, reinterpret_cast<unsigned*>(flags + ntiles));
-    else window_nan_flags<<<dim3(256, ntiles), 256, 0, s>>>(tiles_dev, flags);
-    FSG_LAUNCHED(1);
+    if (fixed) {
+      if (!absmax_fused) {
+        window_absmax<<<dim3(128, ntiles), 256, 0, s>>>(tiles_dev, reinterpret_cast<unsigned*>(flags + ntiles));
+        FSG_LAUNCHED(1);
+      }
+    } else {
+      window_nan_flags<<<dim3(256, ntiles), 256, 0, s>>>(tiles_dev, flags);
+      FSG_LAUNCHED(1);
+    }
     if (fixed) timing_mark(s, true);
     kern<<<grid, threads ? threads : (fixed ? FX_NT : ST_NT), smem, s>>>(A);
     if (fixed) timing_mark(s, false);
@@ -1780,12 +1960,7 @@ static int topousm_strip_prepare_exact(const float* raster_dev, int64_t ld, cons
   }
   J.empty = J.items.empty();
   if (J.empty) return FSG_OK;
-  int nwork = 0;
-  for (int t = 0; t < ntiles; ++t) nwork += tiles[t].core_h > 0 && tiles[t].core_w > 0;
-  J.NS = dec_idx.empty() ? 0 : std::max(1, std::min(AUX_STREAMS, nwork));
-  J.one_small = (TopoScratch::bytes_small(J.maxh, J.maxw) + 255) & ~(size_t)255;
-  J.topo_bytes = (size_t)J.NS * J.one_small;
-  // per (tile, dec) coarse means and void-fill weight tables
+  // per (tile, dec) coarse means, void-fill weight tables and batched decimation items
   const size_t esz = out->dtype == FSG_F32 ? 4 : (out->dtype == FSG_I16 ? 2 : 1);
   J.tk.assign(ntiles, TopoTileK{});
   for (int t = 0; t < ntiles; ++t) {
@@ -1815,7 +1990,15 @@ static int topousm_strip_prepare_exact(const float* raster_dev, int64_t ld, cons
         const size_t go = J.gv.size();
         J.gv.insert(J.gv.end(), gw.begin(), gw.end());
         J.gv.resize((J.gv.size() + 63) & ~(size_t)63);  // 256-byte aligned tables
-        J.work.push_back({t, r, f, Rg, J.dec_bytes, go});
+        DecItem D;
+        std::memset(&D, 0, sizeof(D));
+        D.f = f;
+        D.hs = hs;
+        D.ws = ws;
+        D.rs = std::max(1, (int)std::nearbyint((double)r / f));
+        D.R = Rg;
+        J.ditems.push_back(D);
+        J.dref.push_back({t, 0, go, J.dec_bytes, d == 0});
       }
       J.dec_bytes += ((size_t)hs * ws * sizeof(float) + 255) & ~(size_t)255;
       k.dec[d].h = hs;
@@ -1825,18 +2008,61 @@ static int topousm_strip_prepare_exact(const float* raster_dev, int64_t ld, cons
       k.dec[d].weight = (float)p->weights[dec_idx[d]];
     }
   }
-  if (J.NS > 0) {
+  auto al = [](size_t n) { return (n + 255) & ~(size_t)255; };
+  if (!J.ditems.empty()) {
     int Rg;
     J.g1 = gaussian_weights(1.0, &Rg);
-    st = aux_streams(&J.aux);  // created now, outside any stream capture
-    if (st) return st;
+    // launch chunks: runs of items with the same (f, rs, R) (the row passes' shared-memory
+    // geometry follows the radius), at most nslots items each; scratch slots of four
+    // hs x ws planes (small, vm, wm, sw), up to ~1 GiB in all
+    int mh = 1, mw = 1;
+    for (const DecItem& D : J.ditems) {
+      mh = std::max(mh, D.hs);
+      mw = std::max(mw, D.ws);
+    }
+    J.slot_plane = al((size_t)mh * mw * sizeof(float));
+    J.slot_bytes = 4 * J.slot_plane;
+    const int n = (int)J.ditems.size();
+    J.nslots = (int)std::max<size_t>(1, std::min<size_t>((size_t)n, ((size_t)1 << 30) / J.slot_bytes));
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      const DecItem &x = J.ditems[a], &y = J.ditems[b];
+      return std::make_tuple(x.f, x.rs, x.R) < std::make_tuple(y.f, y.rs, y.R);
+    });
+    std::vector<DecItem> di;
+    std::vector<TopoJob::DecRef> dr;
+    for (int i : order) {
+      di.push_back(J.ditems[i]);
+      dr.push_back(J.dref[i]);
+    }
+    J.ditems.swap(di);
+    J.dref.swap(dr);
+    for (int i = 0; i < n;) {
+      const DecItem& D0 = J.ditems[i];
+      TopoJob::DecChunk c{i, 0, 1, 1, D0.rs, D0.R};
+      while (i < n && c.count < J.nslots && J.ditems[i].f == D0.f && J.ditems[i].rs == D0.rs &&
+             J.ditems[i].R == D0.R) {
+        J.dref[i].slot = c.count++;
+        c.maxhs = std::max(c.maxhs, J.ditems[i].hs);
+        c.maxws = std::max(c.maxws, J.ditems[i].ws);
+        ++i;
+      }
+      if (c.count > 65535) return fail(FSG_ERR_UNSUPPORTED, "too many decimation items in one launch");
+      J.dchunks.push_back(c);
+    }
+    // the windows' max |z| from their downsample when every window with work has one
+    // (the per-window grids cover the whole window)
+    J.absmax_fused = true;
   }
-  auto al = [](size_t n) { return (n + 255) & ~(size_t)255; };
+  J.topo_bytes = (size_t)J.nslots * J.slot_bytes;
   J.g1_off = al(J.topo_bytes + J.dec_bytes);
   J.gv_off = J.g1_off + al(J.g1.size() * sizeof(float) + 1);
   J.tiles_off = J.gv_off + al(J.gv.size() * sizeof(float) + 1);
   J.items_off = J.tiles_off + al(sizeof(TopoTileK) * ntiles);
-  J.flags_off = J.items_off + al(sizeof(StripItem) * J.items.size());
+  J.ditems_off = J.items_off + al(sizeof(StripItem) * J.items.size());
+  J.dflags_off = J.ditems_off + al(sizeof(DecItem) * J.ditems.size());
+  J.flags_off = J.dflags_off + al(sizeof(int) * J.ditems.size() + 1);
   J.total = J.flags_off + sizeof(int) * (ntiles + 1) + 256;
   StripArgs& A = J.A;
   std::memset(&A, 0, sizeof(A));
