@@ -319,6 +319,9 @@ def stencil_workload(args, rank, world, out_dtype="float32"):
     # correctness spot check of the host path against the device planes
     ok = all(torch.equal(host_out[n][::4097, ::4097].cuda().float().nan_to_num(-7.0),
                          outs[n][cy0:cy1][::4097, ::4097].float().nan_to_num(-7.0)) for n in names)
+    link = host_link(host_out[names[0]], outs[names[0]][cy0:cy1], host_dem, dem[wy0:wy1], stream)
+    link["floor_ms"] = round(max(d2h_bytes / (link["d2h_gbs"] * 1e9), h2d_bytes / (link["h2d_gbs"] * 1e9)) * 1e3, 2)
+    link["e2e_frac_of_floor"] = round(link["floor_ms"] / e2e_ms, 3)
     del host_dem, host_out
 
     line = {
@@ -352,11 +355,41 @@ def stencil_workload(args, rank, world, out_dtype="float32"):
                 "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                 "ms_per_step": round(e2e_ms, 3), "matches_device_path": bool(ok),
                 "path": "fsg_stencil_host (C ABI): pinned host DEM and planes; per row band of tiles one "
-                        "H2D block, one kernel call, one D2H block per plane, overlapped on 3 streams"},
+                        "H2D block, one kernel call, one D2H block per plane, overlapped on 3 streams",
+                "host_link": link},
         "gpu_launches": int(launches),
         "clocks": clk,
     }
     return line
+
+
+def host_link(host_a, dev_a, host_b, dev_b, stream) -> dict:
+    """Copy bandwidth of the host link in this process: one device-to-host copy of
+    ``dev_a`` into pinned ``host_a`` and one host-to-device copy of pinned ``host_b``
+    into ``dev_b``, each alone (best of three, CUDA events on ``stream``).  The e2e
+    floor is the larger of (D2H bytes / D2H rate, H2D bytes / H2D rate): the two
+    directions overlap."""
+    import torch
+
+    def best(fn):
+        t = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t.append(e0.elapsed_time(e1))
+        return min(t)
+
+    with torch.cuda.stream(stream):
+        d2h = best(lambda: host_a.copy_(dev_a, non_blocking=True))
+        h2d = best(lambda: dev_b.copy_(host_b, non_blocking=True))
+    nb_a = host_a.numel() * host_a.element_size()
+    nb_b = host_b.numel() * host_b.element_size()
+    return {"d2h_gbs": round(nb_a / (d2h * 1e-3) / 1e9, 1), "h2d_gbs": round(nb_b / (h2d * 1e-3) / 1e9, 1),
+            "probe_bytes": [nb_a, nb_b]}
 
 
 def profiled_traffic(kind: str, px: int):

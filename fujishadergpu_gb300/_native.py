@@ -115,6 +115,7 @@ _SIGNATURES = {
     "fsg_timing_begin": (C.c_int, [C.c_int32]),
     "fsg_timing_end": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "fsg_kernel_errors": (C.c_int, [C.POINTER(C.c_uint32)]),
+    "fsg_scratch_high_water": (C.c_int, [C.POINTER(C.c_uint64), C.c_int32]),
     "fsg_nodata_mask": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                   C.c_void_p, C.c_int64, C.c_void_p]),
     "fsg_stencil": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Tile), C.c_int32,

@@ -26,6 +26,10 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC] + ARCH
 
 
+# Per-source flags (none at present).
+SOURCE_FLAGS = {}
+
+
 def nvcc() -> str:
     for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and os.path.exists(cand):
@@ -51,7 +55,7 @@ def up_to_date() -> bool:
 
 def _compile(src: str, extra) -> str:
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-    cmd = [nvcc()] + NVCC_FLAGS + list(extra) + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + NVCC_FLAGS + SOURCE_FLAGS.get(os.path.basename(src), []) + list(extra) + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {os.path.basename(src)}:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

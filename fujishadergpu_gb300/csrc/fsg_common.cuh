@@ -62,7 +62,10 @@ int tc_take_errors(unsigned* flags);
 int validate_tiles(int32_t raster_h, int32_t raster_w, const fsg_tile* tiles, int32_t ntiles,
                    int min_window);
 
-// Stream-ordered scratch: cudaMallocAsync on `stream`, freed with
+// The library's stream-ordered memory pool of the current device (kept across calls).
+int scratch_pool(cudaMemPool_t* out);
+
+// Stream-ordered scratch from the library's pool on `stream`, freed with
 // cudaFreeAsync on the same stream by the destructor.
 struct StreamScratch {
   void* ptr = nullptr;
@@ -72,10 +75,13 @@ struct StreamScratch {
   StreamScratch& operator=(const StreamScratch&) = delete;
   int alloc(size_t bytes, cudaStream_t s) {
     stream = s;
-    cudaError_t e = cudaMallocAsync(&ptr, bytes ? bytes : 1, s);
+    cudaMemPool_t pool = nullptr;
+    int st = scratch_pool(&pool);
+    if (st) return st;
+    cudaError_t e = cudaMallocFromPoolAsync(&ptr, bytes ? bytes : 1, pool, s);
     if (e != cudaSuccess) {
       ptr = nullptr;
-      return cuda_fail(e, "cudaMallocAsync(scratch)");
+      return cuda_fail(e, "cudaMallocFromPoolAsync(scratch)");
     }
     return FSG_OK;
   }

@@ -582,13 +582,17 @@ struct FastArgs {
 // wait on a tensor copy ran out of polls).
 __device__ unsigned g_kernel_errors;
 
-constexpr unsigned FIX_EDGE = 0x80000000u, FIX_QSHIFT = 28, FIX_UNIT = (1u << FIX_QSHIFT) - 1u;
-// queue the quarters of unit u whose bit is set in qmask (entry = unit | quarter << 28 | edge flag)
-__device__ __forceinline__ void push_fix(const FastArgs& A, int u, bool edge, unsigned qmask) {
+// Fix-up list entry = unit | quarter << 28 | flags.  FIX_BAND: the quarter holds
+// pixels within the stencil's reach of the window edge (np.gradient's one-sided
+// formulas there); the fix-up recomputes those and the pixels whose stencil holds
+// NoData.  No flag: only the latter.
+constexpr unsigned FIX_BAND = 0x40000000u, FIX_QSHIFT = 28, FIX_UNIT = (1u << FIX_QSHIFT) - 1u;
+// queue the quarters of unit u whose bit is set in qmask
+__device__ __forceinline__ void push_fix(const FastArgs& A, int u, unsigned flags, unsigned qmask) {
   const unsigned n = __popc(qmask);
   unsigned i = atomicAdd(A.fix_count, n);
   for (unsigned q = 0; q < NQ; ++q)
-    if ((qmask >> q) & 1u) A.fix_list[i++] = (unsigned)u | (q << FIX_QSHIFT) | (edge ? FIX_EDGE : 0u);
+    if ((qmask >> q) & 1u) A.fix_list[i++] = (unsigned)u | (q << FIX_QSHIFT) | flags;
 }
 
 
@@ -634,9 +638,17 @@ __device__ __forceinline__ f2 S2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ f2 add2(f2 a, f2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ f2 sub2(f2 a, f2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 __device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
+// The same on each component with the scalar _rn intrinsics, which are never
+// contracted: for NumPy's float32 order where terms cancel (z * f[y+1] - z * f[y-1],
+// the curvature and hillshade numerators, the quantiser's a * v + b).  A paired
+// multiply followed by a paired difference was measured to give the once-rounded
+// (fused) result there, even written as PTX mul.rn.f32x2 / sub.rn.f32x2.
+__device__ __forceinline__ f2 nadd2(f2 a, f2 b) { return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)); }
+__device__ __forceinline__ f2 nsub2(f2 a, f2 b) { return make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)); }
+__device__ __forceinline__ f2 nmul2(f2 a, f2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
 // quantize_bits on a pair (the multiply, add and rounding add paired)
 __device__ __forceinline__ uint2 quantize_bits2(f2 v, float qa, float qb, float fmin, float fmax) {
-  f2 x = add2(mul2(v, S2(qa)), S2(qb));
+  f2 x = nadd2(nmul2(v, S2(qa)), S2(qb));
   x.x = isfinite(v.x) ? fminf(fmaxf(x.x, fmin), fmax) : 0.0f;
   x.y = isfinite(v.y) ? fminf(fmaxf(x.y, fmin), fmax) : 0.0f;
   const f2 t = add2(x, S2(12582912.0f));
@@ -682,8 +694,11 @@ __device__ __forceinline__ void pixel_products2(const Light& L, float slx, float
   const f2 one_g2 = add2(S2(1.0f), g2);
   f2 rs1 = S2(0.f);  // rsqrt(1 + p^2 + q^2), when the hillshade computed it
   if (om & (1u << FSG_OUT_HILLSHADE)) {
-    const f2 t = fma2(pz, S2(-slx), fma2(qz, S2(-sly), S2(L.lz)));
-    const f2 n2 = zone ? one_g2 : fma2(pz, pz, fma2(qz, qz, S2(1.0f)));
+    // numerator in NumPy's order, every operation rounded: its terms cancel where the
+    // surface faces away from the light (steep slopes, a z factor > 1); slx, sly carry
+    // the signs of the pixel scales, so pz * -slx is exactly -(e * lx)
+    const f2 t = nadd2(nadd2(nmul2(pz, S2(-slx)), nmul2(qz, S2(-sly))), S2(L.lz));
+    const f2 n2 = zone ? one_g2 : add2(add2(mul2(pz, pz), mul2(qz, qz)), S2(1.0f));
     const f2 rs = P2(rsqrt_approx(n2.x), rsqrt_approx(n2.y));
     rs1 = rs;
     o[FSG_OUT_HILLSHADE] = P2(__saturatef(t.x * rs.x), __saturatef(t.y * rs.y));
@@ -697,7 +712,7 @@ __device__ __forceinline__ void pixel_products2(const Light& L, float slx, float
   }
   if (om & CURVM) {
     constexpr float C = 1.0f / 288.53900817779268f;  // den / 288.54: t = num / den'
-    const f2 p2 = mul2(p, p), q2 = mul2(q, q), pq = mul2(p, q);
+    const f2 p2 = nmul2(p, p), q2 = nmul2(q, q), pq = nmul2(p, q);
     // (1 + p^2 + q^2)^1.5
     const f2 sq1 = (zone && (om & (1u << FSG_OUT_HILLSHADE))) ? mul2(one_g2, rs1)
                                                               : P2(sqrt_approx(one_g2.x), sqrt_approx(one_g2.y));
@@ -715,20 +730,20 @@ __device__ __forceinline__ void pixel_products2(const Light& L, float slx, float
     // terms cancel on smooth terrain, so another rounding order moves k visibly.
     if (om & (1u << FSG_OUT_CURV_MEAN)) {
       const f2 sm = mul2(add2(dxy, dyx), S2(0.5f));
-      const f2 num = add2(sub2(mul2(add2(S2(1.0f), q2), dxx), mul2(pq2, sm)), mul2(add2(S2(1.0f), p2), dyy));
+      const f2 num = nadd2(nsub2(nmul2(nadd2(S2(1.0f), q2), dxx), nmul2(pq2, sm)), nmul2(nadd2(S2(1.0f), p2), dyy));
       o[FSG_OUT_CURV_MEAN] = display(num, fma2(S2(2.0f * C), s15, S2(1e-10f * C)));
     }
     if (om & (1u << FSG_OUT_CURV_GAUSSIAN)) {
-      const f2 num = sub2(mul2(dxx, dyy), mul2(dxy, dxy));
+      const f2 num = nsub2(nmul2(dxx, dyy), nmul2(dxy, dxy));
       const f2 den = mul2(one_g2, one_g2);
       o[FSG_OUT_CURV_GAUSSIAN] = display(P2(-num.x, -num.y), mul2(den, S2(C)));
     }
     if (om & (1u << FSG_OUT_CURV_PLANFORM)) {
-      const f2 num = add2(sub2(mul2(q2, dxx), mul2(pq2, dxy)), mul2(p2, dyy));
+      const f2 num = nadd2(nsub2(nmul2(q2, dxx), nmul2(pq2, dxy)), nmul2(p2, dyy));
       o[FSG_OUT_CURV_PLANFORM] = display(num, fma2(g2c, P2(sqrt_approx(g2.x), sqrt_approx(g2.y)), S2(1e-10f * C)));
     }
     if (om & (1u << FSG_OUT_CURV_PROFILE)) {
-      const f2 num = add2(add2(mul2(p2, dxx), mul2(pq2, dxy)), mul2(q2, dyy));
+      const f2 num = nadd2(nadd2(nmul2(p2, dxx), nmul2(pq2, dxy)), nmul2(q2, dyy));
       o[FSG_OUT_CURV_PROFILE] = display(num, fma2(g2c, s15, S2(1e-10f * C)));
     }
   }
@@ -807,7 +822,6 @@ struct Q4 {
 };
 __device__ __forceinline__ Q4 q4add(Q4 a, Q4 b) { return {add2(a.lo, b.lo), add2(a.hi, b.hi)}; }
 __device__ __forceinline__ Q4 q4sub(Q4 a, Q4 b) { return {sub2(a.lo, b.lo), sub2(a.hi, b.hi)}; }
-__device__ __forceinline__ Q4 q4mul(Q4 a, f2 s) { return {mul2(a.lo, s), mul2(a.hi, s)}; }
 // f(c+1) - f(c-1) for the four columns, left = f(x-1), right = f(x+4)
 __device__ __forceinline__ Q4 q4hdiff(Q4 f, float left, float right) {
   return {sub2(P2(f.lo.y, f.hi.x), P2(left, f.lo.x)), sub2(P2(f.hi.y, right), P2(f.lo.y, f.hi.x))};
@@ -856,10 +870,10 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
     // stencil reach: rows y0-2 .. y1+1 and cols x0-2 .. xo+1 strictly inside
     // the window, so every derivative is a central difference
     const bool interior = y0 - 2 >= TG.wy0 && y1 + 2 <= TG.wy1 && x0 - 2 >= TG.wx0 && xo + 2 <= TG.wx1;
-    if (!interior) {
-      if (lane == 0) push_fix(A, u, true, (1u << NQ) - 1u);
-      continue;
-    }
+    // A unit at the window edge runs here too: the rows and columns its stencil takes
+    // from beyond the window (zeros from the tensor copy outside the raster, stale ring
+    // rows on the cp.async path, which copies nothing outside the window) reach only
+    // the pixels within the stencil's reach of the edge, which the fix-up recomputes.
     // the tile's constants as values: the plane stores below could alias the
     // tile table as far as the compiler knows, which would force reloads
     struct Step {
@@ -898,7 +912,8 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
         }
         return;
       }
-      if (k < nrows) {
+      const int ry = y0 - REACH + k;
+      if (k < nrows && ry >= TG.wy0 && ry < TG.wy1) {  // rows of the window only
         const float* gp = src0 + (long long)k * A.ld;
         const unsigned dst = sbase + (unsigned)((k % RING) * (RW * 4));
         if (vload && lfull) {
@@ -909,8 +924,10 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
             if (xl + m < T.wx1) cp_async4(dst + 16 + 4 * (4 * lane + m), gp + xl + m);
         }
         if (lane == 0) {
-          cp_async4(dst + 8, gp + x0 - 2);
-          cp_async4(dst + 12, gp + x0 - 1);
+          if (x0 - 2 >= TG.wx0) {
+            cp_async4(dst + 8, gp + x0 - 2);
+            cp_async4(dst + 12, gp + x0 - 1);
+          }
           if (x0 + SW + 1 < T.wx1) {
             cp_async4(dst + 4 * (SW + 4), gp + x0 + SW);
             cp_async4(dst + 4 * (SW + 5), gp + x0 + SW + 1);
@@ -1029,8 +1046,11 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
       Q4 pz = p, qz = q;
       if ((OM & (1u << FSG_OUT_HILLSHADE)) && !ZONE) {
         const f2 zf = S2(A.z);
-        pz = dv4(hdiff(q4mul(f0, zf), mul2(e0, zf)), T.g1x);
-        qz = dv4(q4sub(q4mul(fp1, zf), q4mul(fm1, zf)), T.g1y);
+        // z * f rounded before the difference, as NumPy's (dem * z) then np.gradient
+        auto zq = [&](Q4 f) { return Q4{nmul2(f.lo, zf), nmul2(f.hi, zf)}; };
+        pz = dv4(hdiff(zq(f0), nmul2(e0, zf)), T.g1x);
+        const Q4 zp = zq(fp1), zm = zq(fm1);
+        qz = dv4(Q4{nsub2(zp.lo, zm.lo), nsub2(zp.hi, zm.hi)}, T.g1y);
       }
       if (row_nan) {
         Q4 chk = q4add(p, q);
@@ -1124,20 +1144,30 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
       __syncwarp();
       return;
     }
-    // quarters (eight lanes each) holding a pixel whose stencil reached NoData
+    // quarters (eight lanes each) holding a pixel whose stencil reached NoData, and at a
+    // window edge the quarters holding pixels within the stencil's reach of it
     const unsigned bb = __ballot_sync(0xffffffffu, bad);
-    if (bb && lane == 0) {
-      unsigned qm = 0;
+    if (lane == 0) {
+      unsigned qm = 0, qb = 0;
       for (unsigned qq = 0; qq < NQ; ++qq) qm |= ((bb >> (8 * qq)) & 0xffu) ? (1u << qq) : 0u;
-      push_fix(A, u, false, qm);
+      if (!interior) {
+        const bool rows_band = y0 < TG.wy0 + REACH || y1 > TG.wy1 - REACH;
+        for (int qq = 0; qq < NQ; ++qq) {
+          const int qx0 = x0 + qq * FW, qx1 = min(qx0 + FW, xo);
+          if (qx0 < qx1 && (rows_band || qx0 < TG.wx0 + REACH || qx1 > TG.wx1 - REACH)) qb |= 1u << qq;
+        }
+      }
+      if (qb) push_fix(A, u, FIX_BAND, qb);
+      if (qm & ~qb) push_fix(A, u, 0u, qm & ~qb);
     }
   }
   cp_async_wait<0>();
 }
 
 // ------------------------------------------------------------- fix-up pass
-// One CTA per listed unit recomputes all of its pixels with the full
-// reference semantics in shared memory: NoData cells within reach of a valid
+// One CTA per listed quarter recomputes, with the full reference semantics in
+// shared memory, its pixels whose stencil holds NoData or (FIX_BAND) reaches the
+// window edge: NoData cells within reach of a valid
 // output pixel get the NaN-aware Gaussian fill (_nan_utils.py:18-31: separable
 // sigma = 1, radius 4, 'nearest' at the window edges, axis 0 then axis 1 with a
 // float32 intermediate, sums in float-float), then np.gradient with the
@@ -1190,7 +1220,7 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
   const unsigned count = *A.fix_count;
   for (unsigned it = blockIdx.x; it < count; it += gridDim.x) {
     const unsigned e = A.fix_list[it];
-    const bool edge = (e & FIX_EDGE) != 0;
+    const bool band = (e & FIX_BAND) != 0;
     const UnitGeom g = unit_geom(A, (int)(e & FIX_UNIT));
     const FastTile& T = A.tiles[g.t];
     const int x0 = g.x0 + (int)((e >> FIX_QSHIFT) & (NQ - 1)) * FW, y0 = g.y0, y1 = g.y1, xo = min(x0 + FW, g.xo);
@@ -1244,7 +1274,7 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
     __syncthreads();
     // (c) NoData cells within the derivative reach of a valid output pixel:
     //     2 for central differences, 3 where one-sided edge formulas occur
-    const int R = edge ? 3 : 2;
+    const int R = band ? 3 : 2;
     bool any = false;
     if (tid < XE_R) {
       unsigned long long v = 0;
@@ -1262,7 +1292,25 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
         if (tid + k >= 0 && tid + k < XE_R) nbr |= NB[tid + k];
       unsigned long long dil = nbr;
       for (int k = 1; k <= K; ++k) dil |= (nbr << k) | (nbr >> k);
-      AF[tid] = VO[tid] & dil;
+      unsigned long long af = VO[tid] & dil;
+      if (band) {  // the valid pixels within the stencil's reach of the window edge
+        constexpr int EB = CURV ? 2 : 1;
+        const int gy = y0 - 4 + tid;
+        unsigned long long bm = 0;
+        if (gy < T.wy0 + EB || gy >= T.wy1 - EB) {
+          bm = ~0ull;
+        } else {
+          auto cols = [](int a, int b) {  // E columns [a, b) clipped to [0, 64)
+            a = max(a, 0);
+            b = min(b, 64);
+            return a >= b ? 0ull : ((b - a >= 64 ? ~0ull : ((1ull << (b - a)) - 1ull)) << a);
+          };
+          const int l0 = T.wx0 - (x0 - 4), h1 = T.wx1 - (x0 - 4);
+          bm = cols(l0, l0 + EB) | cols(h1 - EB, h1);
+        }
+        af |= VO[tid] & bm;
+      }
+      AF[tid] = af;
     }
     if (__syncthreads_or(any)) {
       // (d) axis-0 sums needed by the axis-1 pass: S columns within 4 of a
@@ -1322,8 +1370,11 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
         const int r = i / XD_C, c = i - (i / XD_C) * XD_C;
         const int gy = y0 - 2 + r, gx = x0 - 2 + c;
         // an interior unit needs the derivatives within one cell of the pixels it recomputes
-        // (D row r, column c = E row r + 2, column c + 2)
-        if (!edge && !(((AF[r + 1] | AF[r + 2] | AF[r + 3]) >> (c + 1)) & 7ull)) continue;
+        // (D row r, column c = E row r + 2, column c + 2); at the window edge the one-sided
+        // second differences of the edge band reach two cells inward, through NoData too
+        if (!(((AF[r + 1] | AF[r + 2] | AF[r + 3]) >> (c + 1)) & 7ull) &&
+            !(band && (gy < T.wy0 + 4 || gy >= T.wy1 - 4 || gx < T.wx0 + 4 || gx >= T.wx1 - 4)))
+          continue;
         float dx = qnan, dy = qnan;
         if (gy >= T.wy0 && gy < T.wy1 && gx >= T.wx0 && gx < T.wx1) {
           // correctly rounded: the second differences amplify their last bit (as in the fast pass)
@@ -1335,14 +1386,14 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
       }
       __syncthreads();
     }
-    // (g) outputs of every pixel of the unit
+    // (g) outputs of the listed pixels
     const Light L{A.lx, A.ly, A.lz, A.slope_unit};
     for (int i = tid; i < SH * FW; i += XNT) {
       const int r = i / FW, c = i - (i / FW) * FW;
       const int gy = y0 + r, gx = x0 + c;
       if (gy >= y1 || gx >= xo) continue;
-      // an interior unit's other pixels keep the fast pass's values (no NoData in their stencil)
-      if (!edge && !((AF[r + 4] >> (c + 4)) & 1ull)) continue;
+      // the other pixels keep the fast pass's values (no NoData and no window edge in their stencil)
+      if (!((AF[r + 4] >> (c + 4)) & 1ull)) continue;
       float o[FSG_STENCIL_NOUT];
       const float z0 = Sv[(r + 8) * XS_C + c + 8];
       if (z0 == z0) {

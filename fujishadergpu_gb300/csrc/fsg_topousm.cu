@@ -383,11 +383,12 @@ __global__ void dec_fill(const DecItem* items) {
   const DecItem& D = items[blockIdx.z];
   if (*D.flag == 0) return;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= D.hs || j >= D.ws) return;
-  const long long o = (long long)i * D.ws + j;
-  const float c = D.small[o], w = D.sw[o];
-  if (c != c && w > 0.5f) D.small[o] = __fdiv_rn(D.ms[o], fmaxf(w, 1e-6f));
+  if (j >= D.ws) return;
+  for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < D.hs; i += gridDim.y * blockDim.y) {
+    const long long o = (long long)i * D.ws + j;
+    const float c = D.small[o], w = D.sw[o];
+    if (c != c && w > 0.5f) D.small[o] = __fdiv_rn(D.ms[o], fmaxf(w, 1e-6f));
+  }
 }
 
 // Column pass of the radius's mean: box(2 rs + 1, reflect) or Gaussian(sigma 1, nearest).
@@ -1863,16 +1864,18 @@ struct TopoJob {
       const dim3 b2(32, 8);
       const dim3 g2((c.maxws + 31) / 32, (c.maxhs + 7) / 8, c.count);
       dec_downsample<<<g2, b2, 0, s>>>(it);
-      // void fill (skipped on the device for grids without NaN cells)
-      dec_fill_cols<<<dim3((c.maxws + NT - 1) / NT, std::min(c.maxhs, 65535), c.count), NT, 0, s>>>(it);
+      // void fill (skipped on the device for grids without NaN cells; the grids of its
+      // column and combine passes stride over rows, so a skipped pass is a few blocks)
+      constexpr int FILL_ROW_BLOCKS = 64;
+      dec_fill_cols<<<dim3((c.maxws + NT - 1) / NT, std::min(c.maxhs, FILL_ROW_BLOCKS), c.count), NT, 0, s>>>(it);
       int th, tw;
       size_t smem;
       row_geometry(c.R, 1, c.maxws, &th, &tw, &smem);
       if (smem > 48 * 1024) FSG_CUDA(cudaFuncSetAttribute(dec_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       dec_rows<<<dim3((c.maxws + tw - 1) / tw, (c.maxhs + th - 1) / th, c.count), NT, smem, s>>>(it, 0, th, tw);
-      dec_fill<<<g2, b2, 0, s>>>(it);
+      dec_fill<<<dim3(g2.x, std::min<unsigned>(g2.y, FILL_ROW_BLOCKS / 8), c.count), b2, 0, s>>>(it);
       // the radius's mean
-      const int chunk = 128;  // rows per block of the box column pass (as launch_box)
+      const int chunk = 32;  // rows per block of the box column pass (its running sums are compensated)
       if (c.rs <= 1)
         dec_mean_cols<<<dim3((c.maxws + NT - 1) / NT, std::min(c.maxhs, 65535), c.count), NT, 0, s>>>(it, chunk);
       else

@@ -50,7 +50,9 @@ enum fsg_dtype { FSG_F32 = 0, FSG_U8 = 1, FSG_I16 = 2 };
  * ptr[(out_y0 + y - core_y0) * ld + (out_x0 + x - core_x0)] (see fsg_tile).
  * For FSG_U8/FSG_I16 the value is encoded as
  *   DN = clip(rint(q_a * v + q_b), q_min, q_max), non-finite v -> 0
- * (io/output_encoding.py:178-190; q_a/q_b from quantize_params :130-175). */
+ * (io/output_encoding.py:178-190; q_a/q_b from quantize_params :130-175).
+ * fsg_stencil / fsg_stencil_host require [q_min, q_max] inside the type's range
+ * ([0, 255] for FSG_U8, [-32768, 32767] for FSG_I16; FSG_ERR_INVALID otherwise). */
 typedef struct fsg_plane {
   void* ptr;          /* device pointer; NULL = output not requested */
   int64_t ld;         /* elements per row */
@@ -104,6 +106,13 @@ int fsg_timing_end(double* total_ms, int32_t* launches);
  * one of its pipeline barriers (its tiles are then incomplete).  No reference
  * counterpart. */
 int fsg_kernel_errors(uint32_t* flags);
+/* Scratch memory.  Entry points that need scratch take it stream-ordered from a
+ * memory pool the library creates per device; up to 16 GiB of freed scratch stays
+ * in the pool for the next call (the device's default pool would hand it back at
+ * every synchronisation and map it again on the next call).  This returns the
+ * pool's high-water mark of bytes in use on the current device since the last
+ * reset (reset != 0: then starts a new one).  No reference counterpart. */
+int fsg_scratch_high_water(uint64_t* bytes, int32_t reset);
 
 /* NoData mask (core/tile_processor.py:185-196): mask_dev[i] = 1 where
  * isnan(v) or (has_nodata and (|v - nodata| <= 1e-6 in float32, or v == nodata)). */
@@ -263,11 +272,12 @@ int fsg_std(const float* values_dev, int64_t n, double* out, void* stream);
  * fixed array that every GPU loading libfsg.so holds until the process exits.
  * Limits: at most 16 percentiles per call (nq > 16 -> FSG_ERR_WORKSPACE); any n.
  * The first call on a device looks up the array's device address (once per
- * device, with that device current); make that first call before any stream
- * capture.  The address stays valid for the life of the device's primary
- * context: do not call it again after cudaDeviceReset on that device.  All calls share the one array: calls that overlap on the GPU (other
- * streams, other host threads) race and must be serialised by the caller.
- * Synchronises `stream`. */
+ * device, with that device current).  The address stays valid for the life of
+ * the device's primary context: do not call it again after cudaDeviceReset on
+ * that device.  All calls share the one array: calls that overlap on the GPU
+ * (other streams, other host threads) race and must be serialised by the
+ * caller.  It synchronises `stream` (twice), so it cannot be captured into a
+ * CUDA graph. */
 int fsg_percentile_noalloc(const float* values_dev, int64_t n, int32_t abs_values, const double* q, int32_t nq,
                            double* out, int64_t* nvalid, void* stream);
 

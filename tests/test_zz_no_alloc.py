@@ -74,56 +74,24 @@ def test_noalloc_rejects_more_percentiles_than_its_array_holds(lib):
     assert e.value.code == N.FSG_ERR_WORKSPACE
 
 
-def _default_pool_high_water():
-    """(get, reset) of the used-memory high-water mark of device 0's default
-    memory pool, the pool cudaMallocAsync draws from, through the CUDA runtime
-    already loaded in this process; None when that runtime cannot be reached."""
-    lib = None
-    for name in ("libcudart.so.13", "libcudart.so"):
-        try:
-            lib = C.CDLL(name)
-            break
-        except OSError:
-            continue
-    if lib is None:
-        return None
-    pool = C.c_void_p()
-    if lib.cudaDeviceGetDefaultMemPool(C.byref(pool), C.c_int(torch.cuda.current_device())) != 0:
-        return None
-    used_mem_high = 8  # cudaMemPoolAttrUsedMemHigh
-
-    def get():
-        v = C.c_uint64()
-        assert lib.cudaMemPoolGetAttribute(pool, used_mem_high, C.byref(v)) == 0
-        return int(v.value)
-
-    def reset():
-        z = C.c_uint64(0)
-        assert lib.cudaMemPoolSetAttribute(pool, used_mem_high, C.byref(z)) == 0
-
-    try:
-        get()
-    except AssertionError:
-        return None
-    return get, reset
-
-
 def test_noalloc_draws_nothing_from_the_stream_ordered_pool(lib):
-    """The allocating entry point takes its scratch from the default pool
-    (cudaMallocAsync); the allocation-free one must leave the pool's high-water
-    mark where it was."""
-    hw = _default_pool_high_water()
-    if hw is None:
-        pytest.skip("CUDA runtime memory-pool attributes not reachable from this process")
-    get, reset = hw
+    """The allocating entry point takes its scratch from the library's stream-ordered
+    pool (fsg_scratch_high_water reports that pool's high-water mark); the
+    allocation-free one must leave the mark where it was."""
+    hw = C.c_uint64()
+
+    def get(reset=0):
+        assert lib.fsg_scratch_high_water(C.byref(hw), C.c_int32(reset)) == 0
+        return int(hw.value)
+
     x = torch.randn(100_000, device="cuda")
     torch.cuda.synchronize()
-    reset()
+    get(reset=1)
     base = get()
     _call(lib.fsg_percentile, x, [50.0, 99.0], False)
     torch.cuda.synchronize()
     assert get() > base, "control: fsg_percentile should draw its scratch from the pool"
-    reset()
+    get(reset=1)
     base = get()
     for _ in range(2):
         _call(lib.fsg_percentile_noalloc, x, [50.0, 99.0], False)
