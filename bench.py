@@ -310,12 +310,17 @@ def stencil_workload(args, rank, world, out_dtype="float32"):
     torch.cuda.synchronize()
     barrier(world)
     e2e_steps = max(2, min(args.steps, 5))
+    marks = [torch.cuda.Event(enable_timing=True) for _ in range(e2e_steps + 1)]
     e0.record(stream)
-    for _ in range(e2e_steps):
+    marks[0].record(stream)
+    for i in range(e2e_steps):
         e2e_step()
+        marks[i + 1].record(stream)
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e2e_steps, world)
+    # per-step times: single steps have run up to ~40 % slower than the steady ones
+    e2e_each = [round(marks[i].elapsed_time(marks[i + 1]), 2) for i in range(e2e_steps)]
     # correctness spot check of the host path against the device planes
     ok = all(torch.equal(host_out[n][::4097, ::4097].cuda().float().nan_to_num(-7.0),
                          outs[n][cy0:cy1][::4097, ::4097].float().nan_to_num(-7.0)) for n in names)
@@ -353,7 +358,7 @@ def stencil_workload(args, rank, world, out_dtype="float32"):
                      "step_achieved": round(step_gbs, 1), "step_frac": round(step_gbs / hbm, 4)},
         "e2e": {"value": round(px / (e2e_ms * 1e-3) / 1e6, 1), "unit": "Mpix/s",
                 "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
-                "ms_per_step": round(e2e_ms, 3), "matches_device_path": bool(ok),
+                "ms_per_step": round(e2e_ms, 3), "ms_each_step": e2e_each, "matches_device_path": bool(ok),
                 "path": "fsg_stencil_host (C ABI): pinned host DEM and planes; per row band of tiles one "
                         "H2D block, one kernel call, one D2H block per plane, overlapped on 3 streams",
                 "host_link": link},

@@ -638,17 +638,17 @@ __device__ __forceinline__ f2 S2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ f2 add2(f2 a, f2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ f2 sub2(f2 a, f2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 __device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
-// The same on each component with the scalar _rn intrinsics, which are never
-// contracted: for NumPy's float32 order where terms cancel (z * f[y+1] - z * f[y-1],
-// the curvature and hillshade numerators, the quantiser's a * v + b).  A paired
-// multiply followed by a paired difference was measured to give the once-rounded
-// (fused) result there, even written as PTX mul.rn.f32x2 / sub.rn.f32x2.
+// Sums and differences on each component with the scalar _rn intrinsics, which are
+// never contracted: for NumPy's float32 order where terms cancel (z * f[y+1] -
+// z * f[y-1], the curvature and hillshade numerators, the quantiser's a * v + b).  A
+// paired multiply followed by a paired difference was measured to give the
+// once-rounded (fused) result there, even written as PTX mul.rn.f32x2 / sub.rn.f32x2;
+// a paired product consumed by these scalar sums stays rounded.
 __device__ __forceinline__ f2 nadd2(f2 a, f2 b) { return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)); }
 __device__ __forceinline__ f2 nsub2(f2 a, f2 b) { return make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)); }
-__device__ __forceinline__ f2 nmul2(f2 a, f2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
 // quantize_bits on a pair (the multiply, add and rounding add paired)
 __device__ __forceinline__ uint2 quantize_bits2(f2 v, float qa, float qb, float fmin, float fmax) {
-  f2 x = nadd2(nmul2(v, S2(qa)), S2(qb));
+  f2 x = nadd2(mul2(v, S2(qa)), S2(qb));
   x.x = isfinite(v.x) ? fminf(fmaxf(x.x, fmin), fmax) : 0.0f;
   x.y = isfinite(v.y) ? fminf(fmaxf(x.y, fmin), fmax) : 0.0f;
   const f2 t = add2(x, S2(12582912.0f));
@@ -697,7 +697,7 @@ __device__ __forceinline__ void pixel_products2(const Light& L, float slx, float
     // numerator in NumPy's order, every operation rounded: its terms cancel where the
     // surface faces away from the light (steep slopes, a z factor > 1); slx, sly carry
     // the signs of the pixel scales, so pz * -slx is exactly -(e * lx)
-    const f2 t = nadd2(nadd2(nmul2(pz, S2(-slx)), nmul2(qz, S2(-sly))), S2(L.lz));
+    const f2 t = nadd2(nadd2(mul2(pz, S2(-slx)), mul2(qz, S2(-sly))), S2(L.lz));
     const f2 n2 = zone ? one_g2 : add2(add2(mul2(pz, pz), mul2(qz, qz)), S2(1.0f));
     const f2 rs = P2(rsqrt_approx(n2.x), rsqrt_approx(n2.y));
     rs1 = rs;
@@ -712,7 +712,7 @@ __device__ __forceinline__ void pixel_products2(const Light& L, float slx, float
   }
   if (om & CURVM) {
     constexpr float C = 1.0f / 288.53900817779268f;  // den / 288.54: t = num / den'
-    const f2 p2 = nmul2(p, p), q2 = nmul2(q, q), pq = nmul2(p, q);
+    const f2 p2 = mul2(p, p), q2 = mul2(q, q), pq = mul2(p, q);
     // (1 + p^2 + q^2)^1.5
     const f2 sq1 = (zone && (om & (1u << FSG_OUT_HILLSHADE))) ? mul2(one_g2, rs1)
                                                               : P2(sqrt_approx(one_g2.x), sqrt_approx(one_g2.y));
@@ -730,20 +730,20 @@ __device__ __forceinline__ void pixel_products2(const Light& L, float slx, float
     // terms cancel on smooth terrain, so another rounding order moves k visibly.
     if (om & (1u << FSG_OUT_CURV_MEAN)) {
       const f2 sm = mul2(add2(dxy, dyx), S2(0.5f));
-      const f2 num = nadd2(nsub2(nmul2(nadd2(S2(1.0f), q2), dxx), nmul2(pq2, sm)), nmul2(nadd2(S2(1.0f), p2), dyy));
+      const f2 num = nadd2(nsub2(mul2(nadd2(S2(1.0f), q2), dxx), mul2(pq2, sm)), mul2(nadd2(S2(1.0f), p2), dyy));
       o[FSG_OUT_CURV_MEAN] = display(num, fma2(S2(2.0f * C), s15, S2(1e-10f * C)));
     }
     if (om & (1u << FSG_OUT_CURV_GAUSSIAN)) {
-      const f2 num = nsub2(nmul2(dxx, dyy), nmul2(dxy, dxy));
+      const f2 num = nsub2(mul2(dxx, dyy), mul2(dxy, dxy));
       const f2 den = mul2(one_g2, one_g2);
       o[FSG_OUT_CURV_GAUSSIAN] = display(P2(-num.x, -num.y), mul2(den, S2(C)));
     }
     if (om & (1u << FSG_OUT_CURV_PLANFORM)) {
-      const f2 num = nadd2(nsub2(nmul2(q2, dxx), nmul2(pq2, dxy)), nmul2(p2, dyy));
+      const f2 num = nadd2(nsub2(mul2(q2, dxx), mul2(pq2, dxy)), mul2(p2, dyy));
       o[FSG_OUT_CURV_PLANFORM] = display(num, fma2(g2c, P2(sqrt_approx(g2.x), sqrt_approx(g2.y)), S2(1e-10f * C)));
     }
     if (om & (1u << FSG_OUT_CURV_PROFILE)) {
-      const f2 num = nadd2(nadd2(nmul2(p2, dxx), nmul2(pq2, dxy)), nmul2(q2, dyy));
+      const f2 num = nadd2(nadd2(mul2(p2, dxx), mul2(pq2, dxy)), mul2(q2, dyy));
       o[FSG_OUT_CURV_PROFILE] = display(num, fma2(g2c, s15, S2(1e-10f * C)));
     }
   }
@@ -1047,8 +1047,14 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
       if ((OM & (1u << FSG_OUT_HILLSHADE)) && !ZONE) {
         const f2 zf = S2(A.z);
         // z * f rounded before the difference, as NumPy's (dem * z) then np.gradient
-        auto zq = [&](Q4 f) { return Q4{nmul2(f.lo, zf), nmul2(f.hi, zf)}; };
-        pz = dv4(hdiff(zq(f0), nmul2(e0, zf)), T.g1x);
+        auto zq = [&](Q4 f) { return Q4{mul2(f.lo, zf), mul2(f.hi, zf)}; };
+        const Q4 zc = zq(f0);
+        const f2 ze = mul2(e0, zf);
+        float left = __shfl_up_sync(0xffffffffu, zc.hi.y, 1), right = __shfl_down_sync(0xffffffffu, zc.lo.x, 1);
+        if (e0lane) left = ze.y;
+        if (e31lane) right = ze.x;
+        pz = dv4(Q4{nsub2(P2(zc.lo.y, zc.hi.x), P2(left, zc.lo.x)), nsub2(P2(zc.hi.y, right), P2(zc.lo.y, zc.hi.x))},
+                 T.g1x);
         const Q4 zp = zq(fp1), zm = zq(fm1);
         qz = dv4(Q4{nsub2(zp.lo, zm.lo), nsub2(zp.hi, zm.hi)}, T.g1y);
       }
@@ -1181,9 +1187,28 @@ constexpr int XS_R = SH + 16, XS_C = FW + 16;  // 80 x 46
 constexpr int XE_R = SH + 8, XE_C = FW + 8;    // 72 x 38
 constexpr int XD_R = SH + 4, XD_C = FW + 4;    // 68 x 34
 constexpr int XNT = 256;
+constexpr int XL_ROWS = 96;  // row offsets of a compacted cell list (rows <= XS_R)
 constexpr size_t FIX_SMEM = sizeof(float) * (XS_R * XS_C + XE_R * XE_C) +
                             sizeof(float) * 2 * XE_R * XS_C +            // axis-0 sums (aliases D)
-                            sizeof(unsigned long long) * 5 * XE_R;        // row bitmasks
+                            sizeof(unsigned long long) * 5 * XE_R +       // row bitmasks
+                            sizeof(int) * XL_ROWS +                       // compacted list: row offsets
+                            sizeof(unsigned short) * XE_R * XS_C;         //   and (row << 8 | column) entries
+static_assert(XS_R <= XL_ROWS - 1 && XS_C <= 64, "compacted list: 16-bit entries, one offset slot spare");
+
+// Position of the k-th (0-based) set bit of m (k < popcount(m)).
+__device__ __forceinline__ int nth_bit64(unsigned long long m, int k) {
+  int pos = 0;
+#pragma unroll
+  for (int w = 32; w >= 1; w >>= 1) {
+    const int c = __popcll(m & ((1ull << w) - 1ull));
+    if (k >= c) {
+      k -= c;
+      m >>= w;
+      pos += w;
+    }
+  }
+  return pos;
+}
 static_assert(2 * XD_R * XD_C <= 2 * XE_R * XS_C, "derivative planes alias the axis-0 sums");
 static_assert(XE_C <= 64 && XS_C <= 64, "row bitmasks are 64 bits");
 
@@ -1214,9 +1239,48 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
   unsigned long long* ND = NB + XE_R;   // cells to fill (E columns)
   unsigned long long* NV = ND + XE_R;   // axis-0 sums to form (S columns)
   unsigned long long* AF = NV + XE_R;   // valid outputs whose stencil holds NoData (the fast pass's others stand)
+  int* LOFF = reinterpret_cast<int*>(AF + XE_R);                      // [XL_ROWS] list row offsets, total last
+  unsigned short* LST = reinterpret_cast<unsigned short*>(LOFF + XL_ROWS);  // [XE_R * XS_C] (row << 8 | column)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const bool hn = A.has_nodata != 0;
   const float qnan = __int_as_float(0x7fc00000);
+  // The cells of a stage (set bits of its per-row masks) as one list, so that every
+  // lane of a pass works on a cell that needs it: per-row counts scanned by warp 0
+  // (three rows per lane), then each warp writes its rows' columns in order.
+  // Called by every thread (two barriers); returns the number of cells.
+  auto compact = [&](int nrows, auto rowmask) -> int {
+    if (warp == 0) {
+      int c3[3], sum = 0;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const int r = 3 * lane + j;
+        c3[j] = r < nrows ? __popcll(rowmask(r)) : 0;
+        sum += c3[j];
+      }
+      int incl = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += n;
+      }
+      int base = incl - sum;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const int r = 3 * lane + j;
+        if (r < nrows) LOFF[r] = base;
+        base += c3[j];
+      }
+      if (lane == 31) LOFF[XL_ROWS - 1] = incl;
+    }
+    __syncthreads();
+    for (int r = warp; r < nrows; r += XNT / 32) {
+      const unsigned long long m = rowmask(r);
+      const int n = __popcll(m), o = LOFF[r];
+      for (int k = lane; k < n; k += 32) LST[o + k] = (unsigned short)((r << 8) | nth_bit64(m, k));
+    }
+    __syncthreads();
+    return LOFF[XL_ROWS - 1];
+  };
   const unsigned count = *A.fix_count;
   for (unsigned it = blockIdx.x; it < count; it += gridDim.x) {
     const unsigned e = A.fix_list[it];
@@ -1329,9 +1393,9 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
       FF gw[5];
 #pragma unroll
       for (int j = 0; j < 5; ++j) gw[j] = A.gw[j];
-      for (int i = tid; i < XE_R * XS_C; i += XNT) {
-        const int r = i / XS_C, sc = i - (i / XS_C) * XS_C;
-        if (!((NV[r] >> sc) & 1ull)) continue;
+      const int nv = compact(XE_R, [&](int r) { return NV[r]; });
+      for (int li = tid; li < nv; li += XNT) {
+        const int r = LST[li] >> 8, sc = LST[li] & 255, i = r * XS_C + sc;
         const int gy = y0 - 4 + r;
         float xv[9], xw[9];
 #pragma unroll
@@ -1347,9 +1411,9 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
       }
       __syncthreads();
       // (e) axis-1 pass and the normalised fill value of each cell to fill
-      for (int i = tid; i < XE_R * XE_C; i += XNT) {
-        const int r = i / XE_C, c = i - (i / XE_C) * XE_C;
-        if (!((ND[r] >> c) & 1ull)) continue;
+      const int nd = compact(XE_R, [&](int r) { return ND[r]; });
+      for (int li = tid; li < nd; li += XNT) {
+        const int r = LST[li] >> 8, c = LST[li] & 255, i = r * XE_C + c;
         const int gx = x0 - 4 + c;
         float xv[9], xw[9];
 #pragma unroll
@@ -1366,15 +1430,27 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
     auto fe = [&](int gy, int gx) { return Fv[(gy - (y0 - 4)) * XE_C + (gx - (x0 - 4))]; };
     // (f) first derivatives around the unit (curvature)
     if (CURV) {
-      for (int i = tid; i < XD_R * XD_C; i += XNT) {
-        const int r = i / XD_C, c = i - (i / XD_C) * XD_C;
+      // the derivatives within one cell of the pixels recomputed (D row r, column c = E row
+      // r + 2, column c + 2); at the window edge the one-sided second differences of the
+      // edge band reach two cells inward, through NoData too
+      const int ndv = compact(XD_R, [&](int r) {
+        const unsigned long long a3 = AF[r + 1] | AF[r + 2] | AF[r + 3];
+        unsigned long long m = (a3 >> 1) | (a3 >> 2) | (a3 >> 3);
+        if (band) {
+          const int gy = y0 - 2 + r;
+          if (gy < T.wy0 + 4 || gy >= T.wy1 - 4) {
+            m = ~0ull;
+          } else {
+            const int l1 = T.wx0 + 4 - (x0 - 2), h0 = T.wx1 - 4 - (x0 - 2);  // D columns [0, l1) and [h0, XD_C)
+            if (l1 > 0) m |= l1 >= 64 ? ~0ull : ((1ull << l1) - 1ull);
+            if (h0 < XD_C) m |= ~0ull << max(h0, 0);
+          }
+        }
+        return m & ((1ull << XD_C) - 1ull);
+      });
+      for (int li = tid; li < ndv; li += XNT) {
+        const int r = LST[li] >> 8, c = LST[li] & 255, i = r * XD_C + c;
         const int gy = y0 - 2 + r, gx = x0 - 2 + c;
-        // an interior unit needs the derivatives within one cell of the pixels it recomputes
-        // (D row r, column c = E row r + 2, column c + 2); at the window edge the one-sided
-        // second differences of the edge band reach two cells inward, through NoData too
-        if (!(((AF[r + 1] | AF[r + 2] | AF[r + 3]) >> (c + 1)) & 7ull) &&
-            !(band && (gy < T.wy0 + 4 || gy >= T.wy1 - 4 || gx < T.wx0 + 4 || gx >= T.wx1 - 4)))
-          continue;
         float dx = qnan, dy = qnan;
         if (gy >= T.wy0 && gy < T.wy1 && gx >= T.wx0 && gx < T.wx1) {
           // correctly rounded: the second differences amplify their last bit (as in the fast pass)
@@ -1388,12 +1464,12 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
     }
     // (g) outputs of the listed pixels
     const Light L{A.lx, A.ly, A.lz, A.slope_unit};
-    for (int i = tid; i < SH * FW; i += XNT) {
-      const int r = i / FW, c = i - (i / FW) * FW;
+    // (the other pixels keep the fast pass's values: no NoData and no window edge in their stencil)
+    const int no = compact(SH, [&](int r) { return (AF[r + 4] >> 4) & ((1ull << FW) - 1ull); });
+    for (int li = tid; li < no; li += XNT) {
+      const int r = LST[li] >> 8, c = LST[li] & 255;
       const int gy = y0 + r, gx = x0 + c;
       if (gy >= y1 || gx >= xo) continue;
-      // the other pixels keep the fast pass's values (no NoData and no window edge in their stencil)
-      if (!((AF[r + 4] >> (c + 4)) & 1ull)) continue;
       float o[FSG_STENCIL_NOUT];
       const float z0 = Sv[(r + 8) * XS_C + c + 8];
       if (z0 == z0) {

@@ -1875,7 +1875,7 @@ struct TopoJob {
       dec_rows<<<dim3((c.maxws + tw - 1) / tw, (c.maxhs + th - 1) / th, c.count), NT, smem, s>>>(it, 0, th, tw);
       dec_fill<<<dim3(g2.x, std::min<unsigned>(g2.y, FILL_ROW_BLOCKS / 8), c.count), b2, 0, s>>>(it);
       // the radius's mean
-      const int chunk = 32;  // rows per block of the box column pass (its running sums are compensated)
+      const int chunk = 128;  // rows per block of the box column pass (as launch_box)
       if (c.rs <= 1)
         dec_mean_cols<<<dim3((c.maxws + NT - 1) / NT, std::min(c.maxhs, 65535), c.count), NT, 0, s>>>(it, chunk);
       else
