@@ -1290,16 +1290,29 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
     const int x0 = g.x0 + (int)((e >> FIX_QSHIFT) & (NQ - 1)) * FW, y0 = g.y0, y1 = g.y1, xo = min(x0 + FW, g.xo);
     if (x0 >= xo) continue;
     // (a) source region: cells inside the window copied with cp.async (all in
-    //     flight at once), the rest NaN (never read); then NoData -> NaN
+    //     flight at once; four cells per 16-byte copy where the row allows), the
+    //     rest NaN (never read); then NoData -> NaN
     {
+      static_assert(XS_C % 4 == 0, "16-byte chunks of the source rows");
       const unsigned sv0 = (unsigned)__cvta_generic_to_shared(Sv);
-      for (int i = tid; i < XS_R * XS_C; i += XNT) {
-        const int r = i / XS_C, c = i - (i / XS_C) * XS_C;
+      for (int q = tid; q < XS_R * (XS_C / 4); q += XNT) {
+        const int r = q / (XS_C / 4), c = 4 * (q - r * (XS_C / 4)), i = r * XS_C + c;
         const int gy = y0 - 8 + r, gx = x0 - 8 + c;
-        if (gy >= T.wy0 && gy < T.wy1 && gx >= T.wx0 && gx < T.wx1)
-          cp_async4(sv0 + 4u * (unsigned)i, A.raster + (long long)gy * A.ld + gx);
-        else
-          Sv[i] = qnan;
+        if (gy < T.wy0 || gy >= T.wy1) {
+#pragma unroll
+          for (int m = 0; m < 4; ++m) Sv[i + m] = qnan;
+          continue;
+        }
+        const float* row = A.raster + (long long)gy * A.ld;
+        if (gx >= T.wx0 && gx + 3 < T.wx1 && (reinterpret_cast<uintptr_t>(row + gx) & 15) == 0) {
+          cp_async16(sv0 + 4u * (unsigned)i, row + gx);
+        } else {
+#pragma unroll
+          for (int m = 0; m < 4; ++m) {
+            if (gx + m >= T.wx0 && gx + m < T.wx1) cp_async4(sv0 + 4u * (unsigned)(i + m), row + gx + m);
+            else Sv[i + m] = qnan;
+          }
+        }
       }
       cp_async_commit();
       cp_async_wait<0>();
