@@ -1188,7 +1188,7 @@ constexpr int XE_R = SH + 8, XE_C = FW + 8;    // 72 x 38
 constexpr int XD_R = SH + 4, XD_C = FW + 4;    // 68 x 34
 constexpr int XNT = 256;
 constexpr int XL_ROWS = 96;  // row offsets of a compacted cell list (rows <= XS_R)
-constexpr size_t FIX_SMEM = sizeof(float) * (XS_R * XS_C + XE_R * XE_C) +
+constexpr size_t FIX_SMEM = sizeof(float) * XS_R * XS_C +                  // source (filled in place)
                             sizeof(float) * 2 * XE_R * XS_C +            // axis-0 sums (aliases D)
                             sizeof(unsigned long long) * 5 * XE_R +       // row bitmasks
                             sizeof(int) * XL_ROWS +                       // compacted list: row offsets
@@ -1223,14 +1223,14 @@ __device__ __forceinline__ float deriv_d(const Axis& a, int k, int lo, int hi, F
 }
 
 template <unsigned OM, bool ALLF32>
-__global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_constant__ FastArgs A) {
+__global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_constant__ FastArgs A) {
   constexpr bool CURV = (OM & ((1u << FSG_OUT_CURV_MEAN) | (1u << FSG_OUT_CURV_GAUSSIAN) |
                                (1u << FSG_OUT_CURV_PLANFORM) | (1u << FSG_OUT_CURV_PROFILE))) != 0;
   constexpr bool DIV = (OM & ((1u << FSG_OUT_DX) | (1u << FSG_OUT_DY))) != 0;
   extern __shared__ __align__(16) unsigned char fix_smem[];
+  // the source region; the fills of stage (e) go in place, so its E part is the filled surface
   float* Sv = reinterpret_cast<float*>(fix_smem);
-  float* Fv = Sv + XS_R * XS_C;
-  float* VV = Fv + XE_R * XE_C;
+  float* VV = Sv + XS_R * XS_C;
   float* VW = VV + XE_R * XS_C;
   float* DX = VV;  // reused once the fills are done
   float* DY = DX + XD_R * XD_C;
@@ -1323,8 +1323,7 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
         __syncthreads();
       }
     }
-    // (b) row bitmasks of valid output pixels and of in-window NoData cells;
-    //     E starts as a copy of the source values
+    // (b) row bitmasks of valid output pixels and of in-window NoData cells
     for (int r = warp; r < XE_R; r += XNT / 32) {
       const int gy = y0 - 4 + r;
       const bool row_out = gy >= y0 && gy < y1, row_win = gy >= T.wy0 && gy < T.wy1;
@@ -1335,7 +1334,6 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
         bool o = false, n = false;
         if (c < XE_C) {
           const float v = Sv[(r + 4) * XS_C + c + 4];
-          Fv[r * XE_C + c] = v;
           const int gx = x0 - 4 + c;
           o = row_out && gx >= x0 && gx < xo && v == v;
           n = row_win && gx >= T.wx0 && gx < T.wx1 && v != v;
@@ -1426,7 +1424,7 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
       // (e) axis-1 pass and the normalised fill value of each cell to fill
       const int nd = compact(XE_R, [&](int r) { return ND[r]; });
       for (int li = tid; li < nd; li += XNT) {
-        const int r = LST[li] >> 8, c = LST[li] & 255, i = r * XE_C + c;
+        const int r = LST[li] >> 8, c = LST[li] & 255;
         const int gx = x0 - 4 + c;
         float xv[9], xw[9];
 #pragma unroll
@@ -1436,11 +1434,11 @@ __global__ void __launch_bounds__(XNT, 3) stencil_fixup_kernel(const __grid_cons
           xw[j] = VW[r * XS_C + sc];
         }
         const float sv = gsum_ff(gw, xv), sw = gsum_ff(gw, xw);
-        Fv[i] = sw > 0.0f ? __fdiv_rn(sv, sw) : 0.0f;
+        Sv[(r + 4) * XS_C + c + 4] = sw > 0.0f ? __fdiv_rn(sv, sw) : 0.0f;  // after every read of (d)
       }
       __syncthreads();
     }
-    auto fe = [&](int gy, int gx) { return Fv[(gy - (y0 - 4)) * XE_C + (gx - (x0 - 4))]; };
+    auto fe = [&](int gy, int gx) { return Sv[(gy - (y0 - 8)) * XS_C + (gx - (x0 - 8))]; };
     // (f) first derivatives around the unit (curvature)
     if (CURV) {
       // the derivatives within one cell of the pixels recomputed (D row r, column c = E row
