@@ -397,6 +397,28 @@ def host_link(host_a, dev_a, host_b, dev_b, stream) -> dict:
             "probe_bytes": [nb_a, nb_b]}
 
 
+def profiled_value(kind: str, key: str):
+    """The number on the ``key:`` line of the committed ncu summary profiles/<kind>.txt."""
+    p = os.path.join(ROOT, "profiles", f"{kind}.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            if line.strip().startswith(key + ":"):
+                return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+def clocks_max_mhz():
+    """clocks.max.sm of GPU 0 from nvidia-smi, or None."""
+    try:
+        r = subprocess.run(["nvidia-smi", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits", "-i", "0"],
+                           capture_output=True, text=True, timeout=20)
+        return float(r.stdout.strip().splitlines()[0])
+    except Exception:
+        return None
+
+
 def profiled_traffic(kind: str, px: int):
     """DRAM read+write bytes of the dominant kernel's launch, scaled to ``px`` pixels from
     the ``dram_bytes_per_px:`` line of the committed ncu summary (None if absent)."""
@@ -501,6 +523,21 @@ def topousm_section(args):
                                        "topousm_tc (tcgen05 split-BF16 banded box means + epilogue)"),
                             "kernel_ms": round(kms, 3), "step_achieved": round(gbs, 1),
                             "step_frac": round(gbs / hbm, 4)}}
+        if path == "exact":
+            # the kernel is bound by instruction issue (64-bit integer box sums), so the
+            # HBM fraction above is small by construction: its issue roofline from the
+            # profiled instructions per pixel and the SM count and clock
+            ipx = profiled_value("topousm_hybrid_8k", "issue_slots_per_px")
+            if ipx:
+                import torch
+                prop = torch.cuda.get_device_properties(torch.cuda.current_device())
+                clk_ghz = float((clocks_max_mhz() or 2070.0)) / 1e3
+                peak_ti = prop.multi_processor_count * 4 * 32 * clk_ghz  # lane issue slots / ns
+                ach = ipx * px / (kms * 1e-3) / 1e12                     # T lane issue slots / s
+                sec["issue_roofline"] = {"bound": "issue", "issue_slots_per_px": ipx,
+                                         "achieved": round(ach, 2), "peak": round(peak_ti / 1e3, 2),
+                                         "unit": "T lane-slots/s", "frac": round(ach / (peak_ti / 1e3), 4),
+                                         "peak_kind": "SMs x 4 schedulers x 32 lanes x max SM clock"}
         if path == "tensor":
             fl = tc_issued_flops(full_res, n_cta)
             tf = fl / (kms * 1e-3) / 1e12

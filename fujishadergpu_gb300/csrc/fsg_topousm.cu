@@ -272,6 +272,7 @@ struct DecItem {
   float* ms;                    // coarse mean (hs x ws); first the void fill's numerator
   int* flag;                    // any NaN cell in small
   unsigned* zmax;               // nullable: max |z| over the window's valid cells (float bits)
+  int* tnan;                    // with zmax: set to 1 when the window holds NoData or a non-finite value
 };
 
 __device__ __forceinline__ AView dec_view(float* p, const DecItem& D) { return AView{p, D.ws, D.hs, D.ws}; }
@@ -284,6 +285,7 @@ __global__ void dec_downsample(const DecItem* items) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   float amax = 0.f;
+  bool dirty = false;  // NoData or a non-finite value among this thread's cells
   if (i < D.hs && j < D.ws) {
     float tot = 0.f, cnt = 0.f;
     const int y0 = i * D.f, x0 = j * D.f;
@@ -292,6 +294,8 @@ __global__ void dec_downsample(const DecItem* items) {
         tot = __fadd_rn(tot, v);
         cnt = __fadd_rn(cnt, 1.f);
         amax = fmaxf(amax, fabsf(v));
+      } else {
+        dirty = true;
       }
     };
     const float* p0 = D.z.p + (long long)y0 * D.z.ld + x0;
@@ -325,6 +329,7 @@ __global__ void dec_downsample(const DecItem* items) {
     if (m != m) atomicOr(D.flag, 1);
   }
   if (D.zmax) {  // block-uniform: block maximum, one atomic only where it raises the running value
+    if (__syncthreads_or(dirty) && threadIdx.x == 0 && threadIdx.y == 0) *D.tnan = 1;
     __shared__ float wmax[8];
     for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
@@ -851,10 +856,11 @@ typedef unsigned long long u64;
 
 // max |z| over the valid cells of every window, as float bits (atomicMax on
 // the bit pattern orders non-negative floats); blockIdx.y = tile.
-__global__ void window_absmax(const TopoTileK* tiles, unsigned* zmax) {
+__global__ void window_absmax(const TopoTileK* tiles, unsigned* zmax, int* nan_flags) {
   const TopoTileK& T = tiles[blockIdx.y];
   const ZView& z = T.z;
   float m[4] = {0.f, 0.f, 0.f, 0.f};
+  bool dirty = false;  // NoData or a non-finite value seen (the window's flag in nan_flags)
   for (int y = blockIdx.x; y < z.h; y += gridDim.x) {
     const float* row = z.p + (long long)y * z.ld;
     // scalar head up to a 16-byte boundary, float4 body, scalar tail
@@ -863,6 +869,7 @@ __global__ void window_absmax(const TopoTileK* tiles, unsigned* zmax) {
     for (int x = threadIdx.x; x < head; x += blockDim.x) {
       const float v = __ldg(row + x);
       if (!is_nodata(v, z.ndf, z.has_nodata != 0)) m[0] = fmaxf(m[0], fabsf(v));
+      dirty |= !isfinite(v) || is_nodata(v, z.ndf, z.has_nodata != 0);
     }
     if (((uintptr_t)row & 3) == 0) {
       const float4* r4 = reinterpret_cast<const float4*>(row + head);
@@ -870,20 +877,25 @@ __global__ void window_absmax(const TopoTileK* tiles, unsigned* zmax) {
         const float4 v = __ldg(r4 + k);
         const float e[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
+        for (int q = 0; q < 4; ++q) {
           if (!is_nodata(e[q], z.ndf, z.has_nodata != 0)) m[q] = fmaxf(m[q], fabsf(e[q]));
+          dirty |= !isfinite(e[q]) || is_nodata(e[q], z.ndf, z.has_nodata != 0);
+        }
       }
     } else {
       for (int x = head + threadIdx.x; x < head + 4 * nv; x += blockDim.x) {
         const float v = __ldg(row + x);
         if (!is_nodata(v, z.ndf, z.has_nodata != 0)) m[1] = fmaxf(m[1], fabsf(v));
+        dirty |= !isfinite(v) || is_nodata(v, z.ndf, z.has_nodata != 0);
       }
     }
     for (int x = head + 4 * nv + threadIdx.x; x < z.w; x += blockDim.x) {
       const float v = __ldg(row + x);
       if (!is_nodata(v, z.ndf, z.has_nodata != 0)) m[2] = fmaxf(m[2], fabsf(v));
+      dirty |= !isfinite(v) || is_nodata(v, z.ndf, z.has_nodata != 0);
     }
   }
+  if (__syncthreads_or(dirty) && threadIdx.x == 0) nan_flags[blockIdx.y] = 1;
   float mm = fmaxf(fmaxf(m[0], m[1]), fmaxf(m[2], m[3]));
   for (int o = 16; o > 0; o >>= 1) mm = fmaxf(mm, __shfl_xor_sync(0xffffffffu, mm, o));
   __shared__ float wm[32];
@@ -1203,7 +1215,11 @@ struct HySmem {
 };
 
 // HNT threads (>= the strip's output columns), G rows per group, MINB CTAs per SM.
-template <int NR, int HNT, int G, int MINB>
+// CLEAN: the items of windows without NoData (partition_items sorts them out with the
+// windows' flags from the pass that took their max |z|): the cells carry no valid-count
+// bits and every box holds (2r+1)^2 cells -- the same sums and means as the general
+// kernel, with fewer instructions.
+template <int NR, int HNT, int G, int MINB, bool CLEAN>
 __global__ void __launch_bounds__(HNT, MINB) topousm_hybrid(const __grid_constant__ StripArgs A) {
   static_assert(NR >= 2, "the hybrid kernel needs a ring radius and a large radius");
   extern __shared__ __align__(16) u64 fsm[];
@@ -1270,8 +1286,13 @@ __global__ void __launch_bounds__(HNT, MINB) topousm_hybrid(const __grid_constan
 #pragma unroll
       for (int m = 0; m < 8; ++m) {
         const float xv = v[m];
-        const bool ok = !is_nodata(xv, z.ndf, z.has_nodata != 0);
-        const u64 q = ok ? ((u64)__float2ll_rn(__fmul_rn(xv, sk)) << FX_CB) + 1ull : 0ull;
+        u64 q;
+        if constexpr (CLEAN) {
+          q = (u64)__float2ll_rn(__fmul_rn(xv, sk));
+        } else {
+          const bool ok = !is_nodata(xv, z.ndf, z.has_nodata != 0);
+          q = ok ? ((u64)__float2ll_rn(__fmul_rn(xv, sk)) << FX_CB) + 1ull : 0ull;
+        }
         acc += q;
         pm[m] = acc;
       }
@@ -1405,11 +1426,19 @@ __global__ void __launch_bounds__(HNT, MINB) topousm_hybrid(const __grid_constan
               }
             }
             const long long S = (long long)D[q];
-            const int cnt = (int)S & ((1 << FX_CB) - 1);
-            const float num = __fmul_rn(__ll2float_rn(S >> FX_CB), isk);
-            const float dn = (float)max(cnt, 1), rr = rcp_approx(dn);  // Markstein-corrected num / cnt
-            const float qq = __fmul_rn(num, rr);
-            const float mean = cnt > 0 ? __fmaf_rn(__fmaf_rn(-qq, dn, num), rr, qq) : 0.f;
+            float mean;
+            if constexpr (CLEAN) {  // S is the value sum, the count (2r+1)^2 ('reflect' keeps boxes full)
+              const float num = __fmul_rn(__ll2float_rn(S), isk);
+              const float dn = __fmul_rn(A.fn[q], A.fn[q]), rr = rcp_approx(dn);
+              const float qq = __fmul_rn(num, rr);
+              mean = __fmaf_rn(__fmaf_rn(-qq, dn, num), rr, qq);
+            } else {
+              const int cnt = (int)S & ((1 << FX_CB) - 1);
+              const float num = __fmul_rn(__ll2float_rn(S >> FX_CB), isk);
+              const float dn = (float)max(cnt, 1), rr = rcp_approx(dn);  // Markstein-corrected num / cnt
+              const float qq = __fmul_rn(num, rr);
+              mean = cnt > 0 ? __fmaf_rn(__fmaf_rn(-qq, dn, num), rr, qq) : 0.f;
+            }
             const float dq = __fmul_rn(wq[q], __fsub_rn(zv, mean));
             a = q == 0 ? dq : __fadd_rn(a, dq);
           }
@@ -1434,7 +1463,7 @@ __global__ void __launch_bounds__(HNT, MINB) topousm_hybrid(const __grid_constan
             a = __fadd_rn(a, __fmul_rn(Dk.weight, __fsub_rn(zv, mean)));
           }
           float v;
-          if (is_nodata(zv, z.ndf, z.has_nodata != 0)) {
+          if (!CLEAN && is_nodata(zv, z.ndf, z.has_nodata != 0)) {
             v = kQNaN;
           } else {
             float large = 0.f;
@@ -1467,6 +1496,18 @@ __global__ void __launch_bounds__(HNT, MINB) topousm_hybrid(const __grid_constan
       __syncthreads();
     }
   }
+}
+
+// The strip items split by their window's NoData flag: items of windows without
+// NoData to `clean`, the others to `dirty` (counts zeroed before the launch; the
+// order within a list does not matter: every item writes its own pixels).
+__global__ void partition_items(const StripItem* items, int n, const TopoTileK* tiles, StripItem* clean,
+                                int* nclean, StripItem* dirty, int* ndirty) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const StripItem it = items[i];
+  if (*tiles[it.tile].nan_flag == 0) clean[atomicAdd(nclean, 1)] = it;
+  else dirty[atomicAdd(ndirty, 1)] = it;
 }
 
 // flag[t] = any NoData in window t (ZView per tile); blockIdx.y = tile.
@@ -1799,6 +1840,13 @@ struct TopoJob {
          dflags_off = 0, flags_off = 0, total = 0;
   StripArgs A;
   void (*kern)(StripArgs) = nullptr;
+  // hybrid kernel split by the windows' NoData flags (split): kern = the items of windows
+  // without NoData, kern2 = the others (and every item of the tensor path's fix-up list);
+  // partition_items builds the two lists (A: clean, A2: the rest) on the device
+  bool split = false;
+  void (*kern2)(StripArgs) = nullptr;
+  StripArgs A2;
+  size_t part_off = 0;
   size_t smem = 0;
   int threads = 0;  // block size (0: FX_NT for the fixed kernels, ST_NT otherwise)
   // bound device state
@@ -1832,10 +1880,21 @@ struct TopoJob {
       D.g1 = g1d;
       D.flag = dflags + i;
       D.zmax = r.zmax ? reinterpret_cast<unsigned*>(flags + ntiles) : nullptr;
+      D.tnan = r.zmax ? flags + r.t : nullptr;
     }
     A.tiles = reinterpret_cast<const TopoTileK*>(base + tiles_off);
     A.items = reinterpret_cast<const StripItem*>(base + items_off);
     A.zmax = reinterpret_cast<const unsigned*>(flags + ntiles);
+    if (split && !tc) {  // the device-built lists of partition_items
+      int* counts = reinterpret_cast<int*>(base + part_off);
+      StripItem* lists = reinterpret_cast<StripItem*>(base + part_off + 256);
+      const size_t stride = ((sizeof(StripItem) * items.size() + 255) & ~(size_t)255) / sizeof(StripItem);
+      A2 = A;
+      A.items = lists;
+      A.nitems_dev = counts;
+      A2.items = lists + stride;
+      A2.nitems_dev = counts + 1;
+    }
     if (tc) {
       StripItem* fix = reinterpret_cast<StripItem*>(base + fix_off);
       int* fixc = reinterpret_cast<int*>(base + fixc_off);
@@ -1905,25 +1964,41 @@ struct TopoJob {
       // of the listed tiles read, otherwise the strips reach further and the windows
       // are scanned first (by the decimation's downsample when every window has one).
       if (A.R != 32 && !absmax_fused) {
-        window_absmax<<<dim3(128, ntiles), 256, 0, s>>>(tiles_dev, reinterpret_cast<unsigned*>(flags + ntiles));
+        window_absmax<<<dim3(128, ntiles), 256, 0, s>>>(tiles_dev, reinterpret_cast<unsigned*>(flags + ntiles), flags);
         FSG_LAUNCHED(1);
       }
       timing_mark(s, true);
       int st2 = tc_launch(TA, tc_smem, s);
       timing_mark(s, false);
       if (st2) return st2;
-      kern<<<grid, threads ? threads : FX_NT, smem, s>>>(A);  // the listed tiles, exact NaN-aware means
+      (split ? kern2 : kern)<<<grid, threads ? threads : FX_NT, smem, s>>>(A);  // the listed tiles, exact NaN-aware means
       FSG_LAUNCHED(1);
       return FSG_OK;
     }
     if (fixed) {
       if (!absmax_fused) {
-        window_absmax<<<dim3(128, ntiles), 256, 0, s>>>(tiles_dev, reinterpret_cast<unsigned*>(flags + ntiles));
+        window_absmax<<<dim3(128, ntiles), 256, 0, s>>>(tiles_dev, reinterpret_cast<unsigned*>(flags + ntiles), flags);
         FSG_LAUNCHED(1);
       }
     } else {
       window_nan_flags<<<dim3(256, ntiles), 256, 0, s>>>(tiles_dev, flags);
       FSG_LAUNCHED(1);
+    }
+    if (split) {
+      int* counts = reinterpret_cast<int*>(base + part_off);
+      FSG_CUDA(cudaMemsetAsync(counts, 0, 2 * sizeof(int), s));
+      const int n = (int)items.size();
+      partition_items<<<(n + 255) / 256, 256, 0, s>>>(reinterpret_cast<const StripItem*>(base + items_off), n,
+                                                      tiles_dev, const_cast<StripItem*>(A.items), counts,
+                                                      const_cast<StripItem*>(A2.items), counts + 1);
+      FSG_LAUNCHED(1);
+      timing_mark(s, true);
+      kern<<<grid, threads, smem, s>>>(A);
+      FSG_LAUNCHED(1);
+      kern2<<<grid, threads, smem, s>>>(A2);
+      FSG_LAUNCHED(1);
+      timing_mark(s, false);
+      return FSG_OK;
     }
     if (fixed) timing_mark(s, true);
     kern<<<grid, threads ? threads : (fixed ? FX_NT : ST_NT), smem, s>>>(A);
@@ -2066,7 +2141,9 @@ static int topousm_strip_prepare_exact(const float* raster_dev, int64_t ld, cons
   J.ditems_off = J.items_off + al(sizeof(StripItem) * J.items.size());
   J.dflags_off = J.ditems_off + al(sizeof(DecItem) * J.ditems.size());
   J.flags_off = J.dflags_off + al(sizeof(int) * J.ditems.size() + 1);
-  J.total = J.flags_off + sizeof(int) * (ntiles + 1) + 256;
+  // the split of the items by NoData (hybrid kernel): two counts, then the two lists
+  J.part_off = al(J.flags_off + sizeof(int) * (ntiles + 1));
+  J.total = J.part_off + 256 + 2 * al(sizeof(StripItem) * J.items.size()) + 256;
   StripArgs& A = J.A;
   std::memset(&A, 0, sizeof(A));
   A.nitems = (int)J.items.size();
@@ -2106,23 +2183,32 @@ static int topousm_strip_prepare_exact(const float* raster_dev, int64_t ld, cons
     const int hy_ring = 2 * Rs + HG + 1;
     const size_t hsmem = HySmem::bytes(hy_ring, HG);
     if ((narrow ? 3 : 2) * (hsmem + 1024) <= (size_t)di.smem_per_sm && nfull <= HY_MAXNR) {
+      // two launches over device-built item lists: the items of windows without NoData
+      // (CLEAN arithmetic), then the rest; the tensor path's fix-up takes the general kernel
       if (narrow) {
         switch (nfull) {
-          case 2: J.kern = topousm_hybrid<2, 192, 4, 3>; break;
-          case 3: J.kern = topousm_hybrid<3, 192, 4, 3>; break;
-          default: J.kern = topousm_hybrid<4, 192, 4, 3>; break;
+          case 2: J.kern = topousm_hybrid<2, 192, 4, 3, true>; J.kern2 = topousm_hybrid<2, 192, 4, 3, false>;
+                  J.split = true; break;
+          case 3: J.kern = topousm_hybrid<3, 192, 4, 3, true>; J.kern2 = topousm_hybrid<3, 192, 4, 3, false>;
+                  J.split = true; break;
+          default: J.kern = topousm_hybrid<4, 192, 4, 3, true>; J.kern2 = topousm_hybrid<4, 192, 4, 3, false>;
+                   J.split = true; break;
         }
       } else {
         switch (nfull) {
-          case 2: J.kern = topousm_hybrid<2, 256, 8, 2>; break;
-          case 3: J.kern = topousm_hybrid<3, 256, 8, 2>; break;
-          default: J.kern = topousm_hybrid<4, 256, 8, 2>; break;
+          case 2: J.kern = topousm_hybrid<2, 256, 8, 2, true>; J.kern2 = topousm_hybrid<2, 256, 8, 2, false>;
+                  J.split = true; break;
+          case 3: J.kern = topousm_hybrid<3, 256, 8, 2, true>; J.kern2 = topousm_hybrid<3, 256, 8, 2, false>;
+                  J.split = true; break;
+          default: J.kern = topousm_hybrid<4, 256, 8, 2, true>; J.kern2 = topousm_hybrid<4, 256, 8, 2, false>;
+                   J.split = true; break;
         }
       }
       J.threads = narrow ? 192 : 256;
       A.ring = hy_ring;
       J.smem = hsmem;
       FSG_CUDA(cudaFuncSetAttribute(J.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)J.smem));
+      FSG_CUDA(cudaFuncSetAttribute(J.kern2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)J.smem));
       int per = 0;
       FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, J.kern, J.threads, J.smem));
       J.grid = std::min((int)J.items.size(), di.sms * std::max(1, per));
