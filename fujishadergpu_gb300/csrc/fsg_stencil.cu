@@ -694,10 +694,9 @@ __device__ __forceinline__ void pixel_products2(const Light& L, float slx, float
   const f2 one_g2 = add2(S2(1.0f), g2);
   f2 rs1 = S2(0.f);  // rsqrt(1 + p^2 + q^2), when the hillshade computed it
   if (om & (1u << FSG_OUT_HILLSHADE)) {
-    // numerator in NumPy's order, every operation rounded: its terms cancel where the
-    // surface faces away from the light (steep slopes, a z factor > 1); slx, sly carry
-    // the signs of the pixel scales, so pz * -slx is exactly -(e * lx)
-    const f2 t = nadd2(nadd2(mul2(pz, S2(-slx)), mul2(qz, S2(-sly))), S2(L.lz));
+    // the reference forms the numerator in float64 (its light vector is a float64
+    // scalar): two fused multiply-adds stay closer to that than four roundings
+    const f2 t = fma2(pz, S2(-slx), fma2(qz, S2(-sly), S2(L.lz)));
     const f2 n2 = zone ? one_g2 : add2(add2(mul2(pz, pz), mul2(qz, qz)), S2(1.0f));
     const f2 rs = P2(rsqrt_approx(n2.x), rsqrt_approx(n2.y));
     rs1 = rs;
