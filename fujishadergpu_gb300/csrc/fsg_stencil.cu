@@ -569,9 +569,10 @@ struct FastArgs {
   int slope_unit;
   const FastTile* tiles;
   int ntiles, total_units;
-  unsigned* fix_list;   // unit quarters for the fix-up pass: unit | quarter << 28 | FIX_EDGE (touches a window edge)
+  unsigned* fix_list;   // unit quarters for the fix-up pass: unit | quarter << 28 | FIX_BAND
   unsigned* fix_count;  // number of entries in fix_list
   unsigned* queue;      // work queue: next unit of the flattened tile list (zeroed per launch)
+  unsigned* fix_queue;  // work queue of the fix-up pass: next entry of fix_list (zeroed per launch)
   FF gw[5];                   // Gaussian fill weights (float-float)
   PlaneK planes[FSG_STENCIL_NOUT];
   int use_tma;                // tmap describes the raster (16-byte aligned base and row pitch)
@@ -1281,7 +1282,14 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
     return LOFF[XL_ROWS - 1];
   };
   const unsigned count = *A.fix_count;
-  for (unsigned it = blockIdx.x; it < count; it += gridDim.x) {
+  // listed quarters popped from a queue (their costs differ: NoData fills, edge bands)
+  __shared__ unsigned s_it;
+  for (;;) {
+    if (tid == 0) s_it = atomicAdd(A.fix_queue, 1u);
+    __syncthreads();
+    const unsigned it = s_it;
+    __syncthreads();  // every thread has the entry before the next pop overwrites it
+    if (it >= count) break;
     const unsigned e = A.fix_list[it];
     const bool band = (e & FIX_BAND) != 0;
     const UnitGeom g = unit_geom(A, (int)(e & FIX_UNIT));
@@ -1623,7 +1631,7 @@ struct StencilJob {
     return fast ? (sizeof(FastTile) * ft.size() + 255) & ~(size_t)255
                 : (tk.size() > (size_t)INLINE_TILES ? (sizeof(TileK) * tk.size() + 255) & ~(size_t)255 : 0);
   }
-  size_t device_bytes() const { return tiles_bytes() + (fast ? sizeof(unsigned) * ((size_t)NQ * units + 2) : 0); }
+  size_t device_bytes() const { return tiles_bytes() + (fast ? sizeof(unsigned) * ((size_t)NQ * units + 3) : 0); }
   // point the kernel arguments at the tables / fix-up list in `dev`
   void bind(void* dev) {
     if (fast) {
@@ -1631,7 +1639,8 @@ struct StencilJob {
       F.tiles = static_cast<const FastTile*>(dev);
       F.fix_count = fix;
       F.queue = fix + 1;
-      F.fix_list = fix + 2;
+      F.fix_queue = fix + 2;
+      F.fix_list = fix + 3;
     } else if (tk.size() > (size_t)INLINE_TILES) {
       A.tiles_dev = static_cast<const TileK*>(dev);
     }
@@ -1671,7 +1680,7 @@ struct StencilJob {
   int enqueue(cudaStream_t s) const {
     if (empty) return FSG_OK;
     if (fast) {
-      FSG_CUDA(cudaMemsetAsync(F.fix_count, 0, 2 * sizeof(unsigned), s));  // fix-up count and queue head
+      FSG_CUDA(cudaMemsetAsync(F.fix_count, 0, 3 * sizeof(unsigned), s));  // fix-up count and both queue heads
       timing_mark(s, true);
       fastk<<<fgrid, FSG_FAST_NT, FAST_SMEM, s>>>(F);
       timing_mark(s, false);
