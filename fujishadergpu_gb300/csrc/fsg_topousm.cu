@@ -1794,6 +1794,23 @@ static bool strip_path_ok(const std::vector<int>& radii, double pixel_size, int*
   return true;
 }
 
+// A second stream per device, on which the strip kernel over the windows with NoData
+// runs beside the one over the windows without (their items are disjoint): one after
+// the other, two half-full waves of a small job would take two wave times.  Created
+// once per device, outside any stream capture; each job forks and joins it with its
+// own events.
+static int side_stream(cudaStream_t* out) {
+  static std::mutex mu;
+  static cudaStream_t pool[64] = {};
+  int dev = 0;
+  FSG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(FSG_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(mu);
+  if (!pool[dev]) FSG_CUDA(cudaStreamCreateWithFlags(&pool[dev], cudaStreamNonBlocking));
+  *out = pool[dev];
+  return FSG_OK;
+}
+
 // One topousm_fast strip-path job: host images of every device table (tile
 // descriptors, strip items, Gaussian weight tables), the layout of its device
 // buffer and the launch parameters.  The eager entry point uploads the images
@@ -1806,6 +1823,8 @@ struct TopoJob {
   TopoJob& operator=(const TopoJob&) = delete;
   ~TopoJob() {
     if (TA) tc_release(TA);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
   }
   bool empty = true, fixed = false;
   // tensor-core path (fsg_topousm_tc.cu): its CTA tiles, the device-built list of
@@ -1847,6 +1866,8 @@ struct TopoJob {
   void (*kern2)(StripArgs) = nullptr;
   StripArgs A2;
   size_t part_off = 0;
+  cudaStream_t side = nullptr;  // kern2 runs here, beside kern
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   size_t smem = 0;
   int threads = 0;  // block size (0: FX_NT for the fixed kernels, ST_NT otherwise)
   // bound device state
@@ -1993,10 +2014,14 @@ struct TopoJob {
                                                       const_cast<StripItem*>(A2.items), counts + 1);
       FSG_LAUNCHED(1);
       timing_mark(s, true);
+      FSG_CUDA(cudaEventRecord(fork_ev, s));
+      FSG_CUDA(cudaStreamWaitEvent(side, fork_ev, 0));
       kern<<<grid, threads, smem, s>>>(A);
       FSG_LAUNCHED(1);
-      kern2<<<grid, threads, smem, s>>>(A2);
+      kern2<<<grid, threads, smem, side>>>(A2);
       FSG_LAUNCHED(1);
+      FSG_CUDA(cudaEventRecord(join_ev, side));
+      FSG_CUDA(cudaStreamWaitEvent(s, join_ev, 0));
       timing_mark(s, false);
       return FSG_OK;
     }
@@ -2209,6 +2234,10 @@ static int topousm_strip_prepare_exact(const float* raster_dev, int64_t ld, cons
       J.smem = hsmem;
       FSG_CUDA(cudaFuncSetAttribute(J.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)J.smem));
       FSG_CUDA(cudaFuncSetAttribute(J.kern2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)J.smem));
+      st = side_stream(&J.side);
+      if (st) return st;
+      FSG_CUDA(cudaEventCreateWithFlags(&J.fork_ev, cudaEventDisableTiming));
+      FSG_CUDA(cudaEventCreateWithFlags(&J.join_ev, cudaEventDisableTiming));
       int per = 0;
       FSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, J.kern, J.threads, J.smem));
       J.grid = std::min((int)J.items.size(), di.sms * std::max(1, per));

@@ -101,3 +101,24 @@ def test_openness_ray_offsets_match_numpy(built_lib, ndir, dist):
             for (x, y) in ray:
                 assert (ox[k], oy[k]) == (x, y), (mode, d, k)
                 k += 1
+
+
+@pytest.mark.parametrize("dtype,qmin,qmax", [("uint8", 0, 300), ("uint8", -1, 255), ("int16", -40000, 32767),
+                                             ("int16", -32768, 40000)])
+def test_stencil_rejects_code_ranges_outside_the_type(built_lib, dtype, qmin, qmax):
+    """Integer planes store codes clamped to [q_min, q_max]: a range outside the type is
+    rejected (FSG_ERR_INVALID) before the call touches the device, so the call returns
+    without reading its pointers (placeholders here)."""
+    import ctypes as C
+    from fujishadergpu_gb300 import _native as N
+    from fujishadergpu_gb300.algorithms import _stencil as S
+    planes = (N.Plane * N.FSG_STENCIL_NOUT)()
+    planes[0].ptr = 0x100000
+    planes[0].ld = 64
+    planes[0].dtype = N.DTYPE_CODES[dtype]
+    planes[0].q_a, planes[0].q_b, planes[0].q_min, planes[0].q_max = 1.0, 0.0, qmin, qmax
+    tiles = (N.Tile * 1)(S.whole_window_tile(64, 64, 1.0, -1.0))
+    params = S.make_params(pixel_size=1.0)
+    st = N.lib().fsg_stencil(C.c_void_p(0x200000), 64, 64, 64, tiles, 1, C.byref(params), planes, None)
+    assert st == -1, st
+    assert b"code range" in N.lib().fsg_last_error()
