@@ -1183,9 +1183,9 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
 //   E  filled values        rows -4 .. SH+4, cols -4 .. FW+4
 //   D  first derivatives    rows -2 .. SH+2, cols -2 .. FW+2 (curvature only)
 // for each quarter (FW columns) of the unit.
-constexpr int XS_R = SH + 16, XS_C = FW + 16;  // 80 x 46
-constexpr int XE_R = SH + 8, XE_C = FW + 8;    // 72 x 38
-constexpr int XD_R = SH + 4, XD_C = FW + 4;    // 68 x 34
+constexpr int XS_R = SH + 16, XS_C = FW + 16;  // 80 x 48
+constexpr int XE_R = SH + 8, XE_C = FW + 8;    // 72 x 40
+constexpr int XD_R = SH + 4, XD_C = FW + 4;    // 68 x 36
 constexpr int XNT = 256;
 constexpr int XL_ROWS = 96;  // row offsets of a compacted cell list (rows <= XS_R)
 constexpr size_t FIX_SMEM = sizeof(float) * XS_R * XS_C +                  // source (filled in place)
@@ -1210,6 +1210,9 @@ __device__ __forceinline__ int nth_bit64(unsigned long long m, int k) {
   return pos;
 }
 static_assert(2 * XD_R * XD_C <= 2 * XE_R * XS_C, "derivative planes alias the axis-0 sums");
+// the output list of stage (g) sits after the derivative planes, in the axis-0 sums' tail
+constexpr int XG_OFF = 2 * XD_R * XD_C;
+static_assert(XG_OFF + XL_ROWS + (SH * FW + 1) / 2 <= 2 * XE_R * XS_C, "output list in the sums' tail");
 static_assert(XE_C <= 64 && XS_C <= 64, "row bitmasks are 64 bits");
 
 template <bool DIV, class Fn>
@@ -1245,57 +1248,77 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
   const bool hn = A.has_nodata != 0;
   const float qnan = __int_as_float(0x7fc00000);
   // The cells of a stage (set bits of its per-row masks) as one list, so that every
-  // lane of a pass works on a cell that needs it: per-row counts scanned by warp 0
+  // lane of a pass works on a cell that needs it: per-row counts scanned by one warp
   // (three rows per lane), then each warp writes its rows' columns in order.
-  // Called by every thread (two barriers); returns the number of cells.
-  auto compact = [&](int nrows, auto rowmask) -> int {
-    if (warp == 0) {
-      int c3[3], sum = 0;
+  // compact / compact2 are called by every thread (two barriers) and return the
+  // number of cells.
+  auto scan_rows = [&](int nrows, auto rowmask, int* loff) {  // one warp: per-row counts -> offsets, total last
+    int c3[3], sum = 0;
 #pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        const int r = 3 * lane + j;
-        c3[j] = r < nrows ? __popcll(rowmask(r)) : 0;
-        sum += c3[j];
-      }
-      int incl = sum;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int n = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += n;
-      }
-      int base = incl - sum;
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        const int r = 3 * lane + j;
-        if (r < nrows) LOFF[r] = base;
-        base += c3[j];
-      }
-      if (lane == 31) LOFF[XL_ROWS - 1] = incl;
+    for (int j = 0; j < 3; ++j) {
+      const int r = 3 * lane + j;
+      c3[j] = r < nrows ? __popcll(rowmask(r)) : 0;
+      sum += c3[j];
     }
-    __syncthreads();
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int n = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += n;
+    }
+    int base = incl - sum;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int r = 3 * lane + j;
+      if (r < nrows) loff[r] = base;
+      base += c3[j];
+    }
+    if (lane == 31) loff[XL_ROWS - 1] = incl;
+  };
+  auto write_rows = [&](int nrows, auto rowmask, const int* loff, unsigned short* lst) {  // every warp
     for (int r = warp; r < nrows; r += XNT / 32) {
       const unsigned long long m = rowmask(r);
-      const int n = __popcll(m), o = LOFF[r];
-      for (int k = lane; k < n; k += 32) LST[o + k] = (unsigned short)((r << 8) | nth_bit64(m, k));
+      const int n = __popcll(m), o = loff[r];
+      for (int k = lane; k < n; k += 32) lst[o + k] = (unsigned short)((r << 8) | nth_bit64(m, k));
     }
+  };
+  auto compact = [&](int nrows, auto rowmask) -> int {
+    if (warp == 0) scan_rows(nrows, rowmask, LOFF);
+    __syncthreads();
+    write_rows(nrows, rowmask, LOFF, LST);
     __syncthreads();
     return LOFF[XL_ROWS - 1];
   };
-  const unsigned count = *A.fix_count;
-  // listed quarters popped from a queue (their costs differ: NoData fills, edge bands)
-  __shared__ unsigned s_it;
-  for (;;) {
-    if (tid == 0) s_it = atomicAdd(A.fix_queue, 1u);
+  // two lists in one pass (two barriers instead of four)
+  auto compact2 = [&](int na, auto ma, int nb, auto mb, int* loffb, unsigned short* lstb) -> int2 {
+    if (warp == 0) scan_rows(na, ma, LOFF);
+    else if (warp == 1) scan_rows(nb, mb, loffb);
     __syncthreads();
+    write_rows(na, ma, LOFF, LST);
+    write_rows(nb, mb, loffb, lstb);
+    __syncthreads();
+    return make_int2(LOFF[XL_ROWS - 1], loffb[XL_ROWS - 1]);
+  };
+  const unsigned count = *A.fix_count;
+  // listed quarters popped from a queue (their costs differ: NoData fills, edge bands);
+  // the next entry is popped after the first barrier of the current one
+  __shared__ unsigned s_it;
+  if (tid == 0) s_it = atomicAdd(A.fix_queue, 1u);
+  __syncthreads();
+  for (;;) {
     const unsigned it = s_it;
-    __syncthreads();  // every thread has the entry before the next pop overwrites it
     if (it >= count) break;
     const unsigned e = A.fix_list[it];
     const bool band = (e & FIX_BAND) != 0;
     const UnitGeom g = unit_geom(A, (int)(e & FIX_UNIT));
     const FastTile& T = A.tiles[g.t];
     const int x0 = g.x0 + (int)((e >> FIX_QSHIFT) & (NQ - 1)) * FW, y0 = g.y0, y1 = g.y1, xo = min(x0 + FW, g.xo);
-    if (x0 >= xo) continue;
+    if (x0 >= xo) {  // (not listed by the streaming pass; kept safe)
+      __syncthreads();
+      if (tid == 0) s_it = atomicAdd(A.fix_queue, 1u);
+      __syncthreads();
+      continue;
+    }
     // (a) source region: cells inside the window copied with cp.async (all in
     //     flight at once; four cells per 16-byte copy where the row allows), the
     //     rest NaN (never read); then NoData -> NaN
@@ -1323,12 +1346,15 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
       }
       cp_async_commit();
       cp_async_wait<0>();
-      __syncthreads();
-      if (hn) {
-        for (int i = tid; i < XS_R * XS_C; i += XNT)
-          if (is_nodata(Sv[i], A.ndf, true)) Sv[i] = qnan;
-        __syncthreads();
+      if (hn) {  // each thread its own copies (complete and visible to it after the wait)
+        for (int q = tid; q < XS_R * (XS_C / 4); q += XNT) {
+#pragma unroll
+          for (int m = 0; m < 4; ++m)
+            if (is_nodata(Sv[4 * q + m], A.ndf, true)) Sv[4 * q + m] = qnan;
+        }
       }
+      __syncthreads();
+      if (tid == 0) s_it = atomicAdd(A.fix_queue, 1u);  // every thread has read this entry
     }
     // (b) row bitmasks of valid output pixels and of in-window NoData cells
     for (int r = warp; r < XE_R; r += XNT / 32) {
@@ -1367,6 +1393,16 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
       const unsigned long long need = d & NB[tid];
       ND[tid] = need;
       any = need != 0;
+      {  // axis-0 sums needed by the axis-1 pass: S columns within 4 of a cell to fill, inside the window
+        const unsigned long long n = need << 4;
+        unsigned long long dn = n;
+#pragma unroll
+        for (int k = 1; k <= 4; ++k) dn |= (n << k) | (n >> k);
+        const int c_lo = max(T.wx0 - (x0 - 8), 0), c_hi = min(T.wx1 - (x0 - 8), XS_C);
+        const unsigned long long win =
+            c_hi > c_lo ? (((c_hi - c_lo) >= 64 ? ~0ull : ((1ull << (c_hi - c_lo)) - 1ull)) << c_lo) : 0ull;
+        NV[tid] = dn & win;
+      }
       // outputs whose stencil footprint (a (2K+1)^2 box) contains a NoData cell
       constexpr int K = CURV ? 2 : 1;
       unsigned long long nbr = 0;
@@ -1395,19 +1431,7 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
       AF[tid] = af;
     }
     if (__syncthreads_or(any)) {
-      // (d) axis-0 sums needed by the axis-1 pass: S columns within 4 of a
-      //     cell to fill, inside the window
-      if (tid < XE_R) {
-        const unsigned long long n = ND[tid] << 4;
-        unsigned long long d = n;
-#pragma unroll
-        for (int k = 1; k <= 4; ++k) d |= (n << k) | (n >> k);
-        const int c_lo = max(T.wx0 - (x0 - 8), 0), c_hi = min(T.wx1 - (x0 - 8), XS_C);
-        const unsigned long long win =
-            c_hi > c_lo ? (((c_hi - c_lo) >= 64 ? ~0ull : ((1ull << (c_hi - c_lo)) - 1ull)) << c_lo) : 0ull;
-        NV[tid] = d & win;
-      }
-      __syncthreads();
+      // (d) axis-0 sums of the S cells listed in NV
       FF gw[5];
 #pragma unroll
       for (int j = 0; j < 5; ++j) gw[j] = A.gw[j];
@@ -1446,12 +1470,19 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
       __syncthreads();
     }
     auto fe = [&](int gy, int gx) { return Sv[(gy - (y0 - 8)) * XS_C + (gx - (x0 - 8))]; };
-    // (f) first derivatives around the unit (curvature)
+    // (f) first derivatives around the unit (curvature) and (g) the outputs: both
+    //     cell lists built in one pass, (g)'s after the derivative planes
+    int* LOFF_G = reinterpret_cast<int*>(VV + XG_OFF);
+    unsigned short* LST_G = reinterpret_cast<unsigned short*>(LOFF_G + XL_ROWS);
+    // (g) lists the pixels recomputed; the other pixels keep the fast pass's values (no
+    // NoData and no window edge in their stencil)
+    auto out_rows = [&](int r) { return (AF[r + 4] >> 4) & ((1ull << FW) - 1ull); };
+    int no;
     if (CURV) {
       // the derivatives within one cell of the pixels recomputed (D row r, column c = E row
       // r + 2, column c + 2); at the window edge the one-sided second differences of the
       // edge band reach two cells inward, through NoData too
-      const int ndv = compact(XD_R, [&](int r) {
+      const int2 cnt = compact2(XD_R, [&](int r) {
         const unsigned long long a3 = AF[r + 1] | AF[r + 2] | AF[r + 3];
         unsigned long long m = (a3 >> 1) | (a3 >> 2) | (a3 >> 3);
         if (band) {
@@ -1465,7 +1496,9 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
           }
         }
         return m & ((1ull << XD_C) - 1ull);
-      });
+      }, SH, out_rows, LOFF_G, LST_G);
+      const int ndv = cnt.x;
+      no = cnt.y;
       for (int li = tid; li < ndv; li += XNT) {
         const int r = LST[li] >> 8, c = LST[li] & 255, i = r * XD_C + c;
         const int gy = y0 - 2 + r, gx = x0 - 2 + c;
@@ -1479,13 +1512,16 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
         DY[i] = dy;
       }
       __syncthreads();
+    } else {
+      if (warp == 0) scan_rows(SH, out_rows, LOFF_G);
+      __syncthreads();
+      write_rows(SH, out_rows, LOFF_G, LST_G);
+      __syncthreads();
+      no = LOFF_G[XL_ROWS - 1];
     }
-    // (g) outputs of the listed pixels
     const Light L{A.lx, A.ly, A.lz, A.slope_unit};
-    // (the other pixels keep the fast pass's values: no NoData and no window edge in their stencil)
-    const int no = compact(SH, [&](int r) { return (AF[r + 4] >> 4) & ((1ull << FW) - 1ull); });
     for (int li = tid; li < no; li += XNT) {
-      const int r = LST[li] >> 8, c = LST[li] & 255;
+      const int r = LST_G[li] >> 8, c = LST_G[li] & 255;
       const int gy = y0 + r, gx = x0 + c;
       if (gy >= y1 || gx >= xo) continue;
       float o[FSG_STENCIL_NOUT];
