@@ -1194,21 +1194,8 @@ constexpr size_t FIX_SMEM = sizeof(float) * XS_R * XS_C +                  // so
                             sizeof(int) * XL_ROWS +                       // compacted list: row offsets
                             sizeof(unsigned short) * XE_R * XS_C;         //   and (row << 8 | column) entries
 static_assert(XS_R <= XL_ROWS - 1 && XS_C <= 64, "compacted list: 16-bit entries, one offset slot spare");
+static_assert(XE_R <= 128 && 128 + XE_R <= XNT, "stage (c): one E row per thread in warps 0-3 and in warps 4-7");
 
-// Position of the k-th (0-based) set bit of m (k < popcount(m)).
-__device__ __forceinline__ int nth_bit64(unsigned long long m, int k) {
-  int pos = 0;
-#pragma unroll
-  for (int w = 32; w >= 1; w >>= 1) {
-    const int c = __popcll(m & ((1ull << w) - 1ull));
-    if (k >= c) {
-      k -= c;
-      m >>= w;
-      pos += w;
-    }
-  }
-  return pos;
-}
 static_assert(2 * XD_R * XD_C <= 2 * XE_R * XS_C, "derivative planes alias the axis-0 sums");
 // the output list of stage (g) sits after the derivative planes, in the axis-0 sums' tail
 constexpr int XG_OFF = 2 * XD_R * XD_C;
@@ -1249,15 +1236,20 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
   const float qnan = __int_as_float(0x7fc00000);
   // The cells of a stage (set bits of its per-row masks) as one list, so that every
   // lane of a pass works on a cell that needs it: per-row counts scanned by one warp
-  // (three rows per lane), then each warp writes its rows' columns in order.
-  // compact / compact2 are called by every thread (two barriers) and return the
-  // number of cells.
-  auto scan_rows = [&](int nrows, auto rowmask, int* loff) {  // one warp: per-row counts -> offsets, total last
+  // (three rows per lane; the masks kept in `keep` when given), then each warp writes
+  // its rows, each lane the entry of its column (position = the set bits below it).
+  // compact is called by every thread (two barriers) and returns the number of cells.
+  auto scan_rows = [&](int nrows, auto rowmask, int* loff, unsigned long long* keep) {
     int c3[3], sum = 0;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       const int r = 3 * lane + j;
-      c3[j] = r < nrows ? __popcll(rowmask(r)) : 0;
+      unsigned long long m = 0;
+      if (r < nrows) {
+        m = rowmask(r);
+        if (keep) keep[r] = m;
+      }
+      c3[j] = __popcll(m);
       sum += c3[j];
     }
     int incl = sum;
@@ -1275,29 +1267,24 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
     }
     if (lane == 31) loff[XL_ROWS - 1] = incl;
   };
-  auto write_rows = [&](int nrows, auto rowmask, const int* loff, unsigned short* lst) {  // every warp
+  auto write_rows = [&](int nrows, auto rowmask, const int* loff, unsigned short* lst) {
     for (int r = warp; r < nrows; r += XNT / 32) {
       const unsigned long long m = rowmask(r);
-      const int n = __popcll(m), o = loff[r];
-      for (int k = lane; k < n; k += 32) lst[o + k] = (unsigned short)((r << 8) | nth_bit64(m, k));
+      const int o = loff[r];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int c = 32 * h + lane;
+        if ((m >> c) & 1ull) lst[o + __popcll(m & ((1ull << c) - 1ull))] = (unsigned short)((r << 8) | c);
+      }
     }
   };
-  auto compact = [&](int nrows, auto rowmask) -> int {
-    if (warp == 0) scan_rows(nrows, rowmask, LOFF);
+  auto compact = [&](int nrows, const unsigned long long* rm) -> int {
+    auto mk = [&](int r) { return rm[r]; };
+    if (warp == 0) scan_rows(nrows, mk, LOFF, nullptr);
     __syncthreads();
-    write_rows(nrows, rowmask, LOFF, LST);
+    write_rows(nrows, mk, LOFF, LST);
     __syncthreads();
     return LOFF[XL_ROWS - 1];
-  };
-  // two lists in one pass (two barriers instead of four)
-  auto compact2 = [&](int na, auto ma, int nb, auto mb, int* loffb, unsigned short* lstb) -> int2 {
-    if (warp == 0) scan_rows(na, ma, LOFF);
-    else if (warp == 1) scan_rows(nb, mb, loffb);
-    __syncthreads();
-    write_rows(na, ma, LOFF, LST);
-    write_rows(nb, mb, loffb, lstb);
-    __syncthreads();
-    return make_int2(LOFF[XL_ROWS - 1], loffb[XL_ROWS - 1]);
   };
   const unsigned count = *A.fix_count;
   // listed quarters popped from a queue (their costs differ: NoData fills, edge bands);
@@ -1403,17 +1390,19 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
             c_hi > c_lo ? (((c_hi - c_lo) >= 64 ? ~0ull : ((1ull << (c_hi - c_lo)) - 1ull)) << c_lo) : 0ull;
         NV[tid] = dn & win;
       }
+    } else if (tid >= 128 && tid < 128 + XE_R) {  // (other warps) the outputs to recompute
+      const int er = tid - 128;
       // outputs whose stencil footprint (a (2K+1)^2 box) contains a NoData cell
       constexpr int K = CURV ? 2 : 1;
       unsigned long long nbr = 0;
       for (int k = -K; k <= K; ++k)
-        if (tid + k >= 0 && tid + k < XE_R) nbr |= NB[tid + k];
+        if (er + k >= 0 && er + k < XE_R) nbr |= NB[er + k];
       unsigned long long dil = nbr;
       for (int k = 1; k <= K; ++k) dil |= (nbr << k) | (nbr >> k);
-      unsigned long long af = VO[tid] & dil;
+      unsigned long long af = VO[er] & dil;
       if (band) {  // the valid pixels within the stencil's reach of the window edge
         constexpr int EB = CURV ? 2 : 1;
-        const int gy = y0 - 4 + tid;
+        const int gy = y0 - 4 + er;
         unsigned long long bm = 0;
         if (gy < T.wy0 + EB || gy >= T.wy1 - EB) {
           bm = ~0ull;
@@ -1426,16 +1415,16 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
           const int l0 = T.wx0 - (x0 - 4), h1 = T.wx1 - (x0 - 4);
           bm = cols(l0, l0 + EB) | cols(h1 - EB, h1);
         }
-        af |= VO[tid] & bm;
+        af |= VO[er] & bm;
       }
-      AF[tid] = af;
+      AF[er] = af;
     }
     if (__syncthreads_or(any)) {
       // (d) axis-0 sums of the S cells listed in NV
       FF gw[5];
 #pragma unroll
       for (int j = 0; j < 5; ++j) gw[j] = A.gw[j];
-      const int nv = compact(XE_R, [&](int r) { return NV[r]; });
+      const int nv = compact(XE_R, NV);
       for (int li = tid; li < nv; li += XNT) {
         const int r = LST[li] >> 8, sc = LST[li] & 255, i = r * XS_C + sc;
         const int gy = y0 - 4 + r;
@@ -1453,7 +1442,7 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
       }
       __syncthreads();
       // (e) axis-1 pass and the normalised fill value of each cell to fill
-      const int nd = compact(XE_R, [&](int r) { return ND[r]; });
+      const int nd = compact(XE_R, ND);
       for (int li = tid; li < nd; li += XNT) {
         const int r = LST[li] >> 8, c = LST[li] & 255;
         const int gx = x0 - 4 + c;
@@ -1482,7 +1471,7 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
       // the derivatives within one cell of the pixels recomputed (D row r, column c = E row
       // r + 2, column c + 2); at the window edge the one-sided second differences of the
       // edge band reach two cells inward, through NoData too
-      const int2 cnt = compact2(XD_R, [&](int r) {
+      auto deriv_rows = [&](int r) {
         const unsigned long long a3 = AF[r + 1] | AF[r + 2] | AF[r + 3];
         unsigned long long m = (a3 >> 1) | (a3 >> 2) | (a3 >> 3);
         if (band) {
@@ -1496,7 +1485,15 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
           }
         }
         return m & ((1ull << XD_C) - 1ull);
-      }, SH, out_rows, LOFF_G, LST_G);
+      };
+      // one warp scans each list; NV (free once the fills are done) keeps the derivative masks
+      if (warp == 0) scan_rows(XD_R, deriv_rows, LOFF, NV);
+      else if (warp == 1) scan_rows(SH, out_rows, LOFF_G, nullptr);
+      __syncthreads();
+      write_rows(XD_R, [&](int r) { return NV[r]; }, LOFF, LST);
+      write_rows(SH, out_rows, LOFF_G, LST_G);
+      __syncthreads();
+      const int2 cnt = make_int2(LOFF[XL_ROWS - 1], LOFF_G[XL_ROWS - 1]);
       const int ndv = cnt.x;
       no = cnt.y;
       for (int li = tid; li < ndv; li += XNT) {
@@ -1513,7 +1510,7 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
       }
       __syncthreads();
     } else {
-      if (warp == 0) scan_rows(SH, out_rows, LOFF_G);
+      if (warp == 0) scan_rows(SH, out_rows, LOFF_G, nullptr);
       __syncthreads();
       write_rows(SH, out_rows, LOFF_G, LST_G);
       __syncthreads();
