@@ -105,6 +105,143 @@ __global__ void __launch_bounds__(NT) gauss_axis1(const float* __restrict__ v, c
   }
 }
 
+// Four consecutive outputs of the symmetric correlate1d along one line, centres
+// p0 .. p0+3 of the staged line x(i), each with corr_ff's exact operation
+// sequence (so the results are bit-identical to it).  The four accumulations
+// are independent chains, and the taps pass between neighbouring outputs: at
+// step k output j pairs x(p0+j-k) with x(p0+j+k), and at step k-1 output j's
+// lower tap is output j+1's lower tap of step k (upper: output j-1's), so a
+// step loads two values for four outputs.
+template <class Ld>
+__device__ __forceinline__ void corr4_ff(const FF* __restrict__ g, int R, int p0, Ld x, float out[4]) {
+  FF acc[4];
+  float L[4], U[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    acc[j] = ff_scale(x(p0 + j), g[0]);
+    L[j] = x(p0 + j - R);
+    U[j] = x(p0 + j + R);
+  }
+#pragma unroll 2
+  for (int k = R; k >= 1; --k) {
+    const FF gk = g[k];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[j] = ff_add(acc[j], ff_mul(two_sum(L[j], U[j]), gk));
+    L[0] = L[1];
+    L[1] = L[2];
+    L[2] = L[3];
+    L[3] = x(p0 + 4 - k);
+    U[3] = U[2];
+    U[2] = U[1];
+    U[1] = U[0];
+    U[0] = x(p0 + k - 1);
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) out[j] = __fadd_rn(acc[j].hi, acc[j].lo);
+}
+
+// Shared-memory forms of the two passes (used while the staged lines fit):
+// the weights and the block's source lines (clamped: 'nearest') are staged once,
+// and every thread computes four consecutive outputs along the filter axis with
+// corr4_ff.  Shared memory layout: weights [R+1] float-float, then the value
+// lines, then (two channels) the valid-mask lines.
+constexpr int G0C = 32, G0R = 64;   // axis 0: 32 columns x 64 rows; a thread: one column, 2 x 4 rows
+constexpr int G1C = 256, G1R = 4;   // axis 1: 4 rows x 256 columns; a thread: one row, 4 columns
+constexpr int GNT = 256;
+__host__ __device__ constexpr size_t g0_smem(int R) { return 8 * (size_t)(R + 1) + 2 * 4 * (size_t)(G0R + 2 * R) * G0C; }
+__host__ __device__ constexpr size_t g1_smem(int R) { return 8 * (size_t)(R + 1) + 2 * 4 * (size_t)G1R * (G1C + 2 * R); }
+
+__global__ void __launch_bounds__(GNT) gauss_axis0_s(const float* __restrict__ src, long long ld, int h, int w,
+                                                     const FF* __restrict__ g, int R, int two, const int* nan_flag,
+                                                     float* v, float* wt, long long old) {
+  extern __shared__ __align__(16) unsigned char gsm[];
+  FF* gs = reinterpret_cast<FF*>(gsm);
+  float* sv = reinterpret_cast<float*>(gs + R + 1);
+  const int rows = G0R + 2 * R;
+  float* sw = sv + (size_t)rows * G0C;
+  const bool pair = two || (nan_flag != nullptr && *nan_flag != 0);
+  const int tid = threadIdx.x, x0 = blockIdx.x * G0C, y0 = blockIdx.y * G0R;
+  for (int k = tid; k <= R; k += GNT) gs[k] = g[k];
+  for (int i = tid; i < rows * G0C; i += GNT) {
+    const int r = i / G0C, c = i - (i / G0C) * G0C;
+    const float a = __ldg(src + (long long)clamp_idx(y0 - R + r, h) * ld + min(x0 + c, w - 1));
+    if (pair) {
+      const bool ok = a == a;
+      sv[i] = ok ? a : 0.f;
+      sw[i] = ok ? 1.f : 0.f;
+    } else {
+      sv[i] = a;
+    }
+  }
+  __syncthreads();
+  const int c = tid % G0C, x = x0 + c;
+#pragma unroll 1
+  for (int run = 0; run < 2; ++run) {
+    const int r0 = (tid / G0C) * 8 + run * 4;  // block rows r0 .. r0+3
+    if (y0 + r0 >= h) break;
+    float o[4];
+    corr4_ff(gs, R, r0 + R, [&](int i) { return sv[i * G0C + c]; }, o);
+    if (x < w)
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (y0 + r0 + j < h) v[(long long)(y0 + r0 + j) * old + x] = o[j];
+    if (pair) {
+      corr4_ff(gs, R, r0 + R, [&](int i) { return sw[i * G0C + c]; }, o);
+      if (x < w)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (y0 + r0 + j < h) wt[(long long)(y0 + r0 + j) * old + x] = o[j];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(GNT) gauss_axis1_s(const float* __restrict__ v, const float* __restrict__ wt,
+                                                     long long ld, int h, int w, const FF* __restrict__ g, int R,
+                                                     int mode, const int* nan_flag, float* out, float* out2,
+                                                     long long old) {
+  extern __shared__ __align__(16) unsigned char gsm[];
+  FF* gs = reinterpret_cast<FF*>(gsm);
+  float* sv = reinterpret_cast<float*>(gs + R + 1);
+  const int cols = G1C + 2 * R;
+  float* sw = sv + (size_t)G1R * cols;
+  const bool pair = mode == AX1_PAIR || (nan_flag != nullptr && *nan_flag != 0);
+  const int tid = threadIdx.x, x0 = blockIdx.x * G1C, y0 = blockIdx.y * G1R;
+  for (int k = tid; k <= R; k += GNT) gs[k] = g[k];
+  for (int i = tid; i < G1R * cols; i += GNT) {
+    const int r = i / cols, cc = i - (i / cols) * cols;
+    const long long off = (long long)min(y0 + r, h - 1) * ld + clamp_idx(x0 - R + cc, w);
+    sv[i] = __ldg(v + off);
+    if (pair) sw[i] = __ldg(wt + off);
+  }
+  __syncthreads();
+  const int r = tid / (G1C / 4), c0 = 4 * (tid % (G1C / 4)), y = y0 + r;
+  if (y >= h) return;
+  const float* lv = sv + (size_t)r * cols;
+  float num[4];
+  corr4_ff(gs, R, c0 + R, [&](int i) { return lv[i]; }, num);
+  float* orow = out + (long long)y * old;
+  if (!pair) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (x0 + c0 + j < w) orow[x0 + c0 + j] = num[j];
+    return;
+  }
+  const float* lw = sw + (size_t)r * cols;
+  float den[4];
+  corr4_ff(gs, R, c0 + R, [&](int i) { return lw[i]; }, den);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int x = x0 + c0 + j;
+    if (x >= w) continue;
+    if (mode == AX1_PAIR) {
+      orow[x] = num[j];
+      out2[(long long)y * old + x] = den[j];
+    } else {
+      orow[x] = den[j] > 0.f ? __fdiv_rn(num[j], den[j]) : 0.f;
+    }
+  }
+}
+
 // flag |= any NaN in the h x w array.
 __global__ void any_nan(const float* __restrict__ a, long long ld, int h, int w, int* flag) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -307,6 +444,7 @@ __global__ void masked_store(const __grid_constant__ StoreArgs A) {
 dim3 blocks2d(int h, int w) { return dim3((w + 31) / 32, (h + 7) / 8); }
 
 constexpr size_t kMaxTable = 1 << 16;  // Gaussian weight table bytes (radius <= 8191)
+constexpr size_t kStagedSmem = 160 << 10;  // shared-memory Gaussian passes up to this size (radius <= 283)
 
 struct Arena {
   char* p;
@@ -338,6 +476,23 @@ int gaussian(const float* src, long long ld, int h, int w, double sigma, int mod
     any_nan<<<dim3((w + 255) / 256, std::min(h, 1024)), 256, 0, s>>>(src, ld, h, w, flag);
     FSG_LAUNCHED(1);
     nan_flag = flag;
+  }
+  if (g0_smem(R) <= kStagedSmem && (h + G1R - 1) / G1R <= 65535 && (h + G0R - 1) / G0R <= 65535) {
+    static bool attr_set[64] = {};
+    int dev = 0;
+    FSG_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+      FSG_CUDA(cudaFuncSetAttribute(gauss_axis0_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStagedSmem));
+      FSG_CUDA(cudaFuncSetAttribute(gauss_axis1_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStagedSmem));
+      attr_set[dev] = true;
+    }
+    gauss_axis0_s<<<dim3((w + G0C - 1) / G0C, (h + G0R - 1) / G0R), GNT, g0_smem(R), s>>>(
+        src, ld, h, w, gd, R, mode == AX1_PAIR ? 1 : 0, nan_flag, v, wt, w);
+    FSG_LAUNCHED(1);
+    gauss_axis1_s<<<dim3((w + G1C - 1) / G1C, (h + G1R - 1) / G1R), GNT, g1_smem(R), s>>>(
+        v, wt, w, h, w, gd, R, mode, nan_flag, dst, dst2, dld);
+    FSG_LAUNCHED(1);
+    return FSG_OK;
   }
   const int rpb = 16;
   gauss_axis0<<<dim3((w + NT - 1) / NT, (h + rpb - 1) / rpb), NT, 0, s>>>(
