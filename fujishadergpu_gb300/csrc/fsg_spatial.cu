@@ -307,14 +307,84 @@ __global__ void void_fill(float* coarse, long long ld, int h, int w, const float
 // the source (*nan_flag != 0; NULL: none) the zoom is NaN-aware: the zooms of
 // the NaN -> 0 values and of the valid mask, each rounded to float32, then
 // num / max(den, 1e-6) where den > 1e-3, else NaN.
-__global__ void zoom_linear(const float* __restrict__ a, long long ld, int h, int w, int zh, int zw, double fy,
-                            double fx, const int* nan_flag, float* out, long long old, int y0, int x0, int oh,
-                            int ow) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+// Launched with 32 x 8 threads, one warp per output row.  Where the block's
+// source columns span at most ZL_COLS samples (upsampling), the float64 terms
+// that zoom1_at forms per output are shared: the row terms (ty, 1 - ty, source
+// rows) come from lane 0, the column terms from warp 0, and the row-weighted
+// samples a[iy0][j] * (1 - ty) and a[iy1][j] * ty once per source column j of
+// the row; each output then sums its four terms in zoom1_at's order (the same
+// roundings, so the same float32).  Other blocks evaluate zoom1_at directly.
+constexpr int ZL_COLS = 40;
+__global__ void __launch_bounds__(256) zoom_linear(const float* __restrict__ a, long long ld, int h, int w, int zh,
+                                                   int zw, double fy, double fx, const int* nan_flag, float* out,
+                                                   long long old, int y0, int x0, int oh, int ow) {
+  __shared__ double s_tx[32], s_wx[32];
+  __shared__ int s_ix0[32], s_ix1[32];
+  __shared__ double s_p[8][4][ZL_COLS];  // per row: value rows 0 / 1, mask rows 0 / 1
+  const int lane = threadIdx.x, r = threadIdx.y;
+  const int x = blockIdx.x * 32 + lane, y = blockIdx.y * 8 + r;
+  const bool nan_aware = nan_flag != nullptr && *nan_flag != 0;
+  if (r == 0) {
+    const int zx = min(x0 + min(x, ow - 1), zw - 1);
+    const double cx = __dmul_rn((double)zx, fx), sx = floor(cx);
+    const double tx = __dsub_rn(cx, sx);
+    s_tx[lane] = tx;
+    s_wx[lane] = __dsub_rn(1.0, tx);
+    s_ix0[lane] = clamp_idx((int)sx, w);
+    s_ix1[lane] = clamp_idx((int)sx + 1, w);
+  }
+  __syncthreads();
+  const int j0 = s_ix0[0], nj = s_ix1[31] - j0 + 1;
+  if (nj > ZL_COLS || nj < 1) {  // (uniform over the block) direct evaluation
+    if (x < ow && y < oh) {
+      const int zy = min(y0 + y, zh - 1), zx = min(x0 + x, zw - 1);
+      out[(long long)y * old + x] = zoom1_at(a, ld, h, w, zy, zx, fy, fx, nan_aware);
+    }
+    return;
+  }
+  double ty = 0.0, wy = 0.0;
+  int iy0 = 0, iy1 = 0;
+  if (lane == 0) {
+    const int zy = min(y0 + min(y, oh - 1), zh - 1);
+    const double cy = __dmul_rn((double)zy, fy), sy = floor(cy);
+    ty = __dsub_rn(cy, sy);
+    wy = __dsub_rn(1.0, ty);
+    iy0 = clamp_idx((int)sy, h);
+    iy1 = clamp_idx((int)sy + 1, h);
+  }
+  ty = __shfl_sync(0xffffffffu, ty, 0);
+  wy = __shfl_sync(0xffffffffu, wy, 0);
+  iy0 = __shfl_sync(0xffffffffu, iy0, 0);
+  iy1 = __shfl_sync(0xffffffffu, iy1, 0);
+  for (int j = lane; j < nj; j += 32) {
+    const float v0 = __ldg(a + (long long)iy0 * ld + j0 + j), v1 = __ldg(a + (long long)iy1 * ld + j0 + j);
+    if (nan_aware) {
+      s_p[r][0][j] = __dmul_rn(v0 == v0 ? (double)v0 : 0.0, wy);
+      s_p[r][1][j] = __dmul_rn(v1 == v1 ? (double)v1 : 0.0, ty);
+      s_p[r][2][j] = __dmul_rn(v0 == v0 ? 1.0 : 0.0, wy);
+      s_p[r][3][j] = __dmul_rn(v1 == v1 ? 1.0 : 0.0, ty);
+    } else {
+      s_p[r][0][j] = __dmul_rn((double)v0, wy);
+      s_p[r][1][j] = __dmul_rn((double)v1, ty);
+    }
+  }
+  __syncwarp();
   if (x >= ow || y >= oh) return;
-  const int zy = min(y0 + y, zh - 1), zx = min(x0 + x, zw - 1);
-  out[(long long)y * old + x] = zoom1_at(a, ld, h, w, zy, zx, fy, fx, nan_flag != nullptr && *nan_flag != 0);
+  const int c0 = s_ix0[lane] - j0, c1 = s_ix1[lane] - j0;
+  const double tx = s_tx[lane], wx = s_wx[lane];
+  auto sum4 = [&](const double* p0, const double* p1) {
+    double t = __dmul_rn(p0[c0], wx);
+    t = __dadd_rn(t, __dmul_rn(p0[c1], tx));
+    t = __dadd_rn(t, __dmul_rn(p1[c0], wx));
+    t = __dadd_rn(t, __dmul_rn(p1[c1], tx));
+    return __double2float_rn(t);
+  };
+  float v = sum4(s_p[r][0], s_p[r][1]);
+  if (nan_aware) {
+    const float den = sum4(s_p[r][2], s_p[r][3]);
+    v = den > 1e-3f ? __fdiv_rn(v, fmaxf(den, 1e-6f)) : __int_as_float(0x7fc00000);
+  }
+  out[(long long)y * old + x] = v;
 }
 
 // ------------------------------------------------------ tile pieces
