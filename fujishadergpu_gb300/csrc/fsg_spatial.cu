@@ -105,28 +105,70 @@ __global__ void __launch_bounds__(NT) gauss_axis1(const float* __restrict__ v, c
   }
 }
 
+// Float-float arithmetic on pairs of independent values (the paired FP32
+// instructions: per component the same correctly rounded operation as the
+// scalar form, so the same results).  The products that a later addition
+// consumes are scalar __fmul_rn, which the compiler never contracts into a
+// fused multiply-add (a paired multiply followed by a paired add was seen
+// fused); the fused multiply-adds of the error terms are intended.
+typedef float2 f2;
+struct FF2 {
+  f2 hi, lo;
+};
+__device__ __forceinline__ f2 p_add(f2 a, f2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ f2 p_sub(f2 a, f2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ f2 p_mul_nc(f2 a, f2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
+__device__ __forceinline__ FF2 two_sum2(f2 a, f2 b) {
+  const f2 s = p_add(a, b), bb = p_sub(s, a);
+  return {s, p_add(p_sub(a, p_sub(s, bb)), p_sub(b, bb))};
+}
+__device__ __forceinline__ FF2 fast_two_sum2(f2 a, f2 b) {
+  const f2 s = p_add(a, b);
+  return {s, p_sub(b, p_sub(s, a))};
+}
+__device__ __forceinline__ FF2 ff_mul2(FF2 a, f2 ghi, f2 glo) {  // as ff_mul(a, g) per component
+  const f2 p = p_mul_nc(a.hi, ghi);
+  f2 e = __ffma2_rn(a.hi, ghi, make_float2(-p.x, -p.y));
+  e = __ffma2_rn(a.hi, glo, e);
+  e = __ffma2_rn(a.lo, ghi, e);
+  return fast_two_sum2(p, e);
+}
+__device__ __forceinline__ FF2 ff_add2(FF2 a, FF2 b) {  // as ff_add per component
+  const FF2 s = two_sum2(a.hi, b.hi);
+  return fast_two_sum2(s.hi, p_add(s.lo, p_add(a.lo, b.lo)));
+}
+__device__ __forceinline__ FF2 ff_scale2(f2 x, f2 ghi, f2 glo) {  // as ff_scale per component
+  const f2 p = p_mul_nc(x, ghi);
+  f2 e = __ffma2_rn(x, ghi, make_float2(-p.x, -p.y));
+  e = __ffma2_rn(x, glo, e);
+  return fast_two_sum2(p, e);
+}
+
 // Four consecutive outputs of the symmetric correlate1d along one line, centres
 // p0 .. p0+3 of the staged line x(i), each with corr_ff's exact operation
-// sequence (so the results are bit-identical to it).  The four accumulations
-// are independent chains, and the taps pass between neighbouring outputs: at
-// step k output j pairs x(p0+j-k) with x(p0+j+k), and at step k-1 output j's
-// lower tap is output j+1's lower tap of step k (upper: output j-1's), so a
-// step loads two values for four outputs.
+// sequence (so the results are bit-identical to it), as two pairs on the
+// paired FP32 instructions.  The accumulations are independent chains, and the
+// taps pass between neighbouring outputs: at step k output j pairs x(p0+j-k)
+// with x(p0+j+k), and at step k-1 output j's lower tap is output j+1's lower
+// tap of step k (upper: output j-1's), so a step loads two values for four
+// outputs.
 template <class Ld>
 __device__ __forceinline__ void corr4_ff(const FF* __restrict__ g, int R, int p0, Ld x, float out[4]) {
-  FF acc[4];
   float L[4], U[4];
+  const f2 g0h = make_float2(g[0].hi, g[0].hi), g0l = make_float2(g[0].lo, g[0].lo);
+  FF2 acc01 = ff_scale2(make_float2(x(p0), x(p0 + 1)), g0h, g0l);
+  FF2 acc23 = ff_scale2(make_float2(x(p0 + 2), x(p0 + 3)), g0h, g0l);
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    acc[j] = ff_scale(x(p0 + j), g[0]);
     L[j] = x(p0 + j - R);
     U[j] = x(p0 + j + R);
   }
 #pragma unroll 2
   for (int k = R; k >= 1; --k) {
     const FF gk = g[k];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[j] = ff_add(acc[j], ff_mul(two_sum(L[j], U[j]), gk));
+    const f2 gh = make_float2(gk.hi, gk.hi), gl = make_float2(gk.lo, gk.lo);
+    acc01 = ff_add2(acc01, ff_mul2(two_sum2(make_float2(L[0], L[1]), make_float2(U[0], U[1])), gh, gl));
+    acc23 = ff_add2(acc23, ff_mul2(two_sum2(make_float2(L[2], L[3]), make_float2(U[2], U[3])), gh, gl));
     L[0] = L[1];
     L[1] = L[2];
     L[2] = L[3];
@@ -136,8 +178,11 @@ __device__ __forceinline__ void corr4_ff(const FF* __restrict__ g, int R, int p0
     U[1] = U[0];
     U[0] = x(p0 + k - 1);
   }
-#pragma unroll
-  for (int j = 0; j < 4; ++j) out[j] = __fadd_rn(acc[j].hi, acc[j].lo);
+  const f2 o01 = p_add(acc01.hi, acc01.lo), o23 = p_add(acc23.hi, acc23.lo);
+  out[0] = o01.x;
+  out[1] = o01.y;
+  out[2] = o23.x;
+  out[3] = o23.y;
 }
 
 // Shared-memory forms of the two passes (used while the staged lines fit):
