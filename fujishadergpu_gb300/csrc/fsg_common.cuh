@@ -189,6 +189,44 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
   return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 
+// Float-float arithmetic on pairs of independent values (the paired FP32
+// instructions: per component the same correctly rounded operation as the
+// scalar form, so the same results).  The products that a later addition
+// consumes are scalar __fmul_rn, which the compiler never contracts into a
+// fused multiply-add (a paired multiply followed by a paired add was seen
+// fused); the fused multiply-adds of the error terms are intended.
+struct FF2 {
+  float2 hi, lo;
+};
+__device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 p_mul_nc(float2 a, float2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
+__device__ __forceinline__ FF2 two_sum2(float2 a, float2 b) {
+  const float2 s = p_add(a, b), bb = p_sub(s, a);
+  return {s, p_add(p_sub(a, p_sub(s, bb)), p_sub(b, bb))};
+}
+__device__ __forceinline__ FF2 fast_two_sum2(float2 a, float2 b) {
+  const float2 s = p_add(a, b);
+  return {s, p_sub(b, p_sub(s, a))};
+}
+__device__ __forceinline__ FF2 ff_mul2(FF2 a, float2 ghi, float2 glo) {  // as ff_mul(a, g) per component
+  const float2 p = p_mul_nc(a.hi, ghi);
+  float2 e = __ffma2_rn(a.hi, ghi, make_float2(-p.x, -p.y));
+  e = __ffma2_rn(a.hi, glo, e);
+  e = __ffma2_rn(a.lo, ghi, e);
+  return fast_two_sum2(p, e);
+}
+__device__ __forceinline__ FF2 ff_add2(FF2 a, FF2 b) {  // as ff_add per component
+  const FF2 s = two_sum2(a.hi, b.hi);
+  return fast_two_sum2(s.hi, p_add(s.lo, p_add(a.lo, b.lo)));
+}
+__device__ __forceinline__ FF2 ff_scale2(float2 x, float2 ghi, float2 glo) {  // x (hi + lo) per component
+  const float2 p = p_mul_nc(x, ghi);
+  float2 e = __ffma2_rn(x, ghi, make_float2(-p.x, -p.y));
+  e = __ffma2_rn(x, glo, e);
+  return fast_two_sum2(p, e);
+}
+
 // Hardware approximations (PTX *.approx instructions): relative error ~2^-22.
 __device__ __forceinline__ float ex2_approx(float x) {
   float r;

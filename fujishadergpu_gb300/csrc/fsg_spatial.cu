@@ -105,44 +105,7 @@ __global__ void __launch_bounds__(NT) gauss_axis1(const float* __restrict__ v, c
   }
 }
 
-// Float-float arithmetic on pairs of independent values (the paired FP32
-// instructions: per component the same correctly rounded operation as the
-// scalar form, so the same results).  The products that a later addition
-// consumes are scalar __fmul_rn, which the compiler never contracts into a
-// fused multiply-add (a paired multiply followed by a paired add was seen
-// fused); the fused multiply-adds of the error terms are intended.
 typedef float2 f2;
-struct FF2 {
-  f2 hi, lo;
-};
-__device__ __forceinline__ f2 p_add(f2 a, f2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ f2 p_sub(f2 a, f2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
-__device__ __forceinline__ f2 p_mul_nc(f2 a, f2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
-__device__ __forceinline__ FF2 two_sum2(f2 a, f2 b) {
-  const f2 s = p_add(a, b), bb = p_sub(s, a);
-  return {s, p_add(p_sub(a, p_sub(s, bb)), p_sub(b, bb))};
-}
-__device__ __forceinline__ FF2 fast_two_sum2(f2 a, f2 b) {
-  const f2 s = p_add(a, b);
-  return {s, p_sub(b, p_sub(s, a))};
-}
-__device__ __forceinline__ FF2 ff_mul2(FF2 a, f2 ghi, f2 glo) {  // as ff_mul(a, g) per component
-  const f2 p = p_mul_nc(a.hi, ghi);
-  f2 e = __ffma2_rn(a.hi, ghi, make_float2(-p.x, -p.y));
-  e = __ffma2_rn(a.hi, glo, e);
-  e = __ffma2_rn(a.lo, ghi, e);
-  return fast_two_sum2(p, e);
-}
-__device__ __forceinline__ FF2 ff_add2(FF2 a, FF2 b) {  // as ff_add per component
-  const FF2 s = two_sum2(a.hi, b.hi);
-  return fast_two_sum2(s.hi, p_add(s.lo, p_add(a.lo, b.lo)));
-}
-__device__ __forceinline__ FF2 ff_scale2(f2 x, f2 ghi, f2 glo) {  // as ff_scale per component
-  const f2 p = p_mul_nc(x, ghi);
-  f2 e = __ffma2_rn(x, ghi, make_float2(-p.x, -p.y));
-  e = __ffma2_rn(x, glo, e);
-  return fast_two_sum2(p, e);
-}
 
 // Four consecutive outputs of the symmetric correlate1d along one line, centres
 // p0 .. p0+3 of the staged line x(i), each with corr_ff's exact operation

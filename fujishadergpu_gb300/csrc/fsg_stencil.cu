@@ -204,6 +204,17 @@ __device__ __forceinline__ float gsum_ff(const FF* w, const float* x) {
   for (int k = 4; k >= 1; --k) acc = ff_add(acc, ff_mul(two_sum(x[4 - k], x[4 + k]), w[k]));
   return __fadd_rn(acc.hi, acc.lo);
 }
+// gsum_ff of two tap sets at once (the values and the valid mask of one cell) on the
+// paired FP32 instructions: (gsum_ff(w, a), gsum_ff(w, b)), bit for bit.
+__device__ __forceinline__ float2 gsum_ff2(const FF* w, const float* a, const float* b) {
+  FF2 acc = ff_mul2({make_float2(a[4], b[4]), make_float2(0.f, 0.f)}, make_float2(w[0].hi, w[0].hi),
+                    make_float2(w[0].lo, w[0].lo));
+#pragma unroll
+  for (int k = 4; k >= 1; --k)
+    acc = ff_add2(acc, ff_mul2(two_sum2(make_float2(a[4 - k], b[4 - k]), make_float2(a[4 + k], b[4 + k])),
+                               make_float2(w[k].hi, w[k].hi), make_float2(w[k].lo, w[k].lo)));
+  return p_add(acc.hi, acc.lo);
+}
 
 
 // Output products of one pixel from its derivatives.  Hillshade, slope and
@@ -499,8 +510,9 @@ __global__ void __launch_bounds__(NT, FSG_STENCIL_MINB) stencil_kernel(const __g
           xv[j] = ok ? v : 0.f;
           xw[j] = ok ? 1.f : 0.f;
         }
-        VV[r * WC + xc] = gsum_ff(gw, xv);
-        VW[r * WC + xc] = gsum_ff(gw, xw);
+        const float2 sw2 = gsum_ff2(gw, xv, xw);
+        VV[r * WC + xc] = sw2.x;
+        VW[r * WC + xc] = sw2.y;
       }
       __syncthreads();
       // (e) axis-1 pass and the normalised fill value of each needed cell
@@ -516,8 +528,8 @@ __global__ void __launch_bounds__(NT, FSG_STENCIL_MINB) stencil_kernel(const __g
           xv[j] = VV[r * WC + xc];
           xw[j] = VW[r * WC + xc];
         }
-        const float sv = gsum_ff(gw, xv);
-        const float sw = gsum_ff(gw, xw);
+        const float2 s2 = gsum_ff2(gw, xv, xw);
+        const float sv = s2.x, sw = s2.y;
         F[i] = sw > 0.0f ? __fdiv_rn(sv, sw) : 0.0f;
       }
       __syncthreads();
@@ -1437,8 +1449,9 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
           xv[j] = ok ? v : 0.f;
           xw[j] = ok ? 1.f : 0.f;
         }
-        VV[i] = gsum_ff(gw, xv);
-        VW[i] = gsum_ff(gw, xw);
+        const float2 sw2 = gsum_ff2(gw, xv, xw);
+        VV[i] = sw2.x;
+        VW[i] = sw2.y;
       }
       __syncthreads();
       // (e) axis-1 pass and the normalised fill value of each cell to fill
@@ -1453,7 +1466,8 @@ __global__ void __launch_bounds__(XNT, 4) stencil_fixup_kernel(const __grid_cons
           xv[j] = VV[r * XS_C + sc];
           xw[j] = VW[r * XS_C + sc];
         }
-        const float sv = gsum_ff(gw, xv), sw = gsum_ff(gw, xw);
+        const float2 s2 = gsum_ff2(gw, xv, xw);
+        const float sv = s2.x, sw = s2.y;
         Sv[(r + 4) * XS_C + c + 4] = sw > 0.0f ? __fdiv_rn(sv, sw) : 0.0f;  // after every read of (d)
       }
       __syncthreads();
