@@ -425,6 +425,16 @@ def spatial_tile(raster: _arrays.DevView, win: Tuple[int, int, int, int], core: 
         raise NotImplementedError("agg='stack' yields one band per radius; the tile loop writes one plane")
     acc = buf("acc", ch * cw)[: ch * cw].view(ch, cw)
     resp = buf("resp", ch * cw)[: ch * cw].view(ch, cw)
+    # one reflect padding at the largest depth of the locally computed radii: the padding
+    # at a smaller depth d is its centred sub-array (the same reflected samples)
+    depths = [max(1, min(spatial_depth(product, r), min(wh, ww) - 1)) for r in scales
+              if not (spatial_is_large(product, r, thr) and overview is not None)]
+    dmax = max(depths) if depths else 0
+    if dmax:
+        PH, PW = wh + 2 * dmax, ww + 2 * dmax
+        padded = buf("pad", PH * PW)[: PH * PW].view(PH, PW)
+        N.check(lib.fsg_pad_reflect(C.c_void_p(raster.ptr), raster.ld, raster.h, raster.w, wy, wx, wh, ww, dmax,
+                                    ndv, has_nd, C.c_void_p(padded.data_ptr()), PW, stream))
     for i, (r, w) in enumerate(zip(scales, plan.weights)):
         first = 1 if i == 0 else 0
         direct = plan.op == N.COMBINE_WSUM   # responses of a weighted sum go straight into acc
@@ -439,16 +449,13 @@ def spatial_tile(raster: _arrays.DevView, win: Tuple[int, int, int, int], core: 
         else:
             d = max(1, min(spatial_depth(product, r), min(wh, ww) - 1))
             ph, pw = wh + 2 * d, ww + 2 * d
-            padded = buf("pad", ph * pw)[: ph * pw].view(ph, pw)
-            N.check(lib.fsg_pad_reflect(C.c_void_p(raster.ptr), raster.ld, raster.h, raster.w, wy, wx, wh, ww, d,
-                                        ndv, has_nd, C.c_void_p(padded.data_ptr()), pw, stream))
+            sub = padded.data_ptr() + 4 * ((dmax - d) * PW + (dmax - d))  # the depth-d padding
             pcore = (d + cy - wy, d + cx - wx, ch, cw)
             if product in RAY_PRODUCTS:
-                _ray_spatial_into(product, padded.data_ptr(), pw, ph, pw, pcore, r, kw, pixel_size, psx, psy, resp,
-                                  buf=buf)
+                _ray_spatial_into(product, sub, PW, ph, pw, pcore, r, kw, pixel_size, psx, psy, resp, buf=buf)
             else:
                 smooth = buf("smooth", ph * pw)[: ph * pw].view(ph, pw)
-                _smooth_into(padded.data_ptr(), pw, ph, pw, r, pixel_size, product, smooth)
+                _smooth_into(sub, PW, ph, pw, r, pixel_size, product, smooth)
                 _run_product(smooth.data_ptr(), pw, ph, pw, pcore, product, kw, pixel_size, psx, psy, resp)
         if not (direct and spatial_is_large(product, r, thr) and overview is not None):
             N.check(lib.fsg_combine(C.c_void_p(resp.data_ptr()), cw, ch, cw, plan.op, C.c_float(w), first,
