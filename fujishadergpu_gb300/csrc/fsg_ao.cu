@@ -360,7 +360,7 @@ struct AoJob {
     A.field = reinterpret_cast<float*>(base + o_field);
   }
   int upload(void* dev, cudaStream_t s) const {
-    FSG_CUDA(cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, s));
+    FSG_UPLOAD(dev, host.data(), host.size(), s);
     return FSG_OK;
   }
   int enqueue(cudaStream_t s) const {

@@ -65,6 +65,16 @@ int validate_tiles(int32_t raster_h, int32_t raster_w, const fsg_tile* tiles, in
 // The library's stream-ordered memory pool of the current device (kept across calls).
 int scratch_pool(cudaMemPool_t* out);
 
+// cudaMemcpyAsync(dst, src, bytes, host to device, s) for a call's tables in pageable
+// host memory (copied into pinned staging first, so the call does not wait for the
+// work already queued on s).
+int upload_async(void* dst, const void* src, size_t bytes, cudaStream_t s);
+#define FSG_UPLOAD(dst, src, bytes, s)                             \
+  do {                                                             \
+    const int st_ = ::fsg::upload_async((dst), (src), (bytes), (s)); \
+    if (st_) return st_;                                           \
+  } while (0)
+
 // Stream-ordered scratch from the library's pool on `stream`, freed with
 // cudaFreeAsync on the same stream by the destructor.
 struct StreamScratch {

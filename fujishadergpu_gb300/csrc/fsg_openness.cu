@@ -333,7 +333,7 @@ struct OpenJob {
     A.queue = reinterpret_cast<unsigned*>(base + o_q);
   }
   int upload(void* dev, cudaStream_t s) const {
-    FSG_CUDA(cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, s));
+    FSG_UPLOAD(dev, host.data(), host.size(), s);
     return FSG_OK;
   }
   int enqueue(cudaStream_t s) const {

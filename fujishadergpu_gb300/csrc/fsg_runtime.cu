@@ -1,8 +1,10 @@
 // libfsg.so runtime: version, thread-local error messages, launch accounting,
 // device properties and the NoData mask kernel.
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -103,6 +105,58 @@ int scratch_pool(cudaMemPool_t* out) {
     g_pools[dev] = p;
   }
   *out = g_pools[dev];
+  return FSG_OK;
+}
+
+// Host-to-device copies of a call's tables through pinned staging.  From pageable
+// memory the driver may synchronise with the stream to stage a copy, so a call waited
+// for all the work already queued on its stream (the previous call's) before it could
+// queue its own: back-to-back calls of the host-buffer stencil never overlapped.  From
+// pinned memory the copy is queued like any other.  A per-device ring of kStageSlots
+// pinned slots, each reused once the copy that last read it has run (its event), each
+// grown on demand.
+constexpr int kStageSlots = 32;
+struct StageSlot {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaEvent_t ev = nullptr;
+  bool pending = false;
+};
+struct StageRing {
+  StageSlot slot[kStageSlots];
+  int next = 0;
+};
+std::mutex g_stage_mutex;
+StageRing g_stage[64];
+
+int upload_async(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return FSG_OK;
+  int dev = 0;
+  FSG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(FSG_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_stage_mutex);
+  StageRing& R = g_stage[dev];
+  StageSlot& k = R.slot[R.next];
+  R.next = (R.next + 1) % kStageSlots;
+  if (k.pending) {
+    FSG_CUDA(cudaEventSynchronize(k.ev));
+    k.pending = false;
+  }
+  if (!k.ev) FSG_CUDA(cudaEventCreateWithFlags(&k.ev, cudaEventDisableTiming));
+  if (k.cap < bytes) {
+    if (k.p) {
+      FSG_CUDA(cudaFreeHost(k.p));
+      k.p = nullptr;
+      k.cap = 0;
+    }
+    const size_t cap = (std::max<size_t>(bytes, (size_t)64 << 10) + 4095) & ~(size_t)4095;
+    FSG_CUDA(cudaHostAlloc(&k.p, cap, cudaHostAllocDefault));
+    k.cap = cap;
+  }
+  std::memcpy(k.p, src, bytes);
+  FSG_CUDA(cudaMemcpyAsync(dst, k.p, bytes, cudaMemcpyHostToDevice, s));
+  FSG_CUDA(cudaEventRecord(k.ev, s));
+  k.pending = true;
   return FSG_OK;
 }
 

@@ -547,7 +547,7 @@ int gaussian(const float* src, long long ld, int h, int w, double sigma, int mod
   float* wt = static_cast<float*>(ar.take(sizeof(float) * (size_t)h * w));
   int* flag = static_cast<int*>(ar.take(sizeof(int)));
   if (!gd || !v || !wt || !flag) return fail(FSG_ERR_WORKSPACE, "smoothing scratch exhausted");
-  FSG_CUDA(cudaMemcpyAsync(gd, g.data(), sizeof(FF) * g.size(), cudaMemcpyHostToDevice, s));
+  FSG_UPLOAD(gd, g.data(), sizeof(FF) * g.size(), s);
   const int* nan_flag = nullptr;
   if (mode == AX1_SMOOTH) {
     FSG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));

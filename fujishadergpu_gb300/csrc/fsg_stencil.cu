@@ -1698,9 +1698,9 @@ struct StencilJob {
     else if (tk.size() > (size_t)INLINE_TILES) std::memcpy(dst, tk.data(), sizeof(TileK) * tk.size());
   }
   int upload(void* dev, cudaStream_t s) const {
-    if (fast) FSG_CUDA(cudaMemcpyAsync(dev, ft.data(), sizeof(FastTile) * ft.size(), cudaMemcpyHostToDevice, s));
+    if (fast) FSG_UPLOAD(dev, ft.data(), sizeof(FastTile) * ft.size(), s);
     else if (tk.size() > (size_t)INLINE_TILES)
-      FSG_CUDA(cudaMemcpyAsync(dev, tk.data(), sizeof(TileK) * tk.size(), cudaMemcpyHostToDevice, s));
+      FSG_UPLOAD(dev, tk.data(), sizeof(TileK) * tk.size(), s);
     return FSG_OK;
   }
   // the streaming pass's tensor map of the raster (once its device pointer is final): a 2-D
@@ -2193,7 +2193,7 @@ extern "C" int fsg_stencil_host(const float* raster_host, int64_t ld, int32_t ra
     J.bind(base + job_off[bi]);
     J.pack(image.data() + (job_off[bi] - slots_total));
   }
-  if (tables) FSG_CUDA(cudaMemcpyAsync(base + slots_total, image.data(), tables, cudaMemcpyHostToDevice, caller));
+  if (tables) FSG_UPLOAD(base + slots_total, image.data(), tables, caller);
   FSG_CUDA(cudaEventRecord(S->start, caller));
   for (int i = 0; i < nslot; ++i) FSG_CUDA(cudaStreamWaitEvent(S->s[i], S->start, 0));
   int status = FSG_OK;

@@ -1561,7 +1561,7 @@ struct FilterCtx {
 };
 
 static int upload(float* dst, const std::vector<float>& v, cudaStream_t s) {
-  FSG_CUDA(cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+  FSG_UPLOAD(dst, v.data(), v.size() * sizeof(float), s);
   return FSG_OK;
 }
 
@@ -1926,13 +1926,13 @@ struct TopoJob {
     }
   }
   int upload(cudaStream_t s) const {
-    if (!g1.empty()) FSG_CUDA(cudaMemcpyAsync(base + g1_off, g1.data(), g1.size() * sizeof(float), cudaMemcpyHostToDevice, s));
-    if (!gv.empty()) FSG_CUDA(cudaMemcpyAsync(base + gv_off, gv.data(), gv.size() * sizeof(float), cudaMemcpyHostToDevice, s));
-    FSG_CUDA(cudaMemcpyAsync(base + tiles_off, tk.data(), sizeof(TopoTileK) * ntiles, cudaMemcpyHostToDevice, s));
-    FSG_CUDA(cudaMemcpyAsync(base + items_off, items.data(), sizeof(StripItem) * items.size(), cudaMemcpyHostToDevice, s));
+    if (!g1.empty()) FSG_UPLOAD(base + g1_off, g1.data(), g1.size() * sizeof(float), s);
+    if (!gv.empty()) FSG_UPLOAD(base + gv_off, gv.data(), gv.size() * sizeof(float), s);
+    FSG_UPLOAD(base + tiles_off, tk.data(), sizeof(TopoTileK) * ntiles, s);
+    FSG_UPLOAD(base + items_off, items.data(), sizeof(StripItem) * items.size(), s);
     if (!ditems.empty())
-      FSG_CUDA(cudaMemcpyAsync(base + ditems_off, ditems.data(), sizeof(DecItem) * ditems.size(), cudaMemcpyHostToDevice, s));
-    if (tc) FSG_CUDA(cudaMemcpyAsync(base + tci_off, tc_it.data(), sizeof(int4) * tc_it.size(), cudaMemcpyHostToDevice, s));
+      FSG_UPLOAD(base + ditems_off, ditems.data(), sizeof(DecItem) * ditems.size(), s);
+    if (tc) FSG_UPLOAD(base + tci_off, tc_it.data(), sizeof(int4) * tc_it.size(), s);
     return FSG_OK;
   }
 
