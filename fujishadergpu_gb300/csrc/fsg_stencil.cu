@@ -196,16 +196,10 @@ struct Region {
   }
 };
 
-// scipy's symmetric 9-tap correlate1d, sum x[4]*w0 + (x[0]+x[8])*w4 + ...
-// + (x[3]+x[5])*w1 in float-float, rounded to float32.
-__device__ __forceinline__ float gsum_ff(const FF* w, const float* x) {
-  FF acc = ff_mul({x[4], 0.f}, w[0]);
-#pragma unroll
-  for (int k = 4; k >= 1; --k) acc = ff_add(acc, ff_mul(two_sum(x[4 - k], x[4 + k]), w[k]));
-  return __fadd_rn(acc.hi, acc.lo);
-}
-// gsum_ff of two tap sets at once (the values and the valid mask of one cell) on the
-// paired FP32 instructions: (gsum_ff(w, a), gsum_ff(w, b)), bit for bit.
+// The 9-tap symmetric Gaussian sums of two tap sets at once (the values and the valid
+// mask of one cell), in float-float on the paired FP32 instructions: per set
+// x[4] w0, then the pairs (x[4-k] + x[4+k]) wk from k = 4 inwards (scipy's symmetric
+// correlate1d order), rounded once to float32.
 __device__ __forceinline__ float2 gsum_ff2(const FF* w, const float* a, const float* b) {
   FF2 acc = ff_mul2({make_float2(a[4], b[4]), make_float2(0.f, 0.f)}, make_float2(w[0].hi, w[0].hi),
                     make_float2(w[0].lo, w[0].lo));
