@@ -226,6 +226,31 @@ def test_host_buffer_tile_loop_equals_device_path(fsg, dtype):
         assert np.array_equal(a, b, equal_nan=True), n
 
 
+def test_back_to_back_host_buffer_calls_keep_their_own_tables(fsg):
+    """Calls queued without a synchronisation in between (their tile tables staged in turn
+    through the library's pinned ring, more calls than the ring has slots, different tile
+    grids and rasters) each equal the device path of their own inputs."""
+    from fujishadergpu_gb300 import _arrays
+    from fujishadergpu_gb300.algorithms import _stencil as S
+    params = S.make_params(pixel_size=5.0)
+    runs = []
+    for k in range(40):
+        H, W = 300 + 7 * (k % 5), 410 - 5 * (k % 3)
+        tile = (96, 128, 200)[k % 3]
+        dem = _fbm_nan(H, W, 500 + k, 3)
+        tiles = _tile_descs(H, W, tile, 8, 5.0, -5.0)
+        host_in = torch.from_numpy(dem).pin_memory()
+        host = torch.full((H, W), 7.0).pin_memory()
+        S.launch_host(host_in, tiles, params, {S.OUTPUT_INDEX["curvature_profile"]: S.host_plane(host)})
+        runs.append((dem, tiles, host))
+    torch.cuda.synchronize()
+    for dem, tiles, host in runs:
+        dev = torch.empty(dem.shape, device="cuda")
+        S.launch(_arrays.as_device_f32_2d(torch.from_numpy(dem).cuda()), tiles, params,
+                 {S.OUTPUT_INDEX["curvature_profile"]: S.make_plane(dev)})
+        assert np.array_equal(to_np(dev), host.numpy(), equal_nan=True)
+
+
 @pytest.mark.parametrize("offset", [0, 1])
 def test_tensor_copy_ring_equals_cp_async_ring(fsg, offset):
     """The streaming pass fills its row ring with one tensor-memory copy per row when the raster
