@@ -583,6 +583,7 @@ struct FastArgs {
   PlaneK planes[FSG_STENCIL_NOUT];
   int use_tma;                // tmap describes the raster (16-byte aligned base and row pitch)
   CUtensorMap tmap;           // 2-D float32 raster, box RBOX x 1
+  float qlim[FSG_STENCIL_NOUT][2];  // planes' code bounds (q_min, q_max) as float32
 };
 
 // Device-side failures the host reads with fsg_kernel_errors (bit 0: a streaming-pass
@@ -835,8 +836,11 @@ __device__ __forceinline__ Q4 q4hdiff(Q4 f, float left, float right) {
 
 // ZONE: z factor 1 (hillshade's derivatives are p, q; rows above/below the
 // stencil's own window are then never read again, so they are not kept).
-template <bool CURV, unsigned OM, bool ALLF32, bool ZONE>
+// PK: the planes' types, 1 all float32, 2 all uint8 (each without runtime type tests),
+// 0 any mix (tested per plane).
+template <bool CURV, unsigned OM, int PK, bool ZONE>
 __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kernel(const __grid_constant__ FastArgs A) {
+  constexpr bool ALLF32 = PK == 1, ALLU8 = PK == 2;
   constexpr bool DIV = (OM & ((1u << FSG_OUT_DX) | (1u << FSG_OUT_DY))) != 0;
   constexpr int REACH = CURV ? 2 : 1;  // rows above / below an output row that feed it
   extern __shared__ __align__(1024) float ring_dyn[];  // [warps][RING][RW] floats, then [warps][RING] barriers
@@ -999,7 +1003,7 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
     for (int k = 0; k < FSG_STENCIL_NOUT; ++k) {
       if (!(OM & (1u << k))) continue;
       const PlaneK& P = A.planes[k];
-      const int esz = ALLF32 ? 4 : (P.dtype == FSG_F32 ? 4 : (P.dtype == FSG_I16 ? 2 : 1));
+      const int esz = ALLF32 ? 4 : ALLU8 ? 1 : (P.dtype == FSG_F32 ? 4 : (P.dtype == FSG_I16 ? 2 : 1));
       const long long col = (long long)(T.ox0 + xl - T.cx0);
       optr[k] = static_cast<char*>(P.ptr) + ((long long)(T.oy0 + y0 - T.cy0) * P.ld + col) * esz;
       ostep[k] = P.ld * esz;
@@ -1091,7 +1095,7 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
       for (int kk = 0; kk < FSG_STENCIL_NOUT; ++kk) {
         if (!(OM & (1u << kk))) continue;
         char* dst = optr[kk];
-        if (ALLF32 || A.planes[kk].dtype == FSG_F32) {
+        if (ALLF32 || (!ALLU8 && A.planes[kk].dtype == FSG_F32)) {
           if (vstore[kk] && nout == 4) {
             *reinterpret_cast<float4*>(dst) = make_float4(olo[kk].x, olo[kk].y, ohi[kk].x, ohi[kk].y);
           } else {
@@ -1104,11 +1108,11 @@ __global__ void __launch_bounds__(FSG_FAST_NT, FSG_FAST_MINB) stencil_fast_kerne
         } else {
           // code bit patterns (quantize_bits: the code in the low 8 / 16 bits)
           const PlaneK& P = A.planes[kk];
-          const float fmin = (float)P.qmin, fmax = (float)P.qmax;
+          const float fmin = A.qlim[kk][0], fmax = A.qlim[kk][1];
           const uint2 cl = quantize_bits2(olo[kk], P.qa, P.qb, fmin, fmax);
           const uint2 ch = quantize_bits2(ohi[kk], P.qa, P.qb, fmin, fmax);
           const uint32_t c[4] = {cl.x, cl.y, ch.x, ch.y};
-          if (P.dtype == FSG_U8) {
+          if (ALLU8 || P.dtype == FSG_U8) {
             if (vstore[kk] && nout == 4) {  // one 4-byte store: a warp writes 128 contiguous bytes
               *reinterpret_cast<uint32_t*>(dst) =
                   __byte_perm(__byte_perm(c[0], c[1], 0x0040), __byte_perm(c[2], c[3], 0x0040), 0x5410);
@@ -1839,16 +1843,20 @@ static int stencil_prepare(const float* raster_dev, int64_t ld, int32_t raster_h
   constexpr unsigned HS = 1u << FSG_OUT_HILLSHADE, SL = 1u << FSG_OUT_SLOPE, CM = 1u << FSG_OUT_CURV_MEAN,
                      CG = 1u << FSG_OUT_CURV_GAUSSIAN, CP = 1u << FSG_OUT_CURV_PLANFORM,
                      CR = 1u << FSG_OUT_CURV_PROFILE, DXY = (1u << FSG_OUT_DX) | (1u << FSG_OUT_DY);
-  bool allf32 = true;
+  bool allf32 = true, allu8 = true;
   for (int o = 0; o < FSG_STENCIL_NOUT; ++o)
-    if ((outmask >> o) & 1u) allf32 = allf32 && planes[o].dtype == FSG_F32;
+    if ((outmask >> o) & 1u) {
+      allf32 = allf32 && planes[o].dtype == FSG_F32;
+      allu8 = allu8 && planes[o].dtype == FSG_U8;
+    }
   switch (outmask) {
 #define FSG_CASE(M, C)                                                                         \
   case (M):                                                                                    \
     if (((M) & HS) && A.z_is_one)                                                              \
-      fast = allf32 ? stencil_fast_kernel<C, (M), true, true> : stencil_fast_kernel<C, (M), false, true>; \
+      fast = allf32 ? stencil_fast_kernel<C, (M), 1, true>                                     \
+                    : (allu8 ? stencil_fast_kernel<C, (M), 2, true> : stencil_fast_kernel<C, (M), 0, true>); \
     else                                                                                       \
-      fast = allf32 ? stencil_fast_kernel<C, (M), true, false> : stencil_fast_kernel<C, (M), false, false>; \
+      fast = allf32 ? stencil_fast_kernel<C, (M), 1, false> : stencil_fast_kernel<C, (M), 0, false>; \
     fixup = allf32 ? stencil_fixup_kernel<(M), true> : stencil_fixup_kernel<(M), false>;       \
     break;
     FSG_CASE(HS | SL | CP | CR, true)
@@ -1896,6 +1904,10 @@ static int stencil_prepare(const float* raster_dev, int64_t ld, int32_t raster_h
     F.total_units = units;
     for (int j = 0; j < 5; ++j) F.gw[j] = {A.gw_hi[j], A.gw_lo[j]};
     std::copy(A.planes, A.planes + FSG_STENCIL_NOUT, F.planes);
+    for (int o = 0; o < FSG_STENCIL_NOUT; ++o) {
+      F.qlim[o][0] = (float)A.planes[o].qmin;
+      F.qlim[o][1] = (float)A.planes[o].qmax;
+    }
     J.units = units;
     J.fastk = fast;
     J.fixk = fixup;
