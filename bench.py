@@ -816,6 +816,8 @@ def main():
     ap.add_argument("--size", type=int, default=32768)
     ap.add_argument("--tile", type=int, default=4096)
     ap.add_argument("--halo", type=int, default=8)
+    ap.add_argument("--stencil-dtype", choices=["float32", "uint8"], default="float32",
+                    help="plane type of the headline stencil line (uint8: the extra section's workload alone)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the topousm / openness sections")
     ap.add_argument("--no-fp64-check", action="store_true",
@@ -840,7 +842,7 @@ def main():
         if rank == 0:
             print(json.dumps({"section": args.workload, **sec}))
         return
-    line = stencil_workload(args, rank, world)
+    line = stencil_workload(args, rank, world, out_dtype=args.stencil_dtype)
     if not args.no_extra:
         import torch
         torch.cuda.empty_cache()
