@@ -131,6 +131,12 @@ StageRing g_stage[64];
 
 int upload_async(void* dst, const void* src, size_t bytes, cudaStream_t s) {
   if (bytes == 0) return FSG_OK;
+  // a captured copy would read the slot when the graph replays, after later calls reused
+  // it: direct calls are not capturable (the fsg_*_plan entry points are)
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  FSG_CUDA(cudaStreamIsCapturing(s, &cap));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(FSG_ERR_UNSUPPORTED, "tile tables cannot be uploaded inside a stream capture: capture a plan's launch");
   int dev = 0;
   FSG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return fail(FSG_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
