@@ -115,6 +115,7 @@ int scratch_pool(cudaMemPool_t* out) {
 // pinned memory the copy is queued like any other.  A per-device ring of kStageSlots
 // pinned slots, each reused once the copy that last read it has run (its event), each
 // grown on demand.
+namespace {
 constexpr int kStageSlots = 32;
 struct StageSlot {
   void* p = nullptr;
@@ -128,6 +129,7 @@ struct StageRing {
 };
 std::mutex g_stage_mutex;
 StageRing g_stage[64];
+}  // namespace
 
 int upload_async(void* dst, const void* src, size_t bytes, cudaStream_t s) {
   if (bytes == 0) return FSG_OK;
