@@ -49,7 +49,9 @@ __device__ __forceinline__ float corr_ff(const FF* __restrict__ g, int R, Fn x) 
   return __fadd_rn(acc.hi, acc.lo);
 }
 
-// Axis-0 pass ('nearest').  Channel v: the values (NaN -> 0 when two
+// Axis-0 pass ('nearest'), one output per thread and step: the form for radii
+// whose staged lines exceed the shared-memory passes' budget (gauss_axis0_s /
+// gauss_axis1_s below take the others).  Channel v: the values (NaN -> 0 when two
 // channels are formed); channel w: the valid mask.  Two channels are formed
 // when `two` is set, or when *nan_flag is nonzero.
 __global__ void __launch_bounds__(NT) gauss_axis0(const float* __restrict__ src, long long ld, int h, int w,
