@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "fsg_filters.cuh"
@@ -558,13 +559,18 @@ int gaussian(const float* src, long long ld, int h, int w, double sigma, int mod
     nan_flag = flag;
   }
   if (g0_smem(R) <= kStagedSmem && (h + G1R - 1) / G1R <= 65535 && (h + G0R - 1) / G0R <= 65535) {
+    static std::mutex attr_mutex;
     static bool attr_set[64] = {};
     int dev = 0;
     FSG_CUDA(cudaGetDevice(&dev));
-    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-      FSG_CUDA(cudaFuncSetAttribute(gauss_axis0_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStagedSmem));
-      FSG_CUDA(cudaFuncSetAttribute(gauss_axis1_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStagedSmem));
-      attr_set[dev] = true;
+    if (dev < 0 || dev >= 64) return fail(FSG_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    {
+      std::lock_guard<std::mutex> lk(attr_mutex);
+      if (!attr_set[dev]) {
+        FSG_CUDA(cudaFuncSetAttribute(gauss_axis0_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStagedSmem));
+        FSG_CUDA(cudaFuncSetAttribute(gauss_axis1_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStagedSmem));
+        attr_set[dev] = true;
+      }
     }
     gauss_axis0_s<<<dim3((w + G0C - 1) / G0C, (h + G0R - 1) / G0R), GNT, g0_smem(R), s>>>(
         src, ld, h, w, gd, R, mode == AX1_PAIR ? 1 : 0, nan_flag, v, wt, w);
