@@ -1,0 +1,37 @@
+"""Host-side checks of polynomial constants compiled into the kernels: the coefficients are
+read from the CUDA source and evaluated in float32 the way the kernel does (Horner on t^2
+with fused multiply-adds, emulated in float64 and rounded once per step), so an edit that
+breaks the stated error bound or the reference's cap fails here without a GPU."""
+import os
+import re
+
+import numpy as np
+
+CSRC = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "fujishadergpu_gb300", "csrc")
+
+
+def _occlusion_coefficients():
+    src = open(os.path.join(CSRC, "fsg_ao.cu")).read()
+    body = src[src.index("occlusion2("):]
+    body = body[: body.index("return __fmul2_rn(t, p);")]
+    k = re.search(r"constexpr double OCC_K = ([0-9.eE+-]+) \* \(1\.0 - 1\.0 / ([0-9.]+)\);", src)
+    scale = float(k.group(1)) * (1.0 - 1.0 / float(k.group(2)))
+    # highest coefficient first, as the Horner steps appear in the source
+    hexes = re.findall(r"\(float\)\((-?0x[0-9a-fA-F.]+p-?\d+) \* OCC_K\)", body)
+    return [np.float32(float.fromhex(h) * scale) for h in hexes]
+
+
+def test_occlusion_polynomial_error_and_cap():
+    """min(atan(t) / (pi/4), 1) for t in [0, 1] within 1e-6 (normalised occlusion units), and a
+    saturated ratio (t = 1) gives at most 1, the reference's cap."""
+    coef = _occlusion_coefficients()
+    assert len(coef) >= 5
+    t = np.linspace(0.0, 1.0, 200001, dtype=np.float32)
+    t2 = (t * t).astype(np.float32)
+    p = np.full_like(t2, coef[0])
+    for c in coef[1:]:
+        p = (t2.astype(np.float64) * p.astype(np.float64) + np.float64(c)).astype(np.float32)
+    occ = (t * p).astype(np.float32)
+    ref = np.minimum(np.arctan(t.astype(np.float64)) / (np.pi / 4.0), 1.0)
+    assert np.max(np.abs(occ.astype(np.float64) - ref)) <= 1e-6
+    assert occ[-1] <= 1.0 and occ.max() <= 1.0
