@@ -35,3 +35,38 @@ def test_occlusion_polynomial_error_and_cap():
     ref = np.minimum(np.arctan(t.astype(np.float64)) / (np.pi / 4.0), 1.0)
     assert np.max(np.abs(occ.astype(np.float64) - ref)) <= 1e-6
     assert occ[-1] <= 1.0 and occ.max() <= 1.0
+
+
+def _horner_coefficients(path, start, end, pattern):
+    src = open(os.path.join(CSRC, path)).read()
+    body = src[src.index(start):]
+    body = body[: body.index(end)]
+    return [np.float32(float.fromhex(h)) for h in re.findall(pattern, body)]
+
+
+def _odd_poly32(coef, a):
+    a2 = (a * a).astype(np.float32)
+    p = np.full_like(a2, coef[0])
+    for c in coef[1:]:
+        p = (a2.astype(np.float64) * p.astype(np.float64) + np.float64(c)).astype(np.float32)
+    return (a * p).astype(np.float32)
+
+
+def test_atan_poly_error():
+    """atan_poly (fsg_common.cuh): |atan(a) - a P(a^2)| <= 1.5e-7 rad on [0, 1]."""
+    coef = _horner_coefficients("fsg_common.cuh", "float atan_poly(float x)", "float r = a * p;",
+                                r"(-?0x[0-9a-fA-F.]+p[-+]?\d+)f")
+    assert len(coef) == 8
+    a = np.linspace(0.0, 1.0, 200001, dtype=np.float32)
+    err = np.abs(_odd_poly32(coef, a).astype(np.float64) - np.arctan(a.astype(np.float64)))
+    assert err.max() <= 1.5e-7
+
+
+def test_slope_degree_polynomial_error():
+    """atan_deg_pos2 (fsg_stencil.cu): |degrees(atan(a)) - a P(a^2)| <= 1.1e-4 degree on [0, 1]."""
+    coef = _horner_coefficients("fsg_stencil.cu", "f2 atan_deg_pos2(f2 x)", "f2 r = mul2(a, p);",
+                                r"S2\((-?0x[0-9a-fA-F.]+p[-+]?\d+)f\)")
+    assert len(coef) == 6
+    a = np.linspace(0.0, 1.0, 200001, dtype=np.float32)
+    err = np.abs(_odd_poly32(coef, a).astype(np.float64) - np.degrees(np.arctan(a.astype(np.float64))))
+    assert err.max() <= 1.1e-4
